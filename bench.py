@@ -1,0 +1,332 @@
+"""Benchmark of the GB300 multigrid Runge-Kutta cycle.
+
+Workload (default): 3-D inviscid flow past a D=1 sphere cut into a 192^3
+uniform Cartesian box [-10,10]^3, M=0.5, alpha=0, JST central flux with
+scalar dissipation (k2=0.5, k4=1/64), 5-stage Jameson RK (cstp 1/4,1/6,3/8,
+1/2,1; cdis 1,0,0.56,0,0.44), CFL 2.8 local time step, implicit residual
+smoothing eps=0.6, 4-level W-cycle (192^3/96^3/48^3/24^3).  Synthetic:
+the geometry is generated analytically (there is no dataset).
+
+A step is one multigrid W-cycle at the finest FMG level.  The metric counts
+cell-updates: one physical cell advanced by one full RK update (all five
+stages); per W-cycle that is 192^3 + 3*96^3 + 6*48^3 + 4*24^3 =
+10,450,944 cell-updates (residual-only evaluations are not counted).
+
+    python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+                    [--precision fp64|mixed]
+
+--gpus N > 1 runs one independent replica per GPU (the path does not shard
+across GPUs within one case); value is the whole-job aggregate.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from code_mge_gb300 import _abi as A  # noqa: E402
+from code_mge_gb300 import cases as K  # noqa: E402
+from code_mge_gb300 import schedule as S  # noqa: E402
+
+METRIC = "MG-cycle cell-updates/s (mixed vs FP64 plain); solves/s & p50/p99 latency"
+UNIT = "cell-updates/s"
+
+# Algorithmic HBM bytes per cell-update of one full euler update (FP64,
+# 5-variable fields of 40 B): smoothing stages 11 fields, non-smoothing
+# stages 4 fields, 17 B of scalars per stage, 56 B for the time step.
+BYTES_PER_CELL_UPDATE_IRS = (11 + 4 + 11 + 4 + 11) * 40 + 5 * 17 + 56   # 1,781
+# Compulsory bytes per cell of one k_face launch as designed: reads the
+# per-cell fluxes F (15), sensors (3), w(1:4)+H (5) and lambda (1), writes
+# the convective and dissipative face fluxes (15 + 15): 54 doubles.
+BYTES_PER_CELL_FACE = 54 * 8
+LAUNCHES_PER_UPDATE = {"timestep": 1, "prep": 5, "face": 5, "rec": 5, "combine": 5, "irs_i": 3, "irs_j": 3,
+                       "irs_k_update": 3, "cutcell": 5, "bcond": 5, "rtrms": 1}
+
+
+def workload_case(precision="fp64"):
+    prec = A.MGE_PREC_MIXED if precision == "mixed" else A.MGE_PREC_FP64
+    return K.sphere_box(n=192, nlevel=4, extent=10.0, mach=0.5, mgtype=2, mcyc_fine=400, smoo=0.6,
+                        precision=prec)
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        try:
+            d = json.load(open(p))
+            return d, "measured"
+        except Exception:
+            pass
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def hbm_peak_gbs():
+    d, kind = peaks()
+    for k in ("hbm_gbs", "hbm_GBs", "hbm_copy_gbs"):
+        if k in d:
+            v = d[k]
+            if isinstance(v, dict):
+                v = v.get("burst", v.get("value", next(iter(v.values()))))
+            return float(v), kind
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+                for q, nm in enumerate(names):
+                    if r[5 + q].lower().startswith("active"):
+                        reasons.add(nm)
+            except Exception:
+                continue
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def time_cpu_oracle(case, threads, cycles=1):
+    """Oracle (the reference's algorithm restated in C++) on the same case."""
+    from oracle.oracle import OracleCycle, set_threads
+    set_threads(threads)
+    o = OracleCycle(case)
+    t0 = time.perf_counter()
+    for q in range(cycles):
+        o.cycle(ncyc=q + 1)
+    dt = time.perf_counter() - t0
+    o.close()
+    return dt
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    case = workload_case("fp64")
+    cu = S.cell_updates_per_cycle(case)
+    from oracle.oracle import OracleCycle, set_threads
+    set_threads(threads)
+    o = OracleCycle(case)
+    for q in range(args.warmup):
+        o.cycle(ncyc=q + 1)
+    t0 = time.perf_counter()
+    for q in range(args.steps):
+        o.cycle(ncyc=args.warmup + q + 1)
+    dt = time.perf_counter() - t0
+    v = args.steps * cu / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (analytic sphere geometry)",
+        "config": {"workload": "sphere D=1 in 192^3 box [-10,10]^3, M=0.5, JST scalar, 5-stage RK, CFL 2.8, "
+                               "IRS 0.6, 4-level W-cycle; step = 1 W-cycle", "cells_finest": 192 ** 3,
+                   "cell_updates_per_step": cu},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "%d W-cycles of the 192^3 case, OpenMP over %d host threads" % (args.steps, threads)},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference (Fortran mgsol/pmgsol) cannot be built or run here; the timed CPU implementation is "
+                "the line-by-line C++ restatement of its algorithm",
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args):
+    rank, world, local = dist_env()
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = local
+    from code_mge_gb300.runtime import Cycle, load_library
+    lib = load_library()
+    case = workload_case(args.precision)
+    cu = S.cell_updates_per_cycle(case)
+    L = case.prm.nlevel
+    cyc = Cycle(case, device=dev)
+    for q in range(args.warmup):
+        cyc.cycle(L, ncyc=q + 1)
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+
+    sampler = ClockSampler(dev)
+    barrier()
+    sampler.start()
+    dev_ms = 0.0
+    n_launch0 = lib.mge_launch_count(cyc.ctx)
+    t0 = time.perf_counter()
+    res = []
+    for q in range(args.steps):
+        res.append(cyc.cycle(L, ncyc=args.warmup + q + 1))
+        dev_ms += lib.mge_last_cycle_ms(cyc.ctx)
+    barrier()
+    wall = time.perf_counter() - t0
+    clocks = sampler.stop()
+    n_launch = lib.mge_launch_count(cyc.ctx) - n_launch0
+    dev_s = dev_ms / 1e3
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([dev_s], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_s = float(t.item())
+    value = world * args.steps * cu / dev_s
+
+    # end to end through the C-ABI with host buffers: H2D of the finest state
+    # from pinned memory, one cycle, D2H of the cycle's residual
+    sp = case.levels[L - 1][0]
+    w_host = torch.empty(5 * sp.dims[0] * sp.dims[1] * sp.dims[2], dtype=torch.float64, pin_memory=True)
+    w_np = w_host.numpy()
+    w_np[:] = cyc.field("w", L).ravel()
+    wptr = w_np.ctypes.data_as(C.POINTER(C.c_double))
+    barrier()
+    t0 = time.perf_counter()
+    for q in range(args.steps):
+        rc = lib.mge_upload_state(cyc.ctx, L, 1, wptr)
+        if rc:
+            raise RuntimeError("upload failed %d" % rc)
+        cyc.cycle(L, ncyc=2)
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    e2e = world * args.steps * cu / e2e_s if world == 1 else None
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e = world * args.steps * cu / float(t.item())
+
+    # per-kernel device times (CUDA events on the library stream), finest level
+    ms = np.zeros(len(A.KERNEL_KINDS))
+    lib.mge_kernel_times(cyc.ctx, L, 2, ms.ctypes.data_as(C.POINTER(C.c_double)), len(ms))
+    kt = {k: float(ms[q]) for q, k in enumerate(A.KERNEL_KINDS)}
+    share = {k: kt[k] * LAUNCHES_PER_UPDATE[k] for k in kt}
+    tot = sum(share.values()) or 1.0
+    dom = max(share, key=share.get)
+    peak, pkind = hbm_peak_gbs()
+    ncell = case.finest_cells
+    dims = sp.dims
+    face_cells = (dims[0] - 3) * (dims[1] - 3) * (dims[2] - 3)
+    if dom == "face":
+        alg = BYTES_PER_CELL_FACE * face_cells
+    else:
+        alg = BYTES_PER_CELL_FACE * face_cells
+    achieved = alg / (kt["face"] * 1e-3) / 1e9 if kt["face"] > 0 else 0.0
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if os.path.exists(tf):
+        try:
+            traffic = json.load(open(tf)).get("k_face_bytes_per_launch_192")
+        except Exception:
+            traffic = None
+    upd_ms = sum(kt[k] * LAUNCHES_PER_UPDATE[k] for k in kt)
+    whole_update_gbs = BYTES_PER_CELL_UPDATE_IRS * ncell / (upd_ms * 1e-3) / 1e9 if upd_ms > 0 else 0.0
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        dt = time_cpu_oracle(case, threads=1, cycles=1)
+        cpu = {"value": cu / dt, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": "1 W-cycle of the same 192^3 case on 1 host thread (%.1f s)" % dt}
+    cyc.close()
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if args.precision == "fp64" else "f64-fine/f32-coarse",
+            "data": "synthetic (analytic sphere geometry, free-stream start)",
+            "config": {"workload": "sphere D=1 in 192^3 box [-10,10]^3, M=0.5, JST scalar, 5-stage RK, CFL 2.8, "
+                                   "IRS 0.6, 4-level W-cycle; step = 1 W-cycle", "cells_finest": ncell,
+                       "cell_updates_per_step": cu, "precision": args.precision,
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "l2": "fields of 301 MB each exceed the 129 MB L2 (no flush needed)"},
+            "wall_ms_per_step": 1e3 * wall / args.steps,
+            "residual_last": res[-1] if res else None,
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(w_np.nbytes), "d2h_bytes_per_step": 8},
+            "gpu_launches": None,
+            "roofline": {"bound": "hbm", "kernel": "k_face", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_kind": pkind,
+                         "note": "GB300 FP64 issue rate, not HBM, bounds these kernels"},
+            "whole_update_hbm": {"achieved_gbs": whole_update_gbs, "frac": whole_update_gbs / peak,
+                                 "bytes_per_cell_update": BYTES_PER_CELL_UPDATE_IRS},
+            "kernel_ms": kt, "kernel_share": {k: share[k] / tot for k in share}, "dominant_kernel": dom,
+            "clocks": clocks,
+            "cpu_baseline": cpu,
+        }
+        line["gpu_launches"] = int(n_launch)
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

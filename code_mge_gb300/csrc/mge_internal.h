@@ -1,0 +1,133 @@
+// mge_internal.h -- device data model shared by the kernels and the host
+// runtime of the GB300 multigrid Runge-Kutta cycle.
+//
+// Layout of every per-cell field is the reference's Fortran layout
+// a(0:ib,0:jb,0:kb,nvar): cell (i,j,k) at c = i + Pi*(j + Pj*k), variable v
+// at v*N + c.  Per-cell flux/face scratch uses [dir][var][N].
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace mge {
+
+// One uniform block as the kernels see it (passed by value).
+template <typename T>
+struct DevBlock {
+  int nx, ny, nz;
+  int il, jl, kl, ie, je, ke, ib, jb, kb;
+  int Pi, Pj;
+  long long N;              // (ib+1)(jb+1)(kb+1)
+  // state and stage fields (precision T)
+  T* w;                     // 5N conservative variables
+  T* p;                     // N pressure
+  T* wn;                    // 5N state at the start of euler
+  T* ws;                    // 5N state saved on first coarse entry
+  T* dw;                    // 5N residual
+  T* fw;                    // 5N blended dissipation
+  T* wr;                    // 5N restricted residual (coarse levels)
+  T* qf;                    // 5N multigrid forcing
+  T* vdtim;                 // N local time step
+  T* lam;                   // N radi+radj+radk
+  double* dtim;             // 1 global time step (FP64 bits, atomicMin target)
+  const uint8_t* blank;     // N
+  const uint8_t* marker;    // N
+  const int32_t* cutmap;    // N: -1 or cut-target index
+  // per-stage scratch shared by the blocks of a context
+  T* H;                     // N  rho*E + p
+  T* F;                     // 15N per-cell convective flux [dir][var]
+  T* fp;                    // 3N pressure sensor [dir]
+  T* efs;                   // 15N convective face flux [dir][var] at the upper cell of the face
+  T* dfs;                   // 15N dissipative face flux
+  // metric (uniform, axis-aligned face vectors)
+  double s[3];              // si[0], sj[1], sk[2]
+  double sqrt_ds[3];        // sqrt(s*s) computed on the host
+  double vol;
+  double rvol;              // RN(1/vol)
+  // cut-cell records
+  int nmir;
+  int m0;                   // first record with an empty cloud (nmir if none)
+  const int32_t* rec_i;     // [nmir][8]: ccid(3), faceid, zz, npoint, pad, pad
+  const int32_t* rec_cloud; // [nmir][8][3]
+  const double* rec_coef;   // [nmir][8]
+  const double* rec_nvec;   // [nmir][3]
+  const double* rec_qb;     // [nmir][3]
+  const double* rec_area;   // [nmir] wall-face area
+  T* rec_wsol;              // [nmir][5]
+  T* rec_psol;              // [nmir]
+  T* rec_term;              // [nmir][40] stage terms of efluxb/dfluxb
+  const int32_t* tgt_off;   // [ntgt+1]
+  const int32_t* tgt_ops;   // op = 2*m + role (0: cut cell, 1: neighbour)
+  int bctype[6];
+  double fnv[6][3];
+};
+
+struct StageArgs {
+  int m;            // stage 1..mstage
+  double fn;        // cstp(m)*cfl
+  double cd;        // cdis(m)
+  int dissip_on;    // cdis(m) > 0
+  int scale_fw;     // m > 1
+  int forcing;      // mgl < mlvl
+  int first_forcing;// lfir && m == 1
+  int lres;
+  int irs;          // odd stage with smoo > 0: defer the update to the line sweeps
+  int vt;
+};
+
+struct PhysParams {
+  double gamma, gm1, gm;    // gamma, gamma-1, 1/(gamma-1)
+  double vis2, vis4, cfl, dimcfl;
+  double rho0, p0, c0, u0[3];
+  double e0;                // rho0*h0 - p0
+  double si_far;            // rho0**gamma/p0
+  int matrix;               // matrix dissipation
+  int eqn_ns;
+  double smoo;
+};
+
+// error word bits
+enum : unsigned {
+  ERR_NEGPRESS = 1u,
+  ERR_ZERORHO = 2u,
+  ERR_NAN = 4u,
+};
+
+// IRS pivot tables of one block direction (psmoo.f90:136-166)
+struct IrsTables {
+  const double* e1;   // pivot of row q (index 0..l)
+  const double* e1r;  // RN(1/pivot)
+  const double* e2;   // elimination factor
+};
+
+// kernel launchers (mge_kernels.cu)
+template <typename T> void launch_timestep(const DevBlock<T>& b, const PhysParams& P, unsigned* err, cudaStream_t s);
+template <typename T> void launch_stage(const DevBlock<T>& b, const PhysParams& P, const StageArgs& A, unsigned* err,
+                                        cudaStream_t s);
+template <typename T> void launch_irs(const DevBlock<T>& b, const PhysParams& P, const IrsTables* tab, cudaStream_t s);
+template <typename T> void launch_stage_part(int part, const DevBlock<T>& b, const PhysParams& P, const StageArgs& A,
+                                             unsigned* err, cudaStream_t s);
+template <typename T> void launch_irs_part(int part, const DevBlock<T>& b, const PhysParams& P, const IrsTables* tab,
+                                           cudaStream_t s);
+template <typename T> void launch_cutcell(const DevBlock<T>& b, const PhysParams& P, unsigned* err, cudaStream_t s);
+template <typename T> void launch_bcond(const DevBlock<T>& b, const PhysParams& P, cudaStream_t s);
+template <typename T> void launch_rtrms(const DevBlock<T>& b, const PhysParams& P, int vt, double* partial,
+                                        int npartial, double* out, cudaStream_t s);
+template <typename T> void launch_depvars_all(const DevBlock<T>& b, const PhysParams& P, cudaStream_t s);
+template <typename T> void launch_copy_ws(const DevBlock<T>& b, cudaStream_t s);
+template <typename T> void launch_save_wn(const DevBlock<T>& b, cudaStream_t s);
+template <typename T> void launch_copy_wn(const DevBlock<T>& b, cudaStream_t s);
+template <typename T> void launch_init_free(const DevBlock<T>& b, const PhysParams& P, cudaStream_t s);
+template <typename TC, typename TF>
+void launch_collc(const DevBlock<TC>& c, const DevBlock<TF>& f, const int ratio[3], const int offset[3],
+                  uint8_t* marker_c, cudaStream_t s);
+template <typename TF, typename TC>
+void launch_addw(const DevBlock<TF>& f, const DevBlock<TC>& c, const int ratio[3], const int offset[3], int fmg,
+                 cudaStream_t s);
+template <typename TF, typename TC>
+void launch_embed(const DevBlock<TF>& f, const DevBlock<TC>& c, const int ratio[3], const int offset[3],
+                  const PhysParams& P, cudaStream_t s);
+template <typename T> void launch_forces(const DevBlock<T>& b, const double* origin, const double* h,
+                                         const double* center, double* out7, cudaStream_t s);
+int rtrms_partials(long long ncells);
+
+}  // namespace mge

@@ -1,0 +1,1471 @@
+// mge_kernels.cu -- sm_103a kernels of code_mge's multigrid Runge-Kutta cycle.
+//
+// GB300 executes FP64 at 1/58 of its FP32 rate (about 0.6 TFMA/s against
+// 6.8 TB/s of HBM), so an all-FP64 JST stage is bound by FP64 issue, not by
+// memory.  The stage is therefore split so that every per-cell and per-face
+// quantity is evaluated exactly once (the reference re-evaluates each cell
+// flux for both faces), with the intermediates kept in HBM/L2:
+//
+//   k_prep     per cell: 1/rho, rho*E+p, the cell flux F(w).s for i/j/k
+//              (ceflux, eflux.f90:133-155) and the pressure sensors
+//              (dflux.f90:71-76,131-136,188-193)
+//   k_face     per face: averaged convective flux (eflux.f90:42-98) and the
+//              blended 2nd/4th-difference dissipation (dflux.f90:82-112)
+//   k_rec      per cut-cell record: the efluxb/dfluxb face replacements
+//   k_combine  per cell: dw, fw, forcing, blanking, time-step scaling and,
+//              without smoothing, the update + depvars (euler.f90:127-399)
+//   k_irs_*    implicit residual smoothing lines (psmoo.f90:171-237), the
+//              k-line fused with the update
+//
+// Arithmetic follows the reference expression by expression.  The plain path
+// is compiled with --fmad=false (no contraction); divisions by a quantity
+// whose reciprocal is already known use Markstein's correction
+// (q0 = a*y, r = fma(-q0,b,a), q = fma(r,y,q0) with y = RN(1/b)), which
+// returns the correctly rounded quotient (P. Markstein, IBM J. Res. Dev. 34,
+// 1990), so results stay bit-identical to IEEE a/b at a third of its cost.
+#include <cmath>
+#include <cstdio>
+
+#include "mge_internal.h"
+
+namespace mge {
+
+// --------------------------------------------------------------- helpers
+__device__ __forceinline__ double mdiv(double a, double b, double y) {
+  double q = a * y;
+  double r = fma(-q, b, a);
+  return fma(r, y, q);
+}
+__device__ __forceinline__ float mdiv(float a, float b, float y) {
+  float q = a * y;
+  float r = fmaf(-q, b, a);
+  return fmaf(r, y, q);
+}
+template <typename T> __device__ __forceinline__ T fdimT(T a, T b) { return a > b ? a - b : T(0); }
+template <typename T> __device__ __forceinline__ T fmaxT(T a, T b) { return a > b ? a : b; }
+template <typename T> __device__ __forceinline__ T fminT(T a, T b) { return a < b ? a : b; }
+
+// depvars_one, depvars.f90:48-49
+template <typename T> __device__ __forceinline__ T depvars(T gamma, const T* w) {
+  T qq = T(0.5) * (w[1] * w[1] + w[2] * w[2] + w[3] * w[3]) / w[0];
+  return (gamma - T(1)) * fdimT(w[4], qq);
+}
+
+struct Idx {
+  int i, j, k;
+};
+__device__ __forceinline__ long long cidx(int Pi, int Pj, int i, int j, int k) {
+  return (long long)i + (long long)Pi * ((long long)j + (long long)Pj * (long long)k);
+}
+
+inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
+
+// --------------------------------------------------------------- timestep (timestep.f90:39-115)
+// TC is the arithmetic precision (FP64 in the plain path, FP32 in the mixed one).
+template <typename T, typename TC>
+__global__ void k_timestep(DevBlock<T> b, PhysParams P, unsigned* err) {
+  const int nxl = b.nx, nyl = b.ny;
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long tot = (long long)b.nx * b.ny * b.nz;
+  if (t >= tot) return;
+  int i = 2 + (int)(t % nxl);
+  int j = 2 + (int)((t / nxl) % nyl);
+  int k = 2 + (int)(t / ((long long)nxl * nyl));
+  const long long N = b.N;
+  const long long c = cidx(b.Pi, b.Pj, i, j, k);
+  const TC gamma = (TC)P.gamma;
+  TC w0 = (TC)b.w[c], w1 = (TC)b.w[N + c], w2 = (TC)b.w[2 * N + c], w3 = (TC)b.w[3 * N + c];
+  TC pc = (TC)b.p[c];
+  TC cc = gamma * pc / w0;
+  if (cc < TC(0) || cc != cc) {
+    atomicOr(err, ERR_NEGPRESS);
+    return;
+  }
+  cc = sqrt(fmaxT(cc, TC(0)));
+  TC y = TC(1) / w0;
+  TC uu = mdiv(w1, w0, y), uv = mdiv(w2, w0, y), uw = mdiv(w3, w0, y);
+  // face vectors are axis-aligned: |u.s| = |u_d s_d|, |s| precomputed
+  TC ri = fabs(uu * (TC)b.s[0]) + cc * (TC)b.sqrt_ds[0];
+  TC rj = fabs(uv * (TC)b.s[1]) + cc * (TC)b.sqrt_ds[1];
+  TC rk = fabs(uw * (TC)b.s[2]) + cc * (TC)b.sqrt_ds[2];
+  TC lsum = ri + rj + rk;
+  TC fict = (TC)b.vol / lsum;
+  const TC plim = TC(0.001);
+  TC pip = (TC)b.p[c + 1], pim = (TC)b.p[c - 1];
+  TC pjp = (TC)b.p[c + b.Pi], pjm = (TC)b.p[c - b.Pi];
+  long long pl = (long long)b.Pi * b.Pj;
+  TC pkp = (TC)b.p[c + pl], pkm = (TC)b.p[c - pl];
+  TC p2 = TC(2) * pc;
+  TC dpi = fabs((pip - p2 + pim) / (pip + p2 + pim + plim));
+  TC dpj = fabs((pjp - p2 + pjm) / (pjp + p2 + pjm + plim));
+  TC dpk = fabs((pkp - p2 + pkm) / (pkp + p2 + pkm + plim));
+  TC r = TC(1) / (TC(1) + fminT((TC)P.dimcfl, TC(2) * (dpi + dpj + dpk)));
+  TC vd = fict * r;
+  // global minimum (timestep.f90:112), over every physical cell before blanking
+  double vdd = (double)vd;
+  if (vdd >= 0.0) atomicMin((unsigned long long*)b.dtim, (unsigned long long)__double_as_longlong(vdd));
+  if (b.blank[c] == 0) {  // timestep.f90:212-223
+    b.vdtim[c] = T(0);
+    b.lam[c] = T(0);
+  } else {
+    b.vdtim[c] = (T)vd;
+    b.lam[c] = (T)lsum;
+  }
+}
+
+template <typename T> __global__ void k_set_scalar(T* p, double v) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *p = (T)v;
+}
+// dtim travels as the bit pattern of a double (atomicMin on positive doubles)
+__global__ void k_dtim_reset(double* p) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *p = 10.0;
+}
+template <typename T> __global__ void k_dtim_convert(double* src, T* dst) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *dst = (T)(*src);
+}
+
+// --------------------------------------------------------------- stage: per-cell pass
+// Box [1..ie]x[1..je]x[1..ke]: every cell whose flux or sensor a face needs.
+template <typename T>
+__global__ void k_prep(DevBlock<T> b, int dissip_on) {
+  const int ex = b.ie, ey = b.je;  // count = ie (cells 1..ie)
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long tot = (long long)b.ie * b.je * b.ke;
+  if (t >= tot) return;
+  int i = 1 + (int)(t % ex);
+  int j = 1 + (int)((t / ex) % ey);
+  int k = 1 + (int)(t / ((long long)ex * ey));
+  const long long N = b.N;
+  const long long c = cidx(b.Pi, b.Pj, i, j, k);
+  T w[5];
+#pragma unroll
+  for (int v = 0; v < 5; v++) w[v] = b.w[v * N + c];
+  T p = b.p[c];
+  T y = T(1) / w[0];
+  T Hc = w[4] + p;
+  b.H[c] = Hc;
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    T s = (T)b.s[d];
+    T f0 = w[1 + d] * s;  // sum(w(2:4)*ss) with the two zero components dropped
+    T f1 = mdiv(f0 * w[1], w[0], y);
+    T f2 = mdiv(f0 * w[2], w[0], y);
+    T f3 = mdiv(f0 * w[3], w[0], y);
+    if (d == 0) f1 = f1 + p * s;
+    if (d == 1) f2 = f2 + p * s;
+    if (d == 2) f3 = f3 + p * s;
+    T f4 = mdiv(f0 * Hc, w[0], y);
+    T* F = b.F + (long long)(d * 5) * N + c;
+    F[0] = f0;
+    F[N] = f1;
+    F[2 * N] = f2;
+    F[3 * N] = f3;
+    F[4 * N] = f4;
+  }
+  if (dissip_on) {
+    const long long pl = (long long)b.Pi * b.Pj;
+    // i: abs(p(i-1) +2p(i) +p(i+1)), dflux.f90:71-76
+    {
+      T pm = b.p[c - 1], pp = b.p[c + 1], p2 = T(2) * p;
+      T pb = fabs(pm + p2 + pp);
+      b.fp[c] = (pb > T(0)) ? fabs(pm - p2 + pp) / pb : T(0);
+    }
+    // j: abs(p(j+1) +2p(j) +p(j-1)), dflux.f90:131-136
+    {
+      T pm = b.p[c - b.Pi], pp = b.p[c + b.Pi], p2 = T(2) * p;
+      T pb = fabs(pp + p2 + pm);
+      b.fp[N + c] = (pb > T(0)) ? fabs(pp - p2 + pm) / pb : T(0);
+    }
+    // k: abs(p(k-1) +2p(k) +p(k+1)), dflux.f90:188-193
+    {
+      T pm = b.p[c - pl], pp = b.p[c + pl], p2 = T(2) * p;
+      T pb = fabs(pm + p2 + pp);
+      b.fp[2 * N + c] = (pb > T(0)) ? fabs(pm - p2 + pp) / pb : T(0);
+    }
+  }
+}
+
+// dflux_matrix, dflux.f90:283-339, with general face vector ss
+template <typename T>
+__device__ void dflux_matrix(T gamma, const T* u1, const T* u2, const T* dw, const T* ss, T* ff) {
+  T gam1 = gamma - T(1), epsn = T(1), epsl = T(1);
+  T rr = T(0.5) * (u1[0] + u2[0]);
+  T us[3];
+  for (int q = 0; q < 3; q++) us[q] = T(0.5) * (u1[q + 1] + u2[q + 1]) / rr;
+  T ee = T(0.5) * (u1[4] + u2[4]) / rr;
+  T qq = T(0.5) * (us[0] * us[0] + us[1] * us[1] + us[2] * us[2]);
+  T c2 = gamma * gam1 * (ee - qq);
+  T hh = c2 / gam1 + qq;
+  T sss = ss[0] * ss[0] + ss[1] * ss[1] + ss[2] * ss[2];
+  T cs = sqrt(c2 * sss);
+  T qn = ss[0] * us[0] + ss[1] * us[1] + ss[2] * us[2];
+  T e0 = fabs(qn) + cs;
+  T e1 = fmaxT(epsn * e0, (T)fabs(qn + cs));
+  T e2 = fmaxT(epsn * e0, (T)fabs(qn - cs));
+  T e3 = fmaxT(epsl * e0, (T)fabs(qn));
+  T s1 = T(0.5) * (e1 + e2), s2 = T(0.5) * (e1 - e2), s3 = e3;
+  T ak1 = (s1 - s3) / c2 * gam1;
+  T ak2 = s2 / cs;
+  T ak3 = c2 / gam1 / sss;
+  T d0 = dw[0], d1 = dw[1], d2 = dw[2], d3 = dw[3], d4 = dw[4];
+  T vd = qq * d0 - us[0] * d1 - us[1] * d2 - us[2] * d3 + d4;
+  T qd = qn * d0 - ss[0] * d1 - ss[1] * d2 - ss[2] * d3;
+  ff[0] = ak1 * vd - ak2 * qd + s3 * d0;
+  ff[1] = ak1 * (us[0] * vd - ss[0] * ak3 * qd) + ak2 * (gam1 * ss[0] * vd - us[0] * qd) + s3 * d1;
+  ff[2] = ak1 * (us[1] * vd - ss[1] * ak3 * qd) + ak2 * (gam1 * ss[1] * vd - us[1] * qd) + s3 * d2;
+  ff[3] = ak1 * (us[2] * vd - ss[2] * ak3 * qd) + ak2 * (gam1 * ss[2] * vd - us[2] * qd) + s3 * d3;
+  ff[4] = ak1 * (hh * vd - qn * ak3 * qd) + ak2 * (gam1 * qn * vd - hh * qd) + s3 * d4;
+}
+
+// --------------------------------------------------------------- stage: per-face pass
+// Thread (i,j,k) in [2..ie]x[2..je]x[2..ke] owns the lower face of cell
+// (i,j,k) in each direction whose tangential indices are physical.
+template <typename T, int D>
+__device__ __forceinline__ void face_dir(const DevBlock<T>& b, const PhysParams& P, int dissip_on, T cd, int i, int j,
+                                         int k) {
+  const long long N = b.N;
+  const long long st = D == 0 ? 1 : (D == 1 ? (long long)b.Pi : (long long)b.Pi * b.Pj);
+  const long long c = cidx(b.Pi, b.Pj, i, j, k);
+  const int q = D == 0 ? i : (D == 1 ? j : k);      // face between q-1 and q
+  const int lq = D == 0 ? b.il : (D == 1 ? b.jl : b.kl);
+  const int eq = lq + 1, bq = lq + 2;
+  // convective: efs(q) = 0.5*(F(q) + F(q-1))
+  const T* F = b.F + (long long)(D * 5) * N;
+  T* E = b.efs + (long long)(D * 5) * N;
+#pragma unroll
+  for (int v = 0; v < 5; v++) E[v * N + c] = T(0.5) * (F[v * N + c] + F[v * N + c - st]);
+  if (!dissip_on) return;
+  // dissipation face q (dflux.f90:87-111)
+  const T* fpd = b.fp + (long long)D * N;
+  T f_m2 = (q - 2 == 0) ? T(0) : fpd[c - 2 * st];
+  T f_m1 = fpd[c - st];
+  T f_0 = fpd[c];
+  T f_p1 = (q + 1 == bq) ? T(0) : fpd[c + st];
+  T ep = fmaxT(fmaxT(fmaxT(f_m2, f_m1), f_0), f_p1);
+  // lambda at ghost cells equals the adjacent physical cell (timestep.f90:227-282)
+  long long cm = (q - 1 < 2) ? c : c - st;
+  long long cp = (q > lq) ? c - st : c;
+  T lam = T(0.5) * (b.lam[cm] + b.lam[cp]);
+  T dis2 = (T)P.vis2 * ep;
+  T dis4 = (T)P.vis4;
+  dis4 = fdimT(dis4, dis2);
+  dis2 = dis2 * cd;
+  dis4 = dis4 * cd;
+  // diw(q) = w(q)-w(q-1); diw(1) = diw(2); diw(ib) = diw(ie)
+  T wq[4][5];  // w at q-2, q-1, q, q+1 (enthalpy in slot 4)
+  const int lo = (q - 2 >= 0) ? 0 : 1;
+  const int hi = (q + 1 <= bq) ? 3 : 2;
+#pragma unroll
+  for (int a = 0; a < 4; a++) {
+    if (a < lo || a > hi) continue;
+    long long ca = c + (a - 2) * st;
+#pragma unroll
+    for (int v = 0; v < 4; v++) wq[a][v] = b.w[v * N + ca];
+    wq[a][4] = b.H[ca];
+  }
+  T out[5];
+#pragma unroll
+  for (int v = 0; v < 5; v++) {
+    T d0 = wq[2][v] - wq[1][v];
+    T dm = (q - 1 == 1) ? d0 : wq[1][v] - wq[0][v];
+    T dp = (q + 1 == bq) ? d0 : wq[3][v] - wq[2][v];
+    T t3 = dp - T(2) * d0 + dm;
+    out[v] = dis2 * d0 - dis4 * t3;
+  }
+  if (!P.matrix) {
+#pragma unroll
+    for (int v = 0; v < 5; v++) out[v] = out[v] * lam;
+  } else {
+    T ss[3] = {T(0), T(0), T(0)};
+    ss[D] = (T)b.s[D];
+    T ff[5];
+    dflux_matrix((T)P.gamma, wq[1], wq[2], out, ss, ff);
+#pragma unroll
+    for (int v = 0; v < 5; v++) out[v] = ff[v];
+  }
+  T* Df = b.dfs + (long long)(D * 5) * N;
+#pragma unroll
+  for (int v = 0; v < 5; v++) Df[v * N + c] = out[v];
+  (void)eq;
+}
+
+template <typename T>
+__global__ void k_face(DevBlock<T> b, PhysParams P, int dissip_on, T cd) {
+  const int ex = b.ie - 1, ey = b.je - 1;  // 2..ie
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long tot = (long long)(b.ie - 1) * (b.je - 1) * (b.ke - 1);
+  if (t >= tot) return;
+  int i = 2 + (int)(t % ex);
+  int j = 2 + (int)((t / ex) % ey);
+  int k = 2 + (int)(t / ((long long)ex * ey));
+  bool jp = j <= b.jl, kp = k <= b.kl, ip = i <= b.il;
+  if (jp && kp) face_dir<T, 0>(b, P, dissip_on, cd, i, j, k);
+  if (ip && kp) face_dir<T, 1>(b, P, dissip_on, cd, i, j, k);
+  if (ip && jp) face_dir<T, 2>(b, P, dissip_on, cd, i, j, k);
+}
+
+// --------------------------------------------------------------- stage: cut-cell record terms
+// rec_term layout per record (40 values): [0,5) efluxb subtrahend,
+// [5,10) first addend, [10,15) second addend, [15,20) X0, [20,25) Z0,
+// [25,30) X1, [30,35) Z1 (dfluxb: fw(t) = fw(t) - X; fw(t) = fw(t) + Z).
+template <typename T>
+__device__ __forceinline__ void ceflux_axis(int D, const T* w, T p, T s, T* f) {
+  T f0 = w[1 + D] * s;
+  T y = T(1) / w[0];
+  f[0] = f0;
+  f[1] = mdiv(f0 * w[1], w[0], y);
+  f[2] = mdiv(f0 * w[2], w[0], y);
+  f[3] = mdiv(f0 * w[3], w[0], y);
+  f[1 + D] = f[1 + D] + p * s;
+  f[4] = mdiv(f0 * (w[4] + p), w[0], y);
+}
+
+template <typename T>
+__global__ void k_rec(DevBlock<T> b, PhysParams P, int dissip_on, T cd, unsigned* err) {
+  int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= b.nmir) return;
+  const long long N = b.N;
+  const int* ri = b.rec_i + 8 * m;
+  int i = ri[0], j = ri[1], k = ri[2], id = ri[3], zz = ri[4];
+  int D = zz - 1;
+  const long long st = D == 0 ? 1 : (D == 1 ? (long long)b.Pi : (long long)b.Pi * b.Pj);
+  const long long c = cidx(b.Pi, b.Pj, i, j, k);
+  T* R = b.rec_term + 40LL * m;
+  T s = (T)b.s[D];
+  T wc[5];
+  for (int v = 0; v < 5; v++) wc[v] = b.w[v * N + c];
+  if (fabs(wc[0]) < T(1.0e-8)) atomicOr(err, ERR_ZERORHO);
+  T psol = b.rec_psol[m];
+  T wsol[5];
+  for (int v = 0; v < 5; v++) wsol[v] = b.rec_wsol[5 * m + v];
+  // efluxb.f90:66-110
+  T f1[5], f2[5], f3[5];
+  ceflux_axis<T>(D, wc, b.p[c], s, f1);
+  ceflux_axis<T>(D, wsol, psol, s, f2);
+  const T* E = b.efs + (long long)(D * 5) * N;
+  const bool plus = (id >= 4);  // solid on the + side
+  long long cn = plus ? c - st : c + st;
+  T wnb[5];
+  for (int v = 0; v < 5; v++) wnb[v] = b.w[v * N + cn];
+  ceflux_axis<T>(D, wnb, b.p[cn], s, f3);
+  for (int v = 0; v < 5; v++) {
+    T fs = T(0.5) * (f1[v] + f2[v]);
+    T fa = T(0.5) * (f1[v] + f3[v]);
+    R[v] = E[v * N + c] - E[v * N + c + st];
+    R[5 + v] = plus ? fa : fs;
+    R[10 + v] = plus ? fs : fa;
+  }
+  if (!dissip_on) return;
+  // dfluxb.f90:29-423; w(:,5) is the enthalpy here
+  wsol[4] = wsol[4] + psol;
+  const T* Dd = b.dfs + (long long)(D * 5) * N;
+  auto pp = [&](int a) -> T { return b.p[c + a * st]; };
+  auto ww = [&](int a, int v) -> T { return v < 4 ? b.w[v * N + c + a * st] : b.H[c + a * st]; };
+  auto dd = [&](int a, int v) -> T { return Dd[v * N + c + a * st]; };
+  auto lamc = [&](int a) -> T {
+    // lambda with the ghost-copy rule of timestep.f90:227-282 along the record axis
+    int q = (D == 0 ? i : (D == 1 ? j : k)) + a;
+    int lq = D == 0 ? b.il : (D == 1 ? b.jl : b.kl);
+    int qq = q < 2 ? 2 : (q > lq ? lq : q);
+    return b.lam[c + (long long)(qq - (q - a)) * st];
+  };
+  const int pos = D == 0 ? i : (D == 1 ? j : k);
+  const int lim = D == 0 ? b.ib : (D == 1 ? b.jb : b.kb);
+  T fp[3], ep, lam, dis2, dis4;
+  T fs1[5], fs2[5], diw[3][5];
+  T ssv[3] = {T(0), T(0), T(0)};
+  ssv[D] = s;
+  auto setdis = [&]() {
+    dis2 = (T)P.vis2 * ep;
+    dis4 = (T)P.vis4;
+    dis4 = fdimT(dis4, dis2);
+    dis2 = dis2 * cd;
+    dis4 = dis4 * cd;
+  };
+  if (plus) {
+    for (int v = 0; v < 5; v++) {
+      R[15 + v] = dd(0, v) - dd(1, v);
+      R[25 + v] = dd(-1, v) - dd(0, v);
+    }
+    if (D == 0) {
+      fp[0] = fabs(pp(-2) - T(2) * pp(-1) + pp(0)) / fabs(pp(-2) + T(2) * pp(-1) + pp(0));
+      fp[1] = fabs(pp(-1) - T(2) * pp(0) + psol) / fabs(pp(-1) + T(2) * pp(0) + psol);
+    } else {
+      fp[0] = fabs(pp(0) - T(2) * pp(-1) + pp(-2)) / fabs(pp(0) + T(2) * pp(-1) + pp(-2));
+      fp[1] = fabs(psol - T(2) * pp(0) + pp(-1)) / fabs(psol + T(2) * pp(0) + pp(-1));
+    }
+    ep = fmaxT(fp[0], fp[1]);
+    lam = lamc(0);
+    setdis();
+    for (int v = 0; v < 5; v++) {
+      diw[0][v] = ww(0, v) - ww(-1, v);
+      diw[1][v] = wsol[v] - ww(0, v);
+      diw[2][v] = diw[1][v];
+      fs2[v] = diw[2][v] - T(2) * diw[1][v] + diw[0][v];
+      fs2[v] = dis2 * diw[1][v] - dis4 * fs2[v];
+    }
+    if (!P.matrix) {
+      for (int v = 0; v < 5; v++) fs2[v] = fs2[v] * lam;
+    } else {
+      T wcv[5], tmp[5];
+      for (int v = 0; v < 5; v++) wcv[v] = ww(0, v);
+      dflux_matrix((T)P.gamma, wcv, wsol, fs2, ssv, tmp);
+      for (int v = 0; v < 5; v++) fs2[v] = tmp[v];
+    }
+    if (pos - 3 >= 0)
+      fp[2] = fabs(pp(-1) - T(2) * pp(-2) + pp(-3)) / fabs(pp(-1) + T(2) * pp(-2) + pp(-3));
+    else
+      fp[2] = T(0);
+    ep = fmaxT(fmaxT(fp[0], fp[1]), fp[2]);
+    lam = T(0.5) * (lamc(-1) + lamc(0));
+    setdis();
+    for (int v = 0; v < 5; v++) {
+      diw[0][v] = ww(-1, v) - ww(-2, v);
+      diw[1][v] = ww(0, v) - ww(-1, v);
+      diw[2][v] = wsol[v] - ww(0, v);
+      fs1[v] = diw[2][v] - T(2) * diw[1][v] + diw[0][v];
+      fs1[v] = dis2 * diw[1][v] - dis4 * fs1[v];
+    }
+    if (!P.matrix) {
+      for (int v = 0; v < 5; v++) fs1[v] = fs1[v] * lam;
+    } else {
+      T wa[5], wcv[5], tmp[5];
+      for (int v = 0; v < 5; v++) {
+        wa[v] = ww(-1, v);
+        wcv[v] = ww(0, v);
+      }
+      dflux_matrix((T)P.gamma, wa, wcv, fs1, ssv, tmp);
+      for (int v = 0; v < 5; v++) fs1[v] = tmp[v];
+    }
+    for (int v = 0; v < 5; v++) {
+      R[20 + v] = fs1[v] - fs2[v];
+      R[30 + v] = dd(-1, v) - fs1[v];
+    }
+  } else {
+    for (int v = 0; v < 5; v++) {
+      R[15 + v] = dd(0, v) - dd(1, v);
+      R[25 + v] = dd(1, v) - dd(2, v);
+    }
+    fp[0] = fabs(pp(1) - T(2) * pp(0) + psol) / fabs(pp(1) + T(2) * pp(0) + psol);
+    fp[1] = fabs(pp(2) - T(2) * pp(1) + pp(0)) / fabs(pp(2) + T(2) * pp(1) + pp(0));
+    if (pos + 3 <= lim)
+      fp[2] = fabs(pp(3) - T(2) * pp(2) + pp(1)) / fabs(pp(3) + T(2) * pp(2) + pp(1));
+    else
+      fp[2] = T(0);
+    ep = fmaxT(fmaxT(fp[0], fp[1]), fp[2]);
+    lam = T(0.5) * (lamc(0) + lamc(1));
+    setdis();
+    for (int v = 0; v < 5; v++) {
+      diw[0][v] = ww(0, v) - wsol[v];
+      diw[1][v] = ww(1, v) - ww(0, v);
+      diw[2][v] = ww(2, v) - ww(1, v);
+      fs2[v] = diw[2][v] - T(2) * diw[1][v] + diw[0][v];
+      fs2[v] = dis2 * diw[1][v] - dis4 * fs2[v];
+    }
+    if (!P.matrix) {
+      for (int v = 0; v < 5; v++) fs2[v] = fs2[v] * lam;
+    } else {
+      T wcv[5], wbv[5], tmp[5];
+      for (int v = 0; v < 5; v++) {
+        wcv[v] = ww(0, v);
+        wbv[v] = ww(1, v);
+      }
+      dflux_matrix((T)P.gamma, wcv, wbv, fs2, ssv, tmp);
+      for (int v = 0; v < 5; v++) fs2[v] = tmp[v];
+    }
+    ep = fmaxT(fp[0], fp[1]);
+    lam = lamc(0);
+    setdis();
+    for (int v = 0; v < 5; v++) {
+      diw[1][v] = ww(0, v) - wsol[v];
+      diw[0][v] = diw[1][v];
+      diw[2][v] = ww(1, v) - ww(0, v);
+      fs1[v] = diw[2][v] - T(2) * diw[1][v] + diw[0][v];
+      fs1[v] = dis2 * diw[1][v] - dis4 * fs1[v];
+    }
+    if (!P.matrix) {
+      for (int v = 0; v < 5; v++) fs1[v] = fs1[v] * lam;
+    } else {
+      T wcv[5], tmp[5];
+      for (int v = 0; v < 5; v++) wcv[v] = ww(0, v);
+      dflux_matrix((T)P.gamma, wsol, wcv, fs1, ssv, tmp);
+      for (int v = 0; v < 5; v++) fs1[v] = tmp[v];
+    }
+    for (int v = 0; v < 5; v++) {
+      R[20 + v] = fs1[v] - fs2[v];
+      R[30 + v] = fs2[v] - dd(2, v);
+    }
+  }
+}
+
+// --------------------------------------------------------------- stage: combine + update
+template <typename T>
+__global__ void k_combine(DevBlock<T> b, PhysParams P, StageArgs A) {
+  const int nxl = b.nx, nyl = b.ny;
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long tot = (long long)b.nx * b.ny * b.nz;
+  if (t >= tot) return;
+  int i = 2 + (int)(t % nxl);
+  int j = 2 + (int)((t / nxl) % nyl);
+  int k = 2 + (int)(t / ((long long)nxl * nyl));
+  const long long N = b.N;
+  const long long c = cidx(b.Pi, b.Pj, i, j, k);
+  const long long sj = b.Pi, sk = (long long)b.Pi * b.Pj;
+  const int tg = b.cutmap[c];
+  T dwv[5], fwv[5];
+  const T* Ex = b.efs;
+  const T* Ey = b.efs + 5 * N;
+  const T* Ez = b.efs + 10 * N;
+#pragma unroll
+  for (int v = 0; v < 5; v++) {
+    T a = Ex[v * N + c] - Ex[v * N + c + 1];
+    a = a + Ey[v * N + c] - Ey[v * N + c + sj];
+    a = a + Ez[v * N + c] - Ez[v * N + c + sk];
+    dwv[v] = a;
+  }
+  if (tg >= 0) {  // efluxb.f90:72-110, records of this cut cell in order
+    for (int o = b.tgt_off[tg]; o < b.tgt_off[tg + 1]; o++) {
+      int op = b.tgt_ops[o];
+      if (op & 1) continue;
+      const T* R = b.rec_term + 40LL * (op >> 1);
+#pragma unroll
+      for (int v = 0; v < 5; v++) {
+        dwv[v] = dwv[v] - R[v];
+        dwv[v] = dwv[v] + R[5 + v] - R[10 + v];
+      }
+    }
+  }
+  // fw: blending and dissipation (euler.f90:127-135, dflux.f90:116-238)
+  if (A.dissip_on) {
+    const T* Dx = b.dfs;
+    const T* Dy = b.dfs + 5 * N;
+    const T* Dz = b.dfs + 10 * N;
+    const T fac = T(1) - (T)A.cd;
+#pragma unroll
+    for (int v = 0; v < 5; v++) {
+      T a = A.scale_fw ? b.fw[v * N + c] * fac : T(0);
+      a = a + (Dx[v * N + c] - Dx[v * N + c + 1]);
+      a = a + (Dy[v * N + c] - Dy[v * N + c + sj]);
+      a = a + (Dz[v * N + c] - Dz[v * N + c + sk]);
+      fwv[v] = a;
+    }
+    if (tg >= 0) {  // dfluxb, in record order
+      for (int o = b.tgt_off[tg]; o < b.tgt_off[tg + 1]; o++) {
+        int op = b.tgt_ops[o];
+        const T* R = b.rec_term + 40LL * (op >> 1) + ((op & 1) ? 25 : 15);
+#pragma unroll
+        for (int v = 0; v < 5; v++) {
+          fwv[v] = fwv[v] - R[v];
+          fwv[v] = fwv[v] + R[5 + v];
+        }
+      }
+    }
+#pragma unroll
+    for (int v = 0; v < 5; v++) b.fw[v * N + c] = fwv[v];
+  } else {
+    const T fac = T(1) - (T)A.cd;
+#pragma unroll
+    for (int v = 0; v < 5; v++) {
+      fwv[v] = A.scale_fw ? b.fw[v * N + c] * fac : T(0);
+      if (A.scale_fw) b.fw[v * N + c] = fwv[v];
+    }
+  }
+#pragma unroll
+  for (int v = 0; v < 5; v++) dwv[v] = dwv[v] + fwv[v];
+  if (A.forcing) {  // euler.f90:294-318
+#pragma unroll
+    for (int v = 0; v < 5; v++) {
+      T q;
+      if (A.first_forcing) {
+        q = T(0);
+        if (b.marker[c] == 1) q = T(1) * b.wr[v * N + c] - dwv[v];
+        b.qf[v * N + c] = q;
+      } else {
+        q = b.qf[v * N + c];
+      }
+      dwv[v] = dwv[v] + q;
+    }
+  }
+  const T bl = (T)b.blank[c];
+#pragma unroll
+  for (int v = 0; v < 5; v++) dwv[v] = dwv[v] * bl;
+  if (A.lres) {
+#pragma unroll
+    for (int v = 0; v < 5; v++) b.dw[v * N + c] = dwv[v];
+    return;
+  }
+  // time-step scaling, euler.f90:364-372: de = fn*vdtim/cellvolume
+  T vd = A.vt ? (T)(*b.dtim) : b.vdtim[c];
+  T de = mdiv((T)A.fn * vd, (T)b.vol, (T)b.rvol);
+#pragma unroll
+  for (int v = 0; v < 5; v++) dwv[v] = de * dwv[v];
+  if (A.irs) {
+#pragma unroll
+    for (int v = 0; v < 5; v++) b.dw[v * N + c] = dwv[v];
+    return;
+  }
+  // update, euler.f90:381-399 (steady: lam = 1)
+  T wv[5];
+#pragma unroll
+  for (int v = 0; v < 5; v++) {
+    wv[v] = b.wn[v * N + c] - dwv[v];
+    b.w[v * N + c] = wv[v];
+    b.dw[v * N + c] = dwv[v];
+  }
+  b.p[c] = depvars((T)P.gamma, wv);
+}
+
+// --------------------------------------------------------------- implicit residual smoothing
+// psmoo_old (psmoo.f90:97-242): constant-coefficient Thomas sweeps along
+// i, then j, then k, skipping blanked cells.  One thread per line, the five
+// variables interleaved for FP64 latency hiding.  TC: arithmetic precision.
+template <typename T, typename TC>
+__global__ void k_irs_i(DevBlock<T> b, IrsTables tb, TC bb) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)b.ny * b.nz) return;
+  int j = 2 + (int)(t % b.ny), k = 2 + (int)(t / b.ny);
+  const long long N = b.N;
+  const long long c0 = cidx(b.Pi, b.Pj, 0, j, k);
+  const int il = b.il;
+  TC prev[5];
+  {
+    long long c = c0 + 2;
+    bool on = b.blank[c] != 0;
+    TC e1 = (TC)tb.e1[2];
+#pragma unroll
+    for (int v = 0; v < 5; v++) {
+      TC d = (TC)b.dw[v * N + c];
+      if (on) {
+        d = d / e1;
+        b.dw[v * N + c] = (T)d;
+      }
+      prev[v] = d;
+    }
+  }
+  for (int i = 3; i <= il; i++) {
+    long long c = c0 + i;
+    bool on = b.blank[c] != 0;
+    TC e1 = (TC)tb.e1[i], y = (TC)tb.e1r[i];
+#pragma unroll
+    for (int v = 0; v < 5; v++) {
+      TC d = (TC)b.dw[v * N + c];
+      if (on) {
+        d = mdiv(d - bb * prev[v], e1, y);
+        b.dw[v * N + c] = (T)d;
+      }
+      prev[v] = d;
+    }
+  }
+  // backward: ir = il-1 .. 2 ; prev holds dw(il)
+  for (int ir = il - 1; ir >= 2; ir--) {
+    long long c = c0 + ir;
+    bool on = b.blank[c] != 0;
+    TC e2 = (TC)tb.e2[ir];
+#pragma unroll
+    for (int v = 0; v < 5; v++) {
+      TC d = (TC)b.dw[v * N + c];
+      if (on) {
+        d = d - e2 * prev[v];
+        b.dw[v * N + c] = (T)d;
+      }
+      prev[v] = d;
+    }
+  }
+}
+
+template <typename T, typename TC>
+__global__ void k_irs_j(DevBlock<T> b, IrsTables tb, TC bb) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)b.nx * b.nz) return;
+  int i = 2 + (int)(t % b.nx), k = 2 + (int)(t / b.nx);
+  const long long N = b.N;
+  const long long sj = b.Pi;
+  const long long c0 = cidx(b.Pi, b.Pj, i, 0, k);
+  const int jl = b.jl;
+  TC prev[5];
+  {
+    long long c = c0 + 2 * sj;
+    bool on = b.blank[c] != 0;
+    TC e1 = (TC)tb.e1[2];
+#pragma unroll
+    for (int v = 0; v < 5; v++) {
+      TC d = (TC)b.dw[v * N + c];
+      if (on) {
+        d = d / e1;
+        b.dw[v * N + c] = (T)d;
+      }
+      prev[v] = d;
+    }
+  }
+  for (int j = 3; j <= jl; j++) {
+    long long c = c0 + j * sj;
+    bool on = b.blank[c] != 0;
+    TC e1 = (TC)tb.e1[j], y = (TC)tb.e1r[j];
+#pragma unroll
+    for (int v = 0; v < 5; v++) {
+      TC d = (TC)b.dw[v * N + c];
+      if (on) {
+        d = mdiv(d - bb * prev[v], e1, y);
+        b.dw[v * N + c] = (T)d;
+      }
+      prev[v] = d;
+    }
+  }
+  for (int jr = jl - 1; jr >= 2; jr--) {
+    long long c = c0 + jr * sj;
+    bool on = b.blank[c] != 0;
+    TC e2 = (TC)tb.e2[jr];
+#pragma unroll
+    for (int v = 0; v < 5; v++) {
+      TC d = (TC)b.dw[v * N + c];
+      if (on) {
+        d = d - e2 * prev[v];
+        b.dw[v * N + c] = (T)d;
+      }
+      prev[v] = d;
+    }
+  }
+}
+
+// k-lines, then the update w = wn - dw and depvars (euler.f90:381-399)
+template <typename T, typename TC>
+__global__ void k_irs_k_update(DevBlock<T> b, IrsTables tb, TC bb, PhysParams P) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)b.nx * b.ny) return;
+  int i = 2 + (int)(t % b.nx), j = 2 + (int)(t / b.nx);
+  const long long N = b.N;
+  const long long sk = (long long)b.Pi * b.Pj;
+  const long long c0 = cidx(b.Pi, b.Pj, i, j, 0);
+  const int kl = b.kl;
+  TC prev[5];
+  {
+    long long c = c0 + 2 * sk;
+    bool on = b.blank[c] != 0;
+    TC e1 = (TC)tb.e1[2];
+#pragma unroll
+    for (int v = 0; v < 5; v++) {
+      TC d = (TC)b.dw[v * N + c];
+      if (on) {
+        d = d / e1;
+        b.dw[v * N + c] = (T)d;
+      }
+      prev[v] = d;
+    }
+  }
+  for (int k = 3; k <= kl; k++) {
+    long long c = c0 + k * sk;
+    bool on = b.blank[c] != 0;
+    TC e1 = (TC)tb.e1[k], y = (TC)tb.e1r[k];
+#pragma unroll
+    for (int v = 0; v < 5; v++) {
+      TC d = (TC)b.dw[v * N + c];
+      if (on) {
+        d = mdiv(d - bb * prev[v], e1, y);
+        b.dw[v * N + c] = (T)d;
+      }
+      prev[v] = d;
+    }
+  }
+  const T gamma = (T)P.gamma;
+  auto update = [&](long long c, const TC* dv) {
+    T wv[5];
+#pragma unroll
+    for (int v = 0; v < 5; v++) {
+      wv[v] = b.wn[v * N + c] - (T)dv[v];
+      b.w[v * N + c] = wv[v];
+    }
+    b.p[c] = depvars(gamma, wv);
+  };
+  update(c0 + kl * sk, prev);
+  for (int kr = kl - 1; kr >= 2; kr--) {
+    long long c = c0 + kr * sk;
+    bool on = b.blank[c] != 0;
+    TC e2 = (TC)tb.e2[kr];
+#pragma unroll
+    for (int v = 0; v < 5; v++) {
+      TC d = (TC)b.dw[v * N + c];
+      if (on) {
+        d = d - e2 * prev[v];
+        b.dw[v * N + c] = (T)d;
+      }
+      prev[v] = d;
+    }
+    update(c, prev);
+  }
+}
+
+// --------------------------------------------------------------- bc_cutcell (bc_cutcell.f90:40-268)
+template <typename T>
+__global__ void k_cutcell(DevBlock<T> b, PhysParams P, unsigned* err) {
+  int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= b.nmir || m > b.m0) return;
+  T* ws = b.rec_wsol + 5LL * m;
+  if (m == b.m0) {  // empty cloud: zero this record; the reference returns here
+    for (int v = 0; v < 5; v++) ws[v] = T(0);
+    b.rec_psol[m] = T(0);
+    return;
+  }
+  const long long N = b.N;
+  const int ncl = b.rec_i[8 * m + 5];
+  T nv[3] = {(T)b.rec_nvec[3 * m], (T)b.rec_nvec[3 * m + 1], (T)b.rec_nvec[3 * m + 2]};
+  T qb[3] = {(T)b.rec_qb[3 * m], (T)b.rec_qb[3 * m + 1], (T)b.rec_qb[3 * m + 2]};
+  T nn = sqrt(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2]);
+  for (int q = 0; q < 3; q++) nv[q] = nv[q] / nn;
+  long long cl[8];
+  T cf[8];
+  for (int q = 0; q < ncl; q++) {
+    const int* ijk = b.rec_cloud + (8 * m + q) * 3;
+    cl[q] = cidx(b.Pi, b.Pj, ijk[0], ijk[1], ijk[2]);
+    cf[q] = (T)b.rec_coef[8 * m + q];
+  }
+  T vr[5];
+  for (int v = 0; v < 5; v++) {
+    T a = T(0);
+    for (int q = 0; q < ncl; q++) a = a + cf[q] * b.w[v * N + cl[q]];
+    vr[v] = a;
+  }
+  T pr = T(0);
+  for (int q = 0; q < ncl; q++) pr = pr + cf[q] * b.p[cl[q]];
+  T wsol[5], psol = pr;
+  const T gm1 = (T)P.gamma - T(1);
+  if (!P.eqn_ns) {
+    for (int v = 0; v < 5; v++) wsol[v] = vr[v];
+    T qn = T(2) * (nv[0] * (wsol[1] - wsol[0] * qb[0]) + nv[1] * (wsol[2] - wsol[0] * qb[1]) +
+                   nv[2] * (wsol[3] - wsol[0] * qb[2]));
+    for (int q = 0; q < 3; q++) wsol[1 + q] = wsol[1 + q] - qn * nv[q];
+  } else {
+    wsol[0] = vr[0];
+    for (int q = 0; q < 3; q++) wsol[1 + q] = T(2) * qb[q] * vr[0] - vr[1 + q];
+  }
+  wsol[4] = psol / gm1 + T(0.5) * (wsol[1] * wsol[1] + wsol[2] * wsol[2] + wsol[3] * wsol[3]) / wsol[0];
+  bool nan = false;
+  for (int v = 0; v < 5; v++) nan |= (wsol[v] != wsol[v]);
+  if (nan && !P.eqn_ns) atomicOr(err, ERR_NAN);
+  for (int v = 0; v < 5; v++) ws[v] = wsol[v];
+  b.rec_psol[m] = psol;
+}
+
+// --------------------------------------------------------------- face boundary conditions
+// One launch per face in the order 1..6 of bcond.f90:16-39: later faces read
+// and overwrite ghost cells that earlier faces wrote.
+template <typename T>
+__global__ void k_bc_face(DevBlock<T> b, PhysParams P, int face) {
+  const int ax = (face - 1) % 3;
+  const int na = (ax == 0 ? b.jb : b.ib) + 1;  // first tangential extent
+  const int nbt = (ax == 2 ? b.jb : b.kb) + 1;
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)na * nbt) return;
+  int t1 = (int)(t % na), t2 = (int)(t / na);
+  const int kind = b.bctype[face - 1];
+  const int lcur = ax == 0 ? b.il : (ax == 1 ? b.jl : b.kl);
+  auto at = [&](int q) -> long long {
+    if (ax == 0) return cidx(b.Pi, b.Pj, q, t1, t2);
+    if (ax == 1) return cidx(b.Pi, b.Pj, t1, q, t2);
+    return cidx(b.Pi, b.Pj, t1, t2, q);
+  };
+  const long long N = b.N;
+  int phy1, phy2, dum1, dum2;
+  if (kind == -60) {
+    if (face <= 3) {
+      dum1 = 1; dum2 = 0; phy1 = lcur; phy2 = lcur - 1;
+    } else {
+      phy1 = 2; phy2 = 3; dum1 = lcur + 1; dum2 = lcur + 2;
+    }
+  } else {
+    if (face <= 3) {
+      phy1 = 2; phy2 = 3; dum1 = 1; dum2 = 0;
+    } else {
+      phy1 = lcur; phy2 = lcur - 1; dum1 = lcur + 1; dum2 = lcur + 2;
+    }
+  }
+  const long long d1 = at(dum1), d2 = at(dum2), p1 = at(phy1), p2 = at(phy2);
+  if (kind == -20) {  // bc_far.f90:42-284
+    const T gamma = (T)P.gamma, gm = (T)P.gm;
+    const T fn0 = (T)b.fnv[face - 1][0], fn1 = (T)b.fnv[face - 1][1], fn2 = (T)b.fnv[face - 1][2];
+    const T fnn = (T)b.fnv[face - 1][ax];
+    T wp[5];
+    for (int v = 0; v < 5; v++) wp[v] = b.w[v * N + p1];
+    T pph = b.p[p1];
+    T vel_norm = (wp[1] * fn0 + wp[2] * fn1 + wp[3] * fn2) / wp[0];
+    T out[5], pout;
+    bool set = false;
+    const T u0a = (T)P.u0[ax];
+    if (vel_norm <= T(0)) {
+      T rhoe = wp[0];
+      T ue = wp[1 + ax] / rhoe;
+      T pe = pph;
+      T ce = sqrt(gamma * pe / rhoe);
+      T rpo = ue * fnn + T(2) * ce / (gamma - T(1));
+      T rmi = u0a * fnn - T(2) * (T)P.c0 / (gamma - T(1));
+      T vv[3] = {(T)P.u0[0], (T)P.u0[1], (T)P.u0[2]};
+      vv[ax] = T(0.5) * (rpo + rmi) * fnn;
+      T ci = T(0.25) * (gamma - T(1)) * (rpo - rmi);
+      T si = (T)P.si_far;
+      T cc = ci * ci / gamma;
+      T rhoi = pow(si * cc, gm);
+      T prei = rhoi * cc;
+      out[0] = rhoi;
+      out[1] = rhoi * vv[0];
+      out[2] = rhoi * vv[1];
+      out[3] = rhoi * vv[2];
+      out[4] = prei * gm + T(0.5) * rhoi * (vv[0] * vv[0] + vv[1] * vv[1] + vv[2] * vv[2]);
+      pout = prei;
+      set = true;
+    } else if (vel_norm > T(0)) {
+      T rhoi = wp[0];
+      T vv[3] = {wp[1] / rhoi, wp[2] / rhoi, wp[3] / rhoi};
+      T prei = pph;
+      T si = pow(rhoi, gamma) / prei;
+      T ci = sqrt(gamma * prei / rhoi);
+      T rpo = vv[ax] * fnn + T(2) * ci / (gamma - T(1));
+      T rmi = u0a * fnn - T(2) * (T)P.c0 / (gamma - T(1));
+      T ve[3] = {vv[0], vv[1], vv[2]};
+      ve[ax] = T(0.5) * (rpo + rmi) * fnn;
+      T ce = T(0.25) * (gamma - T(1)) * (rpo - rmi);
+      T cc = ce * ce / gamma;
+      T rhoe = pow(si * cc, gm);
+      T pe = rhoe * cc;
+      out[0] = rhoe;
+      out[1] = rhoe * ve[0];
+      out[2] = rhoe * ve[1];
+      out[3] = rhoe * ve[2];
+      out[4] = pe * gm + T(0.5) * rhoe * (ve[0] * ve[0] + ve[1] * ve[1] + ve[2] * ve[2]);
+      pout = pe;
+      set = true;
+    }
+    if (set) {
+      for (int v = 0; v < 5; v++) b.w[v * N + d1] = out[v];
+      b.p[d1] = pout;
+    }
+    for (int v = 0; v < 5; v++) b.w[v * N + d2] = b.w[v * N + d1];
+    b.p[d2] = b.p[d1];
+  } else if (kind == -50) {  // bc_symm.f90
+    for (int v = 0; v < 5; v++) b.w[v * N + d1] = b.w[v * N + p1];
+    b.w[(1 + ax) * N + d1] = -b.w[(1 + ax) * N + p1];
+    b.p[d1] = b.p[p1];
+    for (int v = 0; v < 5; v++) b.w[v * N + d2] = b.w[v * N + p2];
+    b.w[(1 + ax) * N + d2] = -b.w[(1 + ax) * N + p2];
+    b.p[d2] = b.p[p2];
+  } else if (kind == -80) {  // bc_wall.f90
+    b.w[d1] = b.w[p1];
+    b.w[4 * N + d1] = b.w[4 * N + p1];
+    for (int v = 1; v < 4; v++) b.w[v * N + d1] = -b.w[v * N + p1];
+    b.w[d2] = b.w[p2];
+    b.w[4 * N + d2] = b.w[4 * N + p2];
+    for (int v = 1; v < 4; v++) b.w[v * N + d2] = -b.w[v * N + p2];
+    b.p[d1] = b.p[p1];
+    b.p[d2] = b.p[p1];
+  } else if (kind == -60) {  // bc_periodic.f90
+    for (int v = 0; v < 5; v++) b.w[v * N + d2] = b.w[v * N + p2];
+    for (int v = 0; v < 5; v++) b.w[v * N + d1] = b.w[v * N + p1];
+    b.p[d2] = b.p[p2];
+    b.p[d1] = b.p[p1];
+  }
+}
+
+// bc_corner.f90:23-157 in one block: three dependent phases
+template <typename T>
+__global__ void k_bc_corner(DevBlock<T> b, PhysParams P) {
+  const long long N = b.N;
+  const int il = b.il, jl = b.jl, kl = b.kl, ie = b.ie, je = b.je, ke = b.ke;
+  const T gamma = (T)P.gamma;
+  auto C3 = [&](int i, int j, int k) { return cidx(b.Pi, b.Pj, i, j, k); };
+  auto set3 = [&](long long d, long long a, long long bb, long long cc) {
+    T wv[5];
+    for (int v = 0; v < 5; v++) {
+      wv[v] = b.w[v * N + a] + b.w[v * N + bb] - b.w[v * N + cc];
+      b.w[v * N + d] = wv[v];
+    }
+    b.p[d] = depvars(gamma, wv);
+  };
+  // phase A: edges along k (k = 2..kl) and along j (j = 2..jl)
+  for (int t = threadIdx.x; t < 4 * (kl - 1) + 4 * (jl - 1); t += blockDim.x) {
+    if (t < 4 * (kl - 1)) {
+      int k = 2 + t / 4, e = t % 4;
+      if (e == 0) set3(C3(1, 1, k), C3(2, 1, k), C3(1, 2, k), C3(2, 2, k));
+      else if (e == 1) set3(C3(ie, 1, k), C3(il, 1, k), C3(ie, 2, k), C3(il, 2, k));
+      else if (e == 2) set3(C3(1, je, k), C3(2, je, k), C3(1, jl, k), C3(2, jl, k));
+      else set3(C3(ie, je, k), C3(il, je, k), C3(ie, jl, k), C3(il, jl, k));
+    } else {
+      int u = t - 4 * (kl - 1);
+      int j = 2 + u / 4, e = u % 4;
+      if (e == 0) set3(C3(1, j, 1), C3(2, j, 1), C3(1, j, 2), C3(2, j, 2));
+      else if (e == 1) set3(C3(ie, j, 1), C3(il, j, 1), C3(ie, j, 2), C3(il, j, 2));
+      else if (e == 2) set3(C3(1, j, ke), C3(2, j, ke), C3(1, j, kl), C3(2, j, kl));
+      else set3(C3(ie, j, ke), C3(il, j, ke), C3(ie, j, kl), C3(il, j, kl));
+    }
+  }
+  __syncthreads();
+  // phase B: edges along i (i = 0..ib)
+  for (int t = threadIdx.x; t < 4 * (b.ib + 1); t += blockDim.x) {
+    int i = t / 4, e = t % 4;
+    if (e == 0) set3(C3(i, 1, 1), C3(i, 1, 2), C3(i, 2, 1), C3(i, 2, 2));
+    else if (e == 1) set3(C3(i, 1, ke), C3(i, 2, ke), C3(i, 1, kl), C3(i, 2, kl));
+    else if (e == 2) set3(C3(i, je, 1), C3(i, je, 1), C3(i, jl, 2), C3(i, jl, 2));  // bc_corner.f90:120 as written
+    else set3(C3(i, je, ke), C3(i, jl, ke), C3(i, je, kl), C3(i, jl, kl));
+  }
+  __syncthreads();
+  // phase C: the 8 corners
+  if (threadIdx.x < 8) {
+    int e = threadIdx.x;
+    long long d, a, bq, cq, dq;
+    switch (e) {
+      case 0: d = C3(1, 1, 1); a = C3(2, 1, 1); bq = C3(1, 2, 1); cq = C3(1, 1, 2); dq = C3(2, 2, 2); break;
+      case 1: d = C3(1, 1, ke); a = C3(2, 1, ke); bq = C3(1, 2, ke); cq = C3(1, 1, kl); dq = C3(2, 2, kl); break;
+      case 2: d = C3(1, je, 1); a = C3(2, je, 1); bq = C3(1, jl, 1); cq = C3(1, je, 2); dq = C3(2, jl, 2); break;
+      case 3: d = C3(ie, 1, 1); a = C3(il, 1, 1); bq = C3(ie, 2, 1); cq = C3(ie, 1, 2); dq = C3(il, 2, 2); break;
+      case 4: d = C3(ie, 1, ke); a = C3(il, 1, ke); bq = C3(ie, 2, ke); cq = C3(ie, 1, kl); dq = C3(il, 2, kl); break;
+      case 5: d = C3(ie, je, 1); a = C3(il, je, 1); bq = C3(ie, jl, 1); cq = C3(ie, je, 2); dq = C3(il, jl, 2); break;
+      case 6: d = C3(1, je, ke); a = C3(2, je, ke); bq = C3(1, jl, ke); cq = C3(1, je, kl); dq = C3(2, jl, kl); break;
+      default: d = C3(ie, je, ke); a = C3(il, je, ke); bq = C3(ie, jl, ke); cq = C3(ie, je, kl); dq = C3(il, jl, kl); break;
+    }
+    T wv[5];
+    for (int v = 0; v < 5; v++)
+      wv[v] = (b.w[v * N + a] + b.w[v * N + bq] + b.w[v * N + cq]) * T(2) / T(3) - b.w[v * N + dq];
+    // all eight read only edge cells, so the writes can follow the reads
+    __syncwarp(0xffu);
+    for (int v = 0; v < 5; v++) b.w[v * N + d] = wv[v];
+    b.p[d] = depvars(gamma, wv);
+  }
+}
+
+// --------------------------------------------------------------- residual norm (euler.f90:431-447)
+// Deterministic: fixed partial ranges, fixed-order tree per block, one final block.
+constexpr int RT_THREADS = 256;
+int rtrms_partials(long long ncells) {
+  long long per = (long long)RT_THREADS * 8;
+  long long n = (ncells + per - 1) / per;
+  return (int)(n < 1 ? 1 : (n > 4096 ? 4096 : n));
+}
+
+template <typename T>
+__global__ void k_rtrms_partial(DevBlock<T> b, double cfl, int vt, double* partial, int npart) {
+  __shared__ double sh[RT_THREADS];
+  const long long tot = (long long)b.nx * b.ny * b.nz;
+  const long long per = (tot + npart - 1) / npart;
+  const long long lo = (long long)blockIdx.x * per, hi = min(tot, lo + per);
+  double acc = 0.0;
+  for (long long t = lo + threadIdx.x; t < hi; t += blockDim.x) {
+    int i = 2 + (int)(t % b.nx);
+    int j = 2 + (int)((t / b.nx) % b.ny);
+    int k = 2 + (int)(t / ((long long)b.nx * b.ny));
+    long long c = cidx(b.Pi, b.Pj, i, j, k);
+    double de = cfl * (double)(vt ? *b.dtim : b.vdtim[c]);
+    double rt = 0.0;
+    if (b.blank[c] != 0) rt = (double)b.dw[c] / de;
+    acc = acc + rt * rt;
+  }
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = RT_THREADS / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sh[threadIdx.x] = sh[threadIdx.x] + sh[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
+}
+
+__global__ void k_rtrms_final(const double* partial, int npart, double ncell, double* out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double a = 0.0;
+    for (int q = 0; q < npart; q++) a = a + partial[q];
+    *out = sqrt(a / ncell);
+  }
+}
+
+// --------------------------------------------------------------- small whole-array kernels
+template <typename T>
+__global__ void k_depvars_all(DevBlock<T> b, double gamma) {
+  long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= b.N) return;
+  T wv[5];
+  for (int v = 0; v < 5; v++) wv[v] = b.w[v * b.N + c];
+  b.p[c] = depvars((T)gamma, wv);
+}
+
+template <typename T>
+__global__ void k_copy5(const T* __restrict__ src, T* __restrict__ dst, long long n) {
+  long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < n) dst[c] = src[c];
+}
+
+// wn = w on physical cells, dw = fw = 0 everywhere (euler.f90:80-89)
+template <typename T>
+__global__ void k_save_wn(DevBlock<T> b) {
+  long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= b.N) return;
+  const long long N = b.N;
+  int i = (int)(c % b.Pi);
+  int j = (int)((c / b.Pi) % b.Pj);
+  int k = (int)(c / ((long long)b.Pi * b.Pj));
+  bool phys = i >= 2 && i <= b.il && j >= 2 && j <= b.jl && k >= 2 && k <= b.kl;
+  for (int v = 0; v < 5; v++) {
+    if (phys) b.wn[v * N + c] = b.w[v * N + c];
+    b.dw[v * N + c] = T(0);
+    b.fw[v * N + c] = T(0);
+  }
+}
+
+// wn = w on physical cells only (movco.f90:29-35)
+template <typename T>
+__global__ void k_copy_wn(DevBlock<T> b) {
+  long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= b.N) return;
+  int i = (int)(c % b.Pi);
+  int j = (int)((c / b.Pi) % b.Pj);
+  int k = (int)(c / ((long long)b.Pi * b.Pj));
+  if (!(i >= 2 && i <= b.il && j >= 2 && j <= b.jl && k >= 2 && k <= b.kl)) return;
+  for (int v = 0; v < 5; v++) b.wn[v * b.N + c] = b.w[v * b.N + c];
+}
+
+template <typename T>
+__global__ void k_init_free(DevBlock<T> b, PhysParams P) {
+  long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= b.N) return;
+  const long long N = b.N;
+  double rho0 = P.rho0;
+  b.w[c] = (T)rho0;
+  b.w[N + c] = (T)(rho0 * P.u0[0]);
+  b.w[2 * N + c] = (T)(rho0 * P.u0[1]);
+  b.w[3 * N + c] = (T)(rho0 * P.u0[2]);
+  b.w[4 * N + c] = (T)P.e0;  // rho0*h0 - p0, init_flow.f90:59
+}
+
+// --------------------------------------------------------------- multigrid transfers
+__device__ __forceinline__ void trilinear_factor(double x, double y, double z, double* fac) {
+  fac[0] = (1.0 - x) * (1.0 - y) * (1.0 - z);
+  fac[1] = x * (1.0 - y) * (1.0 - z);
+  fac[2] = (1.0 - x) * y * (1.0 - z);
+  fac[3] = x * y * (1.0 - z);
+  fac[4] = (1.0 - x) * (1.0 - y) * z;
+  fac[5] = x * (1.0 - y) * z;
+  fac[6] = (1.0 - x) * y * z;
+  fac[7] = x * y * z;
+}
+
+struct Xfer {
+  int r[3], o[3];
+};
+
+// collc.f90:58-158 for the coarse cells under one child
+template <typename TC, typename TF>
+__global__ void k_collc(DevBlock<TC> c, DevBlock<TF> f, Xfer X, uint8_t* marker) {
+  const int n0 = f.nx / X.r[0], n1 = f.ny / X.r[1], n2 = f.nz / X.r[2];
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)n0 * n1 * n2) return;
+  int ic[3] = {X.o[0] + 2 + (int)(t % n0), X.o[1] + 2 + (int)((t / n0) % n1), X.o[2] + 2 + (int)(t / ((long long)n0 * n1))};
+  if (ic[0] < 2 || ic[0] > c.il || ic[1] < 2 || ic[1] > c.jl || ic[2] < 2 || ic[2] > c.kl) return;
+  const int lf[3] = {f.il, f.jl, f.kl};
+  int sh[3];
+  double xi[3];
+  for (int d = 0; d < 3; d++) {
+    double tt = ((double)ic[d] - 1.5 - (double)X.o[d]) * (double)X.r[d];
+    int s = (int)floor(tt + 1.5);
+    if (s < 2) s = 2;
+    if (s > lf[d] - 1) s = lf[d] - 1;
+    sh[d] = s;
+    xi[d] = tt + 1.5 - (double)s;
+  }
+  double fac[8];
+  trilinear_factor(xi[0], xi[1], xi[2], fac);
+  const long long cc = cidx(c.Pi, c.Pj, ic[0], ic[1], ic[2]);
+  for (int v = 0; v < 5; v++) {
+    double acc = 0.0;
+    int nn = 0;
+    for (int dk = 0; dk < 2; dk++)
+      for (int dj = 0; dj < 2; dj++)
+        for (int di = 0; di < 2; di++) {
+          long long fq = cidx(f.Pi, f.Pj, sh[0] + di, sh[1] + dj, sh[2] + dk);
+          double val = (double)f.dw[v * f.N + fq] / f.vol;
+          acc = acc + val * fac[nn++];
+        }
+    c.wr[v * c.N + cc] = (TC)(acc * c.vol);
+    acc = 0.0;
+    nn = 0;
+    for (int dk = 0; dk < 2; dk++)
+      for (int dj = 0; dj < 2; dj++)
+        for (int di = 0; di < 2; di++) {
+          long long fq = cidx(f.Pi, f.Pj, sh[0] + di, sh[1] + dj, sh[2] + dk);
+          acc = acc + (double)f.w[v * f.N + fq] * fac[nn++];
+        }
+    c.w[v * c.N + cc] = (TC)acc;
+  }
+  marker[cc] = 1;
+}
+
+__device__ __forceinline__ bool fine_to_coarse(const Xfer& X, int ncp0, int ncp1, int ncp2, int lc0, int lc1, int lc2,
+                                               int i, int j, int k, int* sh, double* fac) {
+  int ic[3] = {i, j, k};
+  int nc[3] = {ncp0, ncp1, ncp2};
+  int lc[3] = {lc0, lc1, lc2};
+  double xi[3];
+  for (int d = 0; d < 3; d++) {
+    double u = (double)X.o[d] + ((double)ic[d] - 1.5) / (double)X.r[d];
+    if (u < 0.0 || u >= (double)nc[d]) return false;
+    int s = (int)floor(u + 1.5);
+    if (s < 2) s = 2;
+    if (s > lc[d] - 1) s = lc[d] - 1;
+    sh[d] = s;
+    xi[d] = u + 1.5 - (double)s;
+  }
+  trilinear_factor(xi[0], xi[1], xi[2], fac);
+  return true;
+}
+
+// addw.f90:83-188: w_f = store_w + I(w_c - ws_c), or I(w_c) in the FMG step
+template <typename TF, typename TC>
+__global__ void k_addw(DevBlock<TF> f, DevBlock<TC> c, Xfer X, int fmg) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)f.nx * f.ny * f.nz) return;
+  int i = 2 + (int)(t % f.nx), j = 2 + (int)((t / f.nx) % f.ny), k = 2 + (int)(t / ((long long)f.nx * f.ny));
+  int sh[3];
+  double fac[8];
+  if (!fine_to_coarse(X, c.nx, c.ny, c.nz, c.il, c.jl, c.kl, i, j, k, sh, fac)) return;
+  const long long q = cidx(f.Pi, f.Pj, i, j, k);
+  if (f.blank[q] == 0) return;
+  for (int v = 0; v < 5; v++) {
+    double acc = 0.0;
+    int nn = 0;
+    for (int dk = 0; dk < 2; dk++)
+      for (int dj = 0; dj < 2; dj++)
+        for (int di = 0; di < 2; di++) {
+          long long cq = cidx(c.Pi, c.Pj, sh[0] + di, sh[1] + dj, sh[2] + dk);
+          double val = (double)c.w[v * c.N + cq];
+          if (!fmg) val = val - (double)c.ws[v * c.N + cq];
+          acc = acc + val * fac[nn++];
+        }
+    if (fmg)
+      f.w[v * f.N + q] = (TF)acc;
+    else
+      f.w[v * f.N + q] = (TF)((double)f.w[v * f.N + q] + acc);
+  }
+}
+
+// bc_embed.f90:47-143: fine ghost cells whose centre lies in the parent
+template <typename TF, typename TC>
+__global__ void k_embed(DevBlock<TF> f, DevBlock<TC> c, Xfer X, double gamma) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= f.N) return;
+  int i = (int)(t % f.Pi), j = (int)((t / f.Pi) % f.Pj), k = (int)(t / ((long long)f.Pi * f.Pj));
+  if (i >= 2 && i <= f.il && j >= 2 && j <= f.jl && k >= 2 && k <= f.kl) return;
+  int sh[3];
+  double fac[8];
+  if (!fine_to_coarse(X, c.nx, c.ny, c.nz, c.il, c.jl, c.kl, i, j, k, sh, fac)) return;
+  const long long q = t;
+  TF wv[5];
+  for (int v = 0; v < 5; v++) wv[v] = f.w[v * f.N + q];
+  if (f.blank[q] != 0) {
+    for (int v = 0; v < 5; v++) {
+      double acc = 0.0;
+      int nn = 0;
+      for (int dk = 0; dk < 2; dk++)
+        for (int dj = 0; dj < 2; dj++)
+          for (int di = 0; di < 2; di++)
+            acc = acc + (double)c.w[v * c.N + cidx(c.Pi, c.Pj, sh[0] + di, sh[1] + dj, sh[2] + dk)] * fac[nn++];
+      wv[v] = (TF)acc;
+      f.w[v * f.N + q] = wv[v];
+    }
+  }
+  f.p[q] = depvars((TF)gamma, wv);
+}
+
+// wall forces from the records (new): 7 sums, fixed order within one block
+template <typename T>
+__global__ void k_forces(DevBlock<T> b, double ox, double oy, double oz, double hx, double hy, double hz, double cx,
+                         double cy, double cz, double* out) {
+  __shared__ double sh[7][256];
+  double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+  const double org[3] = {ox, oy, oz}, h[3] = {hx, hy, hz}, ctr[3] = {cx, cy, cz};
+  for (int m = threadIdx.x; m < b.nmir; m += blockDim.x) {
+    const int* ri = b.rec_i + 8 * m;
+    int ax = ri[4] - 1;
+    double sgn = ri[3] >= 4 ? 1.0 : -1.0;
+    long long c = cidx(b.Pi, b.Pj, ri[0], ri[1], ri[2]);
+    double area = b.rec_area[m];
+    double pw = 0.5 * ((double)b.p[c] + (double)b.rec_psol[m]);
+    double f[3] = {0, 0, 0};
+    f[ax] = pw * area * sgn;
+    double xf[3];
+    for (int d = 0; d < 3; d++) xf[d] = org[d] + ((double)ri[d] - 1.5) * h[d];
+    xf[ax] = xf[ax] + sgn * 0.5 * h[ax];
+    double r[3] = {xf[0] - ctr[0], xf[1] - ctr[1], xf[2] - ctr[2]};
+    acc[0] += f[0];
+    acc[1] += f[1];
+    acc[2] += f[2];
+    acc[3] += r[1] * f[2] - r[2] * f[1];
+    acc[4] += r[2] * f[0] - r[0] * f[2];
+    acc[5] += r[0] * f[1] - r[1] * f[0];
+  }
+  for (int q = 0; q < 6; q++) sh[q][threadIdx.x] = acc[q];
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if (threadIdx.x < s)
+      for (int q = 0; q < 6; q++) sh[q][threadIdx.x] += sh[q][threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x < 6) out[threadIdx.x] = sh[threadIdx.x][0];
+}
+
+// =============================================================== launchers
+constexpr int TPB = 256;
+
+template <typename T>
+void launch_timestep(const DevBlock<T>& b, const PhysParams& P, unsigned* err, cudaStream_t s) {
+  // dtim is accumulated as an FP64 bit pattern in the scalar slot of the double scratch
+  long long n = (long long)b.nx * b.ny * b.nz;
+  k_dtim_reset<<<1, 32, 0, s>>>(b.dtim);
+  k_timestep<T, T><<<nblk(n, TPB), TPB, 0, s>>>(b, P, err);
+}
+
+template <typename T>
+void launch_stage_part(int part, const DevBlock<T>& b, const PhysParams& P, const StageArgs& A, unsigned* err,
+                       cudaStream_t s) {
+  if (part == 0) {
+    long long n1 = (long long)b.ie * b.je * b.ke;
+    k_prep<T><<<nblk(n1, TPB), TPB, 0, s>>>(b, A.dissip_on);
+  } else if (part == 1) {
+    long long n2 = (long long)(b.ie - 1) * (b.je - 1) * (b.ke - 1);
+    k_face<T><<<nblk(n2, TPB), TPB, 0, s>>>(b, P, A.dissip_on, (T)A.cd);
+  } else if (part == 2) {
+    if (b.nmir > 0) k_rec<T><<<nblk(b.nmir, 128), 128, 0, s>>>(b, P, A.dissip_on, (T)A.cd, err);
+  } else {
+    long long n3 = (long long)b.nx * b.ny * b.nz;
+    k_combine<T><<<nblk(n3, TPB), TPB, 0, s>>>(b, P, A);
+  }
+}
+
+template <typename T>
+void launch_stage(const DevBlock<T>& b, const PhysParams& P, const StageArgs& A, unsigned* err, cudaStream_t s) {
+  for (int part = 0; part < 4; part++) launch_stage_part<T>(part, b, P, A, err, s);
+}
+
+template <typename T>
+void launch_irs_part(int part, const DevBlock<T>& b, const PhysParams& P, const IrsTables* tab, cudaStream_t s) {
+  const T bb = (T)(-P.smoo);
+  if (part == 0) k_irs_i<T, T><<<nblk((long long)b.ny * b.nz, 128), 128, 0, s>>>(b, tab[0], bb);
+  if (part == 1) k_irs_j<T, T><<<nblk((long long)b.nx * b.nz, 128), 128, 0, s>>>(b, tab[1], bb);
+  if (part == 2) k_irs_k_update<T, T><<<nblk((long long)b.nx * b.ny, 128), 128, 0, s>>>(b, tab[2], bb, P);
+}
+
+template <typename T>
+void launch_irs(const DevBlock<T>& b, const PhysParams& P, const IrsTables* tab, cudaStream_t s) {
+  for (int part = 0; part < 3; part++) launch_irs_part<T>(part, b, P, tab, s);
+}
+
+template <typename T>
+void launch_cutcell(const DevBlock<T>& b, const PhysParams& P, unsigned* err, cudaStream_t s) {
+  if (b.nmir > 0) k_cutcell<T><<<nblk(b.nmir, 128), 128, 0, s>>>(b, P, err);
+}
+
+template <typename T>
+void launch_bcond(const DevBlock<T>& b, const PhysParams& P, cudaStream_t s) {
+  for (int f = 1; f <= 6; f++) {
+    if (b.bctype[f - 1] == 0) continue;
+    int ax = (f - 1) % 3;
+    long long n = (long long)((ax == 0 ? b.jb : b.ib) + 1) * ((ax == 2 ? b.jb : b.kb) + 1);
+    k_bc_face<T><<<nblk(n, TPB), TPB, 0, s>>>(b, P, f);
+  }
+  k_bc_corner<T><<<1, 512, 0, s>>>(b, P);
+}
+
+template <typename T>
+void launch_rtrms(const DevBlock<T>& b, const PhysParams& P, int vt, double* partial, int npartial, double* out,
+                  cudaStream_t s) {
+  k_rtrms_partial<T><<<npartial, RT_THREADS, 0, s>>>(b, P.cfl, vt, partial, npartial);
+  k_rtrms_final<<<1, 32, 0, s>>>(partial, npartial, (double)b.nx * b.ny * b.nz, out);
+}
+
+template <typename T>
+void launch_depvars_all(const DevBlock<T>& b, const PhysParams& P, cudaStream_t s) {
+  k_depvars_all<T><<<nblk(b.N, TPB), TPB, 0, s>>>(b, P.gamma);
+}
+
+template <typename T>
+void launch_copy_ws(const DevBlock<T>& b, cudaStream_t s) {
+  k_copy5<T><<<nblk(5 * b.N, TPB), TPB, 0, s>>>(b.w, b.ws, 5 * b.N);
+}
+
+template <typename T>
+void launch_save_wn(const DevBlock<T>& b, cudaStream_t s) {
+  k_save_wn<T><<<nblk(b.N, TPB), TPB, 0, s>>>(b);
+}
+
+template <typename T>
+void launch_copy_wn(const DevBlock<T>& b, cudaStream_t s) {
+  k_copy_wn<T><<<nblk(b.N, TPB), TPB, 0, s>>>(b);
+}
+
+template <typename T>
+void launch_init_free(const DevBlock<T>& b, const PhysParams& P, cudaStream_t s) {
+  k_init_free<T><<<nblk(b.N, TPB), TPB, 0, s>>>(b, P);
+}
+
+template <typename TC, typename TF>
+void launch_collc(const DevBlock<TC>& c, const DevBlock<TF>& f, const int ratio[3], const int offset[3],
+                  uint8_t* marker_c, cudaStream_t s) {
+  Xfer X;
+  for (int d = 0; d < 3; d++) {
+    X.r[d] = ratio[d];
+    X.o[d] = offset[d];
+  }
+  long long n = (long long)(f.nx / ratio[0]) * (f.ny / ratio[1]) * (f.nz / ratio[2]);
+  k_collc<TC, TF><<<nblk(n, TPB), TPB, 0, s>>>(c, f, X, marker_c);
+}
+
+template <typename TF, typename TC>
+void launch_addw(const DevBlock<TF>& f, const DevBlock<TC>& c, const int ratio[3], const int offset[3], int fmg,
+                 cudaStream_t s) {
+  Xfer X;
+  for (int d = 0; d < 3; d++) {
+    X.r[d] = ratio[d];
+    X.o[d] = offset[d];
+  }
+  long long n = (long long)f.nx * f.ny * f.nz;
+  k_addw<TF, TC><<<nblk(n, TPB), TPB, 0, s>>>(f, c, X, fmg);
+}
+
+template <typename TF, typename TC>
+void launch_embed(const DevBlock<TF>& f, const DevBlock<TC>& c, const int ratio[3], const int offset[3],
+                  const PhysParams& P, cudaStream_t s) {
+  Xfer X;
+  for (int d = 0; d < 3; d++) {
+    X.r[d] = ratio[d];
+    X.o[d] = offset[d];
+  }
+  k_embed<TF, TC><<<nblk(f.N, TPB), TPB, 0, s>>>(f, c, X, P.gamma);
+}
+
+template <typename T>
+void launch_forces(const DevBlock<T>& b, const double* origin, const double* h, const double* center, double* out7,
+                   cudaStream_t s) {
+  k_forces<T><<<1, 256, 0, s>>>(b, origin[0], origin[1], origin[2], h[0], h[1], h[2], center[0], center[1], center[2],
+                                out7);
+}
+
+// explicit instantiations
+#define MGE_INST(T)                                                                                              \
+  template void launch_timestep<T>(const DevBlock<T>&, const PhysParams&, unsigned*, cudaStream_t);             \
+  template void launch_stage<T>(const DevBlock<T>&, const PhysParams&, const StageArgs&, unsigned*, cudaStream_t); \
+  template void launch_stage_part<T>(int, const DevBlock<T>&, const PhysParams&, const StageArgs&, unsigned*,       \
+                                     cudaStream_t);                                                             \
+  template void launch_irs_part<T>(int, const DevBlock<T>&, const PhysParams&, const IrsTables*, cudaStream_t);  \
+  template void launch_irs<T>(const DevBlock<T>&, const PhysParams&, const IrsTables*, cudaStream_t);           \
+  template void launch_cutcell<T>(const DevBlock<T>&, const PhysParams&, unsigned*, cudaStream_t);              \
+  template void launch_bcond<T>(const DevBlock<T>&, const PhysParams&, cudaStream_t);                           \
+  template void launch_rtrms<T>(const DevBlock<T>&, const PhysParams&, int, double*, int, double*, cudaStream_t); \
+  template void launch_depvars_all<T>(const DevBlock<T>&, const PhysParams&, cudaStream_t);                     \
+  template void launch_copy_ws<T>(const DevBlock<T>&, cudaStream_t);                                            \
+  template void launch_save_wn<T>(const DevBlock<T>&, cudaStream_t);                                            \
+  template void launch_copy_wn<T>(const DevBlock<T>&, cudaStream_t);                                            \
+  template void launch_init_free<T>(const DevBlock<T>&, const PhysParams&, cudaStream_t);                       \
+  template void launch_forces<T>(const DevBlock<T>&, const double*, const double*, const double*, double*, cudaStream_t);
+MGE_INST(double)
+#undef MGE_INST
+template void launch_collc<double, double>(const DevBlock<double>&, const DevBlock<double>&, const int*, const int*,
+                                           uint8_t*, cudaStream_t);
+template void launch_addw<double, double>(const DevBlock<double>&, const DevBlock<double>&, const int*, const int*, int,
+                                          cudaStream_t);
+template void launch_embed<double, double>(const DevBlock<double>&, const DevBlock<double>&, const int*, const int*,
+                                           const PhysParams&, cudaStream_t);
+
+
+}  // namespace mge

@@ -1,0 +1,979 @@
+// mge_runtime.cu -- host runtime and C-ABI of the GB300 multigrid cycle.
+//
+// One mge_ctx owns a case: its level hierarchy of uniform blocks, every field
+// resident in device memory for the whole solve, one CUDA stream, and the
+// CUDA graphs of the multigrid cycle.  The entry points of include/mge_gpu.h
+// replace the reference's calls one for one (timestep.f90, euler.f90,
+// movco.f90, movfin.f90, solver.f90); mge_solve runs solver.f90's FMG loop
+// with each multigrid cycle captured once per FMG level and replayed.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/mge_gpu.h"
+#include "mge_internal.h"
+
+using namespace mge;
+
+#define MGE_STR2(x) #x
+#define MGE_STR(x) MGE_STR2(x)
+
+namespace {
+
+struct HRec {
+  int ccid[3], scid[3], faceid, zz, npoint;
+  int ijk[MGE_MAX_CLOUD][3];
+  double coef[MGE_MAX_CLOUD], nvec[3], qb[3], area;
+};
+
+struct Block {
+  int level = 0, serial = 0;
+  int nx = 0, ny = 0, nz = 0, il = 0, jl = 0, kl = 0, ie = 0, je = 0, ke = 0, ib = 0, jb = 0, kb = 0;
+  int Pi = 0, Pj = 0, Pk = 0;
+  long long N = 0;
+  double h[3] = {0, 0, 0}, origin[3] = {0, 0, 0}, vol = 0;
+  double s[3] = {0, 0, 0};
+  int bctype[6] = {0, 0, 0, 0, 0, 0};
+  double fnv[6][3] = {};
+  int parent = -1, ratio[3] = {1, 1, 1}, offset[3] = {0, 0, 0};
+  std::vector<int32_t> blank_h;
+  std::vector<HRec> recs;
+  // device allocations
+  double *w = nullptr, *p = nullptr, *wn = nullptr, *ws = nullptr, *dw = nullptr, *fw = nullptr, *wr = nullptr,
+         *qf = nullptr, *vdtim = nullptr, *lam = nullptr, *dtim = nullptr;
+  uint8_t *blank = nullptr, *marker = nullptr;
+  int32_t* cutmap = nullptr;
+  int32_t *rec_i = nullptr, *rec_cloud = nullptr, *tgt_off = nullptr, *tgt_ops = nullptr;
+  double *rec_coef = nullptr, *rec_nvec = nullptr, *rec_qb = nullptr, *rec_area = nullptr, *rec_wsol = nullptr,
+         *rec_psol = nullptr, *rec_term = nullptr;
+  double* irs = nullptr;
+  IrsTables tabs[3];
+  double *rt_partial = nullptr, *rt_cur = nullptr, *forces = nullptr;
+  int npart = 1;
+  int m0 = 0;
+  std::vector<double> rtrms;  // host history rtrms(ncyc)
+  DevBlock<double> dev;
+};
+
+}  // namespace
+
+struct mge_ctx {
+  mge_params prm;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<std::vector<Block>> lv;
+  std::string err;
+  unsigned* d_err = nullptr;
+  unsigned* h_err = nullptr;  // pinned
+  double* h_rt = nullptr;     // pinned readback of residuals
+  double* scratch = nullptr;
+  size_t bytes = 0;
+  PhysParams P;
+  bool committed = false;
+  std::vector<void*> allocs;
+  std::vector<cudaGraphExec_t> graphs;  // one captured multigrid cycle per FMG level
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double last_cycle_ms = 0.0;
+  std::vector<long long> graph_kernels;  // kernel nodes per captured cycle
+  long long launches = 0;                // kernels launched through mge_cycle
+};
+
+namespace {
+
+int fail(mge_ctx* c, int code, const std::string& m) {
+  if (c) c->err = m;
+  return code;
+}
+
+int cuda_fail(mge_ctx* c, cudaError_t e, const char* where) {
+  return fail(c, MGE_ECUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(x)                                           \
+  do {                                                  \
+    cudaError_t e_ = (x);                               \
+    if (e_ != cudaSuccess) return cuda_fail(c, e_, #x); \
+  } while (0)
+
+template <typename T>
+int dalloc(mge_ctx* c, T** p, size_t n) {
+  void* q = nullptr;
+  cudaError_t e = cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(c, MGE_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  }
+  c->allocs.push_back(q);
+  c->bytes += std::max<size_t>(n, 1) * sizeof(T);
+  *p = (T*)q;
+  return MGE_OK;
+}
+
+Block* getb(mge_ctx* c, int level, int serial) {
+  if (!c || level < 1 || level > (int)c->lv.size()) return nullptr;
+  auto& L = c->lv[level - 1];
+  if (serial < 1 || serial > (int)L.size()) return nullptr;
+  return &L[serial - 1];
+}
+
+int check_err(mge_ctx* c) {
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "stream");
+  e = cudaMemcpy(c->h_err, c->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(c, e, "error word");
+  unsigned w = *c->h_err;
+  if (w) {
+    cudaMemset(c->d_err, 0, sizeof(unsigned));
+    if (w & ERR_NEGPRESS) return fail(c, MGE_ENEGPRESS, "timestep: negative or NaN c^2 (timestep.f90:45-48)");
+    if (w & ERR_ZERORHO) return fail(c, MGE_EZERORHO, "efluxb: zero density at a cut cell (efluxb.f90:61-64)");
+    if (w & ERR_NAN) return fail(c, MGE_ENAN, "bc_cutcell: wsol is NaN (bc_cutcell.f90:147-156)");
+  }
+  return MGE_OK;
+}
+
+// ---------------------------------------------------------------- device ops
+void enqueue_timestep(mge_ctx* c, Block& b) { launch_timestep<double>(b.dev, c->P, c->d_err, c->stream); }
+
+// euler.f90:1-462 on one block; nstage_limit > 0 stops early (parity probes)
+void enqueue_euler(mge_ctx* c, Block& b, int mgl, int mlvl, bool lres, bool lfir, int nstage_limit, bool rt) {
+  const mge_params& P = c->prm;
+  if (lfir) launch_copy_ws<double>(b.dev, c->stream);
+  launch_save_wn<double>(b.dev, c->stream);
+  const int mstage = (nstage_limit > 0) ? std::min(P.mstage, nstage_limit) : P.mstage;
+  for (int m = 1; m <= mstage; m++) {
+    StageArgs A;
+    A.m = m;
+    A.fn = P.cstp[m - 1] * P.cfl;
+    A.cd = P.cdis[m - 1];
+    A.dissip_on = P.cdis[m - 1] > 0.0;
+    A.scale_fw = m > 1;
+    A.forcing = mgl < mlvl;
+    A.first_forcing = lfir && m == 1;
+    A.lres = lres;
+    A.irs = (m % 2 != 0) && P.smoo > 0.0 && !lres;
+    A.vt = P.vt;
+    launch_stage<double>(b.dev, c->P, A, c->d_err, c->stream);
+    if (lres) return;
+    if (A.irs) launch_irs<double>(b.dev, c->P, b.tabs, c->stream);
+    launch_cutcell<double>(b.dev, c->P, c->d_err, c->stream);
+    launch_bcond<double>(b.dev, c->P, c->stream);
+  }
+  if (rt && (nstage_limit <= 0 || nstage_limit >= P.mstage))
+    launch_rtrms<double>(b.dev, c->P, P.vt, b.rt_partial, b.npart, b.rt_cur, c->stream);
+}
+
+void enqueue_movco(mge_ctx* c, int mgl) {  // movco.f90:21-47
+  for (Block& b : c->lv[mgl - 1]) {
+    cudaMemsetAsync(b.marker, 0, (size_t)b.N, c->stream);
+    if ((int)c->lv.size() > mgl)
+      for (Block& f : c->lv[mgl])
+        if (f.parent == b.serial) launch_collc<double, double>(b.dev, f.dev, f.ratio, f.offset, b.marker, c->stream);
+    launch_depvars_all<double>(b.dev, c->P, c->stream);
+    launch_copy_wn<double>(b.dev, c->stream);
+  }
+  for (Block& b : c->lv[mgl - 1]) launch_bcond<double>(b.dev, c->P, c->stream);
+}
+
+void enqueue_movfin(mge_ctx* c, int mgl, int mlvl) {  // movfin.f90:20-39
+  const bool fmg = (mgl - 1 == mlvl);
+  for (Block& f : c->lv[mgl - 1]) {
+    if (f.parent < 1) continue;
+    Block& pb = c->lv[mgl - 2][f.parent - 1];
+    launch_addw<double, double>(f.dev, pb.dev, f.ratio, f.offset, fmg ? 1 : 0, c->stream);
+  }
+  for (Block& f : c->lv[mgl - 1]) launch_depvars_all<double>(f.dev, c->P, c->stream);
+  for (Block& f : c->lv[mgl - 1]) {  // bc_embed
+    if (f.parent < 1) continue;
+    Block& pb = c->lv[mgl - 2][f.parent - 1];
+    launch_embed<double, double>(f.dev, pb.dev, f.ratio, f.offset, c->P, c->stream);
+  }
+  for (Block& f : c->lv[mgl - 1]) launch_bcond<double>(f.dev, c->P, c->stream);
+}
+
+// solver.f90:127-234, one multigrid cycle at FMG level mlvl (enqueue only)
+void enqueue_cycle(mge_ctx* c, int mlvl) {
+  const mge_params& P = c->prm;
+  std::vector<int> icyc(c->lv.size() + 2, 0);
+  int mgl = mlvl;
+  for (;;) {    // lopmg
+    for (;;) {  // lopr
+      icyc[mgl] += 1;
+      bool lfir = (mgl != mlvl);
+      for (Block& b : c->lv[mgl - 1]) {
+        enqueue_timestep(c, b);
+        enqueue_euler(c, b, mgl, mlvl, false, lfir, 0, mgl == mlvl);
+      }
+      if (mlvl == 1) return;
+      for (Block& b : c->lv[mgl - 1]) enqueue_euler(c, b, mgl, mlvl, true, false, 0, false);
+      mgl = mgl - 1;
+      enqueue_movco(c, mgl);
+      if (mgl == 1) break;
+    }
+    bool lfir = true;
+    for (;;) {  // lopp
+      for (Block& b : c->lv[mgl - 1]) {
+        enqueue_timestep(c, b);
+        enqueue_euler(c, b, mgl, mlvl, false, lfir, 0, false);
+      }
+      lfir = false;
+      mgl = mgl + 1;
+      enqueue_movfin(c, mgl, mlvl);
+      if (mgl == mlvl) return;
+      if (icyc[mgl] != P.mgtype) break;  // cycle lopmg
+      icyc[mgl] = 0;
+    }
+  }
+}
+
+void build_phys(mge_ctx* c) {
+  const mge_params& P = c->prm;
+  PhysParams& Q = c->P;
+  Q.gamma = P.gamma;
+  Q.gm1 = P.gamma - 1.0;
+  Q.gm = 1.0 / (P.gamma - 1.0);
+  Q.vis2 = P.vis2;
+  Q.vis4 = P.vis4;
+  Q.cfl = P.cfl;
+  Q.dimcfl = P.cfl > 1.0 ? P.cfl - 1.0 : 0.0;
+  Q.rho0 = P.rho0;
+  Q.p0 = P.p0;
+  Q.c0 = P.c0;
+  Q.u0[0] = P.u0;
+  Q.u0[1] = P.v0;
+  Q.u0[2] = P.w0;
+  Q.e0 = P.rho0 * P.h0 - P.p0;
+  Q.si_far = std::pow(P.rho0, P.gamma) / P.p0;
+  Q.matrix = P.dissip == MGE_DISSIP_MATRIX;
+  Q.eqn_ns = P.eqntype == MGE_EQN_NS;
+  Q.smoo = P.smoo;
+}
+
+// psmoo.f90:136-166 pivots for a line of l-1 unknowns (rows 2..l)
+void irs_pivots(double smoo, int lm, int l, std::vector<double>& e1, std::vector<double>& e1r, std::vector<double>& e2) {
+  const double aa = 1.0 + 2.0 * smoo, bb = -smoo;
+  e1.assign(l + 2, 1.0);
+  e2.assign(l + 2, 0.0);
+  e1r.assign(l + 2, 1.0);
+  e1[2] = aa;
+  e2[2] = bb / aa;
+  for (int q = 3; q <= lm; q++) {
+    e1[q] = aa - bb * e2[q - 1];
+    e2[q] = bb / e1[q];
+  }
+  e1[l] = aa - bb * e2[lm];
+  for (int q = 0; q <= l; q++) e1r[q] = 1.0 / e1[q];
+}
+
+int commit_block(mge_ctx* c, Block& b, double* scratch) {
+  const long long N = b.N;
+  int rc;
+  if ((rc = dalloc(c, &b.w, 5 * N)) || (rc = dalloc(c, &b.p, N)) || (rc = dalloc(c, &b.wn, 5 * N)) ||
+      (rc = dalloc(c, &b.ws, 5 * N)) || (rc = dalloc(c, &b.dw, 5 * N)) || (rc = dalloc(c, &b.fw, 5 * N)) ||
+      (rc = dalloc(c, &b.wr, 5 * N)) || (rc = dalloc(c, &b.qf, 5 * N)) || (rc = dalloc(c, &b.vdtim, N)) ||
+      (rc = dalloc(c, &b.lam, N)) || (rc = dalloc(c, &b.dtim, 1)) || (rc = dalloc(c, &b.blank, N)) ||
+      (rc = dalloc(c, &b.marker, N)) || (rc = dalloc(c, &b.cutmap, N)))
+    return rc;
+  CK(cudaMemset(b.w, 0, 5 * N * sizeof(double)));
+  CK(cudaMemset(b.p, 0, N * sizeof(double)));
+  CK(cudaMemset(b.wn, 0, 5 * N * sizeof(double)));
+  CK(cudaMemset(b.ws, 0, 5 * N * sizeof(double)));
+  CK(cudaMemset(b.dw, 0, 5 * N * sizeof(double)));
+  CK(cudaMemset(b.fw, 0, 5 * N * sizeof(double)));
+  CK(cudaMemset(b.wr, 0, 5 * N * sizeof(double)));
+  CK(cudaMemset(b.qf, 0, 5 * N * sizeof(double)));
+  CK(cudaMemset(b.vdtim, 0, N * sizeof(double)));
+  CK(cudaMemset(b.lam, 0, N * sizeof(double)));
+  CK(cudaMemset(b.marker, 0, N));
+  std::vector<uint8_t> bl(N);
+  for (long long q = 0; q < N; q++) bl[q] = b.blank_h[q] != 0 ? 1 : 0;
+  CK(cudaMemcpy(b.blank, bl.data(), N, cudaMemcpyHostToDevice));
+  // cut records
+  const int nm = (int)b.recs.size();
+  b.m0 = nm;
+  for (int m = 0; m < nm; m++)
+    if (b.recs[m].npoint == 0) {
+      b.m0 = m;
+      break;
+    }
+  std::vector<int32_t> ri(8 * std::max(nm, 1), 0), rcl(24 * std::max(nm, 1), 0);
+  std::vector<double> rcf(8 * std::max(nm, 1), 0.0), rnv(3 * std::max(nm, 1), 0.0), rqb(3 * std::max(nm, 1), 0.0),
+      rar(std::max(nm, 1), 0.0);
+  for (int m = 0; m < nm; m++) {
+    const HRec& t = b.recs[m];
+    ri[8 * m + 0] = t.ccid[0];
+    ri[8 * m + 1] = t.ccid[1];
+    ri[8 * m + 2] = t.ccid[2];
+    ri[8 * m + 3] = t.faceid;
+    ri[8 * m + 4] = t.zz;
+    ri[8 * m + 5] = t.npoint;
+    for (int q = 0; q < MGE_MAX_CLOUD; q++) {
+      rcf[8 * m + q] = t.coef[q];
+      for (int e = 0; e < 3; e++) rcl[(8 * m + q) * 3 + e] = t.ijk[q][e];
+    }
+    for (int e = 0; e < 3; e++) {
+      rnv[3 * m + e] = t.nvec[e];
+      rqb[3 * m + e] = t.qb[e];
+    }
+    rar[m] = t.area;
+  }
+  const int nma = std::max(nm, 1);
+  if ((rc = dalloc(c, &b.rec_i, 8 * nma)) || (rc = dalloc(c, &b.rec_cloud, 24 * nma)) ||
+      (rc = dalloc(c, &b.rec_coef, 8 * nma)) || (rc = dalloc(c, &b.rec_nvec, 3 * nma)) ||
+      (rc = dalloc(c, &b.rec_qb, 3 * nma)) || (rc = dalloc(c, &b.rec_area, nma)) ||
+      (rc = dalloc(c, &b.rec_wsol, 5 * nma)) || (rc = dalloc(c, &b.rec_psol, nma)) ||
+      (rc = dalloc(c, &b.rec_term, 40 * nma)))
+    return rc;
+  CK(cudaMemcpy(b.rec_i, ri.data(), ri.size() * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b.rec_cloud, rcl.data(), rcl.size() * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b.rec_coef, rcf.data(), rcf.size() * 8, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b.rec_nvec, rnv.data(), rnv.size() * 8, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b.rec_qb, rqb.data(), rqb.size() * 8, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b.rec_area, rar.data(), rar.size() * 8, cudaMemcpyHostToDevice));
+  CK(cudaMemset(b.rec_wsol, 0, 5 * nma * 8));
+  CK(cudaMemset(b.rec_psol, 0, nma * 8));
+  CK(cudaMemset(b.rec_term, 0, 40 * nma * 8));
+  // cut targets: per physical cell, the (record, role) ops in record order
+  std::vector<int32_t> cutmap(N, -1);
+  std::map<long long, std::vector<int32_t>> tg;
+  auto phys = [&](int i, int j, int k) { return i >= 2 && i <= b.il && j >= 2 && j <= b.jl && k >= 2 && k <= b.kl; };
+  std::vector<long long> order;
+  for (int m = 0; m < nm; m++) {
+    const HRec& t = b.recs[m];
+    int d = t.zz - 1;
+    int e[3] = {0, 0, 0};
+    e[d] = t.faceid >= 4 ? -1 : 1;  // neighbour away from the wall
+    int i = t.ccid[0], j = t.ccid[1], k = t.ccid[2];
+    long long c0 = (long long)i + (long long)b.Pi * ((long long)j + (long long)b.Pj * k);
+    if (phys(i, j, k)) {
+      if (!tg.count(c0)) order.push_back(c0);
+      tg[c0].push_back(2 * m);
+    }
+    int ni = i + e[0], nj = j + e[1], nk = k + e[2];
+    long long c1 = (long long)ni + (long long)b.Pi * ((long long)nj + (long long)b.Pj * nk);
+    if (phys(ni, nj, nk)) {
+      if (!tg.count(c1)) order.push_back(c1);
+      tg[c1].push_back(2 * m + 1);
+    }
+  }
+  std::vector<int32_t> off(1, 0), ops;
+  for (size_t t = 0; t < order.size(); t++) {
+    cutmap[order[t]] = (int32_t)t;
+    for (int32_t op : tg[order[t]]) ops.push_back(op);
+    off.push_back((int32_t)ops.size());
+  }
+  if ((rc = dalloc(c, &b.tgt_off, off.size())) || (rc = dalloc(c, &b.tgt_ops, std::max<size_t>(ops.size(), 1))))
+    return rc;
+  CK(cudaMemcpy(b.cutmap, cutmap.data(), N * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b.tgt_off, off.data(), off.size() * 4, cudaMemcpyHostToDevice));
+  if (!ops.empty()) CK(cudaMemcpy(b.tgt_ops, ops.data(), ops.size() * 4, cudaMemcpyHostToDevice));
+  // IRS tables
+  const int lens[3] = {b.il, b.jl, b.kl}, lms[3] = {b.nx, b.ny, b.nz};
+  size_t tot = 0;
+  for (int d = 0; d < 3; d++) tot += 3 * (size_t)(lens[d] + 2);
+  if ((rc = dalloc(c, &b.irs, tot))) return rc;
+  std::vector<double> all;
+  size_t offs[3][3];
+  for (int d = 0; d < 3; d++) {
+    std::vector<double> e1, e1r, e2;
+    irs_pivots(c->prm.smoo > 0.0 ? c->prm.smoo : 0.0, lms[d], lens[d], e1, e1r, e2);
+    offs[d][0] = all.size();
+    all.insert(all.end(), e1.begin(), e1.end());
+    offs[d][1] = all.size();
+    all.insert(all.end(), e1r.begin(), e1r.end());
+    offs[d][2] = all.size();
+    all.insert(all.end(), e2.begin(), e2.end());
+  }
+  CK(cudaMemcpy(b.irs, all.data(), all.size() * 8, cudaMemcpyHostToDevice));
+  for (int d = 0; d < 3; d++) {
+    b.tabs[d].e1 = b.irs + offs[d][0];
+    b.tabs[d].e1r = b.irs + offs[d][1];
+    b.tabs[d].e2 = b.irs + offs[d][2];
+  }
+  b.npart = rtrms_partials((long long)b.nx * b.ny * b.nz);
+  if ((rc = dalloc(c, &b.rt_partial, b.npart)) || (rc = dalloc(c, &b.rt_cur, 1)) || (rc = dalloc(c, &b.forces, 8)))
+    return rc;
+  CK(cudaMemset(b.rt_cur, 0, 8));
+  // kernel view
+  DevBlock<double>& d = b.dev;
+  std::memset(&d, 0, sizeof(d));
+  d.nx = b.nx; d.ny = b.ny; d.nz = b.nz;
+  d.il = b.il; d.jl = b.jl; d.kl = b.kl; d.ie = b.ie; d.je = b.je; d.ke = b.ke; d.ib = b.ib; d.jb = b.jb; d.kb = b.kb;
+  d.Pi = b.Pi; d.Pj = b.Pj; d.N = N;
+  d.w = b.w; d.p = b.p; d.wn = b.wn; d.ws = b.ws; d.dw = b.dw; d.fw = b.fw; d.wr = b.wr; d.qf = b.qf;
+  d.vdtim = b.vdtim; d.lam = b.lam; d.dtim = b.dtim;
+  d.blank = b.blank; d.marker = b.marker; d.cutmap = b.cutmap;
+  d.H = scratch;
+  d.F = scratch + N;
+  d.fp = scratch + 16 * N;
+  d.efs = scratch + 19 * N;
+  d.dfs = scratch + 34 * N;
+  for (int q = 0; q < 3; q++) {
+    d.s[q] = b.s[q];
+    d.sqrt_ds[q] = std::sqrt(b.s[q] * b.s[q]);
+  }
+  d.vol = b.vol;
+  d.rvol = 1.0 / b.vol;
+  d.nmir = nm;
+  d.m0 = b.m0;
+  d.rec_i = b.rec_i; d.rec_cloud = b.rec_cloud; d.rec_coef = b.rec_coef; d.rec_nvec = b.rec_nvec;
+  d.rec_qb = b.rec_qb; d.rec_area = b.rec_area; d.rec_wsol = b.rec_wsol; d.rec_psol = b.rec_psol;
+  d.rec_term = b.rec_term; d.tgt_off = b.tgt_off; d.tgt_ops = b.tgt_ops;
+  for (int f = 0; f < 6; f++) {
+    d.bctype[f] = b.bctype[f];
+    for (int q = 0; q < 3; q++) d.fnv[f][q] = b.fnv[f][q];
+  }
+  return MGE_OK;
+}
+
+}  // namespace
+
+// ====================================================================== C-ABI
+extern "C" {
+
+int mge_abi_version(void) { return MGE_ABI_VERSION; }
+
+const char* mge_build_info(void) {
+  return "code_mge_gb300 libmge_gpu: sm_103a, FP64 multigrid RK cycle, CUDA " MGE_STR(__CUDACC_VER_MAJOR__);
+}
+
+void mge_params_default(mge_params* p, double gamma, double mach, double alpha, double beta) {
+  std::memset(p, 0, sizeof(*p));
+  p->mstage = 5;
+  const double cs[5] = {0.25, 1.0 / 6.0, 0.375, 0.5, 1.0}, cd[5] = {1.0, 0.0, 0.56, 0.0, 0.44};
+  for (int q = 0; q < 5; q++) {
+    p->cstp[q] = cs[q];
+    p->cdis[q] = cd[q];
+  }
+  p->cfl = 2.8;
+  p->vt = 0;
+  p->vis2 = 0.5;
+  p->vis4 = 0.5 / 32.0;
+  p->smoo = 0.6;
+  p->mgtype = 1;
+  p->gamma = gamma;
+  p->rm = mach;
+  p->alpha = alpha;
+  p->beta = beta;
+  p->rho0 = 1.0;  // input_param.f90:61-69
+  p->p0 = 1.0 / (gamma * std::pow(mach, 2.0));
+  p->c0 = std::sqrt(gamma * p->p0 / p->rho0);
+  p->ei0 = p->p0 / ((gamma - 1.0) * p->rho0);
+  p->u0 = mach * p->c0 * std::cos(beta) * std::cos(alpha);
+  p->v0 = mach * p->c0 * std::cos(beta) * std::sin(alpha);
+  p->w0 = mach * p->c0 * std::sin(beta);
+  p->h0 = gamma * p->ei0 + 0.5 * (p->u0 * p->u0 + p->v0 * p->v0 + p->w0 * p->w0);
+  p->viscl = p->rho0 * p->u0 / 500.0;
+  p->prlmean = 0.72;
+  p->gas_const = p->p0 / p->rho0;
+  p->limfac = 5.0;
+  p->epsentr = 0.05;
+  p->wall_adiabatic = 1;
+  p->nlevel = 1;
+  p->mcyc[0] = 100;
+  p->conv_drop = 1.0e6;
+}
+
+int mge_init(const mge_params* prm, int device, mge_ctx** out) {
+  if (!prm || !out) return MGE_EBADCFG;
+  *out = nullptr;
+  if (prm->nlevel < 1 || prm->nlevel > MGE_MAX_LEVEL || prm->mstage < 1 || prm->mstage > MGE_MAX_STAGE)
+    return MGE_EBADCFG;
+  if (prm->distype != MGE_DIS_CENTRAL || prm->eqntype != MGE_EQN_EULER) return MGE_EBADCFG;
+  if (prm->dissip != MGE_DISSIP_SCALAR && prm->dissip != MGE_DISSIP_MATRIX) return MGE_EBADCFG;
+  if (prm->irs_variant != 0) return MGE_EBADCFG;
+  mge_ctx* c = new mge_ctx();
+  c->prm = *prm;
+  c->device = device;
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&c->d_err, sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMemset(c->d_err, 0, sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMallocHost(&c->h_err, sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMallocHost(&c->h_rt, 64 * sizeof(double));
+  if (e != cudaSuccess) {
+    delete c;
+    return MGE_ECUDA;
+  }
+  c->lv.resize(prm->nlevel);
+  build_phys(c);
+  *out = c;
+  return MGE_OK;
+}
+
+void mge_destroy(mge_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (cudaGraphExec_t g : c->graphs)
+    if (g) cudaGraphExecDestroy(g);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  for (void* q : c->allocs) cudaFree(q);
+  if (c->scratch) cudaFree(c->scratch);
+  if (c->d_err) cudaFree(c->d_err);
+  if (c->h_err) cudaFreeHost(c->h_err);
+  if (c->h_rt) cudaFreeHost(c->h_rt);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+const char* mge_last_error(const mge_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int mge_add_block(mge_ctx* c, const mge_block_desc* d, int level, int serial) {
+  if (!c || !d) return MGE_EBADCFG;
+  if (c->committed) return fail(c, MGE_EBADCFG, "add_block after commit");
+  if (level < 1 || level > (int)c->lv.size()) return fail(c, MGE_EBADCFG, "add_block: bad level");
+  auto& L = c->lv[level - 1];
+  if (serial != (int)L.size() + 1) return fail(c, MGE_EBADCFG, "add_block: serials must be added in order");
+  if (d->nx < 2 || d->ny < 2 || d->nz < 2) return fail(c, MGE_EBADCFG, "add_block: need at least 2 cells per axis");
+  if (d->si[1] != 0.0 || d->si[2] != 0.0 || d->sj[0] != 0.0 || d->sj[2] != 0.0 || d->sk[0] != 0.0 || d->sk[1] != 0.0)
+    return fail(c, MGE_EBADCFG, "add_block: face vectors must be axis-aligned (uniform Cartesian block)");
+  for (int f = 0; f < 6; f++) {
+    int t = d->bctype[f];
+    if (t != 0 && t != -20 && t != -50 && t != -60 && t != -80)
+      return fail(c, MGE_EBADCFG, "add_block: unsupported bctype");
+    if (t == -60 && f < 3 && d->bctype[f + 3] != -60)
+      return fail(c, MGE_EBADCFG, "periodic boundary must appear in pairs (bcond.f90:26-31)");
+  }
+  if (level > 1) {
+    if (d->parent < 1 || d->parent > (int)c->lv[level - 2].size())
+      return fail(c, MGE_EBADCFG, "add_block: parent block must be added first");
+    for (int q = 0; q < 3; q++)
+      if (d->ratio[q] != 1 && d->ratio[q] != 2) return fail(c, MGE_EBADCFG, "add_block: ratio must be 1 or 2");
+    if (d->nx % d->ratio[0] || d->ny % d->ratio[1] || d->nz % d->ratio[2])
+      return fail(c, MGE_EBADCFG, "add_block: cells not divisible by the ratio");
+  }
+  L.emplace_back();
+  Block& b = L.back();
+  b.level = level;
+  b.serial = serial;
+  b.nx = d->nx; b.ny = d->ny; b.nz = d->nz;
+  b.il = b.nx + 1; b.jl = b.ny + 1; b.kl = b.nz + 1;
+  b.ie = b.il + 1; b.je = b.jl + 1; b.ke = b.kl + 1;
+  b.ib = b.il + 2; b.jb = b.jl + 2; b.kb = b.kl + 2;
+  b.Pi = b.ib + 1; b.Pj = b.jb + 1; b.Pk = b.kb + 1;
+  b.N = (long long)b.Pi * b.Pj * b.Pk;
+  for (int q = 0; q < 3; q++) {
+    b.h[q] = d->h[q];
+    b.origin[q] = d->origin[q];
+    b.ratio[q] = d->ratio[q];
+    b.offset[q] = d->offset[q];
+  }
+  b.s[0] = d->si[0];
+  b.s[1] = d->sj[1];
+  b.s[2] = d->sk[2];
+  b.vol = d->cellvolume;
+  for (int f = 0; f < 6; f++) {
+    b.bctype[f] = d->bctype[f];
+    for (int q = 0; q < 3; q++) b.fnv[f][q] = d->facenvec[f][q];
+  }
+  b.parent = d->parent;
+  b.blank_h.assign(b.N, 1);
+  if (d->blank)
+    for (long long q = 0; q < b.N; q++) b.blank_h[q] = d->blank[q];
+  b.recs.resize(d->nmir);
+  for (int m = 0; m < d->nmir; m++) {
+    HRec& t = b.recs[m];
+    for (int q = 0; q < 3; q++) {
+      t.ccid[q] = d->ccid[3 * m + q];
+      t.scid[q] = d->scid[3 * m + q];
+      t.nvec[q] = d->nvec[3 * m + q];
+      t.qb[q] = d->qb ? d->qb[3 * m + q] : 0.0;
+    }
+    t.faceid = d->faceid[m];
+    t.zz = d->zz[m];
+    t.npoint = d->npoint[m];
+    if (t.npoint < 0 || t.npoint > MGE_MAX_CLOUD) return fail(c, MGE_EBADCFG, "add_block: bad cloud size");
+    if (t.zz < 1 || t.zz > 3 || t.faceid < 1 || t.faceid > 6 || (t.faceid - 1) % 3 != t.zz - 1)
+      return fail(c, MGE_EBADCFG, "add_block: faceid/zz mismatch");
+    int lim[3] = {b.ib, b.jb, b.kb}, phys_lo = 2, phys_hi[3] = {b.il, b.jl, b.kl};
+    for (int q = 0; q < 3; q++)
+      if (t.ccid[q] < phys_lo || t.ccid[q] > phys_hi[q]) return fail(c, MGE_EBADCFG, "add_block: cut cell not physical");
+    // the dissipation stencils reach two cells beyond the cut cell along the record axis
+    int ax = t.zz - 1;
+    if (t.ccid[ax] - 2 < 0 || t.ccid[ax] + 2 > lim[ax]) return fail(c, MGE_EBADCFG, "add_block: record too close to edge");
+    for (int q = 0; q < MGE_MAX_CLOUD; q++) {
+      t.coef[q] = d->coef[MGE_MAX_CLOUD * m + q];
+      for (int e = 0; e < 3; e++) {
+        t.ijk[q][e] = d->ijkdex[(MGE_MAX_CLOUD * m + q) * 3 + e];
+        if (q < t.npoint && (t.ijk[q][e] < 0 || t.ijk[q][e] > lim[e]))
+          return fail(c, MGE_EBADCFG, "add_block: cloud cell outside the block");
+      }
+    }
+    double fa = 1.0;
+    for (int e = 0; e < 3; e++)
+      if (e != ax) fa *= d->h[e];
+    t.area = d->area ? d->area[m] : fa;
+  }
+  return MGE_OK;
+}
+
+int mge_commit(mge_ctx* c) {
+  if (!c) return MGE_EBADCFG;
+  if (c->committed) return MGE_OK;
+  CK(cudaSetDevice(c->device));
+  long long maxN = 0;
+  for (auto& L : c->lv) {
+    if (L.empty()) return fail(c, MGE_EBADCFG, "commit: a level has no block");
+    for (Block& b : L) maxN = std::max(maxN, b.N);
+  }
+  // scratch: H(1) F(15) fp(3) efs(15) dfs(15) = 49 fields of the largest block
+  int rc = dalloc(c, &c->scratch, (size_t)49 * maxN);
+  if (rc) return rc;
+  c->allocs.pop_back();  // freed separately
+  for (auto& L : c->lv)
+    for (Block& b : L)
+      if ((rc = commit_block(c, b, c->scratch))) return rc;
+  // the set-up copies ran on the legacy stream; order them before the context stream
+  CK(cudaDeviceSynchronize());
+  c->committed = true;
+  return MGE_OK;
+}
+
+int mge_init_flow(mge_ctx* c) {  // init_flow.f90:46-96
+  if (!c || !c->committed) return MGE_EBADCFG;
+  CK(cudaSetDevice(c->device));
+  for (auto& L : c->lv)
+    for (Block& b : L) {
+      launch_init_free<double>(b.dev, c->P, c->stream);
+      launch_depvars_all<double>(b.dev, c->P, c->stream);
+      launch_cutcell<double>(b.dev, c->P, c->d_err, c->stream);
+      launch_bcond<double>(b.dev, c->P, c->stream);
+    }
+  CK(cudaGetLastError());
+  return check_err(c);
+}
+
+int mge_upload_state(mge_ctx* c, int level, int serial, const double* w) {
+  Block* b = getb(c, level, serial);
+  if (!b || !c->committed) return MGE_ENOTFOUND;
+  CK(cudaSetDevice(c->device));
+  CK(cudaMemcpyAsync(b->w, w, 5 * b->N * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  launch_depvars_all<double>(b->dev, c->P, c->stream);
+  return check_err(c);
+}
+
+int mge_download_state(mge_ctx* c, int level, int serial, double* w, double* p) {
+  Block* b = getb(c, level, serial);
+  if (!b || !c->committed) return MGE_ENOTFOUND;
+  CK(cudaSetDevice(c->device));
+  CK(cudaStreamSynchronize(c->stream));
+  if (w) CK(cudaMemcpy(w, b->w, 5 * b->N * sizeof(double), cudaMemcpyDeviceToHost));
+  if (p) CK(cudaMemcpy(p, b->p, b->N * sizeof(double), cudaMemcpyDeviceToHost));
+  return MGE_OK;
+}
+
+int mge_download_field(mge_ctx* c, int level, int serial, const char* name, double* out, size_t count) {
+  Block* b = getb(c, level, serial);
+  if (!b || !c->committed || !name) return MGE_ENOTFOUND;
+  CK(cudaSetDevice(c->device));
+  CK(cudaStreamSynchronize(c->stream));
+  std::string n(name);
+  const long long N = b->N;
+  double* src = nullptr;
+  size_t len = 0;
+  if (n == "w") { src = b->w; len = 5 * N; }
+  else if (n == "p") { src = b->p; len = N; }
+  else if (n == "dw") { src = b->dw; len = 5 * N; }
+  else if (n == "fw") { src = b->fw; len = 5 * N; }
+  else if (n == "wn") { src = b->wn; len = 5 * N; }
+  else if (n == "ws") { src = b->ws; len = 5 * N; }
+  else if (n == "wr") { src = b->wr; len = 5 * N; }
+  else if (n == "qf") { src = b->qf; len = 5 * N; }
+  else if (n == "vdtim") { src = b->vdtim; len = N; }
+  else if (n == "lam") { src = b->lam; len = N; }
+  else if (n == "wsol") { src = b->rec_wsol; len = 5 * b->recs.size(); }
+  else if (n == "psol") { src = b->rec_psol; len = b->recs.size(); }
+  else if (n == "dtim") { src = b->dtim; len = 1; }
+  if (src) {
+    if (count < len) return fail(c, MGE_EBADCFG, "download_field: buffer too small");
+    if (len) CK(cudaMemcpy(out, src, len * sizeof(double), cudaMemcpyDeviceToHost));
+    return MGE_OK;
+  }
+  if (n == "blank" || n == "marker") {
+    if (count < (size_t)N) return fail(c, MGE_EBADCFG, "download_field: buffer too small");
+    std::vector<uint8_t> t(N);
+    CK(cudaMemcpy(t.data(), n == "blank" ? b->blank : b->marker, N, cudaMemcpyDeviceToHost));
+    for (long long q = 0; q < N; q++) out[q] = (double)t[q];
+    return MGE_OK;
+  }
+  return fail(c, MGE_EBADCFG, "download_field: unknown field " + n);
+}
+
+int mge_timestep(mge_ctx* c, int level, int serial) {
+  Block* b = getb(c, level, serial);
+  if (!b || !c->committed) return MGE_ENOTFOUND;
+  CK(cudaSetDevice(c->device));
+  enqueue_timestep(c, *b);
+  CK(cudaGetLastError());
+  return check_err(c);
+}
+
+static int euler_common(mge_ctx* c, int level, int serial, int ncyc, int mgl, int mlvl, int lres, int lfir,
+                        int nstage) {
+  Block* b = getb(c, level, serial);
+  if (!b || !c->committed) return MGE_ENOTFOUND;
+  CK(cudaSetDevice(c->device));
+  const bool full = !lres && (nstage <= 0 || nstage >= c->prm.mstage);
+  enqueue_euler(c, *b, mgl, mlvl, lres != 0, lfir != 0, nstage, full);
+  CK(cudaGetLastError());
+  int rc = check_err(c);
+  if (rc) return rc;
+  if (full && ncyc >= 0) {
+    double v = 0.0;
+    CK(cudaMemcpy(&v, b->rt_cur, sizeof(double), cudaMemcpyDeviceToHost));
+    if ((int)b->rtrms.size() <= ncyc) b->rtrms.resize(ncyc + 1, 0.0);
+    b->rtrms[ncyc] = v;
+  }
+  return MGE_OK;
+}
+
+int mge_euler(mge_ctx* c, int level, int serial, int itime, int ncyc, int mgl, int mlvl, int lres, int lfir) {
+  (void)itime;
+  return euler_common(c, level, serial, ncyc, mgl, mlvl, lres, lfir, 0);
+}
+
+int mge_euler_partial(mge_ctx* c, int level, int serial, int itime, int ncyc, int mgl, int mlvl, int lres, int lfir,
+                      int nstage) {
+  (void)itime;
+  return euler_common(c, level, serial, ncyc, mgl, mlvl, lres, lfir, nstage);
+}
+
+int mge_movco(mge_ctx* c, int mgl) {
+  if (!c || !c->committed || mgl < 1 || mgl > (int)c->lv.size()) return MGE_ENOTFOUND;
+  CK(cudaSetDevice(c->device));
+  enqueue_movco(c, mgl);
+  CK(cudaGetLastError());
+  return check_err(c);
+}
+
+int mge_movfin(mge_ctx* c, int mgl, int mlvl) {
+  if (!c || !c->committed || mgl < 2 || mgl > (int)c->lv.size()) return MGE_ENOTFOUND;
+  CK(cudaSetDevice(c->device));
+  enqueue_movfin(c, mgl, mlvl);
+  CK(cudaGetLastError());
+  return check_err(c);
+}
+
+int mge_bc_overlap(mge_ctx* c, int mgl) {
+  // one block per level in the hierarchies this library builds: nothing overlaps
+  if (!c || mgl < 1 || mgl > (int)c->lv.size()) return MGE_ENOTFOUND;
+  return MGE_OK;
+}
+
+int mge_get_rtrms(mge_ctx* c, int level, int serial, int ncyc, double* out) {
+  Block* b = getb(c, level, serial);
+  if (!b || !out) return MGE_ENOTFOUND;
+  *out = (ncyc >= 0 && ncyc < (int)b->rtrms.size()) ? b->rtrms[ncyc] : 0.0;
+  return MGE_OK;
+}
+
+int mge_forces_compute(mge_ctx* c, int level, const mge_solve_opts* o, mge_forces* out) {
+  if (!c || !c->committed || level < 1 || level > (int)c->lv.size() || !out) return MGE_ENOTFOUND;
+  CK(cudaSetDevice(c->device));
+  double F[3] = {0, 0, 0}, M[3] = {0, 0, 0};
+  const double ctr[3] = {o ? o->moment_center[0] : 0.0, o ? o->moment_center[1] : 0.0, o ? o->moment_center[2] : 0.0};
+  for (Block& b : c->lv[level - 1]) {
+    if (b.recs.empty()) continue;
+    launch_forces<double>(b.dev, b.origin, b.h, ctr, b.forces, c->stream);
+    double h6[8];
+    CK(cudaMemcpyAsync(h6, b.forces, 6 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    for (int d = 0; d < 3; d++) {
+      F[d] += h6[d];
+      M[d] += h6[3 + d];
+    }
+  }
+  const mge_params& P = c->prm;
+  double qinf = 0.5 * P.rho0 * (P.u0 * P.u0 + P.v0 * P.v0 + P.w0 * P.w0);
+  double aref = (o && o->ref_area > 0.0) ? o->ref_area : 1.0;
+  double ed[3] = {std::cos(P.alpha) * std::cos(P.beta), std::sin(P.alpha) * std::cos(P.beta), std::sin(P.beta)};
+  double el[3] = {-std::sin(P.alpha), std::cos(P.alpha), 0.0};
+  for (int d = 0; d < 3; d++) {
+    out->force[d] = F[d];
+    out->moment[d] = M[d];
+  }
+  out->cd = (F[0] * ed[0] + F[1] * ed[1] + F[2] * ed[2]) / (qinf * aref);
+  out->cl = (F[0] * el[0] + F[1] * el[1] + F[2] * el[2]) / (qinf * aref);
+  return MGE_OK;
+}
+
+static int launch_cycle_graph(mge_ctx* c, int mlvl) {
+  if ((int)c->graphs.size() < (int)c->lv.size() + 1) c->graphs.resize(c->lv.size() + 1, nullptr);
+  if (!c->graphs[mlvl]) {
+    cudaGraph_t g;
+    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    enqueue_cycle(c, mlvl);
+    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&c->graphs[mlvl], g, 0);
+    size_t nn = 0;
+    cudaGraphGetNodes(g, nullptr, &nn);
+    std::vector<cudaGraphNode_t> nodes(nn);
+    if (nn) cudaGraphGetNodes(g, nodes.data(), &nn);
+    long long nk = 0;
+    for (size_t q = 0; q < nn; q++) {
+      cudaGraphNodeType t;
+      if (cudaGraphNodeGetType(nodes[q], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) nk++;
+    }
+    if ((int)c->graph_kernels.size() < (int)c->lv.size() + 1) c->graph_kernels.resize(c->lv.size() + 1, 0);
+    c->graph_kernels[mlvl] = nk;
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaGraphInstantiate");
+  }
+  if (!c->ev0) {
+    CK(cudaEventCreate(&c->ev0));
+    CK(cudaEventCreate(&c->ev1));
+  }
+  CK(cudaEventRecord(c->ev0, c->stream));
+  CK(cudaGraphLaunch(c->graphs[mlvl], c->stream));
+  c->launches += c->graph_kernels[mlvl];
+  CK(cudaEventRecord(c->ev1, c->stream));
+  return MGE_OK;
+}
+
+// residual bookkeeping of solver.f90:160-181 after a cycle at FMG level mlvl
+static int read_cycle_residual(mge_ctx* c, int mlvl, int ncyc, double* max_res, double* ini_res) {
+  auto& fin = c->lv[mlvl - 1];
+  for (size_t q = 0; q < fin.size() && q < 64; q++)
+    CK(cudaMemcpyAsync(c->h_rt + q, fin[q].rt_cur, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaGetLastError());
+  int rc = check_err(c);
+  if (rc) return rc;
+  double mr = 1000.0;
+  for (size_t q = 0; q < fin.size() && q < 64; q++) {
+    double r = c->h_rt[q];
+    if ((int)fin[q].rtrms.size() <= ncyc) fin[q].rtrms.resize(ncyc + 1, 0.0);
+    fin[q].rtrms[ncyc] = r;
+    if (ncyc == 1 && ini_res) *ini_res = r;
+    if (r < mr) mr = r;
+    if (r != r) return fail(c, MGE_ENAN, "NaN residual (solver.f90:180)");
+  }
+  *max_res = mr;
+  return MGE_OK;
+}
+
+int mge_cycle(mge_ctx* c, int mlvl, int ncyc, double* max_res) {
+  if (!c || !c->committed || mlvl < 1 || mlvl > (int)c->lv.size() || !max_res) return MGE_EBADCFG;
+  CK(cudaSetDevice(c->device));
+  int rc = launch_cycle_graph(c, mlvl);
+  if (rc) return rc;
+  rc = read_cycle_residual(c, mlvl, ncyc, max_res, nullptr);
+  if (rc) return rc;
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+  c->last_cycle_ms = ms;
+  return MGE_OK;
+}
+
+double mge_last_cycle_ms(const mge_ctx* c) { return c ? c->last_cycle_ms : 0.0; }
+
+long long mge_launch_count(const mge_ctx* c) { return c ? c->launches : 0; }
+
+int mge_kernel_times(mge_ctx* c, int level, int reps, double* ms_out, int nout) {
+  Block* bp = getb(c, level, 1);
+  if (!bp || !c->committed || reps < 1 || !ms_out) return MGE_EBADCFG;
+  CK(cudaSetDevice(c->device));
+  Block& b = *bp;
+  const mge_params& P = c->prm;
+  const int NK = 11;
+  double tot[NK] = {0};
+  int cnt[NK] = {0};
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  auto timed = [&](int kind, auto&& fn) -> int {
+    CK(cudaEventRecord(e0, c->stream));
+    fn();
+    CK(cudaEventRecord(e1, c->stream));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    tot[kind] += ms;
+    cnt[kind] += 1;
+    return MGE_OK;
+  };
+  int rc = MGE_OK;
+  for (int r = 0; r < reps && !rc; r++) {
+    rc = timed(0, [&] { enqueue_timestep(c, b); });
+    launch_save_wn<double>(b.dev, c->stream);
+    for (int m = 1; m <= P.mstage && !rc; m++) {
+      StageArgs A;
+      A.m = m;
+      A.fn = P.cstp[m - 1] * P.cfl;
+      A.cd = P.cdis[m - 1];
+      A.dissip_on = P.cdis[m - 1] > 0.0;
+      A.scale_fw = m > 1;
+      A.forcing = 0;
+      A.first_forcing = 0;
+      A.lres = 0;
+      A.irs = (m % 2 != 0) && P.smoo > 0.0;
+      A.vt = P.vt;
+      for (int part = 0; part < 4 && !rc; part++)
+        rc = timed(1 + part, [&] { launch_stage_part<double>(part, b.dev, c->P, A, c->d_err, c->stream); });
+      if (A.irs)
+        for (int part = 0; part < 3 && !rc; part++)
+          rc = timed(5 + part, [&] { launch_irs_part<double>(part, b.dev, c->P, b.tabs, c->stream); });
+      if (!rc) rc = timed(8, [&] { launch_cutcell<double>(b.dev, c->P, c->d_err, c->stream); });
+      if (!rc) rc = timed(9, [&] { launch_bcond<double>(b.dev, c->P, c->stream); });
+    }
+    if (!rc) rc = timed(10, [&] { launch_rtrms<double>(b.dev, c->P, P.vt, b.rt_partial, b.npart, b.rt_cur, c->stream); });
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
+  for (int q = 0; q < NK && q < nout; q++) ms_out[q] = cnt[q] ? tot[q] / cnt[q] : 0.0;
+  return check_err(c);
+}
+
+// solver.f90:109-292 with one CUDA graph per FMG level
+int mge_solve(mge_ctx* c, const mge_solve_opts* o, double* hist, int hist_len, int* cycles_done, mge_forces* forces) {
+  if (!c || !c->committed) return MGE_EBADCFG;
+  CK(cudaSetDevice(c->device));
+  const mge_params& P = c->prm;
+  const int nlevel = (int)c->lv.size();
+  const bool use_graph = o ? o->use_graph != 0 : true;
+  int nfin = 0, rc;
+  double ini_res = 1.0, max_res = 0.0;
+  for (int mlvl = 1; mlvl <= nlevel; mlvl++) {
+    for (int ncyc = 1; ncyc <= P.mcyc[mlvl - 1]; ncyc++) {
+      if (use_graph) {
+        if ((rc = launch_cycle_graph(c, mlvl))) return rc;
+      } else {
+        enqueue_cycle(c, mlvl);
+      }
+      if ((rc = read_cycle_residual(c, mlvl, ncyc, &max_res, &ini_res))) return rc;
+      if (mlvl == nlevel) {
+        if (hist && nfin < hist_len) hist[nfin] = max_res;
+        nfin++;
+      }
+      if (mlvl > 1) {  // convergence (solver.f90:237-239); the single-grid level runs all its cycles
+        double drop = P.conv_drop > 0.0 ? P.conv_drop : 1.0e6;
+        if (ini_res / max_res > drop) break;
+      }
+      if (o && o->max_cycles_total > 0 && mlvl == nlevel && nfin >= o->max_cycles_total) break;
+    }
+    if (mlvl < nlevel) {  // FMG prolongation (solver.f90:256-259)
+      enqueue_movfin(c, mlvl + 1, mlvl);
+      CK(cudaGetLastError());
+      if ((rc = check_err(c))) return rc;
+    }
+  }
+  if (cycles_done) *cycles_done = nfin;
+  if (forces) return mge_forces_compute(c, nlevel, o, forces);
+  return MGE_OK;
+}
+
+size_t mge_device_bytes(const mge_ctx* c) { return c ? c->bytes : 0; }
+
+int mge_sync(mge_ctx* c) {
+  if (!c) return MGE_EBADCFG;
+  CK(cudaSetDevice(c->device));
+  return check_err(c);
+}
+
+}  // extern "C"

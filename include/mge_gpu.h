@@ -1,0 +1,226 @@
+/*
+ * mge_gpu.h -- C-ABI of the GB300 multigrid Runge-Kutta residual cycle.
+ *
+ * This is the drop-in boundary for code_mge's solver/euler call chain.  Every
+ * entry point is plain C: pointers, sizes and POD structs, no C++ or torch
+ * types, so the unchanged Fortran driver can bind it through ISO_C_BINDING.
+ *
+ * Array layout of every per-cell field crossing this boundary is the Fortran
+ * layout of the reference's mgrid arrays (make_flow.f90:36-56):
+ *     w(0:ib,0:jb,0:kb,1:5)   column-major, i fastest, variable slowest,
+ *     ib = nx+3, jb = ny+3, kb = nz+3   (two ghost layers on every face,
+ *     physical cells i = 2..il with il = nx+1, psmoo.f90:125-127).
+ * A C caller indexes it as w[v*N + i + (ib+1)*(j + (jb+1)*k)] with
+ * N = (ib+1)*(jb+1)*(kb+1) and v = 0..4.
+ *
+ * Level numbering follows solver.f90: level 1 is the coarsest grid and level
+ * nlevel the finest; the full-multigrid loop runs mlvl = 1..nlevel.
+ *
+ * Return codes: MGE_OK (0) or one of the negative MGE_E* codes below.  The
+ * reference stops the program on the matching condition; the Fortran shim
+ * turns a nonzero code back into that stop.
+ */
+#ifndef MGE_GPU_H
+#define MGE_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MGE_ABI_VERSION 1
+
+/* status codes */
+#define MGE_OK           0
+#define MGE_ENAN        -1  /* NaN residual (solver.f90:180) or NaN wsol (bc_cutcell.f90:147-156) */
+#define MGE_ENEGPRESS   -2  /* c^2 < 0 or NaN in timestep (timestep.f90:45-48) */
+#define MGE_EZERORHO    -3  /* |rho| < 1e-8 at a cut cell (efluxb.f90:61-64) */
+#define MGE_EBADCFG     -4  /* bad distype/dissip/bctype/sizes (euler.f90:213, dflux.f90:107, bcond.f90:26-31) */
+#define MGE_ENOMEM      -5  /* device memory exhausted / admission refused */
+#define MGE_ETIMEOUT    -6  /* a bounded device wait gave up */
+#define MGE_ECUDA       -7  /* any other CUDA runtime error */
+#define MGE_ENOTFOUND   -8  /* unknown level/serial/case handle */
+
+/* character-valued typepara switches, encoded as ints */
+#define MGE_EQN_EULER    0  /* eqntype 'e' */
+#define MGE_EQN_NS       1  /* eqntype 'n' */
+#define MGE_DIS_CENTRAL  0  /* distype 'c'  : JST central flux + dflux */
+#define MGE_DIS_ROE1     1  /* distype 'r1' : first-order Roe flux */
+#define MGE_DIS_ROE2     2  /* distype 'r2' : MUSCL second-order Roe flux */
+#define MGE_DISSIP_SCALAR 0 /* dissip 'scalar' */
+#define MGE_DISSIP_MATRIX 1 /* dissip 'matrix' (dflux_matrix) */
+
+#define MGE_PREC_FP64    0  /* plain: every level and kernel in FP64 */
+#define MGE_PREC_MIXED   1  /* FP32 coarse levels, IRS and time step; FP64 finest R(w), update, norms, forces */
+
+#define MGE_MAX_STAGE   8
+#define MGE_MAX_LEVEL  16
+#define MGE_MAX_CLOUD   8
+
+/*
+ * Solver parameters: the typepara globals that input_param.f90:17-114 fills
+ * from the job sheet, after its own post-processing (cfl made positive with
+ * vt recording the sign, vis4 already divided by 32, free-stream state
+ * non-dimensionalised with rho0 = 1 and p0 = 1/(gamma M^2)).
+ * mge_params_default() fills the same derived quantities from
+ * (gamma, mach, alpha, beta) the way input_param.f90:44-69 does.
+ */
+typedef struct mge_params {
+  int    mstage;                  /* number of RK stages (imstage) */
+  double cstp[MGE_MAX_STAGE];     /* stage coefficients alpha_m */
+  double cdis[MGE_MAX_STAGE];     /* dissipation blending per stage */
+  double cfl;                     /* |cfl| */
+  int    vt;                      /* 1: global time step dtim, 0: local vdtim */
+  double vis2, vis4;              /* k2 and k4 (vis4 already /32) */
+  double smoo;                    /* implicit residual smoothing coefficient */
+  int    mgtype;                  /* 1: V cycle, 2: W cycle */
+  int    eqntype;                 /* MGE_EQN_* */
+  int    distype;                 /* MGE_DIS_* */
+  int    dissip;                  /* MGE_DISSIP_* */
+  double gamma;
+  double rm, alpha, beta;         /* free-stream Mach and angles (radians) */
+  double rho0, p0, c0, ei0, u0, v0, w0, h0;
+  double viscl;                   /* laminar viscosity (NS) */
+  double prlmean;                 /* laminar Prandtl number (NS) */
+  double gas_const;               /* gas constant used for temperature (NS) */
+  double limfac, epsentr;         /* Roe limiter / Harten entropy fix */
+  int    wall_adiabatic;          /* NS cut-cell wall: 1 adiabatic no-slip */
+  int    irs_variant;             /* 0: psmoo_old (what euler calls), 1: psmoo + progon3 */
+  int    precision;               /* MGE_PREC_* */
+  int    nlevel;                  /* number of multigrid levels */
+  int    mcyc[MGE_MAX_LEVEL];     /* cycles per FMG level (mcyc) */
+  double conv_drop;               /* exit when ini_res/max_res > conv_drop (1e6, solver.f90:238) */
+} mge_params;
+
+/*
+ * One uniform Cartesian block (an mgrid of the reference) with its cut-cell
+ * records.  All pointers are borrowed for the duration of mge_add_block only.
+ */
+typedef struct mge_block_desc {
+  int    nx, ny, nz;              /* physical cells (mgrid%ncell) */
+  double h[3];                    /* cell sizes */
+  double origin[3];               /* coordinate of the lower corner of cell (2,2,2) */
+  double cellvolume;
+  double si[3], sj[3], sk[3];     /* face vectors (init_metric.f90:111-177, uniform block) */
+  int    bctype[6];               /* -20 far, -50 symmetry, -60 periodic, -80 wall, 0 none */
+  double facenvec[6][3];          /* outward face normal per face (bc_far.f90:99) */
+  const int32_t* blank;           /* (0:ib,0:jb,0:kb) 0 = solid; NULL = all fluid */
+  /* cut-cell mirror records z(1:nmir) (txcut, efluxb.f90:30-48, bc_cutcell.f90:41-84) */
+  int    nmir;
+  const int32_t* ccid;            /* [nmir][3] cut (fluid) cell */
+  const int32_t* scid;            /* [nmir][3] solid neighbour */
+  const int32_t* faceid;          /* [nmir] 1..6: solid at -i,-j,-k (1,2,3) or +i,+j,+k (4,5,6) */
+  const int32_t* zz;              /* [nmir] axis 1..3 */
+  const int32_t* npoint;          /* [nmir] cloud size (<= MGE_MAX_CLOUD) */
+  const int32_t* ijkdex;          /* [nmir][MGE_MAX_CLOUD][3] cloud cells */
+  const double*  coef;            /* [nmir][MGE_MAX_CLOUD] cloud weights */
+  const double*  nvec;            /* [nmir][3] wall normal (need not be unit) */
+  const double*  qb;              /* [nmir][3] wall velocity; NULL = fixed wall */
+  const double*  area;            /* [nmir] wall-face area for force integration; NULL = face area */
+  /* parent (next coarser level) relation; parent = -1 for the coarsest level */
+  int    parent;                  /* serial of the parent block on level-1 */
+  int    ratio[3];                /* h_parent / h per axis (1 or 2) */
+  int    offset[3];               /* origin = parent origin + offset * h_parent */
+} mge_block_desc;
+
+/* Cut-cell wall forces (new: the reference has no Cl/Cd integrator) */
+typedef struct mge_forces {
+  double force[3];
+  double moment[3];
+  double cl, cd;
+} mge_forces;
+
+/* Options of a whole-hierarchy solve (solver.f90:109-292 on the device) */
+typedef struct mge_solve_opts {
+  int    max_cycles_total;        /* safety cap on finest cycles; 0 = mcyc only */
+  double ref_area;                /* reference area for Cl/Cd */
+  double moment_center[3];
+  int    use_graph;               /* capture the multigrid cycle in a CUDA graph */
+} mge_solve_opts;
+
+typedef struct mge_ctx mge_ctx;
+
+/* Library identity */
+int         mge_abi_version(void);
+const char* mge_build_info(void);
+
+/* Fill derived free-stream quantities the way input_param.f90:44-69 does. */
+void mge_params_default(mge_params* prm, double gamma, double mach,
+                        double alpha, double beta);
+
+/* Context lifetime.  Replaces make_flow allocation (make_flow.f90:36-56). */
+int  mge_init(const mge_params* prm, int device, mge_ctx** out);
+void mge_destroy(mge_ctx* ctx);
+const char* mge_last_error(const mge_ctx* ctx);
+
+/* Add one block at (level, serial); serial counts from 1 per level. */
+int mge_add_block(mge_ctx* ctx, const mge_block_desc* desc, int level, int serial);
+
+/* Finish setup: allocate device fields, upload metrics and records. */
+int mge_commit(mge_ctx* ctx);
+
+/* Free-stream start, then depvars + bc_cutcell + bcond (init_flow.f90:46-96). */
+int mge_init_flow(mge_ctx* ctx);
+
+/* Host <-> device state in the Fortran layout above. p may be NULL. */
+int mge_upload_state(mge_ctx* ctx, int level, int serial, const double* w);
+int mge_download_state(mge_ctx* ctx, int level, int serial, double* w, double* p);
+/* Download any per-cell field by name: "w","p","dw","fw","wn","ws","wr","qf",
+ * "vdtim","lam" (radi+radj+radk), "blank"(as double), "marker"(as double). */
+int mge_download_field(mge_ctx* ctx, int level, int serial, const char* name,
+                       double* out, size_t count);
+
+/* Per-call drop-in entry points (solver.f90:154-155,199,204,218-219,228,258). */
+int mge_timestep(mge_ctx* ctx, int level, int serial);                 /* timestep.f90 */
+int mge_euler(mge_ctx* ctx, int level, int serial, int itime, int ncyc,
+              int mgl, int mlvl, int lres, int lfir);                  /* euler.f90 */
+int mge_movco(mge_ctx* ctx, int mgl);                                  /* movco.f90 */
+int mge_movfin(mge_ctx* ctx, int mgl, int mlvl);                       /* movfin.f90 */
+int mge_bc_overlap(mge_ctx* ctx, int mgl);                             /* bc_overlap.f90 */
+
+/* Residual history entry rtrms(ncyc) of a block (euler.f90:431-447). */
+int mge_get_rtrms(mge_ctx* ctx, int level, int serial, int ncyc, double* out);
+
+/* Whole solve on the device: FMG level loop, V/W cycles, convergence exit.
+ * rtrms_hist receives max_res per finest cycle (job_res.dat), up to hist_len. */
+int mge_solve(mge_ctx* ctx, const mge_solve_opts* opts, double* rtrms_hist,
+              int hist_len, int* cycles_done, mge_forces* forces);
+
+/* One multigrid cycle (the body of solver.f90's lop0 loop, lines 126-234) at
+ * FMG level mlvl, replayed from a CUDA graph captured on the first call for
+ * that level; *max_res receives the residual of the cycle (solver.f90:164-176). */
+int mge_cycle(mge_ctx* ctx, int mlvl, int ncyc, double* max_res);
+
+/* Device time (CUDA events on the context's stream) of the last mge_cycle. */
+double mge_last_cycle_ms(const mge_ctx* ctx);
+
+/* Kernels this library has launched through mge_cycle (graph kernel nodes). */
+long long mge_launch_count(const mge_ctx* ctx);
+
+/* Profiling hook: run one timestep + full euler update on (level, 1) `reps`
+ * times outside any graph, timing each kernel kind with CUDA events; writes
+ * the average ms per launch of {timestep, prep, face, rec, combine, irs_i,
+ * irs_j, irs_k_update, cutcell, bcond, rtrms} into ms_out[0..10].  Advances
+ * the state of that level. */
+int mge_kernel_times(mge_ctx* ctx, int level, int reps, double* ms_out, int nout);
+
+/* Cut-cell wall force integration on the finest level (R-FORCE, new). */
+int mge_forces_compute(mge_ctx* ctx, int level, const mge_solve_opts* opts,
+                       mge_forces* out);
+
+/* Debug / parity: run only stages 1..nstage of one euler call (no rtrms). */
+int mge_euler_partial(mge_ctx* ctx, int level, int serial, int itime, int ncyc,
+                      int mgl, int mlvl, int lres, int lfir, int nstage);
+
+/* Device bytes held by the context (admission control). */
+size_t mge_device_bytes(const mge_ctx* ctx);
+
+/* Synchronise the context's stream; returns the first deferred device error. */
+int mge_sync(mge_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MGE_GPU_H */

@@ -1,0 +1,1723 @@
+/*
+ * mge_oracle.cpp -- CPU FP64 restatement of code_mge's multigrid Runge-Kutta
+ * residual cycle (srcf90/solver.f90 .. srcf90/depvars.f90).
+ *
+ * TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and the
+ * cpu_baseline / reference legs of bench.py load this library, and only as
+ * the checker.  The GPU product (code_mge_gb300) never links or calls it.
+ *
+ * Parity status: UNPINNED against the reference binary (Fortran, not
+ * buildable here: the fcode library, plugin sources and include files are
+ * absent and no Fortran compiler exists).  Every routine below restates the
+ * cited Fortran routine in the same loop order and the same expression order,
+ * compiled with -O2 -ffp-contract=off so that each Fortran expression rounds
+ * exactly as gfortran -O2 on x86-64 (SSE2, no FMA contraction) would.
+ *
+ * Indexing: every per-cell array uses the Fortran layout of make_flow.f90:
+ * a(0:ib,0:jb,0:kb,1:5), i fastest.  Variables are 0-based here (v = 0..4 for
+ * Fortran 1..5).
+ *
+ * Definitions the reference takes from its absent preprocessor library and
+ * that this build defines itself (they are shared with the GPU library):
+ *  - uniform block metric: si = (-hy*hz,0,0), sj = (0,-hx*hz,0),
+ *    sk = (0,0,-hx*hy), cellvolume = hx*hy*hz (what init_metric.f90:111-177
+ *    yields for an exactly representable uniform grid);
+ *  - grid transfer geometry (eval_x2cell, shft_cell, trilinear_factor): a
+ *    fine block with ratio r and integer offset o inside its parent; the
+ *    centre-based 2x2x2 stencil is clamped to the parent's physical cells and
+ *    the local coordinate is kept unclamped (linear extrapolation);
+ *  - cut-cell records and their interpolation clouds are inputs.
+ */
+#include "mge_oracle.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+int g_threads = 1;
+
+struct ORec {
+  int ccid[3], scid[3], faceid, zz, npoint;
+  int ijk[MGE_MAX_CLOUD][3];
+  double coef[MGE_MAX_CLOUD];
+  double nvec[3], qb[3], area;
+  double psol, wsol[5];
+};
+
+struct OBlock {
+  int level = 0, serial = 0;
+  int nx = 0, ny = 0, nz = 0, il = 0, jl = 0, kl = 0, ie = 0, je = 0, ke = 0, ib = 0, jb = 0, kb = 0;
+  size_t Pi = 0, Pj = 0, Pk = 0, N = 0;
+  double h[3] = {0, 0, 0}, origin[3] = {0, 0, 0}, vol = 0;
+  double si[3] = {0, 0, 0}, sj[3] = {0, 0, 0}, sk[3] = {0, 0, 0};
+  int bctype[6] = {0, 0, 0, 0, 0, 0};
+  double fnv[6][3] = {};
+  std::vector<double> w, p, wn, ws, dw, fw, wr, qf, vdtim, radi, radj, radk, epsx, epsy, epsz;
+  std::vector<int> blank, marker;
+  std::vector<double> rtrms;
+  double dtim = 10.0;
+  std::vector<ORec> z;
+  int parent = -1, ratio[3] = {1, 1, 1}, offset[3] = {0, 0, 0};
+
+  inline size_t I(int i, int j, int k) const { return (size_t)i + Pi * ((size_t)j + Pj * (size_t)k); }
+  inline double& W(int i, int j, int k, int v) { return w[(size_t)v * N + I(i, j, k)]; }
+  inline double& P(int i, int j, int k) { return p[I(i, j, k)]; }
+  inline double& DW(int i, int j, int k, int v) { return dw[(size_t)v * N + I(i, j, k)]; }
+  inline double& FW(int i, int j, int k, int v) { return fw[(size_t)v * N + I(i, j, k)]; }
+  inline int BL(int i, int j, int k) const { return blank[I(i, j, k)]; }
+  inline double LAM(int i, int j, int k) const {
+    size_t c = I(i, j, k);
+    return radi[c] + radj[c] + radk[c];
+  }
+};
+
+}  // namespace
+
+struct mgeo_ctx {
+  mge_params prm;
+  std::vector<std::vector<OBlock>> lv;  // lv[level-1][serial-1]
+  std::string err;
+  bool committed = false;
+  int mirr_zero_warned = 0;
+};
+
+namespace {
+
+inline double fdim_(double a, double b) { return a > b ? a - b : 0.0; }  // Fortran DIM
+inline double fmax_(double a, double b) { return a > b ? a : b; }
+inline double fmin_(double a, double b) { return a < b ? a : b; }
+
+int fail(mgeo_ctx* c, int code, const std::string& msg) {
+  c->err = msg;
+  return code;
+}
+
+OBlock* getb(mgeo_ctx* c, int level, int serial) {
+  if (level < 1 || level > (int)c->lv.size()) return nullptr;
+  auto& L = c->lv[level - 1];
+  if (serial < 1 || serial > (int)L.size()) return nullptr;
+  return &L[serial - 1];
+}
+
+/* depvars_one, depvars.f90:48-49:  qq = 0.5*sum(cv(2:4)**2)/cv(1); p = (g-1)*dim(cv(5),qq) */
+inline double depvars_one(const double gamma, double w0, double w1, double w2, double w3, double w4) {
+  double qq = 0.5 * (w1 * w1 + w2 * w2 + w3 * w3) / w0;
+  return (gamma - 1.0) * fdim_(w4, qq);
+}
+
+void depvars_cell(const mge_params& P, OBlock& b, int i, int j, int k) {
+  b.P(i, j, k) = depvars_one(P.gamma, b.W(i, j, k, 0), b.W(i, j, k, 1), b.W(i, j, k, 2), b.W(i, j, k, 3),
+                             b.W(i, j, k, 4));
+}
+
+/* depvars_all, depvars.f90:23-32 over the whole array 0:ib,0:jb,0:kb */
+void depvars_all(const mge_params& P, OBlock& b) {
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+  for (int k = 0; k <= b.kb; k++)
+    for (int j = 0; j <= b.jb; j++)
+      for (int i = 0; i <= b.ib; i++) depvars_cell(P, b, i, j, k);
+}
+
+/* ceflux, eflux.f90:133-155 / ceflux.f90:18-22 */
+inline void ceflux(const double* w, double p, const double* ss, double* fs) {
+  fs[0] = w[1] * ss[0] + w[2] * ss[1] + w[3] * ss[2];
+  fs[1] = fs[0] * w[1] / w[0] + p * ss[0];
+  fs[2] = fs[0] * w[2] / w[0] + p * ss[1];
+  fs[3] = fs[0] * w[3] / w[0] + p * ss[2];
+  fs[4] = fs[0] * (w[4] + p) / w[0];
+}
+
+inline void getw(OBlock& b, int i, int j, int k, double* o) {
+  for (int v = 0; v < 5; v++) o[v] = b.W(i, j, k, v);
+}
+
+/* ------------------------------------------------------------------ timestep.f90 */
+int timestep(mgeo_ctx* c, OBlock& b) {
+  const mge_params& P = c->prm;
+  const double gamma = P.gamma, cfl = P.cfl;
+  const double plim = 0.001;
+  const int i2d = 0;
+  b.dtim = 10.0;  // timestep.f90:36
+  double cfac = 4.0;
+  if (P.eqntype == MGE_EQN_NS) {
+    if (P.distype == MGE_DIS_CENTRAL) cfac = 4.0;       // timestep.f90:119-125
+    else if (P.distype == MGE_DIS_ROE2) cfac = 1.0;
+    else cfac = 2.0;
+  }
+  const bool ns = (P.eqntype == MGE_EQN_NS);
+  int bad = 0;
+  double dtmin = 10.0;
+#pragma omp parallel for num_threads(g_threads) schedule(static) reduction(min : dtmin) reduction(+ : bad)
+  for (int k = 2; k <= b.kl; k++)
+    for (int j = 2; j <= b.jl; j++)
+      for (int i = 2; i <= b.il; i++) {
+        double w0 = b.W(i, j, k, 0);
+        double cc = gamma * b.P(i, j, k) / w0;
+        if (cc < 0.0 || cc != cc) {  // timestep.f90:45-48 (stop)
+          bad++;
+          continue;
+        }
+        cc = std::sqrt(fmax_(cc, 0.0));
+        double uu = b.W(i, j, k, 1) / w0;
+        double uv = b.W(i, j, k, 2) / w0;
+        double uw = b.W(i, j, k, 3) / w0;
+        double dtv = 0.0;
+        if (ns) {  // timestep.f90:141-145
+          double fmue = P.viscl / P.prlmean;
+          double f1 = 4.0 / w0 / 3.0;
+          double f2 = gamma / w0;
+          double fac = fmax_(f1, f2);
+          dtv = fac * fmue / b.vol;
+        }
+        double sx, sy, sz, qs, ds, cs;
+        sx = 0.5 * (b.si[0] + b.si[0]);
+        sy = 0.5 * (b.si[1] + b.si[1]);
+        sz = 0.5 * (b.si[2] + b.si[2]);
+        qs = std::fabs(uu * sx + uv * sy + uw * sz);
+        ds = sx * sx + sy * sy + sz * sz;
+        cs = cc * std::sqrt(ds);
+        double ri = qs + cs, rvi = dtv * ds;
+        sx = 0.5 * (b.sj[0] + b.sj[0]);
+        sy = 0.5 * (b.sj[1] + b.sj[1]);
+        sz = 0.5 * (b.sj[2] + b.sj[2]);
+        qs = std::fabs(uu * sx + uv * sy + uw * sz);
+        ds = sx * sx + sy * sy + sz * sz;
+        cs = cc * std::sqrt(ds);
+        double rj = qs + cs, rvj = dtv * ds;
+        sx = 0.5 * (b.sk[0] + b.sk[0]);
+        sy = 0.5 * (b.sk[1] + b.sk[1]);
+        sz = 0.5 * (b.sk[2] + b.sk[2]);
+        qs = std::fabs(uu * sx + uv * sy + uw * sz);
+        ds = sx * sx + sy * sy + sz * sz;
+        cs = cc * std::sqrt(ds);
+        double rk = qs + cs, rvk = dtv * ds;
+        size_t cidx = b.I(i, j, k);
+        b.radi[cidx] = ri;
+        b.radj[cidx] = rj;
+        b.radk[cidx] = rk;
+        double fict;
+        if (ns)
+          fict = b.vol / (ri + rj + rk + cfac * (rvi + rvj + rvk));  // timestep.f90:177-178
+        else
+          fict = b.vol / (ri + rj + rk);  // timestep.f90:85
+        // execmode == 0 (steady): vdtim = fict (timestep.f90:88-92)
+        double vd = fict;
+        double pc = b.P(i, j, k);
+        double pip = b.P(i + 1, j, k), pim = b.P(i - 1, j, k);
+        double pjp = b.P(i, j + 1, k), pjm = b.P(i, j - 1, k);
+        double pkp = b.P(i, j, k + 1), pkm = b.P(i, j, k - 1);
+        double dpi = std::fabs((pip - 2.0 * pc + pim) / (pip + 2.0 * pc + pim + plim));
+        double dpj = std::fabs((pjp - 2.0 * pc + pjm) / (pjp + 2.0 * pc + pjm + plim));
+        double dpk = std::fabs((pkp - 2.0 * pc + pkm) / (pkp + 2.0 * pc + pkm + plim));
+        double r = 1.0 / (1.0 + fmin_(fdim_(cfl, 1.0), 2.0 * (dpi + dpj + dpk * (1.0 - i2d))));
+        vd = vd * r;  // timestep.f90:108-109
+        b.vdtim[cidx] = vd;
+        if (vd < dtmin) dtmin = vd;  // timestep.f90:112
+      }
+  if (bad) return fail(c, MGE_ENEGPRESS, "timestep: negative or NaN c^2 (timestep.f90:45-48)");
+  b.dtim = dtmin;
+  // zero blanked cells, timestep.f90:212-223
+  for (size_t q = 0; q < b.N; q++)
+    if (b.blank[q] == 0) {
+      b.vdtim[q] = 0.0;
+      b.radi[q] = 0.0;
+      b.radj[q] = 0.0;
+      b.radk[q] = 0.0;
+    }
+  // ghost copies, timestep.f90:227-282
+  std::vector<double>* R[3] = {&b.radi, &b.radj, &b.radk};
+  for (int i = 0; i <= b.ib; i++)
+    for (int j = 0; j <= b.jb; j++)
+      for (int t = 0; t < 3; t++) {
+        std::vector<double>& a = *R[t];
+        a[b.I(i, j, 0)] = a[b.I(i, j, 2)];
+        a[b.I(i, j, 1)] = a[b.I(i, j, 2)];
+        a[b.I(i, j, b.ke)] = a[b.I(i, j, b.kl)];
+        a[b.I(i, j, b.kb)] = a[b.I(i, j, b.kl)];
+      }
+  for (int j = 2; j <= b.jl; j++)
+    for (int k = 0; k <= b.kb; k++)
+      for (int t = 0; t < 3; t++) {
+        std::vector<double>& a = *R[t];
+        a[b.I(0, j, k)] = a[b.I(2, j, k)];
+        a[b.I(1, j, k)] = a[b.I(2, j, k)];
+        a[b.I(b.ie, j, k)] = a[b.I(b.il, j, k)];
+        a[b.I(b.ib, j, k)] = a[b.I(b.il, j, k)];
+      }
+  for (int i = 2; i <= b.il; i++)
+    for (int k = 2; k <= b.kl; k++)
+      for (int t = 0; t < 3; t++) {
+        std::vector<double>& a = *R[t];
+        a[b.I(i, 0, k)] = a[b.I(i, 2, k)];
+        a[b.I(i, 1, k)] = a[b.I(i, 2, k)];
+        a[b.I(i, b.je, k)] = a[b.I(i, b.jl, k)];
+        a[b.I(i, b.jb, k)] = a[b.I(i, b.jl, k)];
+      }
+  // IRS coefficients, timestep.f90:286-309 (used only by the psmoo variant).
+  // min/max follow the NaN-ignoring fmin/fmax convention (0/0 at blanked cells).
+  if (P.smoo > 0.0) {
+    double cflrat = std::sqrt(1.0 + 4.0 * P.smoo);
+    for (int k = 2; k <= b.kl; k++)
+      for (int j = 2; j <= b.jl; j++)
+        for (int i = 2; i <= b.il; i++) {
+          size_t q = b.I(i, j, k);
+          double ri = b.radi[q], rj = b.radj[q], rk = b.radk[q];
+          double reval, ex, t;
+          reval = rj / ri + rk / ri;
+          t = cflrat / (1.0 + 0.0625 * reval);
+          ex = 0.25 * (t * t - 1.0);
+          ex = std::fmin(P.smoo, ex);
+          b.epsx[q] = std::fmax(0.0, ex);
+          reval = rk / rj + ri / rj;
+          t = cflrat / (1.0 + 0.0625 * reval);
+          ex = 0.25 * (t * t - 1.0);
+          ex = std::fmin(P.smoo, ex);
+          b.epsy[q] = std::fmax(0.0, ex);
+          reval = ri / rk + rj / rk;
+          t = cflrat / (1.0 + 0.0625 * reval);
+          ex = 0.25 * (t * t - 1.0);
+          ex = std::fmin(P.smoo, ex);
+          b.epsz[q] = std::fmax(0.0, ex);
+        }
+  }
+  return MGE_OK;
+}
+
+/* ------------------------------------------------------------------ eflux.f90 + efluxb.f90 */
+int eflux(mgeo_ctx* c, OBlock& b) {
+  const size_t N = b.N;
+  std::vector<double> efsx(5 * N, 0.0), efsy(5 * N, 0.0), efsz(5 * N, 0.0);
+  // i-direction, eflux.f90:42-58
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+  for (int k = 2; k <= b.kl; k++)
+    for (int j = 2; j <= b.jl; j++)
+      for (int i = 2; i <= b.ie; i++) {
+        double w1[5], w2[5], f1[5], f2[5];
+        getw(b, i, j, k, w1);
+        getw(b, i - 1, j, k, w2);
+        ceflux(w1, b.P(i, j, k), b.si, f1);
+        ceflux(w2, b.P(i - 1, j, k), b.si, f2);
+        for (int v = 0; v < 5; v++) efsx[v * N + b.I(i, j, k)] = 0.5 * (f1[v] + f2[v]);
+      }
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+  for (int k = 2; k <= b.kl; k++)
+    for (int j = 2; j <= b.jl; j++)
+      for (int i = 2; i <= b.il; i++)
+        for (int v = 0; v < 5; v++)
+          b.DW(i, j, k, v) = efsx[v * N + b.I(i, j, k)] - efsx[v * N + b.I(i + 1, j, k)];
+  // j-direction (i2d == 0 always, input_param.f90:42), eflux.f90:61-79
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+  for (int k = 2; k <= b.kl; k++)
+    for (int j = 2; j <= b.je; j++)
+      for (int i = 2; i <= b.il; i++) {
+        double w1[5], w2[5], f1[5], f2[5];
+        getw(b, i, j, k, w1);
+        getw(b, i, j - 1, k, w2);
+        ceflux(w1, b.P(i, j, k), b.sj, f1);
+        ceflux(w2, b.P(i, j - 1, k), b.sj, f2);
+        for (int v = 0; v < 5; v++) efsy[v * N + b.I(i, j, k)] = 0.5 * (f1[v] + f2[v]);
+      }
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+  for (int k = 2; k <= b.kl; k++)
+    for (int j = 2; j <= b.jl; j++)
+      for (int i = 2; i <= b.il; i++)
+        for (int v = 0; v < 5; v++)
+          b.DW(i, j, k, v) = b.DW(i, j, k, v) + efsy[v * N + b.I(i, j, k)] - efsy[v * N + b.I(i, j + 1, k)];
+  // k-direction, eflux.f90:82-98
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+  for (int k = 2; k <= b.ke; k++)
+    for (int j = 2; j <= b.jl; j++)
+      for (int i = 2; i <= b.il; i++) {
+        double w1[5], w2[5], f1[5], f2[5];
+        getw(b, i, j, k, w1);
+        getw(b, i, j, k - 1, w2);
+        ceflux(w1, b.P(i, j, k), b.sk, f1);
+        ceflux(w2, b.P(i, j, k - 1), b.sk, f2);
+        for (int v = 0; v < 5; v++) efsz[v * N + b.I(i, j, k)] = 0.5 * (f1[v] + f2[v]);
+      }
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+  for (int k = 2; k <= b.kl; k++)
+    for (int j = 2; j <= b.jl; j++)
+      for (int i = 2; i <= b.il; i++)
+        for (int v = 0; v < 5; v++)
+          b.DW(i, j, k, v) = b.DW(i, j, k, v) + efsz[v * N + b.I(i, j, k)] - efsz[v * N + b.I(i, j, k + 1)];
+
+  // efluxb.f90:30-114, records in order
+  for (size_t m = 0; m < b.z.size(); m++) {
+    ORec& t = b.z[m];
+    int id = t.faceid, zz = t.zz;
+    int i = t.ccid[0], j = t.ccid[1], k = t.ccid[2];
+    const double* sc = zz == 1 ? b.si : (zz == 2 ? b.sj : b.sk);  // uniform block: si(icut) == si(isol)
+    const double* ss = sc;
+    if (std::fabs(b.W(i, j, k, 0)) < 1.0e-8)  // efluxb.f90:61-64
+      return fail(c, MGE_EZERORHO, "efluxb: zero density at a cut cell (efluxb.f90:61-64)");
+    double wc[5], f1[5], f2[5], f3[5], fs[5], fa[5], wn[5];
+    getw(b, i, j, k, wc);
+    ceflux(wc, b.P(i, j, k), sc, f1);
+    ceflux(t.wsol, t.psol, ss, f2);
+    for (int v = 0; v < 5; v++) fs[v] = 0.5 * (f1[v] + f2[v]);
+    std::vector<double>* E = zz == 1 ? &efsx : (zz == 2 ? &efsy : &efsz);
+    int di = zz == 1, dj = zz == 2, dk = zz == 3;
+    for (int v = 0; v < 5; v++)
+      b.DW(i, j, k, v) = b.DW(i, j, k, v) - ((*E)[v * N + b.I(i, j, k)] - (*E)[v * N + b.I(i + di, j + dj, k + dk)]);
+    if (id == 4 || id == 5 || id == 6) {  // solid on the + side: keep the - face
+      getw(b, i - di, j - dj, k - dk, wn);
+      ceflux(wn, b.P(i - di, j - dj, k - dk), sc, f3);
+      for (int v = 0; v < 5; v++) {
+        fa[v] = 0.5 * (f1[v] + f3[v]);
+        b.DW(i, j, k, v) = b.DW(i, j, k, v) + fa[v] - fs[v];
+      }
+    } else if (id == 1 || id == 2 || id == 3) {  // solid on the - side: keep the + face
+      getw(b, i + di, j + dj, k + dk, wn);
+      ceflux(wn, b.P(i + di, j + dj, k + dk), sc, f3);
+      for (int v = 0; v < 5; v++) {
+        fa[v] = 0.5 * (f1[v] + f3[v]);
+        b.DW(i, j, k, v) = b.DW(i, j, k, v) + fs[v] - fa[v];
+      }
+    }
+  }
+  return MGE_OK;
+}
+
+/* dflux_matrix, dflux.f90:283-339 (ff may alias dw, as in dfluxb) */
+void dflux_matrix(double gamma, const double* u1, const double* u2, const double* dw, const double* ss,
+                  double* ff) {
+  double gam1 = gamma - 1.0, epsn = 1.0, epsl = 1.0;
+  double rr = 0.5 * (u1[0] + u2[0]);
+  double us[3];
+  for (int q = 0; q < 3; q++) us[q] = 0.5 * (u1[q + 1] + u2[q + 1]) / rr;
+  double ee = 0.5 * (u1[4] + u2[4]) / rr;
+  double qq = 0.5 * (us[0] * us[0] + us[1] * us[1] + us[2] * us[2]);
+  double c2 = gamma * gam1 * (ee - qq);
+  double hh = c2 / gam1 + qq;
+  double sss = ss[0] * ss[0] + ss[1] * ss[1] + ss[2] * ss[2];
+  double cs = std::sqrt(c2 * sss);
+  double qn = ss[0] * us[0] + ss[1] * us[1] + ss[2] * us[2];
+  double e0 = std::fabs(qn) + cs;
+  double e1 = fmax_(epsn * e0, std::fabs(qn + cs));
+  double e2 = fmax_(epsn * e0, std::fabs(qn - cs));
+  double e3 = fmax_(epsl * e0, std::fabs(qn));
+  double s1 = 0.5 * (e1 + e2), s2 = 0.5 * (e1 - e2), s3 = e3;
+  double ak1 = (s1 - s3) / c2 * gam1;
+  double ak2 = s2 / cs;
+  double ak3 = c2 / gam1 / sss;
+  double d0 = dw[0], d1 = dw[1], d2 = dw[2], d3 = dw[3], d4 = dw[4];
+  double vd = qq * d0 - us[0] * d1 - us[1] * d2 - us[2] * d3 + d4;
+  double qd = qn * d0 - ss[0] * d1 - ss[1] * d2 - ss[2] * d3;
+  ff[0] = ak1 * vd - ak2 * qd + s3 * d0;
+  ff[1] = ak1 * (us[0] * vd - ss[0] * ak3 * qd) + ak2 * (gam1 * ss[0] * vd - us[0] * qd) + s3 * d1;
+  ff[2] = ak1 * (us[1] * vd - ss[1] * ak3 * qd) + ak2 * (gam1 * ss[1] * vd - us[1] * qd) + s3 * d2;
+  ff[3] = ak1 * (us[2] * vd - ss[2] * ak3 * qd) + ak2 * (gam1 * ss[2] * vd - us[2] * qd) + s3 * d3;
+  ff[4] = ak1 * (hh * vd - qn * ak3 * qd) + ak2 * (gam1 * qn * vd - hh * qd) + s3 * d4;
+}
+
+/* dfluxb.f90:29-423 for one record; w(:,5) holds the enthalpy while called */
+void dfluxb_rec(mgeo_ctx* c, OBlock& b, int istage, const ORec& t, const std::vector<double>& dfsx,
+                const std::vector<double>& dfsy, const std::vector<double>& dfsz) {
+  const mge_params& P = c->prm;
+  const size_t N = b.N;
+  const double cd = P.cdis[istage - 1];
+  const bool scalar = P.dissip == MGE_DISSIP_SCALAR;
+  int id = t.faceid, zz = t.zz;
+  int i = t.ccid[0], j = t.ccid[1], k = t.ccid[2];
+  double psol = t.psol;
+  double wsol[5];
+  for (int v = 0; v < 5; v++) wsol[v] = t.wsol[v];
+  wsol[4] = wsol[4] + psol;  // dfluxb.f90:38
+  double fp[3], ep, lm, lp, lam, dis2, dis4;
+  double diw[3][5], fs1[5], fs2[5];
+  auto pp = [&](int a) -> double {  // p along the record axis at offset a from the cut cell
+    return zz == 1 ? b.P(i + a, j, k) : (zz == 2 ? b.P(i, j + a, k) : b.P(i, j, k + a));
+  };
+  auto ww = [&](int a, int v) -> double {
+    return zz == 1 ? b.W(i + a, j, k, v) : (zz == 2 ? b.W(i, j + a, k, v) : b.W(i, j, k + a, v));
+  };
+  auto lamc = [&](int a) -> double {
+    return zz == 1 ? b.LAM(i + a, j, k) : (zz == 2 ? b.LAM(i, j + a, k) : b.LAM(i, j, k + a));
+  };
+  const std::vector<double>& D = zz == 1 ? dfsx : (zz == 2 ? dfsy : dfsz);
+  auto dd = [&](int a, int v) -> double {
+    size_t q = zz == 1 ? b.I(i + a, j, k) : (zz == 2 ? b.I(i, j + a, k) : b.I(i, j, k + a));
+    return D[v * N + q];
+  };
+  auto fwr = [&](int a, int v) -> double& {
+    size_t q = zz == 1 ? b.I(i + a, j, k) : (zz == 2 ? b.I(i, j + a, k) : b.I(i, j, k + a));
+    return b.fw[v * N + q];
+  };
+  const double* s_lo = zz == 1 ? b.si : (zz == 2 ? b.sj : b.sk);  // uniform: s(i) == s(i+1)
+  const int lim = zz == 1 ? b.ib : (zz == 2 ? b.jb : b.kb);
+  const int pos = zz == 1 ? i : (zz == 2 ? j : k);
+  auto setdis = [&]() {
+    dis2 = P.vis2 * ep;
+    dis4 = P.vis4;
+    dis4 = fdim_(dis4, dis2);
+    dis2 = dis2 * cd;
+    dis4 = dis4 * cd;
+  };
+  if (id == 4 || id == 5 || id == 6) {
+    for (int v = 0; v < 5; v++) {
+      fwr(0, v) = fwr(0, v) - (dd(0, v) - dd(1, v));
+      fwr(-1, v) = fwr(-1, v) - (dd(-1, v) - dd(0, v));
+    }
+    // the three axes write the same sensors with different operand orders
+    if (zz == 1) {
+      fp[0] = std::fabs(pp(-2) - 2.0 * pp(-1) + pp(0)) / std::fabs(pp(-2) + 2.0 * pp(-1) + pp(0));
+      fp[1] = std::fabs(pp(-1) - 2.0 * pp(0) + psol) / std::fabs(pp(-1) + 2.0 * pp(0) + psol);
+    } else {
+      fp[0] = std::fabs(pp(0) - 2.0 * pp(-1) + pp(-2)) / std::fabs(pp(0) + 2.0 * pp(-1) + pp(-2));
+      fp[1] = std::fabs(psol - 2.0 * pp(0) + pp(-1)) / std::fabs(psol + 2.0 * pp(0) + pp(-1));
+    }
+    ep = fmax_(fp[0], fp[1]);
+    lm = lamc(0);
+    lam = lm;
+    setdis();
+    for (int v = 0; v < 5; v++) {
+      diw[0][v] = ww(0, v) - ww(-1, v);
+      diw[1][v] = wsol[v] - ww(0, v);
+      diw[2][v] = diw[1][v];
+      fs2[v] = diw[2][v] - 2.0 * diw[1][v] + diw[0][v];
+      fs2[v] = dis2 * diw[1][v] - dis4 * fs2[v];
+    }
+    if (scalar) {
+      for (int v = 0; v < 5; v++) fs2[v] = fs2[v] * lam;
+    } else {
+      double wc[5];
+      for (int v = 0; v < 5; v++) wc[v] = ww(0, v);
+      dflux_matrix(P.gamma, wc, wsol, fs2, s_lo, fs2);
+    }
+    if (pos - 3 >= 0)
+      fp[2] = std::fabs(pp(-1) - 2.0 * pp(-2) + pp(-3)) / std::fabs(pp(-1) + 2.0 * pp(-2) + pp(-3));
+    else
+      fp[2] = 0.0;
+    ep = fmax_(fmax_(fp[0], fp[1]), fp[2]);
+    lm = lamc(-1);
+    lp = lamc(0);
+    lam = 0.5 * (lm + lp);
+    setdis();
+    for (int v = 0; v < 5; v++) {
+      diw[0][v] = ww(-1, v) - ww(-2, v);
+      diw[1][v] = ww(0, v) - ww(-1, v);
+      diw[2][v] = wsol[v] - ww(0, v);
+      fs1[v] = diw[2][v] - 2.0 * diw[1][v] + diw[0][v];
+      fs1[v] = dis2 * diw[1][v] - dis4 * fs1[v];
+    }
+    if (scalar) {
+      for (int v = 0; v < 5; v++) fs1[v] = fs1[v] * lam;
+    } else {
+      double wa[5], wc[5];
+      for (int v = 0; v < 5; v++) {
+        wa[v] = ww(-1, v);
+        wc[v] = ww(0, v);
+      }
+      dflux_matrix(P.gamma, wa, wc, fs1, s_lo, fs1);
+    }
+    for (int v = 0; v < 5; v++) {
+      fwr(0, v) = fwr(0, v) + (fs1[v] - fs2[v]);
+      fwr(-1, v) = fwr(-1, v) + (dd(-1, v) - fs1[v]);
+    }
+  } else if (id == 1 || id == 2 || id == 3) {
+    for (int v = 0; v < 5; v++) {
+      fwr(0, v) = fwr(0, v) - (dd(0, v) - dd(1, v));
+      fwr(1, v) = fwr(1, v) - (dd(1, v) - dd(2, v));
+    }
+    fp[0] = std::fabs(pp(1) - 2.0 * pp(0) + psol) / std::fabs(pp(1) + 2.0 * pp(0) + psol);
+    fp[1] = std::fabs(pp(2) - 2.0 * pp(1) + pp(0)) / std::fabs(pp(2) + 2.0 * pp(1) + pp(0));
+    if (pos + 3 <= lim)
+      fp[2] = std::fabs(pp(3) - 2.0 * pp(2) + pp(1)) / std::fabs(pp(3) + 2.0 * pp(2) + pp(1));
+    else
+      fp[2] = 0.0;
+    ep = fmax_(fmax_(fp[0], fp[1]), fp[2]);
+    lm = lamc(0);
+    lp = lamc(1);
+    lam = 0.5 * (lm + lp);
+    setdis();
+    for (int v = 0; v < 5; v++) {
+      diw[0][v] = ww(0, v) - wsol[v];
+      diw[1][v] = ww(1, v) - ww(0, v);
+      diw[2][v] = ww(2, v) - ww(1, v);
+      fs2[v] = diw[2][v] - 2.0 * diw[1][v] + diw[0][v];
+      fs2[v] = dis2 * diw[1][v] - dis4 * fs2[v];
+    }
+    if (scalar) {
+      for (int v = 0; v < 5; v++) fs2[v] = fs2[v] * lam;
+    } else {
+      double wc[5], wb[5];
+      for (int v = 0; v < 5; v++) {
+        wc[v] = ww(0, v);
+        wb[v] = ww(1, v);
+      }
+      dflux_matrix(P.gamma, wc, wb, fs2, s_lo, fs2);
+    }
+    ep = fmax_(fp[0], fp[1]);
+    lp = lamc(0);
+    lam = lp;
+    setdis();
+    for (int v = 0; v < 5; v++) {
+      diw[1][v] = ww(0, v) - wsol[v];
+      diw[0][v] = diw[1][v];
+      diw[2][v] = ww(1, v) - ww(0, v);
+      fs1[v] = diw[2][v] - 2.0 * diw[1][v] + diw[0][v];
+      fs1[v] = dis2 * diw[1][v] - dis4 * fs1[v];
+    }
+    if (scalar) {
+      for (int v = 0; v < 5; v++) fs1[v] = fs1[v] * lam;
+    } else {
+      double wc[5];
+      for (int v = 0; v < 5; v++) wc[v] = ww(0, v);
+      dflux_matrix(P.gamma, wsol, wc, fs1, s_lo, fs1);
+    }
+    for (int v = 0; v < 5; v++) {
+      fwr(0, v) = fwr(0, v) + (fs1[v] - fs2[v]);
+      fwr(1, v) = fwr(1, v) + (fs2[v] - dd(2, v));
+    }
+  }
+}
+
+/* ------------------------------------------------------------------ dflux.f90:1-281 */
+int dflux(mgeo_ctx* c, OBlock& b, int istage) {
+  const mge_params& P = c->prm;
+  const double cd = P.cdis[istage - 1];
+  if (cd <= 0.0) return MGE_OK;
+  const bool scalar = P.dissip == MGE_DISSIP_SCALAR;
+  if (P.dissip != MGE_DISSIP_SCALAR && P.dissip != MGE_DISSIP_MATRIX)
+    return fail(c, MGE_EBADCFG, "dissip must be scalar or matrix (dflux.f90:107)");
+  const size_t N = b.N;
+  const int mx = std::max(b.ib, std::max(b.jb, b.kb));
+  std::vector<double> dfsx(5 * N, 0.0), dfsy(5 * N, 0.0), dfsz(5 * N, 0.0), we(N);
+  // replace energy by enthalpy, dflux.f90:58-65
+  for (size_t q = 0; q < N; q++) {
+    we[q] = b.w[4 * N + q];
+    b.w[4 * N + q] = b.w[4 * N + q] + b.p[q];
+  }
+  auto face = [&](double ep, double lm, double lp, const double* dm, const double* d0, const double* dp1,
+                  const double* wl, const double* wr, const double* ss, double* out) {
+    double lam = 0.5 * (lm + lp);
+    double dis2 = P.vis2 * ep;
+    double dis4 = P.vis4;
+    dis4 = fdim_(dis4, dis2);
+    dis2 = dis2 * cd;
+    dis4 = dis4 * cd;
+    for (int v = 0; v < 5; v++) {
+      double t = dp1[v] - 2.0 * d0[v] + dm[v];
+      out[v] = dis2 * d0[v] - dis4 * t;
+    }
+    if (scalar) {
+      for (int v = 0; v < 5; v++) out[v] = out[v] * lam;
+    } else {
+      double fs[5];
+      dflux_matrix(P.gamma, wl, wr, out, ss, fs);
+      for (int v = 0; v < 5; v++) out[v] = fs[v];
+    }
+  };
+  // i-direction, dflux.f90:68-124
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+  for (int k = 2; k <= b.kl; k++)
+    for (int j = 2; j <= b.jl; j++) {
+      std::vector<double> fp(mx + 1, 0.0), diw((mx + 1) * 5, 0.0);
+      for (int i = 1; i <= b.ie; i++) {
+        double pb = std::fabs(b.P(i - 1, j, k) + 2.0 * b.P(i, j, k) + b.P(i + 1, j, k));
+        if (std::fabs(pb) > 0.0)
+          fp[i] = std::fabs(b.P(i - 1, j, k) - 2.0 * b.P(i, j, k) + b.P(i + 1, j, k)) / pb;
+        else
+          fp[i] = 0.0;
+      }
+      fp[0] = 0.0;
+      fp[b.ib] = 0.0;
+      for (int i = 2; i <= b.ie; i++)
+        for (int v = 0; v < 5; v++) diw[i * 5 + v] = b.W(i, j, k, v) - b.W(i - 1, j, k, v);
+      for (int v = 0; v < 5; v++) {
+        diw[1 * 5 + v] = diw[2 * 5 + v];
+        diw[b.ib * 5 + v] = diw[b.ie * 5 + v];
+      }
+      for (int i = 2; i <= b.ie; i++) {
+        double ep = fmax_(fmax_(fmax_(fp[i - 2], fp[i - 1]), fp[i]), fp[i + 1]);
+        double out[5], wl[5], wr[5];
+        getw(b, i - 1, j, k, wl);
+        getw(b, i, j, k, wr);
+        face(ep, b.LAM(i - 1, j, k), b.LAM(i, j, k), &diw[(i - 1) * 5], &diw[i * 5], &diw[(i + 1) * 5], wl, wr,
+             b.si, out);
+        for (int v = 0; v < 5; v++) dfsx[v * N + b.I(i, j, k)] = out[v];
+      }
+    }
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+  for (int k = 2; k <= b.kl; k++)
+    for (int j = 2; j <= b.jl; j++)
+      for (int i = 2; i <= b.il; i++)
+        for (int v = 0; v < 5; v++)
+          b.FW(i, j, k, v) = b.FW(i, j, k, v) + (dfsx[v * N + b.I(i, j, k)] - dfsx[v * N + b.I(i + 1, j, k)]);
+  // j-direction, dflux.f90:127-182
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+  for (int k = 2; k <= b.kl; k++)
+    for (int i = 2; i <= b.il; i++) {
+      std::vector<double> fp(mx + 1, 0.0), diw((mx + 1) * 5, 0.0);
+      for (int j = 1; j <= b.je; j++) {
+        double pb = std::fabs(b.P(i, j + 1, k) + 2.0 * b.P(i, j, k) + b.P(i, j - 1, k));
+        if (std::fabs(pb) > 0.0)
+          fp[j] = std::fabs(b.P(i, j + 1, k) - 2.0 * b.P(i, j, k) + b.P(i, j - 1, k)) / pb;
+        else
+          fp[j] = 0.0;
+      }
+      fp[0] = 0.0;
+      fp[b.jb] = 0.0;
+      for (int j = 2; j <= b.je; j++)
+        for (int v = 0; v < 5; v++) diw[j * 5 + v] = b.W(i, j, k, v) - b.W(i, j - 1, k, v);
+      for (int v = 0; v < 5; v++) {
+        diw[1 * 5 + v] = diw[2 * 5 + v];
+        diw[b.jb * 5 + v] = diw[b.je * 5 + v];
+      }
+      for (int j = 2; j <= b.je; j++) {
+        double ep = fmax_(fmax_(fmax_(fp[j - 2], fp[j - 1]), fp[j]), fp[j + 1]);
+        double out[5], wl[5], wr[5];
+        getw(b, i, j - 1, k, wl);
+        getw(b, i, j, k, wr);
+        face(ep, b.LAM(i, j - 1, k), b.LAM(i, j, k), &diw[(j - 1) * 5], &diw[j * 5], &diw[(j + 1) * 5], wl, wr,
+             b.sj, out);
+        for (int v = 0; v < 5; v++) dfsy[v * N + b.I(i, j, k)] = out[v];
+      }
+    }
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+  for (int k = 2; k <= b.kl; k++)
+    for (int j = 2; j <= b.jl; j++)
+      for (int i = 2; i <= b.il; i++)
+        for (int v = 0; v < 5; v++)
+          b.FW(i, j, k, v) = b.FW(i, j, k, v) + (dfsy[v * N + b.I(i, j, k)] - dfsy[v * N + b.I(i, j + 1, k)]);
+  // k-direction, dflux.f90:185-238
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+  for (int i = 2; i <= b.il; i++)
+    for (int j = 2; j <= b.jl; j++) {
+      std::vector<double> fp(mx + 1, 0.0), diw((mx + 1) * 5, 0.0);
+      for (int k = 1; k <= b.ke; k++) {
+        double pb = std::fabs(b.P(i, j, k - 1) + 2.0 * b.P(i, j, k) + b.P(i, j, k + 1));
+        if (std::fabs(pb) > 0.0)
+          fp[k] = std::fabs(b.P(i, j, k - 1) - 2.0 * b.P(i, j, k) + b.P(i, j, k + 1)) / pb;
+        else
+          fp[k] = 0.0;
+      }
+      fp[0] = 0.0;
+      fp[b.kb] = 0.0;
+      for (int k = 2; k <= b.ke; k++)
+        for (int v = 0; v < 5; v++) diw[k * 5 + v] = b.W(i, j, k, v) - b.W(i, j, k - 1, v);
+      for (int v = 0; v < 5; v++) {
+        diw[1 * 5 + v] = diw[2 * 5 + v];
+        diw[b.kb * 5 + v] = diw[b.ke * 5 + v];
+      }
+      for (int k = 2; k <= b.ke; k++) {
+        double ep = fmax_(fmax_(fmax_(fp[k - 2], fp[k - 1]), fp[k]), fp[k + 1]);
+        double out[5], wl[5], wr[5];
+        getw(b, i, j, k - 1, wl);
+        getw(b, i, j, k, wr);
+        face(ep, b.LAM(i, j, k - 1), b.LAM(i, j, k), &diw[(k - 1) * 5], &diw[k * 5], &diw[(k + 1) * 5], wl, wr,
+             b.sk, out);
+        for (int v = 0; v < 5; v++) dfsz[v * N + b.I(i, j, k)] = out[v];
+      }
+    }
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+  for (int k = 2; k <= b.kl; k++)
+    for (int j = 2; j <= b.jl; j++)
+      for (int i = 2; i <= b.il; i++)
+        for (int v = 0; v < 5; v++)
+          b.FW(i, j, k, v) = b.FW(i, j, k, v) + (dfsz[v * N + b.I(i, j, k)] - dfsz[v * N + b.I(i, j, k + 1)]);
+  // cut-cell walls, dflux.f90:253
+  for (size_t m = 0; m < b.z.size(); m++) dfluxb_rec(c, b, istage, b.z[m], dfsx, dfsy, dfsz);
+  // restore the energy, dflux.f90:257-263
+  for (size_t q = 0; q < N; q++) b.w[4 * N + q] = we[q];
+  return MGE_OK;
+}
+
+/* ------------------------------------------------------------------ psmoo.f90:97-242 */
+void psmoo_old(mgeo_ctx* c, OBlock& b) {
+  const double smoo = c->prm.smoo;
+  if (smoo <= 0.0) return;
+  const int ilm = b.nx, jlm = b.ny, klm = b.nz, il = b.il, jl = b.jl, kl = b.kl;
+  std::vector<double> ex1(il + 1), ex2(il + 1), ey1(jl + 1), ey2(jl + 1), ez1(kl + 1), ez2(kl + 1);
+  const double aa = 1.0 + 2.0 * smoo, bb = -smoo;
+  auto pivots = [&](std::vector<double>& e1, std::vector<double>& e2, int lm, int l) {
+    e1[2] = aa;
+    e2[2] = bb / aa;
+    for (int q = 3; q <= lm; q++) {
+      e1[q] = aa - bb * e2[q - 1];
+      e2[q] = bb / e1[q];
+    }
+    e1[l] = aa - bb * e2[lm];
+  };
+  pivots(ex1, ex2, ilm, il);
+  pivots(ey1, ey2, jlm, jl);
+  pivots(ez1, ez2, klm, kl);
+  const size_t N = b.N;
+  for (int n = 0; n < 5; n++) {
+    double* d = &b.dw[n * N];
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+    for (int k = 2; k <= kl; k++) {
+      for (int j = 2; j <= jl; j++) {  // i-direction, psmoo.f90:173-188
+        if (b.BL(2, j, k) != 0) d[b.I(2, j, k)] = d[b.I(2, j, k)] / ex1[2];
+        for (int i = 3; i <= il; i++)
+          if (b.BL(i, j, k) != 0) d[b.I(i, j, k)] = (d[b.I(i, j, k)] - bb * d[b.I(i - 1, j, k)]) / ex1[i];
+        for (int i = 2; i <= ilm; i++) {
+          int ir = il + 1 - i;
+          if (b.BL(ir, j, k) != 0) d[b.I(ir, j, k)] = d[b.I(ir, j, k)] - ex2[ir] * d[b.I(ir + 1, j, k)];
+        }
+      }
+      for (int i = 2; i <= il; i++) {  // j-direction, psmoo.f90:191-206
+        if (b.BL(i, 2, k) != 0) d[b.I(i, 2, k)] = d[b.I(i, 2, k)] / ey1[2];
+        for (int j = 3; j <= jl; j++)
+          if (b.BL(i, j, k) != 0) d[b.I(i, j, k)] = (d[b.I(i, j, k)] - bb * d[b.I(i, j - 1, k)]) / ey1[j];
+        for (int j = 2; j <= jlm; j++) {
+          int jr = jl + 1 - j;
+          if (b.BL(i, jr, k) != 0) d[b.I(i, jr, k)] = d[b.I(i, jr, k)] - ey2[jr] * d[b.I(i, jr + 1, k)];
+        }
+      }
+    }
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+    for (int j = 2; j <= jl; j++) {  // k-direction, psmoo.f90:211-237
+      for (int i = 2; i <= il; i++)
+        if (b.BL(i, j, 2) != 0) d[b.I(i, j, 2)] = d[b.I(i, j, 2)] / ez1[2];
+      for (int k = 3; k <= kl; k++)
+        for (int i = 2; i <= il; i++)
+          if (b.BL(i, j, k) != 0) d[b.I(i, j, k)] = (d[b.I(i, j, k)] - bb * d[b.I(i, j, k - 1)]) / ez1[k];
+      for (int k = 2; k <= klm; k++) {
+        int kr = kl + 1 - k;
+        for (int i = 2; i <= il; i++)
+          if (b.BL(i, j, kr) != 0) d[b.I(i, j, kr)] = d[b.I(i, j, kr)] - ez2[kr] * d[b.I(i, j, kr + 1)];
+      }
+    }
+  }
+}
+
+/* progon3.f90:41-60: cyclic tridiagonal sweep */
+void progon3(const double* a, const double* bq, const double* cq, const double* d, double* x, int n) {
+  std::vector<double> w(n + 2), s(n + 2), t(n + 2), u(n + 2), v(n + 2);
+  // Fortran 1-based arrays: element q of a Fortran array is a[q-1]
+  u[1] = 0.0;
+  v[1] = 0.0;
+  w[1] = 1.0;
+  for (int i = 1; i <= n; i++) {
+    int i1 = i + 1;
+    double z = 1.0 / (a[i - 1] + cq[i - 1] * v[i]);
+    v[i1] = -bq[i - 1] * z;
+    u[i1] = (-cq[i - 1] * u[i] + d[i - 1]) * z;
+    w[i1] = -cq[i - 1] * w[i] * z;
+  }
+  s[n] = 1.0;
+  t[n] = 0.0;
+  for (int i = n - 1; i >= 1; i--) {
+    s[i] = v[i + 1] * s[i + 1] + w[i + 1];
+    t[i] = v[i + 1] * t[i + 1] + u[i + 1];
+  }
+  x[n - 1] = (d[n - 1] - bq[n - 1] * t[1] - cq[n - 1] * t[n - 1]) / (a[n - 1] + bq[n - 1] * s[1] + cq[n - 1] * s[n - 1]);
+  for (int i = 1; i <= n - 1; i++) x[i - 1] = s[i] * x[n - 1] + t[i];
+}
+
+/* psmoo.f90:1-95 (variable coefficients from timestep, progon3 lines) */
+void psmoo_var(mgeo_ctx* c, OBlock& b) {
+  if (c->prm.smoo <= 0.0) return;
+  const size_t N = b.N;
+  const int mx = std::max(b.ib, std::max(b.jb, b.kb));
+  auto line = [&](int len, auto idx, const std::vector<double>& eps) {
+    std::vector<double> aa(mx + 1), bb(mx + 1), cc(mx + 1), d(mx + 1), x(mx + 1);
+    for (int q = 2; q <= len; q++) {
+      double e = eps[idx(q)];
+      aa[q] = 1.0 + 2.0 * e;
+      bb[q] = -e;
+      cc[q] = -e;
+    }
+    bb[len] = 0.0;
+    cc[2] = 0.0;
+    for (int n = 0; n < 5; n++) {
+      for (int q = 2; q <= len; q++) d[q] = b.dw[n * N + idx(q)];
+      progon3(&aa[2], &bb[2], &cc[2], &d[2], &x[2], len - 1);
+      for (int q = 2; q <= len; q++) b.dw[n * N + idx(q)] = x[q];
+    }
+  };
+  for (int k = 2; k <= b.kl; k++)
+    for (int j = 2; j <= b.jl; j++) line(b.il, [&](int q) { return b.I(q, j, k); }, b.epsx);
+  for (int k = 2; k <= b.kl; k++)
+    for (int i = 2; i <= b.il; i++) line(b.jl, [&](int q) { return b.I(i, q, k); }, b.epsy);
+  for (int i = 2; i <= b.il; i++)
+    for (int j = 2; j <= b.jl; j++) line(b.kl, [&](int q) { return b.I(i, j, q); }, b.epsz);
+}
+
+/* ------------------------------------------------------------------ boundary conditions */
+/* bc_far.f90:42-284; face = 1..6 */
+void bc_far(mgeo_ctx* c, OBlock& b, int face) {
+  const mge_params& P = c->prm;
+  const double gamma = P.gamma, gm = 1.0 / (gamma - 1.0);
+  const double* fn = b.fnv[face - 1];
+  int ax = (face - 1) % 3;  // 0 i, 1 j, 2 k
+  int phy1, dum1, dum2;
+  int lcur = ax == 0 ? b.il : (ax == 1 ? b.jl : b.kl);
+  int ecur = lcur + 1, bcur = lcur + 2;
+  if (face <= 3) {
+    phy1 = 2;
+    dum1 = 1;
+    dum2 = 0;
+  } else {
+    phy1 = lcur;
+    dum1 = ecur;
+    dum2 = bcur;
+  }
+  const double u0[3] = {P.u0, P.v0, P.w0};
+  int na = ax == 0 ? b.jb : b.ib, nb = ax == 2 ? b.jb : b.kb;
+  // loop bounds: face 1/4 over (j,k), face 2/5 over (i,k), face 3/6 over (i,j)
+  for (int t2 = 0; t2 <= nb; t2++)
+    for (int t1 = 0; t1 <= na; t1++) {
+      auto at = [&](int q, int& i, int& j, int& k) {
+        if (ax == 0) { i = q; j = t1; k = t2; }
+        else if (ax == 1) { i = t1; j = q; k = t2; }
+        else { i = t1; j = t2; k = q; }
+      };
+      int i, j, k;
+      at(phy1, i, j, k);
+      double wp[5];
+      getw(b, i, j, k, wp);
+      double pph = b.P(i, j, k);
+      double vel_norm = (wp[1] * fn[0] + wp[2] * fn[1] + wp[3] * fn[2]) / wp[0];
+      double out[5], pout;
+      bool set = false;
+      double fnn = fn[ax];
+      if (vel_norm <= 0.0) {  // inlet
+        double rhoe = wp[0];
+        double ue = wp[1 + ax] / rhoe;
+        double pe = pph;
+        double ce = std::sqrt(gamma * pe / rhoe);
+        double rpo = ue * fnn + 2.0 * ce / (gamma - 1.0);
+        double rmi = u0[ax] * fnn - 2.0 * P.c0 / (gamma - 1.0);
+        double vv[3] = {u0[0], u0[1], u0[2]};
+        vv[ax] = 0.5 * (rpo + rmi) * fnn;
+        double ci = 0.25 * (gamma - 1.0) * (rpo - rmi);
+        double si = std::pow(P.rho0, gamma) / P.p0;
+        double cc = ci * ci / gamma;
+        double rhoi = std::pow(si * cc, gm);
+        double prei = rhoi * cc;
+        out[0] = rhoi;
+        out[1] = rhoi * vv[0];
+        out[2] = rhoi * vv[1];
+        out[3] = rhoi * vv[2];
+        out[4] = prei * gm + 0.5 * rhoi * (vv[0] * vv[0] + vv[1] * vv[1] + vv[2] * vv[2]);
+        pout = prei;
+        set = true;
+      } else if (vel_norm > 0.0) {  // outlet
+        double rhoi = wp[0];
+        double vv[3] = {wp[1] / rhoi, wp[2] / rhoi, wp[3] / rhoi};
+        double prei = pph;
+        double si = std::pow(rhoi, gamma) / prei;
+        double ci = std::sqrt(gamma * prei / rhoi);
+        double rpo = vv[ax] * fnn + 2.0 * ci / (gamma - 1.0);
+        double rmi = u0[ax] * fnn - 2.0 * P.c0 / (gamma - 1.0);
+        double ve[3] = {vv[0], vv[1], vv[2]};
+        ve[ax] = 0.5 * (rpo + rmi) * fnn;
+        double ce = 0.25 * (gamma - 1.0) * (rpo - rmi);
+        double se = si;
+        double cc = ce * ce / gamma;
+        double rhoe = std::pow(se * cc, gm);
+        double pe = rhoe * cc;
+        out[0] = rhoe;
+        out[1] = rhoe * ve[0];
+        out[2] = rhoe * ve[1];
+        out[3] = rhoe * ve[2];
+        out[4] = pe * gm + 0.5 * rhoe * (ve[0] * ve[0] + ve[1] * ve[1] + ve[2] * ve[2]);
+        pout = pe;
+        set = true;
+      }
+      int i1, j1, k1, i2, j2, k2;
+      at(dum1, i1, j1, k1);
+      at(dum2, i2, j2, k2);
+      if (set) {
+        for (int v = 0; v < 5; v++) b.W(i1, j1, k1, v) = out[v];
+        b.P(i1, j1, k1) = pout;
+      }
+      for (int v = 0; v < 5; v++) b.W(i2, j2, k2, v) = b.W(i1, j1, k1, v);
+      b.P(i2, j2, k2) = b.P(i1, j1, k1);
+    }
+}
+
+/* bc_symm.f90:27-82, bc_wall.f90:28-89, bc_periodic.f90:27-91 */
+void bc_copy_face(OBlock& b, int face, int kind) {
+  int ax = (face - 1) % 3;
+  int lcur = ax == 0 ? b.il : (ax == 1 ? b.jl : b.kl);
+  int phy1, phy2, dum1, dum2;
+  if (kind == -60) {  // periodic
+    if (face <= 3) {
+      dum1 = 1; dum2 = 0; phy1 = lcur; phy2 = lcur - 1;
+    } else {
+      phy1 = 2; phy2 = 3; dum1 = lcur + 1; dum2 = lcur + 2;
+    }
+  } else {
+    if (face <= 3) {
+      phy1 = 2; phy2 = 3; dum1 = 1; dum2 = 0;
+    } else {
+      phy1 = lcur; phy2 = lcur - 1; dum1 = lcur + 1; dum2 = lcur + 2;
+    }
+  }
+  int na = ax == 0 ? b.jb : b.ib, nb = ax == 2 ? b.jb : b.kb;
+  for (int t2 = 0; t2 <= nb; t2++)
+    for (int t1 = 0; t1 <= na; t1++) {
+      auto id = [&](int q) {
+        if (ax == 0) return b.I(q, t1, t2);
+        if (ax == 1) return b.I(t1, q, t2);
+        return b.I(t1, t2, q);
+      };
+      size_t d1 = id(dum1), d2 = id(dum2), p1 = id(phy1), p2 = id(phy2);
+      const size_t N = b.N;
+      if (kind == -50) {  // symmetry: mirror the face-normal momentum
+        for (int v = 0; v < 5; v++) b.w[v * N + d1] = b.w[v * N + p1];
+        b.w[(1 + ax) * N + d1] = -b.w[(1 + ax) * N + p1];
+        b.p[d1] = b.p[p1];
+        for (int v = 0; v < 5; v++) b.w[v * N + d2] = b.w[v * N + p2];
+        b.w[(1 + ax) * N + d2] = -b.w[(1 + ax) * N + p2];
+        b.p[d2] = b.p[p2];
+      } else if (kind == -80) {  // no-slip wall
+        b.w[0 * N + d1] = b.w[0 * N + p1];
+        b.w[4 * N + d1] = b.w[4 * N + p1];
+        for (int v = 1; v < 4; v++) b.w[v * N + d1] = -b.w[v * N + p1];
+        b.w[0 * N + d2] = b.w[0 * N + p2];
+        b.w[4 * N + d2] = b.w[4 * N + p2];
+        for (int v = 1; v < 4; v++) b.w[v * N + d2] = -b.w[v * N + p2];
+        b.p[d1] = b.p[p1];
+        b.p[d2] = b.p[p1];
+      } else {  // periodic
+        for (int v = 0; v < 5; v++) b.w[v * N + d2] = b.w[v * N + p2];
+        for (int v = 0; v < 5; v++) b.w[v * N + d1] = b.w[v * N + p1];
+        b.p[d2] = b.p[p2];
+        b.p[d1] = b.p[p1];
+      }
+    }
+}
+
+/* bc_corner.f90:23-157 */
+void bc_corner(mgeo_ctx* c, OBlock& b) {
+  const mge_params& P = c->prm;
+  const int il = b.il, jl = b.jl, kl = b.kl, ie = b.ie, je = b.je, ke = b.ke;
+  auto set3 = [&](int i, int j, int k, int ia, int ja, int ka, int ib_, int jb_, int kb_, int ic, int jc, int kc) {
+    for (int v = 0; v < 5; v++) b.W(i, j, k, v) = b.W(ia, ja, ka, v) + b.W(ib_, jb_, kb_, v) - b.W(ic, jc, kc, v);
+    depvars_cell(P, b, i, j, k);
+  };
+  for (int k = 2; k <= kl; k++) {
+    set3(1, 1, k, 2, 1, k, 1, 2, k, 2, 2, k);
+    set3(ie, 1, k, il, 1, k, ie, 2, k, il, 2, k);
+    set3(1, je, k, 2, je, k, 1, jl, k, 2, jl, k);
+    set3(ie, je, k, il, je, k, ie, jl, k, il, jl, k);
+  }
+  for (int j = 2; j <= jl; j++) {
+    set3(1, j, 1, 2, j, 1, 1, j, 2, 2, j, 2);
+    set3(ie, j, 1, il, j, 1, ie, j, 2, il, j, 2);
+    set3(1, j, ke, 2, j, ke, 1, j, kl, 2, j, kl);
+    set3(ie, j, ke, il, j, ke, ie, j, kl, il, j, kl);
+  }
+  for (int i = 0; i <= b.ib; i++) {
+    set3(i, 1, 1, i, 1, 2, i, 2, 1, i, 2, 2);
+    set3(i, 1, ke, i, 2, ke, i, 1, kl, i, 2, kl);
+    set3(i, je, 1, i, je, 1, i, jl, 2, i, jl, 2);  // bc_corner.f90:120 as written
+    set3(i, je, ke, i, jl, ke, i, je, kl, i, jl, kl);
+  }
+  auto c8 = [&](int i, int j, int k, int ia, int ja, int ka, int ib_, int jb_, int kb_, int ic, int jc, int kc, int id,
+                int jd, int kd) {
+    for (int v = 0; v < 5; v++)
+      b.W(i, j, k, v) =
+          (b.W(ia, ja, ka, v) + b.W(ib_, jb_, kb_, v) + b.W(ic, jc, kc, v)) * 2.0 / 3.0 - b.W(id, jd, kd, v);
+  };
+  c8(1, 1, 1, 2, 1, 1, 1, 2, 1, 1, 1, 2, 2, 2, 2);
+  c8(1, 1, ke, 2, 1, ke, 1, 2, ke, 1, 1, kl, 2, 2, kl);
+  c8(1, je, 1, 2, je, 1, 1, jl, 1, 1, je, 2, 2, jl, 2);
+  c8(ie, 1, 1, il, 1, 1, ie, 2, 1, ie, 1, 2, il, 2, 2);
+  c8(ie, 1, ke, il, 1, ke, ie, 2, ke, ie, 1, kl, il, 2, kl);
+  c8(ie, je, 1, il, je, 1, ie, jl, 1, ie, je, 2, il, jl, 2);
+  c8(1, je, ke, 2, je, ke, 1, jl, ke, 1, je, kl, 2, jl, kl);
+  c8(ie, je, ke, il, je, ke, ie, jl, ke, ie, je, kl, il, jl, kl);
+  depvars_cell(P, b, 1, 1, 1);
+  depvars_cell(P, b, 1, 1, ke);
+  depvars_cell(P, b, 1, je, 1);
+  depvars_cell(P, b, ie, 1, 1);
+  depvars_cell(P, b, ie, 1, ke);
+  depvars_cell(P, b, ie, je, 1);
+  depvars_cell(P, b, 1, je, ke);
+  depvars_cell(P, b, ie, je, ke);
+}
+
+/* bcond.f90:16-42 */
+int bcond(mgeo_ctx* c, OBlock& b) {
+  for (int f = 1; f <= 6; f++) {
+    int t = b.bctype[f - 1];
+    if (t == 0) continue;
+    if (t == -20) bc_far(c, b, f);
+    else if (t == -50) bc_copy_face(b, f, -50);
+    else if (t == -60) {
+      bc_copy_face(b, f, -60);
+      if (f <= 3 && b.bctype[f + 2] != -60)
+        return fail(c, MGE_EBADCFG, "periodic boundary must appear in pairs (bcond.f90:26-31)");
+    } else if (t == -80) bc_copy_face(b, f, -80);
+    // other codes: the reference prints and continues
+  }
+  bc_corner(c, b);
+  return MGE_OK;
+}
+
+/* bc_cutcell.f90:40-268 (approxbc off: qb from the record, 0 for a fixed wall) */
+int bc_cutcell(mgeo_ctx* c, OBlock& b) {
+  const mge_params& P = c->prm;
+  for (size_t m = 0; m < b.z.size(); m++) {
+    ORec& t = b.z[m];
+    int ncl = t.npoint;
+    double nvec[3] = {t.nvec[0], t.nvec[1], t.nvec[2]};
+    double qb[3] = {t.qb[0], t.qb[1], t.qb[2]};
+    double nn = std::sqrt(nvec[0] * nvec[0] + nvec[1] * nvec[1] + nvec[2] * nvec[2]);
+    for (int q = 0; q < 3; q++) nvec[q] = nvec[q] / nn;
+    double psol = 0.0, wsol[5] = {0, 0, 0, 0, 0};
+    if (ncl == 0) {  // bc_cutcell.f90:65-70: warn, zero this record, leave the routine
+      t.psol = psol;
+      for (int v = 0; v < 5; v++) t.wsol[v] = wsol[v];
+      return MGE_OK;
+    }
+    double var_refl[5] = {0, 0, 0, 0, 0};
+    for (int v = 0; v < 5; v++)
+      for (int q = 0; q < ncl; q++) var_refl[v] = var_refl[v] + t.coef[q] * b.W(t.ijk[q][0], t.ijk[q][1], t.ijk[q][2], v);
+    double p_refl = 0.0;
+    for (int q = 0; q < ncl; q++) p_refl = p_refl + t.coef[q] * b.P(t.ijk[q][0], t.ijk[q][1], t.ijk[q][2]);
+    if (P.eqntype == MGE_EQN_EULER) {
+      psol = p_refl;
+      for (int v = 0; v < 5; v++) wsol[v] = var_refl[v];
+      double qn = 2.0 * (nvec[0] * (wsol[1] - wsol[0] * qb[0]) + nvec[1] * (wsol[2] - wsol[0] * qb[1]) +
+                         nvec[2] * (wsol[3] - wsol[0] * qb[2]));
+      for (int q = 0; q < 3; q++) wsol[1 + q] = wsol[1 + q] - qn * nvec[q];
+      wsol[4] = psol / (P.gamma - 1.0) + 0.5 * (wsol[1] * wsol[1] + wsol[2] * wsol[2] + wsol[3] * wsol[3]) / wsol[0];
+      for (int v = 0; v < 5; v++)
+        if (wsol[v] != wsol[v]) return fail(c, MGE_ENAN, "bc_cutcell: wsol is NaN (bc_cutcell.f90:147-156)");
+    } else {
+      psol = p_refl;
+      for (int v = 0; v < 5; v++) wsol[v] = var_refl[v];
+      for (int q = 0; q < 3; q++) wsol[1 + q] = 2.0 * qb[q] * var_refl[0] - var_refl[1 + q];  // option B, :185
+      wsol[4] = psol / (P.gamma - 1.0) + 0.5 * (wsol[1] * wsol[1] + wsol[2] * wsol[2] + wsol[3] * wsol[3]) / wsol[0];
+    }
+    t.psol = psol;
+    for (int v = 0; v < 5; v++) t.wsol[v] = wsol[v];
+  }
+  return MGE_OK;
+}
+
+/* ------------------------------------------------------------------ euler.f90:1-462 */
+int euler(mgeo_ctx* c, OBlock& b, int itime, int ncyc, int mgl, int mlvl, bool lres, bool lfir, int nstage_limit) {
+  (void)itime;
+  const mge_params& P = c->prm;
+  const size_t N = b.N;
+  const double fcoll = 1.0;
+  if (P.distype != MGE_DIS_CENTRAL)
+    return fail(c, MGE_EBADCFG, "the oracle restates the central scheme (distype 'c') only");
+  if (lfir) b.ws = b.w;  // euler.f90:75-77
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+  for (int k = 2; k <= b.kl; k++)
+    for (int j = 2; j <= b.jl; j++)
+      for (int i = 2; i <= b.il; i++)
+        for (int v = 0; v < 5; v++) b.wn[v * N + b.I(i, j, k)] = b.W(i, j, k, v);
+  std::fill(b.dw.begin(), b.dw.end(), 0.0);
+  std::fill(b.fw.begin(), b.fw.end(), 0.0);
+  const int mstage = std::min(P.mstage, nstage_limit > 0 ? nstage_limit : P.mstage);
+  for (int m = 1; m <= mstage; m++) {
+    double fn = P.cstp[m - 1] * P.cfl;
+    if (m > 1) {
+      double f = 1.0 - P.cdis[m - 1];
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+      for (int k = 2; k <= b.kl; k++)
+        for (int j = 2; j <= b.jl; j++)
+          for (int i = 2; i <= b.il; i++)
+            for (int v = 0; v < 5; v++) b.FW(i, j, k, v) = b.FW(i, j, k, v) * f;
+    }
+    int rc;
+    if (P.cdis[m - 1] > 0.0) {
+      rc = dflux(c, b, m);
+      if (rc) return rc;
+    }
+    rc = eflux(c, b);
+    if (rc) return rc;
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+    for (int k = 2; k <= b.kl; k++)
+      for (int j = 2; j <= b.jl; j++)
+        for (int i = 2; i <= b.il; i++)
+          for (int v = 0; v < 5; v++) b.DW(i, j, k, v) = b.DW(i, j, k, v) + b.FW(i, j, k, v);
+    if (mgl < mlvl) {  // euler.f90:294-318
+      const bool first = lfir && m == 1;
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+      for (int k = 2; k <= b.kl; k++)
+        for (int j = 2; j <= b.jl; j++)
+          for (int i = 2; i <= b.il; i++) {
+            size_t q = b.I(i, j, k);
+            for (int v = 0; v < 5; v++) {
+              if (first) {
+                b.qf[v * N + q] = 0.0;
+                if (b.marker[q] == 1) b.qf[v * N + q] = fcoll * b.wr[v * N + q] - b.dw[v * N + q];
+              }
+              b.dw[v * N + q] = b.dw[v * N + q] + b.qf[v * N + q];
+            }
+          }
+    }
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+    for (int k = 2; k <= b.kl; k++)
+      for (int j = 2; j <= b.jl; j++)
+        for (int i = 2; i <= b.il; i++)
+          for (int v = 0; v < 5; v++) b.DW(i, j, k, v) = b.DW(i, j, k, v) * (double)b.BL(i, j, k);
+    if (lres) return MGE_OK;  // euler.f90:347-361
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+    for (int k = 2; k <= b.kl; k++)
+      for (int j = 2; j <= b.jl; j++)
+        for (int i = 2; i <= b.il; i++) {
+          double de = fn * b.vdtim[b.I(i, j, k)] / b.vol;
+          if (P.vt == 1) de = fn * b.dtim / b.vol;
+          for (int v = 0; v < 5; v++) b.DW(i, j, k, v) = de * b.DW(i, j, k, v);
+        }
+    if (m % 2 != 0) {
+      if (P.irs_variant == 1) psmoo_var(c, b);
+      else psmoo_old(c, b);
+    }
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+    for (int k = 2; k <= b.kl; k++)
+      for (int j = 2; j <= b.jl; j++)
+        for (int i = 2; i <= b.il; i++) {
+          const double lam = 1.0;
+          for (int v = 0; v < 5; v++) b.W(i, j, k, v) = b.wn[v * N + b.I(i, j, k)] - b.DW(i, j, k, v) / lam;
+          depvars_cell(P, b, i, j, k);
+        }
+    rc = bc_cutcell(c, b);
+    if (rc) return rc;
+    rc = bcond(c, b);
+    if (rc) return rc;
+  }
+  if (nstage_limit > 0 && nstage_limit < P.mstage) return MGE_OK;
+  // euler.f90:431-447
+  if ((int)b.rtrms.size() <= ncyc) b.rtrms.resize(ncyc + 1, 0.0);
+  double acc = 0.0;
+  for (int k = 2; k <= b.kl; k++)
+    for (int j = 2; j <= b.jl; j++)
+      for (int i = 2; i <= b.il; i++) {
+        double de = P.cfl * b.vdtim[b.I(i, j, k)];
+        if (P.vt == 1) de = P.cfl * b.dtim;
+        double rt = 0.0;
+        if (b.BL(i, j, k) != 0) rt = b.DW(i, j, k, 0) / de;
+        acc = acc + rt * rt;
+      }
+  b.rtrms[ncyc] = std::sqrt(acc / (double)((long)b.nx * b.ny * b.nz));
+  return MGE_OK;
+}
+
+/* ------------------------------------------------------------------ grid transfer geometry */
+/* Centre-based 2x2x2 stencil on the parent (coarse) grid for a point at
+ * coarse coordinate u (cell q occupies [q-2, q-1)), clamped to [2, lc-1]. */
+inline void coarse_stencil(double u, int lc, int& s, double& xi) {
+  s = (int)std::floor(u + 1.5);
+  if (s < 2) s = 2;
+  if (s > lc - 1) s = lc - 1;
+  xi = u + 1.5 - (double)s;
+}
+inline void trilinear_factor(double x, double y, double z, double* fac) {
+  fac[0] = (1.0 - x) * (1.0 - y) * (1.0 - z);
+  fac[1] = x * (1.0 - y) * (1.0 - z);
+  fac[2] = (1.0 - x) * y * (1.0 - z);
+  fac[3] = x * y * (1.0 - z);
+  fac[4] = (1.0 - x) * (1.0 - y) * z;
+  fac[5] = x * (1.0 - y) * z;
+  fac[6] = (1.0 - x) * y * z;
+  fac[7] = x * y * z;
+}
+
+/* collc.f90:58-158: restrict w and the volume-scaled residual of every child
+ * (fine block at level mgl+1) onto coarse block b; sets marker. */
+void collc(mgeo_ctx* c, OBlock& b) {
+  std::fill(b.marker.begin(), b.marker.end(), 0);
+  if ((int)c->lv.size() < b.level + 1) return;
+  for (OBlock& f : c->lv[b.level]) {
+    if (f.parent != b.serial) continue;
+    int r[3] = {f.ratio[0], f.ratio[1], f.ratio[2]}, o[3] = {f.offset[0], f.offset[1], f.offset[2]};
+    int n[3] = {f.nx / r[0], f.ny / r[1], f.nz / r[2]};
+    int lf[3] = {f.il, f.jl, f.kl};
+    for (int i = o[0] + 2; i <= o[0] + 1 + n[0]; i++) {
+      if (i < 2 || i > b.il) continue;
+      for (int j = o[1] + 2; j <= o[1] + 1 + n[1]; j++) {
+        if (j < 2 || j > b.jl) continue;
+        for (int k = o[2] + 2; k <= o[2] + 1 + n[2]; k++) {
+          if (k < 2 || k > b.kl) continue;
+          int ic[3] = {i, j, k}, sh[3];
+          double xi[3];
+          for (int d = 0; d < 3; d++) {
+            // coarse centre in fine units: (q - 1.5 - o) * r ; fine centres at s - 1.5
+            double t = ((double)ic[d] - 1.5 - (double)o[d]) * (double)r[d];
+            int s = (int)std::floor(t + 1.5);
+            if (s < 2) s = 2;
+            if (s > lf[d] - 1) s = lf[d] - 1;
+            sh[d] = s;
+            xi[d] = t + 1.5 - (double)s;
+          }
+          double fac[8];
+          trilinear_factor(xi[0], xi[1], xi[2], fac);
+          size_t q = b.I(i, j, k);
+          for (int v = 0; v < 5; v++) {
+            double acc = 0.0;
+            int nn = 0;
+            for (int dk = 0; dk < 2; dk++)
+              for (int dj = 0; dj < 2; dj++)
+                for (int di = 0; di < 2; di++) {
+                  double val = f.DW(sh[0] + di, sh[1] + dj, sh[2] + dk, v) / f.vol;
+                  acc = acc + val * fac[nn++];
+                }
+            b.wr[v * b.N + q] = acc * b.vol;
+            acc = 0.0;
+            nn = 0;
+            for (int dk = 0; dk < 2; dk++)
+              for (int dj = 0; dj < 2; dj++)
+                for (int di = 0; di < 2; di++) acc = acc + f.W(sh[0] + di, sh[1] + dj, sh[2] + dk, v) * fac[nn++];
+            b.w[v * b.N + q] = acc;
+          }
+          b.marker[q] = 1;
+        }
+      }
+    }
+  }
+}
+
+/* Stencil of fine cell (i,j,k) of block f on its parent pb. Returns false
+ * when the centre lies outside the parent's physical cells (eval_x2cell err). */
+bool fine_to_coarse(const OBlock& f, const OBlock& pb, int i, int j, int k, int* sh, double* fac) {
+  int ic[3] = {i, j, k};
+  int lc[3] = {pb.il, pb.jl, pb.kl};
+  int ncp[3] = {pb.nx, pb.ny, pb.nz};
+  double xi[3];
+  for (int d = 0; d < 3; d++) {
+    double u = (double)f.offset[d] + ((double)ic[d] - 1.5) / (double)f.ratio[d];
+    if (u < 0.0 || u >= (double)ncp[d]) return false;
+    coarse_stencil(u, lc[d], sh[d], xi[d]);
+  }
+  trilinear_factor(xi[0], xi[1], xi[2], fac);
+  return true;
+}
+
+/* addw.f90:83-188 */
+void addw(mgeo_ctx* c, OBlock& f, int mgl, int mlvl) {
+  if (f.parent < 1) return;
+  OBlock& pb = c->lv[f.level - 2][f.parent - 1];
+  std::vector<double> store_w = f.w;
+  const bool fmg = (mgl - 1 == mlvl);
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+  for (int i = 2; i <= f.il; i++)
+    for (int j = 2; j <= f.jl; j++)
+      for (int k = 2; k <= f.kl; k++) {
+        int sh[3];
+        double fac[8];
+        if (!fine_to_coarse(f, pb, i, j, k, sh, fac)) continue;
+        size_t q = f.I(i, j, k);
+        for (int v = 0; v < 5; v++) {
+          double acc = 0.0;
+          int nn = 0;
+          for (int dk = 0; dk < 2; dk++)
+            for (int dj = 0; dj < 2; dj++)
+              for (int di = 0; di < 2; di++) {
+                size_t cq = pb.I(sh[0] + di, sh[1] + dj, sh[2] + dk);
+                double val = pb.w[v * pb.N + cq];
+                if (!fmg) val = val - pb.ws[v * pb.N + cq];
+                acc = acc + val * fac[nn++];
+              }
+          if (fmg) {
+            if (f.blank[q] != 0) f.w[v * f.N + q] = acc;
+          } else {
+            if (f.blank[q] != 0) f.w[v * f.N + q] = store_w[v * f.N + q] + acc;
+          }
+        }
+      }
+}
+
+/* bc_embed.f90:47-143: fine ghost cells from the parent level */
+void bc_embed(mgeo_ctx* c, int lvl) {
+  if (lvl <= 1) return;
+  for (OBlock& f : c->lv[lvl - 1]) {
+    if (f.parent < 1) continue;
+    OBlock& pb = c->lv[lvl - 2][f.parent - 1];
+    for (int i = 0; i <= f.ib; i++)
+      for (int j = 0; j <= f.jb; j++)
+        for (int k = 0; k <= f.kb; k++) {
+          if (i >= 2 && i <= f.il && j >= 2 && j <= f.jl && k >= 2 && k <= f.kl) continue;
+          int sh[3];
+          double fac[8];
+          if (!fine_to_coarse(f, pb, i, j, k, sh, fac)) continue;
+          size_t q = f.I(i, j, k);
+          if (f.blank[q] != 0) {
+            for (int v = 0; v < 5; v++) {
+              double acc = 0.0;
+              int nn = 0;
+              for (int dk = 0; dk < 2; dk++)
+                for (int dj = 0; dj < 2; dj++)
+                  for (int di = 0; di < 2; di++)
+                    acc = acc + pb.w[v * pb.N + pb.I(sh[0] + di, sh[1] + dj, sh[2] + dk)] * fac[nn++];
+              f.w[v * f.N + q] = acc;
+            }
+          }
+          depvars_cell(c->prm, f, i, j, k);
+        }
+  }
+}
+
+int movco(mgeo_ctx* c, int mgl) {  // movco.f90:21-47
+  if (mgl < 1 || mgl > (int)c->lv.size()) return fail(c, MGE_ENOTFOUND, "movco: bad level");
+  for (OBlock& b : c->lv[mgl - 1]) {
+    collc(c, b);
+    depvars_all(c->prm, b);
+    for (int i = 2; i <= b.il; i++)
+      for (int j = 2; j <= b.jl; j++)
+        for (int k = 2; k <= b.kl; k++)
+          for (int v = 0; v < 5; v++) b.wn[v * b.N + b.I(i, j, k)] = b.W(i, j, k, v);
+  }
+  // bc_overlap(mgl): one block per level, no same-level overlap
+  for (OBlock& b : c->lv[mgl - 1]) {
+    int rc = bcond(c, b);
+    if (rc) return rc;
+  }
+  return MGE_OK;
+}
+
+int movfin(mgeo_ctx* c, int mgl, int mlvl) {  // movfin.f90:20-39
+  if (mgl < 1 || mgl > (int)c->lv.size()) return fail(c, MGE_ENOTFOUND, "movfin: bad level");
+  for (OBlock& b : c->lv[mgl - 1]) addw(c, b, mgl, mlvl);
+  for (OBlock& b : c->lv[mgl - 1]) depvars_all(c->prm, b);
+  bc_embed(c, mgl);
+  for (OBlock& b : c->lv[mgl - 1]) {
+    int rc = bcond(c, b);
+    if (rc) return rc;
+  }
+  return MGE_OK;
+}
+
+/* Wall forces from the cut-cell records (new; the reference has none). */
+void forces_block(mgeo_ctx* c, OBlock& b, const mge_solve_opts* o, double* F, double* M) {
+  for (const ORec& t : b.z) {
+    int ax = t.zz - 1;
+    double sgn = t.faceid >= 4 ? 1.0 : -1.0;
+    double area = t.area;
+    double pw = 0.5 * (b.P(t.ccid[0], t.ccid[1], t.ccid[2]) + t.psol);
+    double f[3] = {0, 0, 0};
+    f[ax] = pw * area * sgn;
+    double xf[3];
+    int ic[3] = {t.ccid[0], t.ccid[1], t.ccid[2]};
+    for (int d = 0; d < 3; d++) xf[d] = b.origin[d] + ((double)ic[d] - 1.5) * b.h[d];
+    xf[ax] = xf[ax] + sgn * 0.5 * b.h[ax];
+    double r[3];
+    for (int d = 0; d < 3; d++) r[d] = xf[d] - (o ? o->moment_center[d] : 0.0);
+    for (int d = 0; d < 3; d++) F[d] += f[d];
+    M[0] += r[1] * f[2] - r[2] * f[1];
+    M[1] += r[2] * f[0] - r[0] * f[2];
+    M[2] += r[0] * f[1] - r[1] * f[0];
+  }
+  (void)c;
+}
+
+}  // namespace
+
+/* ====================================================================== C API */
+extern "C" {
+
+void mgeo_set_threads(int n) { g_threads = n < 1 ? 1 : n; }
+int mgeo_get_threads(void) { return g_threads; }
+
+int mgeo_init(const mge_params* prm, mgeo_ctx** out) {
+  if (!prm || !out) return MGE_EBADCFG;
+  mgeo_ctx* c = new mgeo_ctx();
+  c->prm = *prm;
+  if (prm->nlevel < 1 || prm->nlevel > MGE_MAX_LEVEL || prm->mstage < 1 || prm->mstage > MGE_MAX_STAGE) {
+    delete c;
+    return MGE_EBADCFG;
+  }
+  c->lv.resize(prm->nlevel);
+  *out = c;
+  return MGE_OK;
+}
+
+void mgeo_destroy(mgeo_ctx* c) { delete c; }
+const char* mgeo_last_error(const mgeo_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int mgeo_add_block(mgeo_ctx* c, const mge_block_desc* d, int level, int serial) {
+  if (level < 1 || level > (int)c->lv.size()) return fail(c, MGE_EBADCFG, "add_block: bad level");
+  auto& L = c->lv[level - 1];
+  if (serial != (int)L.size() + 1) return fail(c, MGE_EBADCFG, "add_block: serials must be added in order");
+  if (d->nx < 2 || d->ny < 2 || d->nz < 2) return fail(c, MGE_EBADCFG, "add_block: need at least 2 cells per axis");
+  L.emplace_back();
+  OBlock& b = L.back();
+  b.level = level;
+  b.serial = serial;
+  b.nx = d->nx; b.ny = d->ny; b.nz = d->nz;
+  b.il = b.nx + 1; b.jl = b.ny + 1; b.kl = b.nz + 1;
+  b.ie = b.il + 1; b.je = b.jl + 1; b.ke = b.kl + 1;
+  b.ib = b.il + 2; b.jb = b.jl + 2; b.kb = b.kl + 2;
+  b.Pi = b.ib + 1; b.Pj = b.jb + 1; b.Pk = b.kb + 1;
+  b.N = b.Pi * b.Pj * b.Pk;
+  for (int q = 0; q < 3; q++) {
+    b.h[q] = d->h[q];
+    b.origin[q] = d->origin[q];
+    b.si[q] = d->si[q];
+    b.sj[q] = d->sj[q];
+    b.sk[q] = d->sk[q];
+    b.ratio[q] = d->ratio[q];
+    b.offset[q] = d->offset[q];
+  }
+  b.vol = d->cellvolume;
+  for (int f = 0; f < 6; f++) {
+    b.bctype[f] = d->bctype[f];
+    for (int q = 0; q < 3; q++) b.fnv[f][q] = d->facenvec[f][q];
+  }
+  b.parent = d->parent;
+  const size_t N = b.N;
+  b.w.assign(5 * N, 0.0); b.p.assign(N, 0.0); b.wn.assign(5 * N, 0.0); b.ws.assign(5 * N, 0.0);
+  b.dw.assign(5 * N, 0.0); b.fw.assign(5 * N, 0.0); b.wr.assign(5 * N, 0.0); b.qf.assign(5 * N, 0.0);
+  b.vdtim.assign(N, 0.0); b.radi.assign(N, 0.0); b.radj.assign(N, 0.0); b.radk.assign(N, 0.0);
+  b.epsx.assign(N, 0.0); b.epsy.assign(N, 0.0); b.epsz.assign(N, 0.0);
+  b.blank.assign(N, 1);
+  b.marker.assign(N, 0);
+  if (d->blank)
+    for (size_t q = 0; q < N; q++) b.blank[q] = d->blank[q];
+  b.z.resize(d->nmir);
+  for (int m = 0; m < d->nmir; m++) {
+    ORec& t = b.z[m];
+    for (int q = 0; q < 3; q++) {
+      t.ccid[q] = d->ccid[3 * m + q];
+      t.scid[q] = d->scid[3 * m + q];
+      t.nvec[q] = d->nvec[3 * m + q];
+      t.qb[q] = d->qb ? d->qb[3 * m + q] : 0.0;
+    }
+    t.faceid = d->faceid[m];
+    t.zz = d->zz[m];
+    t.npoint = d->npoint[m];
+    if (t.npoint < 0 || t.npoint > MGE_MAX_CLOUD) return fail(c, MGE_EBADCFG, "add_block: bad cloud size");
+    for (int q = 0; q < MGE_MAX_CLOUD; q++) {
+      t.coef[q] = d->coef[MGE_MAX_CLOUD * m + q];
+      for (int e = 0; e < 3; e++) t.ijk[q][e] = d->ijkdex[(MGE_MAX_CLOUD * m + q) * 3 + e];
+    }
+    int ax = t.zz - 1;
+    double fa = 1.0;
+    for (int e = 0; e < 3; e++)
+      if (e != ax) fa *= d->h[e];
+    t.area = d->area ? d->area[m] : fa;
+    t.psol = 0.0;
+    for (int v = 0; v < 5; v++) t.wsol[v] = 0.0;
+  }
+  return MGE_OK;
+}
+
+int mgeo_commit(mgeo_ctx* c) {
+  for (size_t l = 0; l < c->lv.size(); l++)
+    if (c->lv[l].empty()) return fail(c, MGE_EBADCFG, "commit: a level has no block");
+  c->committed = true;
+  return MGE_OK;
+}
+
+int mgeo_init_flow(mgeo_ctx* c) {  // init_flow.f90:46-96 (free stream, no restart)
+  const mge_params& P = c->prm;
+  for (auto& L : c->lv)
+    for (OBlock& b : L) {
+      for (size_t q = 0; q < b.N; q++) {
+        b.w[0 * b.N + q] = P.rho0;
+        b.w[1 * b.N + q] = P.rho0 * P.u0;
+        b.w[2 * b.N + q] = P.rho0 * P.v0;
+        b.w[3 * b.N + q] = P.rho0 * P.w0;
+        b.w[4 * b.N + q] = P.rho0 * P.h0 - P.p0;
+      }
+      depvars_all(P, b);
+      int rc = bc_cutcell(c, b);
+      if (rc) return rc;
+      rc = bcond(c, b);
+      if (rc) return rc;
+    }
+  return MGE_OK;
+}
+
+int mgeo_upload_state(mgeo_ctx* c, int level, int serial, const double* w) {
+  OBlock* b = getb(c, level, serial);
+  if (!b) return MGE_ENOTFOUND;
+  std::memcpy(b->w.data(), w, 5 * b->N * sizeof(double));
+  depvars_all(c->prm, *b);
+  return MGE_OK;
+}
+
+int mgeo_download_field(mgeo_ctx* c, int level, int serial, const char* name, double* out, size_t count) {
+  OBlock* b = getb(c, level, serial);
+  if (!b) return MGE_ENOTFOUND;
+  std::string n(name);
+  const std::vector<double>* src = nullptr;
+  if (n == "w") src = &b->w;
+  else if (n == "p") src = &b->p;
+  else if (n == "dw") src = &b->dw;
+  else if (n == "fw") src = &b->fw;
+  else if (n == "wn") src = &b->wn;
+  else if (n == "ws") src = &b->ws;
+  else if (n == "wr") src = &b->wr;
+  else if (n == "qf") src = &b->qf;
+  else if (n == "vdtim") src = &b->vdtim;
+  if (src) {
+    if (count < src->size()) return MGE_EBADCFG;
+    std::memcpy(out, src->data(), src->size() * sizeof(double));
+    return MGE_OK;
+  }
+  if (n == "lam") {
+    if (count < b->N) return MGE_EBADCFG;
+    for (size_t q = 0; q < b->N; q++) out[q] = b->radi[q] + b->radj[q] + b->radk[q];
+    return MGE_OK;
+  }
+  if (n == "blank" || n == "marker") {
+    if (count < b->N) return MGE_EBADCFG;
+    const std::vector<int>& a = n == "blank" ? b->blank : b->marker;
+    for (size_t q = 0; q < b->N; q++) out[q] = (double)a[q];
+    return MGE_OK;
+  }
+  if (n == "wsol" || n == "psol") {
+    size_t need = n == "wsol" ? 5 * b->z.size() : b->z.size();
+    if (count < need) return MGE_EBADCFG;
+    for (size_t m = 0; m < b->z.size(); m++) {
+      if (n == "wsol")
+        for (int v = 0; v < 5; v++) out[5 * m + v] = b->z[m].wsol[v];
+      else
+        out[m] = b->z[m].psol;
+    }
+    return MGE_OK;
+  }
+  if (n == "dtim") {
+    out[0] = b->dtim;
+    return MGE_OK;
+  }
+  return MGE_EBADCFG;
+}
+
+int mgeo_timestep(mgeo_ctx* c, int level, int serial) {
+  OBlock* b = getb(c, level, serial);
+  if (!b) return MGE_ENOTFOUND;
+  return timestep(c, *b);
+}
+
+int mgeo_euler(mgeo_ctx* c, int level, int serial, int itime, int ncyc, int mgl, int mlvl, int lres, int lfir) {
+  OBlock* b = getb(c, level, serial);
+  if (!b) return MGE_ENOTFOUND;
+  return euler(c, *b, itime, ncyc, mgl, mlvl, lres != 0, lfir != 0, 0);
+}
+
+int mgeo_euler_partial(mgeo_ctx* c, int level, int serial, int itime, int ncyc, int mgl, int mlvl, int lres,
+                       int lfir, int nstage) {
+  OBlock* b = getb(c, level, serial);
+  if (!b) return MGE_ENOTFOUND;
+  return euler(c, *b, itime, ncyc, mgl, mlvl, lres != 0, lfir != 0, nstage);
+}
+
+int mgeo_movco(mgeo_ctx* c, int mgl) { return movco(c, mgl); }
+int mgeo_movfin(mgeo_ctx* c, int mgl, int mlvl) { return movfin(c, mgl, mlvl); }
+int mgeo_bc_overlap(mgeo_ctx* c, int mgl) {
+  (void)c;
+  (void)mgl;
+  return MGE_OK;
+}
+
+int mgeo_get_rtrms(mgeo_ctx* c, int level, int serial, int ncyc, double* out) {
+  OBlock* b = getb(c, level, serial);
+  if (!b) return MGE_ENOTFOUND;
+  *out = (ncyc >= 0 && ncyc < (int)b->rtrms.size()) ? b->rtrms[ncyc] : 0.0;
+  return MGE_OK;
+}
+
+int mgeo_forces_compute(mgeo_ctx* c, int level, const mge_solve_opts* o, mge_forces* out) {
+  if (level < 1 || level > (int)c->lv.size()) return MGE_ENOTFOUND;
+  double F[3] = {0, 0, 0}, M[3] = {0, 0, 0};
+  for (OBlock& b : c->lv[level - 1]) forces_block(c, b, o, F, M);
+  const mge_params& P = c->prm;
+  double qinf = 0.5 * P.rho0 * (P.u0 * P.u0 + P.v0 * P.v0 + P.w0 * P.w0);
+  double aref = (o && o->ref_area > 0.0) ? o->ref_area : 1.0;
+  double ed[3] = {std::cos(P.alpha) * std::cos(P.beta), std::sin(P.alpha) * std::cos(P.beta), std::sin(P.beta)};
+  double el[3] = {-std::sin(P.alpha), std::cos(P.alpha), 0.0};
+  for (int d = 0; d < 3; d++) {
+    out->force[d] = F[d];
+    out->moment[d] = M[d];
+  }
+  out->cd = (F[0] * ed[0] + F[1] * ed[1] + F[2] * ed[2]) / (qinf * aref);
+  out->cl = (F[0] * el[0] + F[1] * el[1] + F[2] * el[2]) / (qinf * aref);
+  return MGE_OK;
+}
+
+/* one multigrid cycle (solver.f90:126-234) at FMG level mlvl; returns max_res */
+static int oracle_cycle(mgeo_ctx* c, int mlvl, int ncyc, double* max_res_out, double* ini_res_out) {
+  const mge_params& P = c->prm;
+  const int nlevel = (int)c->lv.size();
+  std::vector<int> icyc(nlevel + 2, 0);
+  const int itime = 0;
+  int rc = 0;
+  int mgl = mlvl;
+  for (;;) {    // lopmg
+    for (;;) {  // lopr
+      icyc[mgl] += 1;
+      bool lfir = (mgl != mlvl);
+      for (OBlock& b : c->lv[mgl - 1]) {
+        if ((rc = timestep(c, b))) return rc;
+        if ((rc = euler(c, b, itime, ncyc, mgl, mlvl, false, lfir, 0))) return rc;
+      }
+      if (mgl == mlvl) {  // solver.f90:160-186
+        double max_res = 1000.0;
+        for (OBlock& b : c->lv[mgl - 1]) {
+          double r = b.rtrms[ncyc];
+          if (ncyc == 1 && ini_res_out) *ini_res_out = r;
+          if (r < max_res) max_res = r;
+          if (r != r) return fail(c, MGE_ENAN, "NaN residual (solver.f90:180)");
+        }
+        *max_res_out = max_res;
+      }
+      if (mlvl == 1) return MGE_OK;  // cycle lop0
+      for (OBlock& b : c->lv[mgl - 1])
+        if ((rc = euler(c, b, itime, ncyc, mgl, mlvl, true, false, 0))) return rc;
+      mgl = mgl - 1;
+      if ((rc = movco(c, mgl))) return rc;
+      if (mgl == 1) break;
+    }
+    bool lfir = true;
+    for (;;) {  // lopp
+      for (OBlock& b : c->lv[mgl - 1]) {
+        if ((rc = timestep(c, b))) return rc;
+        if ((rc = euler(c, b, itime, ncyc, mgl, mlvl, false, lfir, 0))) return rc;
+      }
+      lfir = false;
+      mgl = mgl + 1;
+      if ((rc = movfin(c, mgl, mlvl))) return rc;
+      if (mgl == mlvl) return MGE_OK;   // exit lopmg
+      if (icyc[mgl] != P.mgtype) break;  // cycle lopmg (W-cycle re-descent)
+      icyc[mgl] = 0;
+    }
+  }
+}
+
+int mgeo_cycle(mgeo_ctx* c, int mlvl, int ncyc, double* max_res) {
+  if (mlvl < 1 || mlvl > (int)c->lv.size() || !max_res) return MGE_EBADCFG;
+  return oracle_cycle(c, mlvl, ncyc, max_res, nullptr);
+}
+
+/* solver.f90:109-292 (steady: execmode 0, one period, one step) */
+int mgeo_solve(mgeo_ctx* c, const mge_solve_opts* o, double* hist, int hist_len, int* cycles_done,
+               mge_forces* forces) {
+  const mge_params& P = c->prm;
+  const int nlevel = (int)c->lv.size();
+  double max_res = 0.0, ini_res = 1.0;
+  int nfin = 0, rc = 0;
+  for (int mlvl = 1; mlvl <= nlevel; mlvl++) {
+    for (int ncyc = 1; ncyc <= P.mcyc[mlvl - 1]; ncyc++) {
+      if ((rc = oracle_cycle(c, mlvl, ncyc, &max_res, &ini_res))) return rc;
+      if (mlvl == nlevel) {
+        if (hist && nfin < hist_len) hist[nfin] = max_res;
+        nfin++;
+      }
+      if (mlvl > 1) {  // solver.f90:237-239 (skipped by "cycle lop0" on the single-grid level)
+        double drop = P.conv_drop > 0.0 ? P.conv_drop : 1.0e6;
+        if (ini_res / max_res > drop) break;
+      }
+      if (o && o->max_cycles_total > 0 && mlvl == nlevel && nfin >= o->max_cycles_total) break;
+    }
+    if (mlvl < nlevel) {  // FMG prolongation, solver.f90:256-259
+      if ((rc = movfin(c, mlvl + 1, mlvl))) return rc;
+    }
+  }
+  if (cycles_done) *cycles_done = nfin;
+  if (forces) mgeo_forces_compute(c, nlevel, o, forces);
+  return MGE_OK;
+}
+
+}  // extern "C"

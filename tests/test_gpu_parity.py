@@ -1,0 +1,138 @@
+"""GPU parity: the CUDA path against the CPU oracle on identical inputs.
+
+Tolerance: per-stage residual and state, infinity norm of the difference
+relative to the infinity norm of the oracle field, <= 1e-12 (parity.RTOL).
+"""
+import numpy as np
+import pytest
+
+from code_mge_gb300 import _abi as A
+from code_mge_gb300 import cases as K
+from parity import RTOL, compare, pair, small_cylinder, small_sphere
+
+pytestmark = pytest.mark.gpu
+
+CASES = {
+    "cylinder": lambda: small_cylinder(),
+    "sphere": lambda: small_sphere(),
+    "cylinder_matrix": lambda: small_cylinder(dissip=A.MGE_DISSIP_MATRIX),
+    "sphere_global_dt": lambda: small_sphere(cfl=1.5),
+    "ellipsoid_noirs": lambda: K.ellipsoid_box(n=16, nlevel=2, semi=(0.9, 0.6, 0.5), extent=2.5, alpha_deg=5.0,
+                                               smoo=0.0, mcyc_fine=4),
+}
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_init_flow(gpulib, name):
+    g, o = pair(CASES[name]())
+    for L in range(1, g.case.prm.nlevel + 1):
+        compare(g, o, "w", L, phys_only=False)
+        compare(g, o, "p", L, phys_only=False)
+        if g.spec(L).arrays["nmir"]:
+            compare(g, o, "wsol", L)
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_timestep(gpulib, name):
+    g, o = pair(CASES[name](), develop_cycles=3)
+    L = g.case.prm.nlevel
+    g.timestep(L)
+    o.timestep(L)
+    compare(g, o, "vdtim", L)
+    compare(g, o, "lam", L)
+    assert abs(g.field("dtim", L) - o.field("dtim", L)) <= RTOL * abs(o.field("dtim", L))
+
+
+@pytest.mark.parametrize("name", list(CASES))
+@pytest.mark.parametrize("nstage", [1, 2, 3, 4, 5])
+def test_stage(gpulib, name, nstage):
+    g, o = pair(CASES[name](), develop_cycles=3)
+    L = g.case.prm.nlevel
+    for c in (g, o):
+        c.timestep(L)
+        c.euler_partial(L, nstage)
+    compare(g, o, "dw", L)
+    compare(g, o, "fw", L)
+    compare(g, o, "w", L, phys_only=False)
+    compare(g, o, "p", L, phys_only=False)
+    if g.spec(L).arrays["nmir"]:
+        compare(g, o, "wsol", L)
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_euler_rtrms_and_residual(gpulib, name):
+    g, o = pair(CASES[name](), develop_cycles=3)
+    L = g.case.prm.nlevel
+    for c in (g, o):
+        c.timestep(L)
+        c.euler(L, ncyc=1)
+    compare(g, o, "w", L, phys_only=False)
+    rg, ro = g.rtrms(L, 1), o.rtrms(L, 1)
+    assert abs(rg - ro) <= RTOL * abs(ro)
+    for c in (g, o):
+        c.euler(L, ncyc=1, lres=True)
+    compare(g, o, "dw", L)
+
+
+@pytest.mark.parametrize("name", ["cylinder", "sphere"])
+def test_transfer(gpulib, name):
+    g, o = pair(CASES[name](), develop_cycles=3)
+    L = g.case.prm.nlevel
+    for c in (g, o):
+        c.timestep(L)
+        c.euler(L, ncyc=1, mgl=L, mlvl=L)
+        c.euler(L, ncyc=1, mgl=L, mlvl=L, lres=True)
+        c.movco(L - 1)
+    for f in ("w", "wr", "p"):
+        compare(g, o, f, L - 1, phys_only=(f == "wr"))
+    for c in (g, o):
+        c.timestep(L - 1)
+        c.euler(L - 1, ncyc=1, mgl=L - 1, mlvl=L, lfir=True)
+        c.movfin(L, L)
+    compare(g, o, "qf", L - 1)
+    compare(g, o, "w", L, phys_only=False)
+    compare(g, o, "p", L, phys_only=False)
+
+
+@pytest.mark.parametrize("name,mgtype", [("cylinder", 1), ("sphere", 2)])
+def test_solve(gpulib, name, mgtype):
+    case = CASES[name]()
+    case.prm.mgtype = mgtype
+    case.prm.mcyc[0] = 2
+    case.prm.mcyc[case.prm.nlevel - 1] = 5
+    g, o = pair(case)
+    hg, ng, fg = g.solve(use_graph=1)
+    ho, no, fo = o.solve()
+    assert ng == no
+    assert np.max(np.abs(hg - ho) / np.abs(ho)) <= 1e-11
+    L = case.prm.nlevel
+    compare(g, o, "w", L, rtol=1e-11, phys_only=False)
+    assert abs(fg.cd - fo.cd) <= 1e-9 * max(1.0, abs(fo.cd))
+    assert abs(fg.cl - fo.cl) <= 1e-9 * max(1.0, abs(fo.cd))
+
+
+def test_graph_matches_stream(gpulib):
+    case = small_sphere(nlevel=3, n=16, mgtype=2)
+    case.prm.mcyc[0] = 1
+    case.prm.mcyc[1] = 1
+    case.prm.mcyc[2] = 4
+    from code_mge_gb300.runtime import Cycle
+    a = Cycle(case)
+    b = Cycle(case)
+    ha, _, _ = a.solve(use_graph=1)
+    hb, _, _ = b.solve(use_graph=0)
+    assert np.array_equal(ha, hb)
+    assert np.array_equal(a.field("w", 3), b.field("w", 3))
+
+
+def test_embedded_levels(gpulib):
+    case = K.cylinder_embedded(n=24, span=2, nlevel=3, h_fine=0.1, mach=0.3, mcyc_fine=3)
+    case.prm.mcyc[0] = 1
+    case.prm.mcyc[1] = 1
+    g, o = pair(case)
+    hg, ng, _ = g.solve()
+    ho, no, _ = o.solve()
+    assert ng == no
+    assert np.max(np.abs(hg - ho) / np.abs(ho)) <= 1e-11
+    compare(g, o, "w", 3, rtol=1e-11, phys_only=False)
+    compare(g, o, "w", 2, rtol=1e-11, phys_only=False)
