@@ -165,6 +165,7 @@ PRODUCT_ONLY = [
     ("last_cycle_ms", _d, [_vp]),
     ("launch_count", C.c_longlong, [_vp]),
     ("kernel_times", _i, [_vp, _i, _i, _pd, _i]),
+    ("residual_norm_noalloc", _i, [_vp, _vp, _vp, _i, _i, _i, _d, _i, _d, _vp, _vp]),
 ]
 KERNEL_KINDS = ["timestep", "prep", "face", "rec", "combine", "irs_i", "irs_j", "irs_k_update", "cutcell", "bcond",
                 "rtrms"]
@@ -175,7 +176,7 @@ HEADER_SYMBOLS = [
     "mge_last_error", "mge_add_block", "mge_commit", "mge_init_flow", "mge_upload_state",
     "mge_download_state", "mge_download_field", "mge_timestep", "mge_euler", "mge_movco",
     "mge_movfin", "mge_bc_overlap", "mge_get_rtrms", "mge_solve", "mge_forces_compute",
-    "mge_cycle", "mge_last_cycle_ms", "mge_launch_count", "mge_kernel_times", "mge_euler_partial", "mge_device_bytes", "mge_sync",
+    "mge_cycle", "mge_last_cycle_ms", "mge_launch_count", "mge_kernel_times", "mge_residual_norm_noalloc", "mge_euler_partial", "mge_device_bytes", "mge_sync",
 ]
 
 

@@ -206,6 +206,22 @@ long long mge_launch_count(const mge_ctx* ctx);
  * the state of that level. */
 int mge_kernel_times(mge_ctx* ctx, int level, int reps, double* ms_out, int nout);
 
+/* Residual norm rtrms (the quantity of euler.f90:431-447) of one block from
+ * device arrays the caller owns, for callers that cannot allocate device
+ * memory.  No counterpart in the reference: it exists so that a caller that
+ * may not call cudaMalloc (for example inside a stream capture it does not
+ * control, or under a fixed device-memory budget) can still get the norm.
+ * It allocates nothing: its partial sums live in a static 32 KiB device
+ * array, which limits it to nx*ny*nz <= 8,388,608 cells (MGE_EBADCFG beyond).
+ * dw_rho: density residual dw(:,:,:,1); vdtim: local time steps; blank:
+ * int32 blanking, all in the (0:ib,0:jb,0:kb) layout; norm_out: one device
+ * double; stream: a cudaStream_t or NULL.  The first call on a device looks
+ * up the array's device address; make that first call before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU race. */
+int mge_residual_norm_noalloc(const double* dw_rho, const double* vdtim, const int32_t* blank,
+                              int nx, int ny, int nz, double cfl, int vt, double dtim,
+                              double* norm_out, void* stream);
+
 /* Cut-cell wall force integration on the finest level (R-FORCE, new). */
 int mge_forces_compute(mge_ctx* ctx, int level, const mge_solve_opts* opts,
                        mge_forces* out);
