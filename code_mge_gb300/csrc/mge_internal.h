@@ -83,6 +83,7 @@ struct PhysParams {
   int matrix;               // matrix dissipation
   int eqn_ns;
   double smoo;
+  int vt;                   // global time step
 };
 
 // error word bits
@@ -99,7 +100,20 @@ struct IrsTables {
   const double* e2;   // elimination factor
 };
 
+// one euler update as a single cooperative launch (small grids)
+struct EulerLaunch {
+  int mstage, do_timestep, lfir, lres, rt;
+  StageArgs st[8];
+  IrsTables tab[3];
+  double* rt_partial;
+  int npart;
+  double* rt_out;
+  unsigned* err;
+};
+
 // kernel launchers (mge_kernels.cu)
+template <typename T> int launch_euler_coop(const DevBlock<T>& b, const PhysParams& P, const EulerLaunch& L, int device,
+                                            cudaStream_t s);
 template <typename T> void launch_timestep(const DevBlock<T>& b, const PhysParams& P, unsigned* err, cudaStream_t s);
 template <typename T> void launch_stage(const DevBlock<T>& b, const PhysParams& P, const StageArgs& A, unsigned* err,
                                         cudaStream_t s);

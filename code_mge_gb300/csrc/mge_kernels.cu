@@ -26,7 +26,13 @@
 #include <cmath>
 #include <cstdio>
 
+#include <cooperative_groups.h>
+#include <algorithm>
+#include <cstring>
+
 #include "mge_internal.h"
+
+namespace cg = cooperative_groups;
 
 namespace mge {
 
@@ -63,11 +69,10 @@ inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
 // --------------------------------------------------------------- timestep (timestep.f90:39-115)
 // TC is the arithmetic precision (FP64 in the plain path, FP32 in the mixed one).
 template <typename T, typename TC>
-__global__ void k_timestep(DevBlock<T> b, PhysParams P, unsigned* err) {
+__device__ __forceinline__ unsigned long long body_timestep(const DevBlock<T>& b, const PhysParams& P, unsigned* err,
+                                                            long long t) {
   const int nxl = b.nx, nyl = b.ny;
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  long long tot = (long long)b.nx * b.ny * b.nz;
-  if (t >= tot) return;
+  unsigned long long mine = ~0ull;  // bits of this cell's vdtim for the global minimum
   int i = 2 + (int)(t % nxl);
   int j = 2 + (int)((t / nxl) % nyl);
   int k = 2 + (int)(t / ((long long)nxl * nyl));
@@ -77,9 +82,9 @@ __global__ void k_timestep(DevBlock<T> b, PhysParams P, unsigned* err) {
   TC w0 = (TC)b.w[c], w1 = (TC)b.w[N + c], w2 = (TC)b.w[2 * N + c], w3 = (TC)b.w[3 * N + c];
   TC pc = (TC)b.p[c];
   TC cc = gamma * pc / w0;
-  if (cc < TC(0) || cc != cc) {
+  if (cc < TC(0) || cc != cc) {  // timestep.f90:45-48
     atomicOr(err, ERR_NEGPRESS);
-    return;
+    return mine;
   }
   cc = sqrt(fmaxT(cc, TC(0)));
   TC y = TC(1) / w0;
@@ -101,9 +106,8 @@ __global__ void k_timestep(DevBlock<T> b, PhysParams P, unsigned* err) {
   TC dpk = fabs((pkp - p2 + pkm) / (pkp + p2 + pkm + plim));
   TC r = TC(1) / (TC(1) + fminT((TC)P.dimcfl, TC(2) * (dpi + dpj + dpk)));
   TC vd = fict * r;
-  // global minimum (timestep.f90:112), over every physical cell before blanking
   double vdd = (double)vd;
-  if (vdd >= 0.0) atomicMin((unsigned long long*)b.dtim, (unsigned long long)__double_as_longlong(vdd));
+  if (vdd >= 0.0) mine = (unsigned long long)__double_as_longlong(vdd);
   if (b.blank[c] == 0) {  // timestep.f90:212-223
     b.vdtim[c] = T(0);
     b.lam[c] = T(0);
@@ -111,6 +115,38 @@ __global__ void k_timestep(DevBlock<T> b, PhysParams P, unsigned* err) {
     b.vdtim[c] = (T)vd;
     b.lam[c] = (T)lsum;
   }
+  return mine;
+}
+
+// minimum over the calling block, then one atomicMin of its bits on dtim
+// (vdtim >= 0, so the IEEE bit patterns order like the values); every thread
+// of the block must call it
+__device__ __forceinline__ void block_min_to(unsigned long long mine, double* dtim) {
+  __shared__ unsigned long long smin[32];
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned long long q = __shfl_down_sync(0xffffffffu, mine, o);
+    mine = q < mine ? q : mine;
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) smin[wid] = mine;
+  __syncthreads();
+  if (wid == 0) {
+    mine = (lane < (int)(blockDim.x >> 5)) ? smin[lane] : ~0ull;
+    for (int o = 16; o > 0; o >>= 1) {
+      unsigned long long q = __shfl_down_sync(0xffffffffu, mine, o);
+      mine = q < mine ? q : mine;
+    }
+    if (lane == 0 && mine != ~0ull) atomicMin((unsigned long long*)dtim, mine);
+  }
+}
+
+template <typename T, typename TC>
+__global__ void k_timestep(DevBlock<T> b, PhysParams P, unsigned* err) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long mine = ~0ull;
+  if (t < (long long)b.nx * b.ny * b.nz) mine = body_timestep<T, TC>(b, P, err, t);
+  block_min_to(mine, b.dtim);  // global dtim (timestep.f90:112), kept even when vt = 0
 }
 
 template <typename T> __global__ void k_set_scalar(T* p, double v) {
@@ -127,11 +163,8 @@ template <typename T> __global__ void k_dtim_convert(double* src, T* dst) {
 // --------------------------------------------------------------- stage: per-cell pass
 // Box [1..ie]x[1..je]x[1..ke]: every cell whose flux or sensor a face needs.
 template <typename T>
-__global__ void k_prep(DevBlock<T> b, int dissip_on) {
+__device__ __forceinline__ void body_prep(const DevBlock<T>& b, int dissip_on, long long t) {
   const int ex = b.ie, ey = b.je;  // count = ie (cells 1..ie)
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  long long tot = (long long)b.ie * b.je * b.ke;
-  if (t >= tot) return;
   int i = 1 + (int)(t % ex);
   int j = 1 + (int)((t / ex) % ey);
   int k = 1 + (int)(t / ((long long)ex * ey));
@@ -290,11 +323,8 @@ __device__ __forceinline__ void face_dir(const DevBlock<T>& b, const PhysParams&
 }
 
 template <typename T>
-__global__ void k_face(DevBlock<T> b, PhysParams P, int dissip_on, T cd) {
+__device__ __forceinline__ void body_face(const DevBlock<T>& b, const PhysParams& P, int dissip_on, T cd, long long t) {
   const int ex = b.ie - 1, ey = b.je - 1;  // 2..ie
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  long long tot = (long long)(b.ie - 1) * (b.je - 1) * (b.ke - 1);
-  if (t >= tot) return;
   int i = 2 + (int)(t % ex);
   int j = 2 + (int)((t / ex) % ey);
   int k = 2 + (int)(t / ((long long)ex * ey));
@@ -321,9 +351,7 @@ __device__ __forceinline__ void ceflux_axis(int D, const T* w, T p, T s, T* f) {
 }
 
 template <typename T>
-__global__ void k_rec(DevBlock<T> b, PhysParams P, int dissip_on, T cd, unsigned* err) {
-  int m = blockIdx.x * blockDim.x + threadIdx.x;
-  if (m >= b.nmir) return;
+__device__ void body_rec(const DevBlock<T>& b, const PhysParams& P, int dissip_on, T cd, unsigned* err, int m) {
   const long long N = b.N;
   const int* ri = b.rec_i + 8 * m;
   int i = ri[0], j = ri[1], k = ri[2], id = ri[3], zz = ri[4];
@@ -500,11 +528,9 @@ __global__ void k_rec(DevBlock<T> b, PhysParams P, int dissip_on, T cd, unsigned
 
 // --------------------------------------------------------------- stage: combine + update
 template <typename T>
-__global__ void k_combine(DevBlock<T> b, PhysParams P, StageArgs A) {
+__device__ __forceinline__ void body_combine(const DevBlock<T>& b, const PhysParams& P, const StageArgs& A,
+                                             long long t) {
   const int nxl = b.nx, nyl = b.ny;
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  long long tot = (long long)b.nx * b.ny * b.nz;
-  if (t >= tot) return;
   int i = 2 + (int)(t % nxl);
   int j = 2 + (int)((t / nxl) % nyl);
   int k = 2 + (int)(t / ((long long)nxl * nyl));
@@ -616,188 +642,90 @@ __global__ void k_combine(DevBlock<T> b, PhysParams P, StageArgs A) {
 }
 
 // --------------------------------------------------------------- implicit residual smoothing
-// psmoo_old (psmoo.f90:97-242): constant-coefficient Thomas sweeps along
-// i, then j, then k, skipping blanked cells.  One thread per line, the five
-// variables interleaved for FP64 latency hiding.  TC: arithmetic precision.
-template <typename T, typename TC>
-__global__ void k_irs_i(DevBlock<T> b, IrsTables tb, TC bb) {
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long)b.ny * b.nz) return;
-  int j = 2 + (int)(t % b.ny), k = 2 + (int)(t / b.ny);
-  const long long N = b.N;
-  const long long c0 = cidx(b.Pi, b.Pj, 0, j, k);
-  const int il = b.il;
-  TC prev[5];
+// psmoo_old (psmoo.f90:97-242): constant-coefficient Thomas sweeps along i,
+// then j, then k, skipping blanked cells without re-factoring the pivots.
+// One thread per (line, variable); consecutive threads walk consecutive
+// lines of one variable, so the j- and k-sweeps are coalesced.  TC is the
+// arithmetic precision.
+template <typename T, int D>
+__device__ __forceinline__ long long irs_lines(const DevBlock<T>& b) {
+  return D == 0 ? (long long)b.ny * b.nz : (D == 1 ? (long long)b.nx * b.nz : (long long)b.nx * b.ny);
+}
+
+template <typename T, typename TC, int D>
+__device__ __forceinline__ void body_irs(const DevBlock<T>& b, const IrsTables& tb, TC bb, long long t) {
+  const long long lines = irs_lines<T, D>(b);
+  const int v = (int)(t / lines);
+  const long long ln = t - (long long)v * lines;
+  long long c0, st;
+  int l;
+  if (D == 0) {
+    int j = 2 + (int)(ln % b.ny), k = 2 + (int)(ln / b.ny);
+    c0 = cidx(b.Pi, b.Pj, 0, j, k);
+    st = 1;
+    l = b.il;
+  } else if (D == 1) {
+    int i = 2 + (int)(ln % b.nx), k = 2 + (int)(ln / b.nx);
+    c0 = cidx(b.Pi, b.Pj, i, 0, k);
+    st = b.Pi;
+    l = b.jl;
+  } else {
+    int i = 2 + (int)(ln % b.nx), j = 2 + (int)(ln / b.nx);
+    c0 = cidx(b.Pi, b.Pj, i, j, 0);
+    st = (long long)b.Pi * b.Pj;
+    l = b.kl;
+  }
+  T* d = b.dw + (long long)v * b.N;
+  TC prev;
   {
-    long long c = c0 + 2;
-    bool on = b.blank[c] != 0;
-    TC e1 = (TC)tb.e1[2];
-#pragma unroll
-    for (int v = 0; v < 5; v++) {
-      TC d = (TC)b.dw[v * N + c];
-      if (on) {
-        d = d / e1;
-        b.dw[v * N + c] = (T)d;
-      }
-      prev[v] = d;
+    long long c = c0 + 2 * st;
+    TC x = (TC)d[c];
+    if (b.blank[c] != 0) {
+      x = x / (TC)tb.e1[2];
+      d[c] = (T)x;
     }
+    prev = x;
   }
-  for (int i = 3; i <= il; i++) {
-    long long c = c0 + i;
-    bool on = b.blank[c] != 0;
-    TC e1 = (TC)tb.e1[i], y = (TC)tb.e1r[i];
-#pragma unroll
-    for (int v = 0; v < 5; v++) {
-      TC d = (TC)b.dw[v * N + c];
-      if (on) {
-        d = mdiv(d - bb * prev[v], e1, y);
-        b.dw[v * N + c] = (T)d;
-      }
-      prev[v] = d;
+  for (int q = 3; q <= l; q++) {
+    long long c = c0 + q * st;
+    TC x = (TC)d[c];
+    if (b.blank[c] != 0) {
+      x = mdiv(x - bb * prev, (TC)tb.e1[q], (TC)tb.e1r[q]);
+      d[c] = (T)x;
     }
+    prev = x;
   }
-  // backward: ir = il-1 .. 2 ; prev holds dw(il)
-  for (int ir = il - 1; ir >= 2; ir--) {
-    long long c = c0 + ir;
-    bool on = b.blank[c] != 0;
-    TC e2 = (TC)tb.e2[ir];
-#pragma unroll
-    for (int v = 0; v < 5; v++) {
-      TC d = (TC)b.dw[v * N + c];
-      if (on) {
-        d = d - e2 * prev[v];
-        b.dw[v * N + c] = (T)d;
-      }
-      prev[v] = d;
+  for (int q = l - 1; q >= 2; q--) {
+    long long c = c0 + q * st;
+    TC x = (TC)d[c];
+    if (b.blank[c] != 0) {
+      x = x - (TC)tb.e2[q] * prev;
+      d[c] = (T)x;
     }
+    prev = x;
   }
 }
 
-template <typename T, typename TC>
-__global__ void k_irs_j(DevBlock<T> b, IrsTables tb, TC bb) {
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long)b.nx * b.nz) return;
-  int i = 2 + (int)(t % b.nx), k = 2 + (int)(t / b.nx);
+// update after smoothing, euler.f90:381-399 (steady: lam = 1)
+template <typename T>
+__device__ __forceinline__ void body_update(const DevBlock<T>& b, const PhysParams& P, long long t) {
+  int i = 2 + (int)(t % b.nx);
+  int j = 2 + (int)((t / b.nx) % b.ny);
+  int k = 2 + (int)(t / ((long long)b.nx * b.ny));
   const long long N = b.N;
-  const long long sj = b.Pi;
-  const long long c0 = cidx(b.Pi, b.Pj, i, 0, k);
-  const int jl = b.jl;
-  TC prev[5];
-  {
-    long long c = c0 + 2 * sj;
-    bool on = b.blank[c] != 0;
-    TC e1 = (TC)tb.e1[2];
+  const long long c = cidx(b.Pi, b.Pj, i, j, k);
+  T wv[5];
 #pragma unroll
-    for (int v = 0; v < 5; v++) {
-      TC d = (TC)b.dw[v * N + c];
-      if (on) {
-        d = d / e1;
-        b.dw[v * N + c] = (T)d;
-      }
-      prev[v] = d;
-    }
+  for (int v = 0; v < 5; v++) {
+    wv[v] = b.wn[v * N + c] - b.dw[v * N + c];
+    b.w[v * N + c] = wv[v];
   }
-  for (int j = 3; j <= jl; j++) {
-    long long c = c0 + j * sj;
-    bool on = b.blank[c] != 0;
-    TC e1 = (TC)tb.e1[j], y = (TC)tb.e1r[j];
-#pragma unroll
-    for (int v = 0; v < 5; v++) {
-      TC d = (TC)b.dw[v * N + c];
-      if (on) {
-        d = mdiv(d - bb * prev[v], e1, y);
-        b.dw[v * N + c] = (T)d;
-      }
-      prev[v] = d;
-    }
-  }
-  for (int jr = jl - 1; jr >= 2; jr--) {
-    long long c = c0 + jr * sj;
-    bool on = b.blank[c] != 0;
-    TC e2 = (TC)tb.e2[jr];
-#pragma unroll
-    for (int v = 0; v < 5; v++) {
-      TC d = (TC)b.dw[v * N + c];
-      if (on) {
-        d = d - e2 * prev[v];
-        b.dw[v * N + c] = (T)d;
-      }
-      prev[v] = d;
-    }
-  }
-}
-
-// k-lines, then the update w = wn - dw and depvars (euler.f90:381-399)
-template <typename T, typename TC>
-__global__ void k_irs_k_update(DevBlock<T> b, IrsTables tb, TC bb, PhysParams P) {
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long)b.nx * b.ny) return;
-  int i = 2 + (int)(t % b.nx), j = 2 + (int)(t / b.nx);
-  const long long N = b.N;
-  const long long sk = (long long)b.Pi * b.Pj;
-  const long long c0 = cidx(b.Pi, b.Pj, i, j, 0);
-  const int kl = b.kl;
-  TC prev[5];
-  {
-    long long c = c0 + 2 * sk;
-    bool on = b.blank[c] != 0;
-    TC e1 = (TC)tb.e1[2];
-#pragma unroll
-    for (int v = 0; v < 5; v++) {
-      TC d = (TC)b.dw[v * N + c];
-      if (on) {
-        d = d / e1;
-        b.dw[v * N + c] = (T)d;
-      }
-      prev[v] = d;
-    }
-  }
-  for (int k = 3; k <= kl; k++) {
-    long long c = c0 + k * sk;
-    bool on = b.blank[c] != 0;
-    TC e1 = (TC)tb.e1[k], y = (TC)tb.e1r[k];
-#pragma unroll
-    for (int v = 0; v < 5; v++) {
-      TC d = (TC)b.dw[v * N + c];
-      if (on) {
-        d = mdiv(d - bb * prev[v], e1, y);
-        b.dw[v * N + c] = (T)d;
-      }
-      prev[v] = d;
-    }
-  }
-  const T gamma = (T)P.gamma;
-  auto update = [&](long long c, const TC* dv) {
-    T wv[5];
-#pragma unroll
-    for (int v = 0; v < 5; v++) {
-      wv[v] = b.wn[v * N + c] - (T)dv[v];
-      b.w[v * N + c] = wv[v];
-    }
-    b.p[c] = depvars(gamma, wv);
-  };
-  update(c0 + kl * sk, prev);
-  for (int kr = kl - 1; kr >= 2; kr--) {
-    long long c = c0 + kr * sk;
-    bool on = b.blank[c] != 0;
-    TC e2 = (TC)tb.e2[kr];
-#pragma unroll
-    for (int v = 0; v < 5; v++) {
-      TC d = (TC)b.dw[v * N + c];
-      if (on) {
-        d = d - e2 * prev[v];
-        b.dw[v * N + c] = (T)d;
-      }
-      prev[v] = d;
-    }
-    update(c, prev);
-  }
+  b.p[c] = depvars((T)P.gamma, wv);
 }
 
 // --------------------------------------------------------------- bc_cutcell (bc_cutcell.f90:40-268)
 template <typename T>
-__global__ void k_cutcell(DevBlock<T> b, PhysParams P, unsigned* err) {
-  int m = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ void body_cutcell(const DevBlock<T>& b, const PhysParams& P, unsigned* err, int m) {
   if (m >= b.nmir || m > b.m0) return;
   T* ws = b.rec_wsol + 5LL * m;
   if (m == b.m0) {  // empty cloud: zero this record; the reference returns here
@@ -849,12 +777,15 @@ __global__ void k_cutcell(DevBlock<T> b, PhysParams P, unsigned* err) {
 // One launch per face in the order 1..6 of bcond.f90:16-39: later faces read
 // and overwrite ghost cells that earlier faces wrote.
 template <typename T>
-__global__ void k_bc_face(DevBlock<T> b, PhysParams P, int face) {
+__device__ __forceinline__ long long bc_face_items(const DevBlock<T>& b, int face) {
+  const int ax = (face - 1) % 3;
+  return (long long)((ax == 0 ? b.jb : b.ib) + 1) * ((ax == 2 ? b.jb : b.kb) + 1);
+}
+
+template <typename T>
+__device__ void body_bc_face(const DevBlock<T>& b, const PhysParams& P, int face, long long t) {
   const int ax = (face - 1) % 3;
   const int na = (ax == 0 ? b.jb : b.ib) + 1;  // first tangential extent
-  const int nbt = (ax == 2 ? b.jb : b.kb) + 1;
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long)na * nbt) return;
   int t1 = (int)(t % na), t2 = (int)(t / na);
   const int kind = b.bctype[face - 1];
   const int lcur = ax == 0 ? b.il : (ax == 1 ? b.jl : b.kl);
@@ -965,7 +896,7 @@ __global__ void k_bc_face(DevBlock<T> b, PhysParams P, int face) {
 
 // bc_corner.f90:23-157 in one block: three dependent phases
 template <typename T>
-__global__ void k_bc_corner(DevBlock<T> b, PhysParams P) {
+__device__ void body_corner(const DevBlock<T>& b, const PhysParams& P) {
   const long long N = b.N;
   const int il = b.il, jl = b.jl, kl = b.kl, ie = b.ie, je = b.je, ke = b.ke;
   const T gamma = (T)P.gamma;
@@ -1029,6 +960,11 @@ __global__ void k_bc_corner(DevBlock<T> b, PhysParams P) {
   }
 }
 
+template <typename T>
+__global__ void k_bc_corner(DevBlock<T> b, PhysParams P) {
+  body_corner(b, P);
+}
+
 // --------------------------------------------------------------- residual norm (euler.f90:431-447)
 // Deterministic: fixed partial ranges, fixed-order tree per block, one final block.
 constexpr int RT_THREADS = 256;
@@ -1039,11 +975,11 @@ int rtrms_partials(long long ncells) {
 }
 
 template <typename T>
-__global__ void k_rtrms_partial(DevBlock<T> b, double cfl, int vt, double* partial, int npart) {
+__device__ void body_rtrms_partial(const DevBlock<T>& b, double cfl, int vt, double* partial, int npart, int part) {
   __shared__ double sh[RT_THREADS];
   const long long tot = (long long)b.nx * b.ny * b.nz;
   const long long per = (tot + npart - 1) / npart;
-  const long long lo = (long long)blockIdx.x * per, hi = min(tot, lo + per);
+  const long long lo = (long long)part * per, hi = min(tot, lo + per);
   double acc = 0.0;
   for (long long t = lo + threadIdx.x; t < hi; t += blockDim.x) {
     int i = 2 + (int)(t % b.nx);
@@ -1061,15 +997,23 @@ __global__ void k_rtrms_partial(DevBlock<T> b, double cfl, int vt, double* parti
     if (threadIdx.x < s) sh[threadIdx.x] = sh[threadIdx.x] + sh[threadIdx.x + s];
     __syncthreads();
   }
-  if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
+  if (threadIdx.x == 0) partial[part] = sh[0];
+  __syncthreads();
+}
+
+template <typename T>
+__global__ void k_rtrms_partial(DevBlock<T> b, double cfl, int vt, double* partial, int npart) {
+  body_rtrms_partial(b, cfl, vt, partial, npart, blockIdx.x);
+}
+
+__device__ __forceinline__ void body_rtrms_final(const double* partial, int npart, double ncell, double* out) {
+  double a = 0.0;
+  for (int q = 0; q < npart; q++) a = a + partial[q];
+  *out = sqrt(a / ncell);
 }
 
 __global__ void k_rtrms_final(const double* partial, int npart, double ncell, double* out) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) {
-    double a = 0.0;
-    for (int q = 0; q < npart; q++) a = a + partial[q];
-    *out = sqrt(a / ncell);
-  }
+  if (threadIdx.x == 0 && blockIdx.x == 0) body_rtrms_final(partial, npart, ncell, out);
 }
 
 // --------------------------------------------------------------- small whole-array kernels
@@ -1090,9 +1034,7 @@ __global__ void k_copy5(const T* __restrict__ src, T* __restrict__ dst, long lon
 
 // wn = w on physical cells, dw = fw = 0 everywhere (euler.f90:80-89)
 template <typename T>
-__global__ void k_save_wn(DevBlock<T> b) {
-  long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= b.N) return;
+__device__ __forceinline__ void body_save_wn(const DevBlock<T>& b, long long c) {
   const long long N = b.N;
   int i = (int)(c % b.Pi);
   int j = (int)((c / b.Pi) % b.Pj);
@@ -1103,6 +1045,12 @@ __global__ void k_save_wn(DevBlock<T> b) {
     b.dw[v * N + c] = T(0);
     b.fw[v * N + c] = T(0);
   }
+}
+
+template <typename T>
+__global__ void k_save_wn(DevBlock<T> b) {
+  long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < b.N) body_save_wn(b, c);
 }
 
 // wn = w on physical cells only (movco.f90:29-35)
@@ -1305,12 +1253,136 @@ __global__ void k_forces(DevBlock<T> b, double ox, double oy, double oz, double 
   if (threadIdx.x < 6) out[threadIdx.x] = sh[threadIdx.x][0];
 }
 
+// =============================================================== one-launch-per-phase kernels
+template <typename T>
+__global__ void k_prep(DevBlock<T> b, int dissip_on) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < (long long)b.ie * b.je * b.ke) body_prep(b, dissip_on, t);
+}
+template <typename T>
+__global__ void k_face(DevBlock<T> b, PhysParams P, int dissip_on, T cd) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < (long long)(b.ie - 1) * (b.je - 1) * (b.ke - 1)) body_face(b, P, dissip_on, cd, t);
+}
+template <typename T>
+__global__ void k_rec(DevBlock<T> b, PhysParams P, int dissip_on, T cd, unsigned* err) {
+  int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m < b.nmir) body_rec(b, P, dissip_on, cd, err, m);
+}
+template <typename T>
+__global__ void k_combine(DevBlock<T> b, PhysParams P, StageArgs A) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < (long long)b.nx * b.ny * b.nz) body_combine(b, P, A, t);
+}
+template <typename T, typename TC, int D>
+__global__ void k_irs(DevBlock<T> b, IrsTables tb, TC bb) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < 5 * irs_lines<T, D>(b)) body_irs<T, TC, D>(b, tb, bb, t);
+}
+template <typename T>
+__global__ void k_update(DevBlock<T> b, PhysParams P) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < (long long)b.nx * b.ny * b.nz) body_update(b, P, t);
+}
+template <typename T>
+__global__ void k_cutcell(DevBlock<T> b, PhysParams P, unsigned* err) {
+  int m = blockIdx.x * blockDim.x + threadIdx.x;
+  body_cutcell(b, P, err, m);
+}
+template <typename T>
+__global__ void k_bc_face(DevBlock<T> b, PhysParams P, int face) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < bc_face_items(b, face)) body_bc_face(b, P, face, t);
+}
+
+// =============================================================== one euler update in one launch
+// For the small coarse grids of the multigrid hierarchy every phase of
+// euler.f90 is latency-bound, so one cooperative kernel runs them all with a
+// grid-wide barrier between phases instead of ~70 launches.
+struct EulerArgs {
+  int mstage;
+  int do_timestep;   // timestep.f90 before euler (solver.f90:154,218)
+  int lfir, lres, rt;
+  int smoo_on;
+  StageArgs st[8];
+  IrsTables tab[3];
+  double* rt_partial;
+  int npart;
+  double* rt_out;
+  unsigned* err;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_euler_coop(DevBlock<T> b, PhysParams P, EulerArgs E) {
+  cg::grid_group g = cg::this_grid();
+  const long long gt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long gs = (long long)gridDim.x * blockDim.x;
+  const long long ncell = (long long)b.nx * b.ny * b.nz;
+  if (E.do_timestep) {
+    if (gt == 0) *b.dtim = 10.0;
+    g.sync();
+    for (long long base = (long long)blockIdx.x * blockDim.x; base < ncell; base += gs) {
+      long long t = base + threadIdx.x;
+      unsigned long long mine = ~0ull;
+      if (t < ncell) mine = body_timestep<T, T>(b, P, E.err, t);
+      block_min_to(mine, b.dtim);
+    }
+    g.sync();
+  }
+  if (E.lfir)
+    for (long long q = gt; q < 5 * b.N; q += gs) b.ws[q] = b.w[q];
+  for (long long q = gt; q < b.N; q += gs) body_save_wn(b, q);
+  g.sync();
+  const long long nprep = (long long)b.ie * b.je * b.ke;
+  const long long nface = (long long)(b.ie - 1) * (b.je - 1) * (b.ke - 1);
+  for (int m = 1; m <= E.mstage; m++) {
+    const StageArgs& A = E.st[m - 1];
+    for (long long t = gt; t < nprep; t += gs) body_prep(b, A.dissip_on, t);
+    g.sync();
+    for (long long t = gt; t < nface; t += gs) body_face(b, P, A.dissip_on, (T)A.cd, t);
+    g.sync();
+    if (b.nmir > 0) {
+      for (long long t = gt; t < b.nmir; t += gs) body_rec(b, P, A.dissip_on, (T)A.cd, E.err, (int)t);
+      g.sync();
+    }
+    for (long long t = gt; t < ncell; t += gs) body_combine(b, P, A, t);
+    g.sync();
+    if (E.lres) return;
+    if (A.irs) {
+      const T bb = (T)(-P.smoo);
+      for (long long t = gt; t < 5 * irs_lines<T, 0>(b); t += gs) body_irs<T, T, 0>(b, E.tab[0], bb, t);
+      g.sync();
+      for (long long t = gt; t < 5 * irs_lines<T, 1>(b); t += gs) body_irs<T, T, 1>(b, E.tab[1], bb, t);
+      g.sync();
+      for (long long t = gt; t < 5 * irs_lines<T, 2>(b); t += gs) body_irs<T, T, 2>(b, E.tab[2], bb, t);
+      g.sync();
+      for (long long t = gt; t < ncell; t += gs) body_update(b, P, t);
+      g.sync();
+    }
+    for (long long t = gt; t < b.nmir; t += gs) body_cutcell(b, P, E.err, (int)t);
+    g.sync();
+    for (int f = 1; f <= 6; f++) {
+      if (b.bctype[f - 1] == 0) continue;
+      const long long nf = bc_face_items(b, f);
+      for (long long t = gt; t < nf; t += gs) body_bc_face(b, P, f, t);
+      g.sync();
+    }
+    if (blockIdx.x == 0) body_corner(b, P);
+    g.sync();
+  }
+  if (E.rt) {
+    for (int part = blockIdx.x; part < E.npart; part += gridDim.x)
+      body_rtrms_partial(b, P.cfl, P.vt, E.rt_partial, E.npart, part);
+    g.sync();
+    if (gt == 0) body_rtrms_final(E.rt_partial, E.npart, (double)ncell, E.rt_out);
+  }
+}
+
 // =============================================================== launchers
 constexpr int TPB = 256;
 
 template <typename T>
 void launch_timestep(const DevBlock<T>& b, const PhysParams& P, unsigned* err, cudaStream_t s) {
-  // dtim is accumulated as an FP64 bit pattern in the scalar slot of the double scratch
   long long n = (long long)b.nx * b.ny * b.nz;
   k_dtim_reset<<<1, 32, 0, s>>>(b.dtim);
   k_timestep<T, T><<<nblk(n, TPB), TPB, 0, s>>>(b, P, err);
@@ -1341,9 +1413,13 @@ void launch_stage(const DevBlock<T>& b, const PhysParams& P, const StageArgs& A,
 template <typename T>
 void launch_irs_part(int part, const DevBlock<T>& b, const PhysParams& P, const IrsTables* tab, cudaStream_t s) {
   const T bb = (T)(-P.smoo);
-  if (part == 0) k_irs_i<T, T><<<nblk((long long)b.ny * b.nz, 128), 128, 0, s>>>(b, tab[0], bb);
-  if (part == 1) k_irs_j<T, T><<<nblk((long long)b.nx * b.nz, 128), 128, 0, s>>>(b, tab[1], bb);
-  if (part == 2) k_irs_k_update<T, T><<<nblk((long long)b.nx * b.ny, 128), 128, 0, s>>>(b, tab[2], bb, P);
+  const long long ncell = (long long)b.nx * b.ny * b.nz;
+  if (part == 0) k_irs<T, T, 0><<<nblk(5 * (long long)b.ny * b.nz, 128), 128, 0, s>>>(b, tab[0], bb);
+  if (part == 1) k_irs<T, T, 1><<<nblk(5 * (long long)b.nx * b.nz, 128), 128, 0, s>>>(b, tab[1], bb);
+  if (part == 2) {
+    k_irs<T, T, 2><<<nblk(5 * (long long)b.nx * b.ny, 128), 128, 0, s>>>(b, tab[2], bb);
+    k_update<T><<<nblk(ncell, TPB), TPB, 0, s>>>(b, P);
+  }
 }
 
 template <typename T>
@@ -1372,6 +1448,48 @@ void launch_rtrms(const DevBlock<T>& b, const PhysParams& P, int vt, double* par
                   cudaStream_t s) {
   k_rtrms_partial<T><<<npartial, RT_THREADS, 0, s>>>(b, P.cfl, vt, partial, npartial);
   k_rtrms_final<<<1, 32, 0, s>>>(partial, npartial, (double)b.nx * b.ny * b.nz, out);
+}
+
+// grid of the cooperative kernel: every block resident at once
+template <typename T>
+int coop_grid(int device) {
+  static int cached[64] = {0};
+  if (device < 0 || device >= 64) return 0;
+  if (cached[device]) return cached[device];
+  int nsm = 0, per = 0;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_euler_coop<T>, 256, 0);
+  int coop = 0;
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device);
+  cached[device] = (coop && per > 0) ? nsm * per : -1;
+  return cached[device];
+}
+
+template <typename T>
+int launch_euler_coop(const DevBlock<T>& b, const PhysParams& P, const EulerLaunch& L, int device, cudaStream_t s) {
+  int grid = coop_grid<T>(device);
+  if (grid <= 0) return -1;
+  long long work = (long long)(b.ie) * b.je * b.ke;
+  int need = (int)std::min<long long>((work + 255) / 256, (long long)grid);
+  if (need < 1) need = 1;
+  EulerArgs E;
+  memset(&E, 0, sizeof(E));
+  E.mstage = L.mstage;
+  E.do_timestep = L.do_timestep;
+  E.lfir = L.lfir;
+  E.lres = L.lres;
+  E.rt = L.rt;
+  for (int m = 0; m < L.mstage && m < 8; m++) E.st[m] = L.st[m];
+  for (int d = 0; d < 3; d++) E.tab[d] = L.tab[d];
+  E.rt_partial = L.rt_partial;
+  E.npart = L.npart;
+  E.rt_out = L.rt_out;
+  E.err = L.err;
+  DevBlock<T> bb = b;
+  PhysParams pp = P;
+  void* args[] = {&bb, &pp, &E};
+  cudaError_t e = cudaLaunchCooperativeKernel((void*)k_euler_coop<T>, need, 256, args, 0, s);
+  return e == cudaSuccess ? 0 : -2;
 }
 
 template <typename T>
@@ -1448,6 +1566,7 @@ void launch_forces(const DevBlock<T>& b, const double* origin, const double* h, 
   template void launch_stage_part<T>(int, const DevBlock<T>&, const PhysParams&, const StageArgs&, unsigned*,       \
                                      cudaStream_t);                                                             \
   template void launch_irs_part<T>(int, const DevBlock<T>&, const PhysParams&, const IrsTables*, cudaStream_t);  \
+  template int launch_euler_coop<T>(const DevBlock<T>&, const PhysParams&, const EulerLaunch&, int, cudaStream_t); \
   template void launch_irs<T>(const DevBlock<T>&, const PhysParams&, const IrsTables*, cudaStream_t);           \
   template void launch_cutcell<T>(const DevBlock<T>&, const PhysParams&, unsigned*, cudaStream_t);              \
   template void launch_bcond<T>(const DevBlock<T>&, const PhysParams&, cudaStream_t);                           \

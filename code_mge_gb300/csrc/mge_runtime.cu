@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <string>
@@ -80,6 +81,7 @@ struct mge_ctx {
   double last_cycle_ms = 0.0;
   std::vector<long long> graph_kernels;  // kernel nodes per captured cycle
   long long launches = 0;                // kernels launched through mge_cycle
+  long long coop_max_cells = 300000;     // blocks up to this size run euler as one cooperative launch
 };
 
 namespace {
@@ -138,32 +140,57 @@ int check_err(mge_ctx* c) {
 // ---------------------------------------------------------------- device ops
 void enqueue_timestep(mge_ctx* c, Block& b) { launch_timestep<double>(b.dev, c->P, c->d_err, c->stream); }
 
-// euler.f90:1-462 on one block; nstage_limit > 0 stops early (parity probes)
-void enqueue_euler(mge_ctx* c, Block& b, int mgl, int mlvl, bool lres, bool lfir, int nstage_limit, bool rt) {
+StageArgs stage_args(const mge_params& P, int m, int mgl, int mlvl, bool lres, bool lfir) {
+  StageArgs A;
+  A.m = m;
+  A.fn = P.cstp[m - 1] * P.cfl;
+  A.cd = P.cdis[m - 1];
+  A.dissip_on = P.cdis[m - 1] > 0.0;
+  A.scale_fw = m > 1;
+  A.forcing = mgl < mlvl;
+  A.first_forcing = lfir && m == 1;
+  A.lres = lres;
+  A.irs = (m % 2 != 0) && P.smoo > 0.0 && !lres;
+  A.vt = P.vt;
+  return A;
+}
+
+// timestep.f90 (optionally) followed by euler.f90:1-462 on one block;
+// nstage_limit > 0 stops after that stage (parity probes)
+void enqueue_euler(mge_ctx* c, Block& b, int mgl, int mlvl, bool lres, bool lfir, int nstage_limit, bool rt,
+                   bool with_timestep = false) {
   const mge_params& P = c->prm;
+  const int mstage = (nstage_limit > 0) ? std::min(P.mstage, nstage_limit) : P.mstage;
+  const bool want_rt = rt && (nstage_limit <= 0 || nstage_limit >= P.mstage) && !lres;
+  if ((long long)b.nx * b.ny * b.nz <= c->coop_max_cells) {
+    EulerLaunch L;
+    std::memset(&L, 0, sizeof(L));
+    L.mstage = mstage;
+    L.do_timestep = with_timestep;
+    L.lfir = lfir;
+    L.lres = lres;
+    L.rt = want_rt;
+    for (int m = 1; m <= mstage; m++) L.st[m - 1] = stage_args(P, m, mgl, mlvl, lres, lfir);
+    for (int d = 0; d < 3; d++) L.tab[d] = b.tabs[d];
+    L.rt_partial = b.rt_partial;
+    L.npart = b.npart;
+    L.rt_out = b.rt_cur;
+    L.err = c->d_err;
+    if (launch_euler_coop<double>(b.dev, c->P, L, c->device, c->stream) == 0) return;
+    cudaGetLastError();  // cooperative launch unavailable: fall through to per-phase launches
+  }
+  if (with_timestep) enqueue_timestep(c, b);
   if (lfir) launch_copy_ws<double>(b.dev, c->stream);
   launch_save_wn<double>(b.dev, c->stream);
-  const int mstage = (nstage_limit > 0) ? std::min(P.mstage, nstage_limit) : P.mstage;
   for (int m = 1; m <= mstage; m++) {
-    StageArgs A;
-    A.m = m;
-    A.fn = P.cstp[m - 1] * P.cfl;
-    A.cd = P.cdis[m - 1];
-    A.dissip_on = P.cdis[m - 1] > 0.0;
-    A.scale_fw = m > 1;
-    A.forcing = mgl < mlvl;
-    A.first_forcing = lfir && m == 1;
-    A.lres = lres;
-    A.irs = (m % 2 != 0) && P.smoo > 0.0 && !lres;
-    A.vt = P.vt;
+    StageArgs A = stage_args(P, m, mgl, mlvl, lres, lfir);
     launch_stage<double>(b.dev, c->P, A, c->d_err, c->stream);
     if (lres) return;
     if (A.irs) launch_irs<double>(b.dev, c->P, b.tabs, c->stream);
     launch_cutcell<double>(b.dev, c->P, c->d_err, c->stream);
     launch_bcond<double>(b.dev, c->P, c->stream);
   }
-  if (rt && (nstage_limit <= 0 || nstage_limit >= P.mstage))
-    launch_rtrms<double>(b.dev, c->P, P.vt, b.rt_partial, b.npart, b.rt_cur, c->stream);
+  if (want_rt) launch_rtrms<double>(b.dev, c->P, P.vt, b.rt_partial, b.npart, b.rt_cur, c->stream);
 }
 
 void enqueue_movco(mge_ctx* c, int mgl) {  // movco.f90:21-47
@@ -203,10 +230,7 @@ void enqueue_cycle(mge_ctx* c, int mlvl) {
     for (;;) {  // lopr
       icyc[mgl] += 1;
       bool lfir = (mgl != mlvl);
-      for (Block& b : c->lv[mgl - 1]) {
-        enqueue_timestep(c, b);
-        enqueue_euler(c, b, mgl, mlvl, false, lfir, 0, mgl == mlvl);
-      }
+      for (Block& b : c->lv[mgl - 1]) enqueue_euler(c, b, mgl, mlvl, false, lfir, 0, mgl == mlvl, true);
       if (mlvl == 1) return;
       for (Block& b : c->lv[mgl - 1]) enqueue_euler(c, b, mgl, mlvl, true, false, 0, false);
       mgl = mgl - 1;
@@ -215,10 +239,7 @@ void enqueue_cycle(mge_ctx* c, int mlvl) {
     }
     bool lfir = true;
     for (;;) {  // lopp
-      for (Block& b : c->lv[mgl - 1]) {
-        enqueue_timestep(c, b);
-        enqueue_euler(c, b, mgl, mlvl, false, lfir, 0, false);
-      }
+      for (Block& b : c->lv[mgl - 1]) enqueue_euler(c, b, mgl, mlvl, false, lfir, 0, false, true);
       lfir = false;
       mgl = mgl + 1;
       enqueue_movfin(c, mgl, mlvl);
@@ -250,6 +271,7 @@ void build_phys(mge_ctx* c) {
   Q.matrix = P.dissip == MGE_DISSIP_MATRIX;
   Q.eqn_ns = P.eqntype == MGE_EQN_NS;
   Q.smoo = P.smoo;
+  Q.vt = P.vt;
 }
 
 // psmoo.f90:136-166 pivots for a line of l-1 unknowns (rows 2..l)
@@ -500,6 +522,7 @@ int mge_init(const mge_params* prm, int device, mge_ctx** out) {
   }
   c->lv.resize(prm->nlevel);
   build_phys(c);
+  if (const char* e = getenv("MGE_COOP_MAX_CELLS")) c->coop_max_cells = atoll(e);
   *out = c;
   return MGE_OK;
 }

@@ -25,9 +25,23 @@ def exact_fraction(a, b):
     return float(np.mean(a == b)) if a.size else 1.0
 
 
-def pair(case, develop_cycles=0):
+PATHS = ("coop", "phases")
+
+
+def set_path(path):
+    """Small blocks run euler as one cooperative launch; 'phases' forces one
+    launch per phase (the path of large blocks)."""
+    import os
+    if path == "phases":
+        os.environ["MGE_COOP_MAX_CELLS"] = "0"
+    else:
+        os.environ.pop("MGE_COOP_MAX_CELLS", None)
+
+
+def pair(case, develop_cycles=0, path="coop"):
     """(gpu, oracle) Cycles on the same case; optionally develop the flow on the
     oracle for a few cycles and load that state into both."""
+    set_path(path)
     o = OracleCycle(case)
     g = Cycle(case)
     if develop_cycles:

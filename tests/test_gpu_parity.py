@@ -8,7 +8,7 @@ import pytest
 
 from code_mge_gb300 import _abi as A
 from code_mge_gb300 import cases as K
-from parity import RTOL, compare, pair, small_cylinder, small_sphere
+from parity import PATHS, RTOL, compare, pair, set_path, small_cylinder, small_sphere
 
 pytestmark = pytest.mark.gpu
 
@@ -43,10 +43,11 @@ def test_timestep(gpulib, name):
     assert abs(g.field("dtim", L) - o.field("dtim", L)) <= RTOL * abs(o.field("dtim", L))
 
 
+@pytest.mark.parametrize("path", PATHS)
 @pytest.mark.parametrize("name", list(CASES))
 @pytest.mark.parametrize("nstage", [1, 2, 3, 4, 5])
-def test_stage(gpulib, name, nstage):
-    g, o = pair(CASES[name](), develop_cycles=3)
+def test_stage(gpulib, name, nstage, path):
+    g, o = pair(CASES[name](), develop_cycles=3, path=path)
     L = g.case.prm.nlevel
     for c in (g, o):
         c.timestep(L)
@@ -59,9 +60,10 @@ def test_stage(gpulib, name, nstage):
         compare(g, o, "wsol", L)
 
 
+@pytest.mark.parametrize("path", PATHS)
 @pytest.mark.parametrize("name", list(CASES))
-def test_euler_rtrms_and_residual(gpulib, name):
-    g, o = pair(CASES[name](), develop_cycles=3)
+def test_euler_rtrms_and_residual(gpulib, name, path):
+    g, o = pair(CASES[name](), develop_cycles=3, path=path)
     L = g.case.prm.nlevel
     for c in (g, o):
         c.timestep(L)
@@ -74,9 +76,10 @@ def test_euler_rtrms_and_residual(gpulib, name):
     compare(g, o, "dw", L)
 
 
+@pytest.mark.parametrize("path", PATHS)
 @pytest.mark.parametrize("name", ["cylinder", "sphere"])
-def test_transfer(gpulib, name):
-    g, o = pair(CASES[name](), develop_cycles=3)
+def test_transfer(gpulib, name, path):
+    g, o = pair(CASES[name](), develop_cycles=3, path=path)
     L = g.case.prm.nlevel
     for c in (g, o):
         c.timestep(L)
@@ -94,13 +97,14 @@ def test_transfer(gpulib, name):
     compare(g, o, "p", L, phys_only=False)
 
 
+@pytest.mark.parametrize("path", PATHS)
 @pytest.mark.parametrize("name,mgtype", [("cylinder", 1), ("sphere", 2)])
-def test_solve(gpulib, name, mgtype):
+def test_solve(gpulib, name, mgtype, path):
     case = CASES[name]()
     case.prm.mgtype = mgtype
     case.prm.mcyc[0] = 2
     case.prm.mcyc[case.prm.nlevel - 1] = 5
-    g, o = pair(case)
+    g, o = pair(case, path=path)
     hg, ng, fg = g.solve(use_graph=1)
     ho, no, fo = o.solve()
     assert ng == no
@@ -111,7 +115,9 @@ def test_solve(gpulib, name, mgtype):
     assert abs(fg.cl - fo.cl) <= 1e-9 * max(1.0, abs(fo.cd))
 
 
-def test_graph_matches_stream(gpulib):
+@pytest.mark.parametrize("path", PATHS)
+def test_graph_matches_stream(gpulib, path):
+    set_path(path)
     case = small_sphere(nlevel=3, n=16, mgtype=2)
     case.prm.mcyc[0] = 1
     case.prm.mcyc[1] = 1
@@ -125,14 +131,36 @@ def test_graph_matches_stream(gpulib):
     assert np.array_equal(a.field("w", 3), b.field("w", 3))
 
 
-def test_embedded_levels(gpulib):
+@pytest.mark.parametrize("path", PATHS)
+def test_embedded_levels(gpulib, path):
     case = K.cylinder_embedded(n=24, span=2, nlevel=3, h_fine=0.1, mach=0.3, mcyc_fine=3)
     case.prm.mcyc[0] = 1
     case.prm.mcyc[1] = 1
-    g, o = pair(case)
+    g, o = pair(case, path=path)
     hg, ng, _ = g.solve()
     ho, no, _ = o.solve()
     assert ng == no
     assert np.max(np.abs(hg - ho) / np.abs(ho)) <= 1e-11
     compare(g, o, "w", 3, rtol=1e-11, phys_only=False)
     compare(g, o, "w", 2, rtol=1e-11, phys_only=False)
+
+
+def test_mixed_paths_in_one_hierarchy(gpulib):
+    """Coarse levels cooperative, finest per-phase: the split the 192^3 bench uses."""
+    import os
+    case = small_sphere(nlevel=3, n=32, mgtype=2)
+    case.prm.mcyc[0] = 1
+    case.prm.mcyc[1] = 1
+    case.prm.mcyc[2] = 3
+    os.environ["MGE_COOP_MAX_CELLS"] = str(16 ** 3)
+    try:
+        from code_mge_gb300.runtime import Cycle
+        from oracle.oracle import OracleCycle
+        g = Cycle(case)
+        o = OracleCycle(case)
+    finally:
+        os.environ.pop("MGE_COOP_MAX_CELLS", None)
+    hg, _, _ = g.solve()
+    ho, _, _ = o.solve()
+    assert np.max(np.abs(hg - ho) / np.abs(ho)) <= 1e-11
+    compare(g, o, "w", 3, rtol=1e-11, phys_only=False)
