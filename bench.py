@@ -35,6 +35,7 @@ sys.path.insert(0, ROOT)
 
 from code_mge_gb300 import _abi as A  # noqa: E402
 from code_mge_gb300 import cases as K  # noqa: E402
+from code_mge_gb300 import replicas as R  # noqa: E402
 from code_mge_gb300 import schedule as S  # noqa: E402
 
 METRIC = "MG-cycle cell-updates/s (mixed vs FP64 plain); solves/s & p50/p99 latency"
@@ -52,10 +53,26 @@ LAUNCHES_PER_UPDATE = {"timestep": 1, "prep": 5, "face": 5, "rec": 5, "combine":
                        "irs_k_update": 3, "cutcell": 5, "bcond": 5, "rtrms": 1}
 
 
-def workload_case(precision="fp64"):
+def workload_case(precision="fp64", n=192):
     prec = A.MGE_PREC_MIXED if precision == "mixed" else A.MGE_PREC_FP64
-    return K.sphere_box(n=192, nlevel=4, extent=10.0, mach=0.5, mgtype=2, mcyc_fine=400, smoo=0.6,
+    return K.sphere_box(n=n, nlevel=4, extent=10.0, mach=0.5, mgtype=2, mcyc_fine=400, smoo=0.6,
                         precision=prec)
+
+
+def run_profile(args):
+    """Short run for the ncu captures: set up the workload, one warm cycle,
+    then one timed update of the finest level through the per-kernel path."""
+    from code_mge_gb300.runtime import Cycle, load_library
+    lib = load_library()
+    n = 96 if args.workload == "sphere96" else 192
+    case = workload_case(args.precision, n=n)
+    cyc = Cycle(case)
+    cyc.cycle(case.prm.nlevel, ncyc=1)
+    ms = np.zeros(len(A.KERNEL_KINDS))
+    lib.mge_kernel_times(cyc.ctx, case.prm.nlevel, 1, ms.ctypes.data_as(C.POINTER(C.c_double)), len(ms))
+    print(json.dumps({"profile_run": args.workload, "kernel_ms": dict(zip(A.KERNEL_KINDS, ms.tolist()))}))
+    cyc.close()
+    return 0
 
 
 def peaks():
@@ -197,9 +214,8 @@ def run_gpu(args):
         cyc.cycle(L, ncyc=q + 1)
 
     def barrier():
-        if world > 1:
-            import torch.distributed as dist
-            dist.barrier()
+        torch.cuda.synchronize(dev)
+        R.barrier()
         torch.cuda.synchronize(dev)
 
     sampler = ClockSampler(dev)
@@ -216,13 +232,10 @@ def run_gpu(args):
     wall = time.perf_counter() - t0
     clocks = sampler.stop()
     n_launch = lib.mge_launch_count(cyc.ctx) - n_launch0
-    dev_s = dev_ms / 1e3
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([dev_s], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dev_s = float(t.item())
-    value = world * args.steps * cu / dev_s
+    # replicas: every rank ran the same cycles; units of all ranks over the
+    # slowest rank's device time
+    dev_s = R.max_over_ranks(dev_ms / 1e3)
+    value = R.whole_job_rate(args.steps * cu, dev_ms / 1e3)
 
     # end to end through the C-ABI with host buffers: H2D of the finest state
     # from pinned memory, one cycle, D2H of the cycle's residual
@@ -240,12 +253,7 @@ def run_gpu(args):
         cyc.cycle(L, ncyc=2)
     barrier()
     e2e_s = time.perf_counter() - t0
-    e2e = world * args.steps * cu / e2e_s if world == 1 else None
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e = world * args.steps * cu / float(t.item())
+    e2e = R.whole_job_rate(args.steps * cu, e2e_s)
 
     # per-kernel device times (CUDA events on the library stream), finest level
     ms = np.zeros(len(A.KERNEL_KINDS))
@@ -312,6 +320,65 @@ def run_gpu(args):
     return 0
 
 
+def run_pattern(args):
+    """The batched sweep and the serving loop (one JSON line each)."""
+    from code_mge_gb300 import serving as SV
+    from code_mge_gb300.runtime import load_library
+    load_library()
+    if args.pattern == "batched":
+        sizes = tuple(int(x) for x in args.sizes.split(","))
+        reqs = SV.batched_sweep_requests(args.cases, sizes=sizes, precision=A.MGE_PREC_MIXED, tol=args.tol,
+                                         max_cycles=args.max_cycles)
+        for r in reqs:
+            r.arrival = 0.0
+        srv = SV.Server(SV.GpuBackend(coop_ctas=args.coop_ctas), max_active=args.cases)
+        for r in reqs:
+            srv.submit(r)
+        t0 = time.perf_counter()
+        done = srv.run()
+        tb = time.perf_counter() - t0
+        batched = SV.summarize(done, tb)
+        # the FP64 plain path on the same cases, one at a time
+        plain, t0 = [], time.perf_counter()
+        for r in SV.batched_sweep_requests(args.cases, sizes=sizes, precision=A.MGE_PREC_FP64, tol=args.tol,
+                                           max_cycles=args.max_cycles):
+            one = SV.Server(SV.GpuBackend(coop_ctas=0), max_active=1)
+            one.submit(r)
+            plain += one.run()
+        tp = time.perf_counter() - t0
+        serial = SV.summarize(plain, tp)
+        mix = {r.rid: r for r in done}
+        dcd = [abs(mix[r.rid].cd - r.cd) for r in plain if r.error is None and mix[r.rid].error is None]
+        line = {"pattern": "batched sweep", "metric": "converged solves/s", "unit": "solves/s",
+                "value": batched["solves_per_s"], "baseline_fp64_serial": serial["solves_per_s"],
+                "speedup": batched["solves_per_s"] / serial["solves_per_s"] if serial["solves_per_s"] else None,
+                "max_abs_dcd_vs_fp64": max(dcd) if dcd else None, "cases": args.cases,
+                "config": {"sizes": sizes, "tol_drop": args.tol, "levels": 3, "cycle": "W",
+                           "precision": "FP32 coarse / FP64 fine", "seed": 20261203},
+                "batched": batched, "fp64_serial": serial, "peak_active": srv.peak_active}
+        print(json.dumps(line), flush=True)
+        return 0
+    # serving loop
+    lo, hi = [int(x) for x in args.sizes.split(",")][:2] if "," in args.sizes else (64, 256)
+    reqs = SV.poisson_requests(args.rate, args.duration, sizes=(lo, hi), tol=args.tol, max_cycles=args.max_cycles)
+    srv = SV.Server(SV.GpuBackend(coop_ctas=args.coop_ctas))
+    t_start = time.perf_counter()
+    for r in reqs:
+        r.arrival += t_start
+        srv.submit(r)
+    done = srv.run(deadline=t_start + args.duration + args.drain)
+    wall = time.perf_counter() - t_start
+    st = SV.summarize(done, wall)
+    line = {"pattern": "serving", "metric": "solves/s & p50/p99 time-to-converged", "unit": "solves/s",
+            "value": st["solves_per_s"], "p50_s": st["p50_s"], "p99_s": st["p99_s"],
+            "submitted": len(reqs), "completed": st["completed"], "unfinished": len(reqs) - len(done),
+            "peak_active": srv.peak_active,
+            "config": {"arrivals": "Poisson %.1f req/s for %.0f s (seed 20261204)" % (args.rate, args.duration),
+                       "sizes": [lo, hi], "tol_drop": args.tol, "precision": "FP32 coarse / FP64 fine"}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -320,7 +387,22 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--pattern", default=None, choices=["batched", "serving"])
+    ap.add_argument("--cases", type=int, default=64)
+    ap.add_argument("--sizes", default="32,48,64,96,128")
+    ap.add_argument("--tol", type=float, default=1e-8)
+    ap.add_argument("--max-cycles", type=int, default=2000)
+    ap.add_argument("--rate", type=float, default=4.0)
+    ap.add_argument("--duration", type=float, default=300.0)
+    ap.add_argument("--drain", type=float, default=120.0)
+    ap.add_argument("--coop-ctas", type=int, default=32)
+    ap.add_argument("--workload", default="sphere192", choices=["sphere192", "sphere96"])
+    ap.add_argument("--profile", action="store_true", help="short run for ncu captures")
     args = ap.parse_args()
+    if args.profile:
+        return run_profile(args)
+    if args.pattern:
+        return run_pattern(args)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

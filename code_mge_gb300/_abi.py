@@ -125,6 +125,7 @@ class MgeSolveOpts(C.Structure):
         ("ref_area", _d),
         ("moment_center", _d * 3),
         ("use_graph", _i),
+        ("refine_drop", _d),
     ]
 
 
@@ -165,6 +166,14 @@ PRODUCT_ONLY = [
     ("last_cycle_ms", _d, [_vp]),
     ("launch_count", C.c_longlong, [_vp]),
     ("kernel_times", _i, [_vp, _i, _i, _pd, _i]),
+    ("coop_trace", _i, [_vp, _i, _pd, _i]),
+    ("cycle_async", _i, [_vp, _i]),
+    ("cycle_poll", _i, [_vp, _i, _pd]),
+    ("prolong_async", _i, [_vp, _i]),
+    ("set_coop_ctas", _i, [_vp, _i]),
+    ("tuned", _i, [_vp, _i, _i, C.POINTER(_i), C.POINTER(_i)]),
+    ("set_precision", _i, [_vp, _i]),
+    ("device_mem", _i, [_i, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
     ("residual_norm_noalloc", _i, [_vp, _vp, _vp, _i, _i, _i, _d, _i, _d, _vp, _vp]),
 ]
 KERNEL_KINDS = ["timestep", "prep", "face", "rec", "combine", "irs_i", "irs_j", "irs_k_update", "cutcell", "bcond",
@@ -176,7 +185,8 @@ HEADER_SYMBOLS = [
     "mge_last_error", "mge_add_block", "mge_commit", "mge_init_flow", "mge_upload_state",
     "mge_download_state", "mge_download_field", "mge_timestep", "mge_euler", "mge_movco",
     "mge_movfin", "mge_bc_overlap", "mge_get_rtrms", "mge_solve", "mge_forces_compute",
-    "mge_cycle", "mge_last_cycle_ms", "mge_launch_count", "mge_kernel_times", "mge_residual_norm_noalloc", "mge_euler_partial", "mge_device_bytes", "mge_sync",
+    "mge_cycle", "mge_cycle_async", "mge_cycle_poll", "mge_prolong_async", "mge_set_coop_ctas", "mge_device_mem", "mge_tuned", "mge_set_precision",
+    "mge_coop_trace", "mge_last_cycle_ms", "mge_launch_count", "mge_kernel_times", "mge_residual_norm_noalloc", "mge_euler_partial", "mge_device_bytes", "mge_sync",
 ]
 
 

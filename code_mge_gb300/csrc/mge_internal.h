@@ -13,6 +13,7 @@ namespace mge {
 // One uniform block as the kernels see it (passed by value).
 template <typename T>
 struct DevBlock {
+  typedef T value_type;
   int nx, ny, nz;
   int il, jl, kl, ie, je, ke, ib, jb, kb;
   int Pi, Pj;
@@ -38,8 +39,11 @@ struct DevBlock {
   T* fp;                    // 3N pressure sensor [dir]
   T* efs;                   // 15N convective face flux [dir][var] at the upper cell of the face
   T* dfs;                   // 15N dissipative face flux
+  T* vt;                    // 4N velocity and temperature (Navier-Stokes)
+  T* vfs;                   // 15N viscous face flux (Navier-Stokes)
   // metric (uniform, axis-aligned face vectors)
   double s[3];              // si[0], sj[1], sk[2]
+  double hx, hy, hz;        // cell sizes (viscous gradients)
   double sqrt_ds[3];        // sqrt(s*s) computed on the host
   double vol;
   double rvol;              // RN(1/vol)
@@ -54,7 +58,7 @@ struct DevBlock {
   const double* rec_area;   // [nmir] wall-face area
   T* rec_wsol;              // [nmir][5]
   T* rec_psol;              // [nmir]
-  T* rec_term;              // [nmir][40] stage terms of efluxb/dfluxb
+  T* rec_term;              // [nmir][50] stage terms of efluxb/dfluxb and the viscous wall
   const int32_t* tgt_off;   // [ntgt+1]
   const int32_t* tgt_ops;   // op = 2*m + role (0: cut cell, 1: neighbour)
   int bctype[6];
@@ -84,6 +88,11 @@ struct PhysParams {
   int eqn_ns;
   double smoo;
   int vt;                   // global time step
+  int distype;              // MGE_DIS_* (0 central, 1 Roe first order, 2 Roe MUSCL)
+  double viscl, kt, gas_const, prlmean;  // laminar viscosity, heat conductivity, R, Pr
+  double cfac;              // viscous weight of the time step (timestep.f90:119-125)
+  double epsentr;           // Harten entropy fix
+  double lim_e2[5];         // van Albada floor per primitive variable
 };
 
 // error word bits
@@ -109,19 +118,23 @@ struct EulerLaunch {
   int npart;
   double* rt_out;
   unsigned* err;
+  unsigned long long* trace;  // optional phase timestamps (profiling hook)
+  int max_ctas;               // cap on the cooperative grid (0: occupancy limit)
 };
 
 // kernel launchers (mge_kernels.cu)
 template <typename T> int launch_euler_coop(const DevBlock<T>& b, const PhysParams& P, const EulerLaunch& L, int device,
-                                            cudaStream_t s);
-template <typename T> void launch_timestep(const DevBlock<T>& b, const PhysParams& P, unsigned* err, cudaStream_t s);
+                                            cudaStream_t s, bool aux32 = false);
+template <typename T> void launch_timestep(const DevBlock<T>& b, const PhysParams& P, unsigned* err, cudaStream_t s,
+                                           bool aux32 = false);
 template <typename T> void launch_stage(const DevBlock<T>& b, const PhysParams& P, const StageArgs& A, unsigned* err,
                                         cudaStream_t s);
-template <typename T> void launch_irs(const DevBlock<T>& b, const PhysParams& P, const IrsTables* tab, cudaStream_t s);
+template <typename T> void launch_irs(const DevBlock<T>& b, const PhysParams& P, const IrsTables* tab, cudaStream_t s,
+                                      bool aux32 = false, const int* variant = nullptr);
 template <typename T> void launch_stage_part(int part, const DevBlock<T>& b, const PhysParams& P, const StageArgs& A,
                                              unsigned* err, cudaStream_t s);
 template <typename T> void launch_irs_part(int part, const DevBlock<T>& b, const PhysParams& P, const IrsTables* tab,
-                                           cudaStream_t s);
+                                           cudaStream_t s, bool aux32 = false, const int* variant = nullptr);
 template <typename T> void launch_cutcell(const DevBlock<T>& b, const PhysParams& P, unsigned* err, cudaStream_t s);
 template <typename T> void launch_bcond(const DevBlock<T>& b, const PhysParams& P, cudaStream_t s);
 template <typename T> void launch_rtrms(const DevBlock<T>& b, const PhysParams& P, int vt, double* partial,
@@ -143,5 +156,7 @@ void launch_embed(const DevBlock<TF>& f, const DevBlock<TC>& c, const int ratio[
 template <typename T> void launch_forces(const DevBlock<T>& b, const double* origin, const double* h,
                                          const double* center, double* out7, cudaStream_t s);
 int rtrms_partials(long long ncells);
+void init_kernel_attributes();
+void launch_convert(const void* src, bool src32, void* dst, bool dst32, long long n, cudaStream_t s);
 
 }  // namespace mge

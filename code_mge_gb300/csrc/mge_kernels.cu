@@ -94,7 +94,19 @@ __device__ __forceinline__ unsigned long long body_timestep(const DevBlock<T>& b
   TC rj = fabs(uv * (TC)b.s[1]) + cc * (TC)b.sqrt_ds[1];
   TC rk = fabs(uw * (TC)b.s[2]) + cc * (TC)b.sqrt_ds[2];
   TC lsum = ri + rj + rk;
-  TC fict = (TC)b.vol / lsum;
+  TC fict;
+  if (P.eqn_ns) {  // viscous spectral radii, timestep.f90:141-178
+    const TC fmue = (TC)P.viscl / (TC)P.prlmean;
+    const TC f1 = TC(4) / w0 / TC(3);
+    const TC f2 = gamma / w0;
+    const TC fac = fmaxT(f1, f2);
+    const TC dtv = fac * fmue / (TC)b.vol;
+    const TC s0 = (TC)b.s[0], s1 = (TC)b.s[1], s2 = (TC)b.s[2];
+    TC rvi = dtv * (s0 * s0), rvj = dtv * (s1 * s1), rvk = dtv * (s2 * s2);
+    fict = (TC)b.vol / (lsum + (TC)P.cfac * (rvi + rvj + rvk));
+  } else {
+    fict = (TC)b.vol / lsum;
+  }
   const TC plim = TC(0.001);
   TC pip = (TC)b.p[c + 1], pim = (TC)b.p[c - 1];
   TC pjp = (TC)b.p[c + b.Pi], pjm = (TC)b.p[c - b.Pi];
@@ -163,7 +175,7 @@ template <typename T> __global__ void k_dtim_convert(double* src, T* dst) {
 // --------------------------------------------------------------- stage: per-cell pass
 // Box [1..ie]x[1..je]x[1..ke]: every cell whose flux or sensor a face needs.
 template <typename T>
-__device__ __forceinline__ void body_prep(const DevBlock<T>& b, int dissip_on, long long t) {
+__device__ __forceinline__ void body_prep(const DevBlock<T>& b, const PhysParams& P, int dissip_on, long long t) {
   const int ex = b.ie, ey = b.je;  // count = ie (cells 1..ie)
   int i = 1 + (int)(t % ex);
   int j = 1 + (int)((t / ex) % ey);
@@ -177,6 +189,12 @@ __device__ __forceinline__ void body_prep(const DevBlock<T>& b, int dissip_on, l
   T y = T(1) / w[0];
   T Hc = w[4] + p;
   b.H[c] = Hc;
+  if (P.eqn_ns && dissip_on) {  // velocity and temperature, zero in solid cells (euler.f90:140-154)
+    const bool solid = b.blank[c] == 0;
+#pragma unroll
+    for (int a = 0; a < 3; a++) b.vt[a * N + c] = solid ? T(0) : mdiv(w[1 + a], w[0], y);
+    b.vt[3 * N + c] = solid ? T(0) : p / (w[0] * (T)P.gas_const);
+  }
 #pragma unroll
   for (int d = 0; d < 3; d++) {
     T s = (T)b.s[d];
@@ -250,6 +268,149 @@ __device__ void dflux_matrix(T gamma, const T* u1, const T* u2, const T* dw, con
   ff[4] = ak1 * (hh * vd - qn * ak3 * qd) + ak2 * (gam1 * qn * vd - hh * qd) + s3 * d4;
 }
 
+
+// --------------------------------------------------------------- Roe, MUSCL and viscous faces
+// (the reference's roepak/viscpak sources are not in its tree; these follow
+// the published methods, as the oracle does: Roe 1981 with Harten's entropy
+// fix, MUSCL with the van Albada limiter, central-gradient laminar stresses)
+template <typename T>
+__device__ __forceinline__ T van_albada(T a, T b, T e2) {
+  // smooth form, no cut-off at a*b <= 0: with e2 > 0 a cut-off would make the
+  // slope jump by up to b/3 when a changes sign
+  return ((b * b + e2) * a + (a * a + e2) * b) / (a * a + b * b + T(2) * e2);
+}
+
+template <typename T>
+__device__ void roe_diss(const PhysParams& P, int d, T S, const T* wl, T pl, const T* wr, T pr, T* out) {
+  const T g = (T)P.gamma;
+  T ul[3], ur[3];
+  for (int a = 0; a < 3; a++) {
+    ul[a] = wl[1 + a] / wl[0];
+    ur[a] = wr[1 + a] / wr[0];
+  }
+  T hl = (wl[4] + pl) / wl[0], hr = (wr[4] + pr) / wr[0];
+  T rt = sqrt(wr[0] / wl[0]);
+  T rh = rt * wl[0];
+  T uh[3];
+  for (int a = 0; a < 3; a++) uh[a] = (ul[a] + rt * ur[a]) / (T(1) + rt);
+  T hh = (hl + rt * hr) / (T(1) + rt);
+  T q2 = uh[0] * uh[0] + uh[1] * uh[1] + uh[2] * uh[2];
+  T c2 = (g - T(1)) * (hh - T(0.5) * q2);
+  T ch = sqrt(fmaxT(c2, (T)1e-300));
+  T un = uh[d];
+  T dr = wr[0] - wl[0], dp = pr - pl, dun = ur[d] - ul[d];
+  T du[3] = {ur[0] - ul[0], ur[1] - ul[1], ur[2] - ul[2]};
+  T delta = (T)P.epsentr * (fabs(un) + ch);
+  auto fix = [&](T lam) {
+    T a = fabs(lam);
+    return (a < delta && delta > T(0)) ? (lam * lam + delta * delta) / (T(2) * delta) : a;
+  };
+  T l1 = fix(un - ch), l2 = fix(un), l5 = fix(un + ch);
+  T a1 = (dp - rh * ch * dun) / (T(2) * c2);
+  T a2 = dr - dp / c2;
+  T a5 = (dp + rh * ch * dun) / (T(2) * c2);
+  T sh[3];
+  for (int a = 0; a < 3; a++) sh[a] = rh * (du[a] - (a == d ? dun : T(0)));
+  T k1[5], k5[5];
+  k1[0] = T(1);
+  k5[0] = T(1);
+  for (int a = 0; a < 3; a++) {
+    k1[1 + a] = uh[a] - (a == d ? ch : T(0));
+    k5[1 + a] = uh[a] + (a == d ? ch : T(0));
+  }
+  k1[4] = hh - ch * un;
+  k5[4] = hh + ch * un;
+  T res[5];
+  res[0] = l1 * a1 * k1[0] + l2 * a2 + l5 * a5 * k5[0];
+  for (int a = 0; a < 3; a++) res[1 + a] = l1 * a1 * k1[1 + a] + l2 * (a2 * uh[a] + sh[a]) + l5 * a5 * k5[1 + a];
+  res[4] = l1 * a1 * k1[4] + l2 * (a2 * T(0.5) * q2 + (uh[0] * sh[0] + uh[1] * sh[1] + uh[2] * sh[2])) + l5 * a5 * k5[4];
+  for (int v = 0; v < 5; v++) out[v] = T(0.5) * S * res[v];
+}
+
+// face q (between q-1 and q) along D at cell c: cell states, MUSCL when order 2
+template <typename T, int D>
+__device__ void face_states(const DevBlock<T>& b, const PhysParams& P, long long c, int q, int order, T* wl, T* pl,
+                            T* wr, T* pr) {
+  const long long N = b.N;
+  const long long st = D == 0 ? 1 : (D == 1 ? (long long)b.Pi : (long long)b.Pi * b.Pj);
+  for (int v = 0; v < 5; v++) {
+    wl[v] = b.w[v * N + c - st];
+    wr[v] = b.w[v * N + c];
+  }
+  *pl = b.p[c - st];
+  *pr = b.p[c];
+  if (order < 2) return;
+  const int lq = D == 0 ? b.il : (D == 1 ? b.jl : b.kl);
+  if (q - 2 < 0 || q + 1 > lq + 2) return;
+  if (b.blank[c - 2 * st] == 0 || b.blank[c - st] == 0 || b.blank[c] == 0 || b.blank[c + st] == 0) return;
+  T qv[4][5];  // primitive (rho,u,v,w,p) at q-2..q+1
+  for (int o = 0; o < 4; o++) {
+    long long co = c + (o - 2) * st;
+    T r = b.w[co];
+    qv[o][0] = r;
+    for (int a = 0; a < 3; a++) qv[o][1 + a] = b.w[(1 + a) * N + co] / r;
+    qv[o][4] = b.p[co];
+  }
+  T L[5], R[5];
+  for (int kq = 0; kq < 5; kq++) {
+    T dm = qv[1][kq] - qv[0][kq], d0 = qv[2][kq] - qv[1][kq], dp = qv[3][kq] - qv[2][kq];
+    T e2 = (T)P.lim_e2[kq];
+    L[kq] = qv[1][kq] + T(0.5) * van_albada(dm, d0, e2);
+    R[kq] = qv[2][kq] - T(0.5) * van_albada(d0, dp, e2);
+  }
+  if (L[0] <= T(0) || R[0] <= T(0) || L[4] <= T(0) || R[4] <= T(0)) return;
+  const T gm1 = (T)P.gamma - T(1);
+  wl[0] = L[0];
+  wr[0] = R[0];
+  for (int a = 0; a < 3; a++) {
+    wl[1 + a] = L[0] * L[1 + a];
+    wr[1 + a] = R[0] * R[1 + a];
+  }
+  wl[4] = L[4] / gm1 + T(0.5) * L[0] * (L[1] * L[1] + L[2] * L[2] + L[3] * L[3]);
+  wr[4] = R[4] / gm1 + T(0.5) * R[0] * (R[1] * R[1] + R[2] * R[2] + R[3] * R[3]);
+  *pl = L[4];
+  *pr = R[4];
+}
+
+template <typename T>
+__device__ __forceinline__ void ceflux_gen(int D, const T* w, T p, T s, T* f) {
+  T f0 = w[1 + D] * s;
+  f[0] = f0;
+  f[1] = f0 * w[1] / w[0];
+  f[2] = f0 * w[2] / w[0];
+  f[3] = f0 * w[3] / w[0];
+  f[1 + D] = f[1 + D] + p * s;
+  f[4] = f0 * (w[4] + p) / w[0];
+}
+
+// laminar viscous flux through face q along D (at cell c), times S
+template <typename T, int D>
+__device__ void visc_face(const DevBlock<T>& b, const PhysParams& P, long long c, T S, T* out) {
+  const long long N = b.N;
+  const long long st[3] = {1, (long long)b.Pi, (long long)b.Pi * b.Pj};
+  const long long cl = c - st[D];
+  const double h[3] = {b.hx, b.hy, b.hz};
+  T g[4][3];
+  for (int a = 0; a < 4; a++) {
+    const T* f = b.vt + (long long)a * N;
+    for (int t = 0; t < 3; t++) {
+      if (t == D)
+        g[a][t] = (f[c] - f[cl]) / (T)h[D];
+      else
+        g[a][t] = ((f[c + st[t]] - f[c - st[t]]) + (f[cl + st[t]] - f[cl - st[t]])) / (T(4) * (T)h[t]);
+    }
+  }
+  const T mu = (T)P.viscl, kt = (T)P.kt;
+  T div = g[0][0] + g[1][1] + g[2][2];
+  T tau[3];
+  for (int a = 0; a < 3; a++) tau[a] = mu * (g[a][D] + g[D][a]) - (a == D ? (T(2) / T(3)) * mu * div : T(0));
+  T uf[3];
+  for (int a = 0; a < 3; a++) uf[a] = T(0.5) * (b.vt[a * N + cl] + b.vt[a * N + c]);
+  out[0] = T(0);
+  for (int a = 0; a < 3; a++) out[1 + a] = S * tau[a];
+  out[4] = S * ((uf[0] * tau[0] + uf[1] * tau[1] + uf[2] * tau[2]) + kt * g[3][D]);
+}
+
 // --------------------------------------------------------------- stage: per-face pass
 // Thread (i,j,k) in [2..ie]x[2..je]x[2..ke] owns the lower face of cell
 // (i,j,k) in each direction whose tangential indices are physical.
@@ -262,9 +423,38 @@ __device__ __forceinline__ void face_dir(const DevBlock<T>& b, const PhysParams&
   const int q = D == 0 ? i : (D == 1 ? j : k);      // face between q-1 and q
   const int lq = D == 0 ? b.il : (D == 1 ? b.jl : b.kl);
   const int eq = lq + 1, bq = lq + 2;
+  T* E = b.efs + (long long)(D * 5) * N;
+  if (P.eqn_ns && dissip_on) {  // viscous face flux, blended like the dissipation
+    T o[5];
+    visc_face<T, D>(b, P, c, (T)fabs(b.s[D]), o);
+    T* V = b.vfs + (long long)(D * 5) * N;
+#pragma unroll
+    for (int v = 0; v < 5; v++) V[v * N + c] = cd * o[v];
+  }
+  if (P.distype != 0) {  // Roe: central part of the (reconstructed) states, upwind part into dfs
+    T wl[5], wr[5], pl, pr;
+    face_states<T, D>(b, P, c, q, P.distype == 2 ? 2 : 1, wl, &pl, wr, &pr);
+    if (P.distype == 2) {
+      T f1[5], f2[5];
+      ceflux_gen<T>(D, wr, pr, (T)b.s[D], f1);
+      ceflux_gen<T>(D, wl, pl, (T)b.s[D], f2);
+#pragma unroll
+      for (int v = 0; v < 5; v++) E[v * N + c] = T(0.5) * (f1[v] + f2[v]);
+    } else {
+      const T* F = b.F + (long long)(D * 5) * N;
+#pragma unroll
+      for (int v = 0; v < 5; v++) E[v * N + c] = T(0.5) * (F[v * N + c] + F[v * N + c - st]);
+    }
+    if (!dissip_on) return;
+    T o[5];
+    roe_diss<T>(P, D, (T)fabs(b.s[D]), wl, pl, wr, pr, o);
+    T* Df = b.dfs + (long long)(D * 5) * N;
+#pragma unroll
+    for (int v = 0; v < 5; v++) Df[v * N + c] = cd * o[v];
+    return;
+  }
   // convective: efs(q) = 0.5*(F(q) + F(q-1))
   const T* F = b.F + (long long)(D * 5) * N;
-  T* E = b.efs + (long long)(D * 5) * N;
 #pragma unroll
   for (int v = 0; v < 5; v++) E[v * N + c] = T(0.5) * (F[v * N + c] + F[v * N + c - st]);
   if (!dissip_on) return;
@@ -351,14 +541,14 @@ __device__ __forceinline__ void ceflux_axis(int D, const T* w, T p, T s, T* f) {
 }
 
 template <typename T>
-__device__ void body_rec(const DevBlock<T>& b, const PhysParams& P, int dissip_on, T cd, unsigned* err, int m) {
+__device__ __noinline__ void rec_terms(const DevBlock<T>& b, const PhysParams& P, int dissip_on, T cd, unsigned* err,
+                                       int m, T* R) {
   const long long N = b.N;
   const int* ri = b.rec_i + 8 * m;
   int i = ri[0], j = ri[1], k = ri[2], id = ri[3], zz = ri[4];
   int D = zz - 1;
   const long long st = D == 0 ? 1 : (D == 1 ? (long long)b.Pi : (long long)b.Pi * b.Pj);
   const long long c = cidx(b.Pi, b.Pj, i, j, k);
-  T* R = b.rec_term + 40LL * m;
   T s = (T)b.s[D];
   T wc[5];
   for (int v = 0; v < 5; v++) wc[v] = b.w[v * N + c];
@@ -384,6 +574,46 @@ __device__ void body_rec(const DevBlock<T>& b, const PhysParams& P, int dissip_o
     R[10 + v] = plus ? fs : fa;
   }
   if (!dissip_on) return;
+  const long long qn = plus ? c + st : c;  // the wall face's upper cell
+  if (P.eqn_ns) {  // no-slip adiabatic wall face: normal gradients to the mirror state only
+    const T* V = b.vfs + (long long)(D * 5) * N;
+    T u[3], ug[3], qbv[3] = {(T)b.rec_qb[3 * m], (T)b.rec_qb[3 * m + 1], (T)b.rec_qb[3 * m + 2]};
+    const double hh[3] = {b.hx, b.hy, b.hz};
+    for (int a = 0; a < 3; a++) {
+      u[a] = wc[1 + a] / wc[0];
+      ug[a] = T(2) * qbv[a] - u[a];
+    }
+    const T mu = (T)P.viscl, S = (T)fabs(b.s[D]);
+    T o[5];
+    T tau[3];
+    for (int a = 0; a < 3; a++) {
+      T gn = plus ? (ug[a] - u[a]) / (T)hh[D] : (u[a] - ug[a]) / (T)hh[D];
+      tau[a] = (a == D) ? (T(4) / T(3)) * mu * gn : mu * gn;
+    }
+    o[0] = T(0);
+    for (int a = 0; a < 3; a++) o[1 + a] = S * tau[a];
+    o[4] = S * (qbv[0] * tau[0] + qbv[1] * tau[1] + qbv[2] * tau[2]);
+    for (int v = 0; v < 5; v++) {
+      R[40 + v] = plus ? -V[v * N + qn] : V[v * N + qn];
+      R[45 + v] = plus ? -(cd * o[v]) : cd * o[v];
+    }
+  }
+  if (P.distype != 0) {  // Roe: the wall face's upwind flux taken to the ghost state
+    const T* Dd = b.dfs + (long long)(D * 5) * N;
+    T o[5];
+    const T S = (T)fabs(b.s[D]);
+    if (plus)
+      roe_diss<T>(P, D, S, wc, b.p[c], wsol, psol, o);
+    else
+      roe_diss<T>(P, D, S, wsol, psol, wc, b.p[c], o);
+    for (int v = 0; v < 5; v++) {
+      R[15 + v] = plus ? -Dd[v * N + qn] : Dd[v * N + qn];
+      R[20 + v] = plus ? -(cd * o[v]) : cd * o[v];
+      R[25 + v] = T(0);
+      R[30 + v] = T(0);
+    }
+    return;
+  }
   // dfluxb.f90:29-423; w(:,5) is the enthalpy here
   wsol[4] = wsol[4] + psol;
   const T* Dd = b.dfs + (long long)(D * 5) * N;
@@ -528,8 +758,16 @@ __device__ void body_rec(const DevBlock<T>& b, const PhysParams& P, int dissip_o
 
 // --------------------------------------------------------------- stage: combine + update
 template <typename T>
+__global__ void k_rec(DevBlock<T> b, PhysParams P, int dissip_on, T cd, unsigned* err) {
+  int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m < b.nmir) rec_terms(b, P, dissip_on, cd, err, m, b.rec_term + 50LL * m);
+}
+
+// INLINE_REC: compute each record's terms here (one-launch euler) instead of
+// reading them from the record pass (per-phase launches)
+template <typename T, bool INLINE_REC>
 __device__ __forceinline__ void body_combine(const DevBlock<T>& b, const PhysParams& P, const StageArgs& A,
-                                             long long t) {
+                                             unsigned* err, long long t) {
   const int nxl = b.nx, nyl = b.ny;
   int i = 2 + (int)(t % nxl);
   int j = 2 + (int)((t / nxl) % nyl);
@@ -549,52 +787,92 @@ __device__ __forceinline__ void body_combine(const DevBlock<T>& b, const PhysPar
     a = a + Ez[v * N + c] - Ez[v * N + c + sk];
     dwv[v] = a;
   }
-  if (tg >= 0) {  // efluxb.f90:72-110, records of this cut cell in order
-    for (int o = b.tgt_off[tg]; o < b.tgt_off[tg + 1]; o++) {
-      int op = b.tgt_ops[o];
-      if (op & 1) continue;
-      const T* R = b.rec_term + 40LL * (op >> 1);
-#pragma unroll
-      for (int v = 0; v < 5; v++) {
-        dwv[v] = dwv[v] - R[v];
-        dwv[v] = dwv[v] + R[5 + v] - R[10 + v];
-      }
-    }
-  }
   // fw: blending and dissipation (euler.f90:127-135, dflux.f90:116-238)
+  const T fac = T(1) - (T)A.cd;
   if (A.dissip_on) {
     const T* Dx = b.dfs;
     const T* Dy = b.dfs + 5 * N;
     const T* Dz = b.dfs + 10 * N;
-    const T fac = T(1) - (T)A.cd;
+    T vis[5];
+#pragma unroll
+    for (int v = 0; v < 5; v++) vis[v] = A.scale_fw ? b.fw[v * N + c] * fac : T(0);
+    if (P.eqn_ns) {  // viscous faces, then the viscous wall faces in record order
+      const T* Vx = b.vfs;
+      const T* Vy = b.vfs + 5 * N;
+      const T* Vz = b.vfs + 10 * N;
+#pragma unroll
+      for (int v = 0; v < 5; v++) {
+        T a = vis[v];
+        a = a + (Vx[v * N + c] - Vx[v * N + c + 1]);
+        a = a + (Vy[v * N + c] - Vy[v * N + c + sj]);
+        a = a + (Vz[v * N + c] - Vz[v * N + c + sk]);
+        vis[v] = a;
+      }
+      if (tg >= 0) {
+        T Rv[INLINE_REC ? 50 : 1];
+        for (int o = b.tgt_off[tg]; o < b.tgt_off[tg + 1]; o++) {
+          const int op = b.tgt_ops[o];
+          if (op & 1) continue;
+          const T* R;
+          if (INLINE_REC) {
+            rec_terms(b, P, A.dissip_on, (T)A.cd, err, op >> 1, Rv);
+            R = Rv;
+          } else {
+            R = b.rec_term + 50LL * (op >> 1);
+          }
+#pragma unroll
+          for (int v = 0; v < 5; v++) {
+            vis[v] = vis[v] - R[40 + v];
+            vis[v] = vis[v] + R[45 + v];
+          }
+        }
+      }
+    }
 #pragma unroll
     for (int v = 0; v < 5; v++) {
-      T a = A.scale_fw ? b.fw[v * N + c] * fac : T(0);
+      T a = vis[v];
       a = a + (Dx[v * N + c] - Dx[v * N + c + 1]);
       a = a + (Dy[v * N + c] - Dy[v * N + c + sj]);
       a = a + (Dz[v * N + c] - Dz[v * N + c + sk]);
       fwv[v] = a;
     }
-    if (tg >= 0) {  // dfluxb, in record order
-      for (int o = b.tgt_off[tg]; o < b.tgt_off[tg + 1]; o++) {
-        int op = b.tgt_ops[o];
-        const T* R = b.rec_term + 40LL * (op >> 1) + ((op & 1) ? 25 : 15);
+  } else {
+#pragma unroll
+    for (int v = 0; v < 5; v++) fwv[v] = A.scale_fw ? b.fw[v * N + c] * fac : T(0);
+  }
+  if (tg >= 0) {
+    // cut-cell wall faces, this cell's records in record order: efluxb on dw
+    // (efluxb.f90:72-110) and dfluxb on fw (dfluxb.f90:47-420)
+    T Rl[INLINE_REC ? 50 : 1];
+    for (int o = b.tgt_off[tg]; o < b.tgt_off[tg + 1]; o++) {
+      const int op = b.tgt_ops[o];
+      const T* R;
+      if (INLINE_REC) {
+        rec_terms(b, P, A.dissip_on, (T)A.cd, err, op >> 1, Rl);
+        R = Rl;
+      } else {
+        R = b.rec_term + 50LL * (op >> 1);
+      }
+      if (!(op & 1)) {
 #pragma unroll
         for (int v = 0; v < 5; v++) {
-          fwv[v] = fwv[v] - R[v];
-          fwv[v] = fwv[v] + R[5 + v];
+          dwv[v] = dwv[v] - R[v];
+          dwv[v] = dwv[v] + R[5 + v] - R[10 + v];
+        }
+      }
+      if (A.dissip_on) {
+        const T* Rd = R + ((op & 1) ? 25 : 15);
+#pragma unroll
+        for (int v = 0; v < 5; v++) {
+          fwv[v] = fwv[v] - Rd[v];
+          fwv[v] = fwv[v] + Rd[5 + v];
         }
       }
     }
+  }
+  if (A.dissip_on || A.scale_fw) {
 #pragma unroll
     for (int v = 0; v < 5; v++) b.fw[v * N + c] = fwv[v];
-  } else {
-    const T fac = T(1) - (T)A.cd;
-#pragma unroll
-    for (int v = 0; v < 5; v++) {
-      fwv[v] = A.scale_fw ? b.fw[v * N + c] * fac : T(0);
-      if (A.scale_fw) b.fw[v * N + c] = fwv[v];
-    }
   }
 #pragma unroll
   for (int v = 0; v < 5; v++) dwv[v] = dwv[v] + fwv[v];
@@ -625,7 +903,9 @@ __device__ __forceinline__ void body_combine(const DevBlock<T>& b, const PhysPar
   T de = mdiv((T)A.fn * vd, (T)b.vol, (T)b.rvol);
 #pragma unroll
   for (int v = 0; v < 5; v++) dwv[v] = de * dwv[v];
-  if (A.irs) {
+  if (A.irs || INLINE_REC) {
+    // with the record terms computed inline, other threads of this pass
+    // still read w and p of this cell: the update waits for the barrier
 #pragma unroll
     for (int v = 0; v < 5; v++) b.dw[v * N + c] = dwv[v];
     return;
@@ -704,6 +984,96 @@ __device__ __forceinline__ void body_irs(const DevBlock<T>& b, const IrsTables& 
     }
     prev = x;
   }
+}
+
+// Shared-memory variant of body_irs: a block stages LT whole lines of one
+// variable (and their blanking) in shared memory with coalesced loads, each
+// of its first LT threads runs the reference's sweep on one line there, and
+// the block writes the lines back coalesced.  Arithmetic and order per line
+// are those of body_irs.
+template <typename T, typename TC, int D, int LT>
+__global__ void __launch_bounds__(LT) k_irs_smem(DevBlock<T> b, IrsTables tb, TC bb) {
+  extern __shared__ unsigned char smem_raw[];
+  const long long lines = irs_lines<T, D>(b);
+  const long long ntile = (lines + LT - 1) / LT;
+  const int v = (int)(blockIdx.x / ntile);
+  const long long tile = blockIdx.x - (long long)v * ntile;
+  const long long l0 = tile * LT;
+  const int nl = (int)min((long long)LT, lines - l0);
+  const int l = (D == 0) ? b.il : (D == 1 ? b.jl : b.kl);   // rows 2..l
+  const int len = l - 1;
+  const int S = (D == 0) ? (len | 1) : LT;                  // odd row stride for line-major tiles
+  TC* x = (TC*)smem_raw;
+  unsigned char* bl = smem_raw + sizeof(TC) * (size_t)LT * (len + 1);
+  T* d = b.dw + (long long)v * b.N;
+  const long long N = b.N;
+  (void)N;
+  // element (line r, row q) of the tile -> global cell
+  auto cell = [&](int r, int q) -> long long {
+    long long ln = l0 + r;
+    if (D == 0) {
+      int j = 2 + (int)(ln % b.ny), k = 2 + (int)(ln / b.ny);
+      return cidx(b.Pi, b.Pj, 2 + q, j, k);
+    } else if (D == 1) {
+      int i = 2 + (int)(ln % b.nx), k = 2 + (int)(ln / b.nx);
+      return cidx(b.Pi, b.Pj, i, 2 + q, k);
+    } else {
+      int i = 2 + (int)(ln % b.nx), j = 2 + (int)(ln / b.nx);
+      return cidx(b.Pi, b.Pj, i, j, 2 + q);
+    }
+  };
+  auto sidx = [&](int r, int q) -> int { return D == 0 ? r * S + q : q * LT + r; };
+  const int tot = nl * len;
+  for (int e = threadIdx.x; e < LT * len; e += blockDim.x) {
+    int r, q;
+    if (D == 0) { r = e / len; q = e - r * len; } else { q = e / LT; r = e - q * LT; }
+    if (r < nl) {
+      long long c = cell(r, q);
+      x[sidx(r, q)] = (TC)d[c];
+      bl[sidx(r, q)] = b.blank[c];
+    }
+  }
+  __syncthreads();
+  const int r = threadIdx.x;
+  if (r < nl) {
+    TC prev;
+    {
+      TC xv = x[sidx(r, 0)];
+      if (bl[sidx(r, 0)] != 0) {
+        xv = xv / (TC)tb.e1[2];
+        x[sidx(r, 0)] = xv;
+      }
+      prev = xv;
+    }
+    for (int q = 1; q < len; q++) {
+      TC xv = x[sidx(r, q)];
+      if (bl[sidx(r, q)] != 0) {
+        xv = mdiv(xv - bb * prev, (TC)tb.e1[q + 2], (TC)tb.e1r[q + 2]);
+        x[sidx(r, q)] = xv;
+      }
+      prev = xv;
+    }
+    for (int q = len - 2; q >= 0; q--) {
+      TC xv = x[sidx(r, q)];
+      if (bl[sidx(r, q)] != 0) {
+        xv = xv - (TC)tb.e2[q + 2] * prev;
+        x[sidx(r, q)] = xv;
+      }
+      prev = xv;
+    }
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < LT * len; e += blockDim.x) {
+    int rr, q;
+    if (D == 0) { rr = e / len; q = e - rr * len; } else { q = e / LT; rr = e - q * LT; }
+    if (rr < nl) d[cell(rr, q)] = (T)x[sidx(rr, q)];
+  }
+  (void)tot;
+}
+
+template <typename TC, int LT>
+size_t irs_smem_bytes(int len) {
+  return sizeof(TC) * (size_t)LT * (len + 1) + (size_t)LT * (len + 1);
 }
 
 // update after smoothing, euler.f90:381-399 (steady: lam = 1)
@@ -1255,9 +1625,9 @@ __global__ void k_forces(DevBlock<T> b, double ox, double oy, double oz, double 
 
 // =============================================================== one-launch-per-phase kernels
 template <typename T>
-__global__ void k_prep(DevBlock<T> b, int dissip_on) {
+__global__ void k_prep(DevBlock<T> b, PhysParams P, int dissip_on) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < (long long)b.ie * b.je * b.ke) body_prep(b, dissip_on, t);
+  if (t < (long long)b.ie * b.je * b.ke) body_prep(b, P, dissip_on, t);
 }
 template <typename T>
 __global__ void k_face(DevBlock<T> b, PhysParams P, int dissip_on, T cd) {
@@ -1265,14 +1635,9 @@ __global__ void k_face(DevBlock<T> b, PhysParams P, int dissip_on, T cd) {
   if (t < (long long)(b.ie - 1) * (b.je - 1) * (b.ke - 1)) body_face(b, P, dissip_on, cd, t);
 }
 template <typename T>
-__global__ void k_rec(DevBlock<T> b, PhysParams P, int dissip_on, T cd, unsigned* err) {
-  int m = blockIdx.x * blockDim.x + threadIdx.x;
-  if (m < b.nmir) body_rec(b, P, dissip_on, cd, err, m);
-}
-template <typename T>
-__global__ void k_combine(DevBlock<T> b, PhysParams P, StageArgs A) {
+__global__ void k_combine(DevBlock<T> b, PhysParams P, StageArgs A, unsigned* err) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < (long long)b.nx * b.ny * b.nz) body_combine(b, P, A, t);
+  if (t < (long long)b.nx * b.ny * b.nz) body_combine<T, false>(b, P, A, err, t);
 }
 template <typename T, typename TC, int D>
 __global__ void k_irs(DevBlock<T> b, IrsTables tb, TC bb) {
@@ -1310,11 +1675,29 @@ struct EulerArgs {
   int npart;
   double* rt_out;
   unsigned* err;
+  unsigned long long* trace;  // optional: globaltimer after every barrier (block 0, thread 0)
 };
 
-template <typename T>
-__global__ void __launch_bounds__(256) k_euler_coop(DevBlock<T> b, PhysParams P, EulerArgs E) {
-  cg::grid_group g = cg::this_grid();
+__device__ __forceinline__ unsigned long long gtimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+template <typename T, typename TA>
+__global__ void __launch_bounds__(256, 2) k_euler_coop(DevBlock<T> b, PhysParams P, EulerArgs E) {
+  cg::grid_group g_ = cg::this_grid();
+  int ntr = 0;
+  struct Sync {
+    cg::grid_group& g;
+    unsigned long long* tr;
+    int& n;
+    __device__ void sync() {
+      g.sync();
+      if (tr && blockIdx.x == 0 && threadIdx.x == 0 && n < 255) tr[1 + n++] = gtimer();
+    }
+  } g{g_, E.trace, ntr};
+  if (E.trace && blockIdx.x == 0 && threadIdx.x == 0) E.trace[0] = gtimer();
   const long long gt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long gs = (long long)gridDim.x * blockDim.x;
   const long long ncell = (long long)b.nx * b.ny * b.nz;
@@ -1324,7 +1707,7 @@ __global__ void __launch_bounds__(256) k_euler_coop(DevBlock<T> b, PhysParams P,
     for (long long base = (long long)blockIdx.x * blockDim.x; base < ncell; base += gs) {
       long long t = base + threadIdx.x;
       unsigned long long mine = ~0ull;
-      if (t < ncell) mine = body_timestep<T, T>(b, P, E.err, t);
+      if (t < ncell) mine = body_timestep<T, TA>(b, P, E.err, t);
       block_min_to(mine, b.dtim);
     }
     g.sync();
@@ -1337,28 +1720,24 @@ __global__ void __launch_bounds__(256) k_euler_coop(DevBlock<T> b, PhysParams P,
   const long long nface = (long long)(b.ie - 1) * (b.je - 1) * (b.ke - 1);
   for (int m = 1; m <= E.mstage; m++) {
     const StageArgs& A = E.st[m - 1];
-    for (long long t = gt; t < nprep; t += gs) body_prep(b, A.dissip_on, t);
+    for (long long t = gt; t < nprep; t += gs) body_prep(b, P, A.dissip_on, t);
     g.sync();
     for (long long t = gt; t < nface; t += gs) body_face(b, P, A.dissip_on, (T)A.cd, t);
     g.sync();
-    if (b.nmir > 0) {
-      for (long long t = gt; t < b.nmir; t += gs) body_rec(b, P, A.dissip_on, (T)A.cd, E.err, (int)t);
-      g.sync();
-    }
-    for (long long t = gt; t < ncell; t += gs) body_combine(b, P, A, t);
+    for (long long t = gt; t < ncell; t += gs) body_combine<T, true>(b, P, A, E.err, t);
     g.sync();
     if (E.lres) return;
     if (A.irs) {
-      const T bb = (T)(-P.smoo);
-      for (long long t = gt; t < 5 * irs_lines<T, 0>(b); t += gs) body_irs<T, T, 0>(b, E.tab[0], bb, t);
+      const TA bb = (TA)(-P.smoo);
+      for (long long t = gt; t < 5 * irs_lines<T, 0>(b); t += gs) body_irs<T, TA, 0>(b, E.tab[0], bb, t);
       g.sync();
-      for (long long t = gt; t < 5 * irs_lines<T, 1>(b); t += gs) body_irs<T, T, 1>(b, E.tab[1], bb, t);
+      for (long long t = gt; t < 5 * irs_lines<T, 1>(b); t += gs) body_irs<T, TA, 1>(b, E.tab[1], bb, t);
       g.sync();
-      for (long long t = gt; t < 5 * irs_lines<T, 2>(b); t += gs) body_irs<T, T, 2>(b, E.tab[2], bb, t);
-      g.sync();
-      for (long long t = gt; t < ncell; t += gs) body_update(b, P, t);
+      for (long long t = gt; t < 5 * irs_lines<T, 2>(b); t += gs) body_irs<T, TA, 2>(b, E.tab[2], bb, t);
       g.sync();
     }
+    for (long long t = gt; t < ncell; t += gs) body_update(b, P, t);
+    g.sync();
     for (long long t = gt; t < b.nmir; t += gs) body_cutcell(b, P, E.err, (int)t);
     g.sync();
     for (int f = 1; f <= 6; f++) {
@@ -1376,16 +1755,20 @@ __global__ void __launch_bounds__(256) k_euler_coop(DevBlock<T> b, PhysParams P,
     g.sync();
     if (gt == 0) body_rtrms_final(E.rt_partial, E.npart, (double)ncell, E.rt_out);
   }
+  if (E.trace && blockIdx.x == 0 && threadIdx.x == 0) E.trace[255] = (unsigned long long)ntr;
 }
 
 // =============================================================== launchers
 constexpr int TPB = 256;
 
 template <typename T>
-void launch_timestep(const DevBlock<T>& b, const PhysParams& P, unsigned* err, cudaStream_t s) {
+void launch_timestep(const DevBlock<T>& b, const PhysParams& P, unsigned* err, cudaStream_t s, bool aux32) {
   long long n = (long long)b.nx * b.ny * b.nz;
   k_dtim_reset<<<1, 32, 0, s>>>(b.dtim);
-  k_timestep<T, T><<<nblk(n, TPB), TPB, 0, s>>>(b, P, err);
+  if (aux32)
+    k_timestep<T, float><<<nblk(n, TPB), TPB, 0, s>>>(b, P, err);
+  else
+    k_timestep<T, T><<<nblk(n, TPB), TPB, 0, s>>>(b, P, err);
 }
 
 template <typename T>
@@ -1393,15 +1776,15 @@ void launch_stage_part(int part, const DevBlock<T>& b, const PhysParams& P, cons
                        cudaStream_t s) {
   if (part == 0) {
     long long n1 = (long long)b.ie * b.je * b.ke;
-    k_prep<T><<<nblk(n1, TPB), TPB, 0, s>>>(b, A.dissip_on);
+    k_prep<T><<<nblk(n1, TPB), TPB, 0, s>>>(b, P, A.dissip_on);
   } else if (part == 1) {
     long long n2 = (long long)(b.ie - 1) * (b.je - 1) * (b.ke - 1);
     k_face<T><<<nblk(n2, TPB), TPB, 0, s>>>(b, P, A.dissip_on, (T)A.cd);
   } else if (part == 2) {
     if (b.nmir > 0) k_rec<T><<<nblk(b.nmir, 128), 128, 0, s>>>(b, P, A.dissip_on, (T)A.cd, err);
-  } else {
+  } else if (part == 3) {
     long long n3 = (long long)b.nx * b.ny * b.nz;
-    k_combine<T><<<nblk(n3, TPB), TPB, 0, s>>>(b, P, A);
+    k_combine<T><<<nblk(n3, TPB), TPB, 0, s>>>(b, P, A, err);
   }
 }
 
@@ -1410,21 +1793,49 @@ void launch_stage(const DevBlock<T>& b, const PhysParams& P, const StageArgs& A,
   for (int part = 0; part < 4; part++) launch_stage_part<T>(part, b, P, A, err, s);
 }
 
-template <typename T>
-void launch_irs_part(int part, const DevBlock<T>& b, const PhysParams& P, const IrsTables* tab, cudaStream_t s) {
-  const T bb = (T)(-P.smoo);
+// the line-sweep variant: 0 = one thread per (line, variable) in global
+// memory, 1 = shared-memory tiles of 64 lines; the autotuner picks per block
+// and direction
+template <typename T, typename TC, int D>
+void launch_irs_dir(const DevBlock<T>& b, const IrsTables& tb, TC bb, cudaStream_t s, int variant) {
+  const long long lines = D == 0 ? (long long)b.ny * b.nz : (D == 1 ? (long long)b.nx * b.nz : (long long)b.nx * b.ny);
+  const int len = (D == 0 ? b.il : (D == 1 ? b.jl : b.kl)) - 1;
+  constexpr int LT = 64;
+  const size_t sm = irs_smem_bytes<TC, LT>(len | 1);
+  if (variant == 1 && sm <= 200 * 1024) {
+    const long long grid = 5 * ((lines + LT - 1) / LT);
+    k_irs_smem<T, TC, D, LT><<<(unsigned)grid, LT, sm, s>>>(b, tb, bb);
+  } else {
+    k_irs<T, TC, D><<<nblk(5 * lines, 128), 128, 0, s>>>(b, tb, bb);
+  }
+}
+
+template <typename T, typename TC>
+void launch_irs_part_t(int part, const DevBlock<T>& b, const PhysParams& P, const IrsTables* tab, cudaStream_t s,
+                       const int* variant) {
+  const TC bb = (TC)(-P.smoo);
   const long long ncell = (long long)b.nx * b.ny * b.nz;
-  if (part == 0) k_irs<T, T, 0><<<nblk(5 * (long long)b.ny * b.nz, 128), 128, 0, s>>>(b, tab[0], bb);
-  if (part == 1) k_irs<T, T, 1><<<nblk(5 * (long long)b.nx * b.nz, 128), 128, 0, s>>>(b, tab[1], bb);
+  if (part == 0) launch_irs_dir<T, TC, 0>(b, tab[0], bb, s, variant ? variant[0] : 0);
+  if (part == 1) launch_irs_dir<T, TC, 1>(b, tab[1], bb, s, variant ? variant[1] : 0);
   if (part == 2) {
-    k_irs<T, T, 2><<<nblk(5 * (long long)b.nx * b.ny, 128), 128, 0, s>>>(b, tab[2], bb);
+    launch_irs_dir<T, TC, 2>(b, tab[2], bb, s, variant ? variant[2] : 0);
     k_update<T><<<nblk(ncell, TPB), TPB, 0, s>>>(b, P);
   }
 }
 
 template <typename T>
-void launch_irs(const DevBlock<T>& b, const PhysParams& P, const IrsTables* tab, cudaStream_t s) {
-  for (int part = 0; part < 3; part++) launch_irs_part<T>(part, b, P, tab, s);
+void launch_irs_part(int part, const DevBlock<T>& b, const PhysParams& P, const IrsTables* tab, cudaStream_t s,
+                     bool aux32, const int* variant) {
+  if (aux32)
+    launch_irs_part_t<T, float>(part, b, P, tab, s, variant);
+  else
+    launch_irs_part_t<T, T>(part, b, P, tab, s, variant);
+}
+
+template <typename T>
+void launch_irs(const DevBlock<T>& b, const PhysParams& P, const IrsTables* tab, cudaStream_t s, bool aux32,
+                const int* variant) {
+  for (int part = 0; part < 3; part++) launch_irs_part<T>(part, b, P, tab, s, aux32, variant);
 }
 
 template <typename T>
@@ -1450,15 +1861,41 @@ void launch_rtrms(const DevBlock<T>& b, const PhysParams& P, int vt, double* par
   k_rtrms_final<<<1, 32, 0, s>>>(partial, npartial, (double)b.nx * b.ny * b.nz, out);
 }
 
+template <typename TS, typename TD>
+__global__ void k_convert(const TS* __restrict__ a, TD* __restrict__ b, long long n) {
+  long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < n) b[q] = (TD)a[q];
+}
+
+void launch_convert(const void* src, bool src32, void* dst, bool dst32, long long n, cudaStream_t s) {
+  if (n <= 0) return;
+  if (src32 && !dst32) k_convert<float, double><<<nblk(n, TPB), TPB, 0, s>>>((const float*)src, (double*)dst, n);
+  else if (!src32 && dst32) k_convert<double, float><<<nblk(n, TPB), TPB, 0, s>>>((const double*)src, (float*)dst, n);
+  else if (src32) k_convert<float, float><<<nblk(n, TPB), TPB, 0, s>>>((const float*)src, (float*)dst, n);
+  else k_convert<double, double><<<nblk(n, TPB), TPB, 0, s>>>((const double*)src, (double*)dst, n);
+}
+
+// opt-in shared memory of the tiled line sweeps; called once per device at set-up
+void init_kernel_attributes() {
+#define MGE_SMEM_ATTR(T, TC)                                                                                     \
+  cudaFuncSetAttribute(k_irs_smem<T, TC, 0, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);     \
+  cudaFuncSetAttribute(k_irs_smem<T, TC, 1, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);     \
+  cudaFuncSetAttribute(k_irs_smem<T, TC, 2, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  MGE_SMEM_ATTR(double, double)
+  MGE_SMEM_ATTR(double, float)
+  MGE_SMEM_ATTR(float, float)
+#undef MGE_SMEM_ATTR
+}
+
 // grid of the cooperative kernel: every block resident at once
-template <typename T>
+template <typename T, typename TA>
 int coop_grid(int device) {
   static int cached[64] = {0};
   if (device < 0 || device >= 64) return 0;
   if (cached[device]) return cached[device];
   int nsm = 0, per = 0;
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_euler_coop<T>, 256, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_euler_coop<T, TA>, 256, 0);
   int coop = 0;
   cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device);
   cached[device] = (coop && per > 0) ? nsm * per : -1;
@@ -1466,11 +1903,13 @@ int coop_grid(int device) {
 }
 
 template <typename T>
-int launch_euler_coop(const DevBlock<T>& b, const PhysParams& P, const EulerLaunch& L, int device, cudaStream_t s) {
-  int grid = coop_grid<T>(device);
+int launch_euler_coop(const DevBlock<T>& b, const PhysParams& P, const EulerLaunch& L, int device, cudaStream_t s,
+                      bool aux32) {
+  int grid = aux32 ? coop_grid<T, float>(device) : coop_grid<T, T>(device);
   if (grid <= 0) return -1;
   long long work = (long long)(b.ie) * b.je * b.ke;
   int need = (int)std::min<long long>((work + 255) / 256, (long long)grid);
+  if (L.max_ctas > 0 && need > L.max_ctas) need = L.max_ctas;
   if (need < 1) need = 1;
   EulerArgs E;
   memset(&E, 0, sizeof(E));
@@ -1485,10 +1924,12 @@ int launch_euler_coop(const DevBlock<T>& b, const PhysParams& P, const EulerLaun
   E.npart = L.npart;
   E.rt_out = L.rt_out;
   E.err = L.err;
+  E.trace = L.trace;
   DevBlock<T> bb = b;
   PhysParams pp = P;
   void* args[] = {&bb, &pp, &E};
-  cudaError_t e = cudaLaunchCooperativeKernel((void*)k_euler_coop<T>, need, 256, args, 0, s);
+  void* fn = aux32 ? (void*)k_euler_coop<T, float> : (void*)k_euler_coop<T, T>;
+  cudaError_t e = cudaLaunchCooperativeKernel(fn, need, 256, args, 0, s);
   return e == cudaSuccess ? 0 : -2;
 }
 
@@ -1561,13 +2002,16 @@ void launch_forces(const DevBlock<T>& b, const double* origin, const double* h, 
 
 // explicit instantiations
 #define MGE_INST(T)                                                                                              \
-  template void launch_timestep<T>(const DevBlock<T>&, const PhysParams&, unsigned*, cudaStream_t);             \
+  template void launch_timestep<T>(const DevBlock<T>&, const PhysParams&, unsigned*, cudaStream_t, bool);       \
   template void launch_stage<T>(const DevBlock<T>&, const PhysParams&, const StageArgs&, unsigned*, cudaStream_t); \
   template void launch_stage_part<T>(int, const DevBlock<T>&, const PhysParams&, const StageArgs&, unsigned*,       \
                                      cudaStream_t);                                                             \
-  template void launch_irs_part<T>(int, const DevBlock<T>&, const PhysParams&, const IrsTables*, cudaStream_t);  \
-  template int launch_euler_coop<T>(const DevBlock<T>&, const PhysParams&, const EulerLaunch&, int, cudaStream_t); \
-  template void launch_irs<T>(const DevBlock<T>&, const PhysParams&, const IrsTables*, cudaStream_t);           \
+  template void launch_irs_part<T>(int, const DevBlock<T>&, const PhysParams&, const IrsTables*, cudaStream_t,    \
+                                   bool, const int*);                                                           \
+  template int launch_euler_coop<T>(const DevBlock<T>&, const PhysParams&, const EulerLaunch&, int, cudaStream_t,  \
+                                    bool);                                                                      \
+  template void launch_irs<T>(const DevBlock<T>&, const PhysParams&, const IrsTables*, cudaStream_t, bool,       \
+                              const int*);                                                                      \
   template void launch_cutcell<T>(const DevBlock<T>&, const PhysParams&, unsigned*, cudaStream_t);              \
   template void launch_bcond<T>(const DevBlock<T>&, const PhysParams&, cudaStream_t);                           \
   template void launch_rtrms<T>(const DevBlock<T>&, const PhysParams&, int, double*, int, double*, cudaStream_t); \
@@ -1578,13 +2022,19 @@ void launch_forces(const DevBlock<T>& b, const double* origin, const double* h, 
   template void launch_init_free<T>(const DevBlock<T>&, const PhysParams&, cudaStream_t);                       \
   template void launch_forces<T>(const DevBlock<T>&, const double*, const double*, const double*, double*, cudaStream_t);
 MGE_INST(double)
+MGE_INST(float)
 #undef MGE_INST
-template void launch_collc<double, double>(const DevBlock<double>&, const DevBlock<double>&, const int*, const int*,
-                                           uint8_t*, cudaStream_t);
-template void launch_addw<double, double>(const DevBlock<double>&, const DevBlock<double>&, const int*, const int*, int,
-                                          cudaStream_t);
-template void launch_embed<double, double>(const DevBlock<double>&, const DevBlock<double>&, const int*, const int*,
-                                           const PhysParams&, cudaStream_t);
+#define MGE_XFER(TC, TF)                                                                                         \
+  template void launch_collc<TC, TF>(const DevBlock<TC>&, const DevBlock<TF>&, const int*, const int*, uint8_t*,   \
+                                     cudaStream_t);                                                             \
+  template void launch_addw<TF, TC>(const DevBlock<TF>&, const DevBlock<TC>&, const int*, const int*, int,          \
+                                    cudaStream_t);                                                              \
+  template void launch_embed<TF, TC>(const DevBlock<TF>&, const DevBlock<TC>&, const int*, const int*,              \
+                                     const PhysParams&, cudaStream_t);
+MGE_XFER(double, double)
+MGE_XFER(float, double)
+MGE_XFER(float, float)
+#undef MGE_XFER
 
 
 }  // namespace mge

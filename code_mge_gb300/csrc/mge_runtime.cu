@@ -7,11 +7,14 @@
 // movco.f90, movfin.f90, solver.f90); mge_solve runs solver.f90's FMG loop
 // with each multigrid cycle captured once per FMG level and replayed.
 #include <algorithm>
+#include <type_traits>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <mutex>
+#include <tuple>
 #include <string>
 #include <vector>
 
@@ -43,22 +46,38 @@ struct Block {
   int parent = -1, ratio[3] = {1, 1, 1}, offset[3] = {0, 0, 0};
   std::vector<int32_t> blank_h;
   std::vector<HRec> recs;
-  // device allocations
-  double *w = nullptr, *p = nullptr, *wn = nullptr, *ws = nullptr, *dw = nullptr, *fw = nullptr, *wr = nullptr,
-         *qf = nullptr, *vdtim = nullptr, *lam = nullptr, *dtim = nullptr;
+  // device allocations; state fields hold doubles, or floats when f32
+  bool f32 = false;    // FP32 storage and arithmetic (coarse levels of the mixed mode)
+  bool aux32 = false;  // FP32 time step and smoothing on FP64 storage (finest level of the mixed mode)
+  bool use_coop = false;   // run timestep + euler as one cooperative launch
+  int irs_var[3] = {0, 0, 0};  // line-sweep variant per direction (autotuned)
+  size_t esz = 8;
+  void *w = nullptr, *p = nullptr, *wn = nullptr, *ws = nullptr, *dw = nullptr, *fw = nullptr, *wr = nullptr,
+       *qf = nullptr, *vdtim = nullptr, *lam = nullptr;
+  double* dtim = nullptr;
   uint8_t *blank = nullptr, *marker = nullptr;
   int32_t* cutmap = nullptr;
   int32_t *rec_i = nullptr, *rec_cloud = nullptr, *tgt_off = nullptr, *tgt_ops = nullptr;
-  double *rec_coef = nullptr, *rec_nvec = nullptr, *rec_qb = nullptr, *rec_area = nullptr, *rec_wsol = nullptr,
-         *rec_psol = nullptr, *rec_term = nullptr;
+  double *rec_coef = nullptr, *rec_nvec = nullptr, *rec_qb = nullptr, *rec_area = nullptr;
+  void *rec_wsol = nullptr, *rec_psol = nullptr, *rec_term = nullptr;
   double* irs = nullptr;
   IrsTables tabs[3];
   double *rt_partial = nullptr, *rt_cur = nullptr, *forces = nullptr;
   int npart = 1;
   int m0 = 0;
   std::vector<double> rtrms;  // host history rtrms(ncyc)
-  DevBlock<double> dev;
+  DevBlock<double> dev;       // view when !f32
+  DevBlock<float> dev32;      // view when f32
 };
+
+// run f on the block's typed view: f(DevBlock<double>&) or f(DevBlock<float>&)
+template <typename F>
+void with_dev(Block& b, F&& f) {
+  if (b.f32)
+    f(b.dev32);
+  else
+    f(b.dev);
+}
 
 }  // namespace
 
@@ -82,6 +101,12 @@ struct mge_ctx {
   std::vector<long long> graph_kernels;  // kernel nodes per captured cycle
   long long launches = 0;                // kernels launched through mge_cycle
   long long coop_max_cells = 300000;     // blocks up to this size run euler as one cooperative launch
+  int coop_max_ctas = 0;                 // cap on the cooperative grid (0: all resident blocks)
+  cudaEvent_t ev_done = nullptr;         // end of an asynchronous cycle
+  bool autotune = true;                  // tune launch forms at init_flow
+  bool tune_path = true;                 // ... including cooperative vs per-phase euler
+  int pending_mlvl = 0;                  // level of the cycle in flight (0: none)
+  unsigned long long* coop_trace = nullptr;
 };
 
 namespace {
@@ -138,7 +163,12 @@ int check_err(mge_ctx* c) {
 }
 
 // ---------------------------------------------------------------- device ops
-void enqueue_timestep(mge_ctx* c, Block& b) { launch_timestep<double>(b.dev, c->P, c->d_err, c->stream); }
+void enqueue_timestep(mge_ctx* c, Block& b) {
+  with_dev(b, [&](auto& D) {
+    using T = typename std::remove_reference_t<decltype(D)>::value_type;
+    launch_timestep<T>(D, c->P, c->d_err, c->stream, b.aux32);
+  });
+}
 
 StageArgs stage_args(const mge_params& P, int m, int mgl, int mlvl, bool lres, bool lfir) {
   StageArgs A;
@@ -162,7 +192,7 @@ void enqueue_euler(mge_ctx* c, Block& b, int mgl, int mlvl, bool lres, bool lfir
   const mge_params& P = c->prm;
   const int mstage = (nstage_limit > 0) ? std::min(P.mstage, nstage_limit) : P.mstage;
   const bool want_rt = rt && (nstage_limit <= 0 || nstage_limit >= P.mstage) && !lres;
-  if ((long long)b.nx * b.ny * b.nz <= c->coop_max_cells) {
+  if (b.use_coop) {
     EulerLaunch L;
     std::memset(&L, 0, sizeof(L));
     L.mstage = mstage;
@@ -176,21 +206,68 @@ void enqueue_euler(mge_ctx* c, Block& b, int mgl, int mlvl, bool lres, bool lfir
     L.npart = b.npart;
     L.rt_out = b.rt_cur;
     L.err = c->d_err;
-    if (launch_euler_coop<double>(b.dev, c->P, L, c->device, c->stream) == 0) return;
+    L.trace = c->coop_trace;
+    L.max_ctas = c->coop_max_ctas;
+    int rc = -1;
+    with_dev(b, [&](auto& D) {
+      using T = typename std::remove_reference_t<decltype(D)>::value_type;
+      rc = launch_euler_coop<T>(D, c->P, L, c->device, c->stream, b.aux32);
+    });
+    if (rc == 0) return;
     cudaGetLastError();  // cooperative launch unavailable: fall through to per-phase launches
   }
   if (with_timestep) enqueue_timestep(c, b);
-  if (lfir) launch_copy_ws<double>(b.dev, c->stream);
-  launch_save_wn<double>(b.dev, c->stream);
-  for (int m = 1; m <= mstage; m++) {
-    StageArgs A = stage_args(P, m, mgl, mlvl, lres, lfir);
-    launch_stage<double>(b.dev, c->P, A, c->d_err, c->stream);
-    if (lres) return;
-    if (A.irs) launch_irs<double>(b.dev, c->P, b.tabs, c->stream);
-    launch_cutcell<double>(b.dev, c->P, c->d_err, c->stream);
-    launch_bcond<double>(b.dev, c->P, c->stream);
-  }
-  if (want_rt) launch_rtrms<double>(b.dev, c->P, P.vt, b.rt_partial, b.npart, b.rt_cur, c->stream);
+  with_dev(b, [&](auto& D) {
+    using T = typename std::remove_reference_t<decltype(D)>::value_type;
+    if (lfir) launch_copy_ws<T>(D, c->stream);
+    launch_save_wn<T>(D, c->stream);
+    for (int m = 1; m <= mstage; m++) {
+      StageArgs A = stage_args(P, m, mgl, mlvl, lres, lfir);
+      launch_stage<T>(D, c->P, A, c->d_err, c->stream);
+      if (lres) return;
+      if (A.irs) launch_irs<T>(D, c->P, b.tabs, c->stream, b.aux32, b.irs_var);
+      launch_cutcell<T>(D, c->P, c->d_err, c->stream);
+      launch_bcond<T>(D, c->P, c->stream);
+    }
+    if (want_rt) launch_rtrms<T>(D, c->P, P.vt, b.rt_partial, b.npart, b.rt_cur, c->stream);
+  });
+}
+
+// the restriction of one child onto its parent, in the pair's precisions
+void enqueue_collc(mge_ctx* c, Block& b, Block& f) {
+  with_dev(b, [&](auto& DC) {
+    using TC = typename std::remove_reference_t<decltype(DC)>::value_type;
+    with_dev(f, [&](auto& DF) {
+      using TF = typename std::remove_reference_t<decltype(DF)>::value_type;
+      if constexpr (sizeof(TC) <= sizeof(TF)) launch_collc<TC, TF>(DC, DF, f.ratio, f.offset, b.marker, c->stream);
+    });
+  });
+}
+
+void enqueue_addw_embed(mge_ctx* c, Block& f, Block& pb, bool fmg, bool embed) {
+  with_dev(f, [&](auto& DF) {
+    using TF = typename std::remove_reference_t<decltype(DF)>::value_type;
+    with_dev(pb, [&](auto& DC) {
+      using TC = typename std::remove_reference_t<decltype(DC)>::value_type;
+      if constexpr (sizeof(TC) <= sizeof(TF)) {
+        if (embed)
+          launch_embed<TF, TC>(DF, DC, f.ratio, f.offset, c->P, c->stream);
+        else
+          launch_addw<TF, TC>(DF, DC, f.ratio, f.offset, fmg ? 1 : 0, c->stream);
+      }
+    });
+  });
+}
+
+void enqueue_simple(mge_ctx* c, Block& b, int what) {
+  with_dev(b, [&](auto& D) {
+    using T = typename std::remove_reference_t<decltype(D)>::value_type;
+    if (what == 0) launch_depvars_all<T>(D, c->P, c->stream);
+    if (what == 1) launch_copy_wn<T>(D, c->stream);
+    if (what == 2) launch_bcond<T>(D, c->P, c->stream);
+    if (what == 3) launch_init_free<T>(D, c->P, c->stream);
+    if (what == 4) launch_cutcell<T>(D, c->P, c->d_err, c->stream);
+  });
 }
 
 void enqueue_movco(mge_ctx* c, int mgl) {  // movco.f90:21-47
@@ -198,11 +275,11 @@ void enqueue_movco(mge_ctx* c, int mgl) {  // movco.f90:21-47
     cudaMemsetAsync(b.marker, 0, (size_t)b.N, c->stream);
     if ((int)c->lv.size() > mgl)
       for (Block& f : c->lv[mgl])
-        if (f.parent == b.serial) launch_collc<double, double>(b.dev, f.dev, f.ratio, f.offset, b.marker, c->stream);
-    launch_depvars_all<double>(b.dev, c->P, c->stream);
-    launch_copy_wn<double>(b.dev, c->stream);
+        if (f.parent == b.serial) enqueue_collc(c, b, f);
+    enqueue_simple(c, b, 0);
+    enqueue_simple(c, b, 1);
   }
-  for (Block& b : c->lv[mgl - 1]) launch_bcond<double>(b.dev, c->P, c->stream);
+  for (Block& b : c->lv[mgl - 1]) enqueue_simple(c, b, 2);
 }
 
 void enqueue_movfin(mge_ctx* c, int mgl, int mlvl) {  // movfin.f90:20-39
@@ -210,15 +287,15 @@ void enqueue_movfin(mge_ctx* c, int mgl, int mlvl) {  // movfin.f90:20-39
   for (Block& f : c->lv[mgl - 1]) {
     if (f.parent < 1) continue;
     Block& pb = c->lv[mgl - 2][f.parent - 1];
-    launch_addw<double, double>(f.dev, pb.dev, f.ratio, f.offset, fmg ? 1 : 0, c->stream);
+    enqueue_addw_embed(c, f, pb, fmg, false);
   }
-  for (Block& f : c->lv[mgl - 1]) launch_depvars_all<double>(f.dev, c->P, c->stream);
+  for (Block& f : c->lv[mgl - 1]) enqueue_simple(c, f, 0);
   for (Block& f : c->lv[mgl - 1]) {  // bc_embed
     if (f.parent < 1) continue;
     Block& pb = c->lv[mgl - 2][f.parent - 1];
-    launch_embed<double, double>(f.dev, pb.dev, f.ratio, f.offset, c->P, c->stream);
+    enqueue_addw_embed(c, f, pb, fmg, true);
   }
-  for (Block& f : c->lv[mgl - 1]) launch_bcond<double>(f.dev, c->P, c->stream);
+  for (Block& f : c->lv[mgl - 1]) enqueue_simple(c, f, 2);
 }
 
 // solver.f90:127-234, one multigrid cycle at FMG level mlvl (enqueue only)
@@ -272,6 +349,16 @@ void build_phys(mge_ctx* c) {
   Q.eqn_ns = P.eqntype == MGE_EQN_NS;
   Q.smoo = P.smoo;
   Q.vt = P.vt;
+  Q.distype = P.distype;
+  Q.viscl = P.viscl;
+  Q.gas_const = P.gas_const;
+  Q.prlmean = P.prlmean;
+  Q.kt = P.viscl * P.gamma * P.gas_const / ((P.gamma - 1.0) * P.prlmean);
+  Q.cfac = P.distype == MGE_DIS_CENTRAL ? 4.0 : (P.distype == MGE_DIS_ROE2 ? 1.0 : 2.0);
+  Q.epsentr = P.epsentr;
+  const double u0n = std::sqrt(P.u0 * P.u0 + P.v0 * P.v0 + P.w0 * P.w0);
+  const double ref[5] = {P.rho0, u0n, u0n, u0n, P.p0};
+  for (int q = 0; q < 5; q++) Q.lim_e2[q] = 1e-6 * ref[q] * ref[q] / (P.limfac > 0.0 ? P.limfac : 1.0);
 }
 
 // psmoo.f90:136-166 pivots for a line of l-1 unknowns (rows 2..l)
@@ -290,25 +377,63 @@ void irs_pivots(double smoo, int lm, int l, std::vector<double>& e1, std::vector
   for (int q = 0; q <= l; q++) e1r[q] = 1.0 / e1[q];
 }
 
+int valloc(mge_ctx* c, void** p, size_t n, size_t esz) {
+  uint8_t* q = nullptr;
+  int rc = dalloc(c, &q, n * esz);
+  if (rc) return rc;
+  *p = q;
+  cudaError_t e = cudaMemset(q, 0, std::max<size_t>(n * esz, 1));
+  return e == cudaSuccess ? MGE_OK : cuda_fail(c, e, "cudaMemset");
+}
+
+template <typename T>
+void fill_view(Block& b, DevBlock<T>& d, void* scratch) {
+  const long long N = b.N;
+  std::memset(&d, 0, sizeof(d));
+  d.nx = b.nx; d.ny = b.ny; d.nz = b.nz;
+  d.il = b.il; d.jl = b.jl; d.kl = b.kl; d.ie = b.ie; d.je = b.je; d.ke = b.ke; d.ib = b.ib; d.jb = b.jb; d.kb = b.kb;
+  d.Pi = b.Pi; d.Pj = b.Pj; d.N = N;
+  d.w = (T*)b.w; d.p = (T*)b.p; d.wn = (T*)b.wn; d.ws = (T*)b.ws; d.dw = (T*)b.dw; d.fw = (T*)b.fw;
+  d.wr = (T*)b.wr; d.qf = (T*)b.qf; d.vdtim = (T*)b.vdtim; d.lam = (T*)b.lam; d.dtim = b.dtim;
+  d.blank = b.blank; d.marker = b.marker; d.cutmap = b.cutmap;
+  T* sc = (T*)scratch;
+  d.H = sc;
+  d.F = sc + N;
+  d.fp = sc + 16 * N;
+  d.efs = sc + 19 * N;
+  d.dfs = sc + 34 * N;
+  d.vt = sc + 49 * N;
+  d.vfs = sc + 53 * N;
+  d.hx = b.h[0];
+  d.hy = b.h[1];
+  d.hz = b.h[2];
+  for (int q = 0; q < 3; q++) {
+    d.s[q] = b.s[q];
+    d.sqrt_ds[q] = std::sqrt(b.s[q] * b.s[q]);
+  }
+  d.vol = b.vol;
+  d.rvol = 1.0 / b.vol;
+  d.nmir = (int)b.recs.size();
+  d.m0 = b.m0;
+  d.rec_i = b.rec_i; d.rec_cloud = b.rec_cloud; d.rec_coef = b.rec_coef; d.rec_nvec = b.rec_nvec;
+  d.rec_qb = b.rec_qb; d.rec_area = b.rec_area; d.rec_wsol = (T*)b.rec_wsol; d.rec_psol = (T*)b.rec_psol;
+  d.rec_term = (T*)b.rec_term; d.tgt_off = b.tgt_off; d.tgt_ops = b.tgt_ops;
+  for (int f = 0; f < 6; f++) {
+    d.bctype[f] = b.bctype[f];
+    for (int q = 0; q < 3; q++) d.fnv[f][q] = b.fnv[f][q];
+  }
+}
+
 int commit_block(mge_ctx* c, Block& b, double* scratch) {
   const long long N = b.N;
+  const size_t es = b.esz;
   int rc;
-  if ((rc = dalloc(c, &b.w, 5 * N)) || (rc = dalloc(c, &b.p, N)) || (rc = dalloc(c, &b.wn, 5 * N)) ||
-      (rc = dalloc(c, &b.ws, 5 * N)) || (rc = dalloc(c, &b.dw, 5 * N)) || (rc = dalloc(c, &b.fw, 5 * N)) ||
-      (rc = dalloc(c, &b.wr, 5 * N)) || (rc = dalloc(c, &b.qf, 5 * N)) || (rc = dalloc(c, &b.vdtim, N)) ||
-      (rc = dalloc(c, &b.lam, N)) || (rc = dalloc(c, &b.dtim, 1)) || (rc = dalloc(c, &b.blank, N)) ||
+  if ((rc = valloc(c, &b.w, 5 * N, es)) || (rc = valloc(c, &b.p, N, es)) || (rc = valloc(c, &b.wn, 5 * N, es)) ||
+      (rc = valloc(c, &b.ws, 5 * N, es)) || (rc = valloc(c, &b.dw, 5 * N, es)) || (rc = valloc(c, &b.fw, 5 * N, es)) ||
+      (rc = valloc(c, &b.wr, 5 * N, es)) || (rc = valloc(c, &b.qf, 5 * N, es)) || (rc = valloc(c, &b.vdtim, N, es)) ||
+      (rc = valloc(c, &b.lam, N, es)) || (rc = dalloc(c, &b.dtim, 1)) || (rc = dalloc(c, &b.blank, N)) ||
       (rc = dalloc(c, &b.marker, N)) || (rc = dalloc(c, &b.cutmap, N)))
     return rc;
-  CK(cudaMemset(b.w, 0, 5 * N * sizeof(double)));
-  CK(cudaMemset(b.p, 0, N * sizeof(double)));
-  CK(cudaMemset(b.wn, 0, 5 * N * sizeof(double)));
-  CK(cudaMemset(b.ws, 0, 5 * N * sizeof(double)));
-  CK(cudaMemset(b.dw, 0, 5 * N * sizeof(double)));
-  CK(cudaMemset(b.fw, 0, 5 * N * sizeof(double)));
-  CK(cudaMemset(b.wr, 0, 5 * N * sizeof(double)));
-  CK(cudaMemset(b.qf, 0, 5 * N * sizeof(double)));
-  CK(cudaMemset(b.vdtim, 0, N * sizeof(double)));
-  CK(cudaMemset(b.lam, 0, N * sizeof(double)));
   CK(cudaMemset(b.marker, 0, N));
   std::vector<uint8_t> bl(N);
   for (long long q = 0; q < N; q++) bl[q] = b.blank_h[q] != 0 ? 1 : 0;
@@ -346,8 +471,8 @@ int commit_block(mge_ctx* c, Block& b, double* scratch) {
   if ((rc = dalloc(c, &b.rec_i, 8 * nma)) || (rc = dalloc(c, &b.rec_cloud, 24 * nma)) ||
       (rc = dalloc(c, &b.rec_coef, 8 * nma)) || (rc = dalloc(c, &b.rec_nvec, 3 * nma)) ||
       (rc = dalloc(c, &b.rec_qb, 3 * nma)) || (rc = dalloc(c, &b.rec_area, nma)) ||
-      (rc = dalloc(c, &b.rec_wsol, 5 * nma)) || (rc = dalloc(c, &b.rec_psol, nma)) ||
-      (rc = dalloc(c, &b.rec_term, 40 * nma)))
+      (rc = valloc(c, &b.rec_wsol, 5 * nma, es)) || (rc = valloc(c, &b.rec_psol, nma, es)) ||
+      (rc = valloc(c, &b.rec_term, 50 * nma, es)))
     return rc;
   CK(cudaMemcpy(b.rec_i, ri.data(), ri.size() * 4, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(b.rec_cloud, rcl.data(), rcl.size() * 4, cudaMemcpyHostToDevice));
@@ -355,9 +480,6 @@ int commit_block(mge_ctx* c, Block& b, double* scratch) {
   CK(cudaMemcpy(b.rec_nvec, rnv.data(), rnv.size() * 8, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(b.rec_qb, rqb.data(), rqb.size() * 8, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(b.rec_area, rar.data(), rar.size() * 8, cudaMemcpyHostToDevice));
-  CK(cudaMemset(b.rec_wsol, 0, 5 * nma * 8));
-  CK(cudaMemset(b.rec_psol, 0, nma * 8));
-  CK(cudaMemset(b.rec_term, 0, 40 * nma * 8));
   // cut targets: per physical cell, the (record, role) ops in record order
   std::vector<int32_t> cutmap(N, -1);
   std::map<long long, std::vector<int32_t>> tg;
@@ -420,34 +542,10 @@ int commit_block(mge_ctx* c, Block& b, double* scratch) {
     return rc;
   CK(cudaMemset(b.rt_cur, 0, 8));
   // kernel view
-  DevBlock<double>& d = b.dev;
-  std::memset(&d, 0, sizeof(d));
-  d.nx = b.nx; d.ny = b.ny; d.nz = b.nz;
-  d.il = b.il; d.jl = b.jl; d.kl = b.kl; d.ie = b.ie; d.je = b.je; d.ke = b.ke; d.ib = b.ib; d.jb = b.jb; d.kb = b.kb;
-  d.Pi = b.Pi; d.Pj = b.Pj; d.N = N;
-  d.w = b.w; d.p = b.p; d.wn = b.wn; d.ws = b.ws; d.dw = b.dw; d.fw = b.fw; d.wr = b.wr; d.qf = b.qf;
-  d.vdtim = b.vdtim; d.lam = b.lam; d.dtim = b.dtim;
-  d.blank = b.blank; d.marker = b.marker; d.cutmap = b.cutmap;
-  d.H = scratch;
-  d.F = scratch + N;
-  d.fp = scratch + 16 * N;
-  d.efs = scratch + 19 * N;
-  d.dfs = scratch + 34 * N;
-  for (int q = 0; q < 3; q++) {
-    d.s[q] = b.s[q];
-    d.sqrt_ds[q] = std::sqrt(b.s[q] * b.s[q]);
-  }
-  d.vol = b.vol;
-  d.rvol = 1.0 / b.vol;
-  d.nmir = nm;
-  d.m0 = b.m0;
-  d.rec_i = b.rec_i; d.rec_cloud = b.rec_cloud; d.rec_coef = b.rec_coef; d.rec_nvec = b.rec_nvec;
-  d.rec_qb = b.rec_qb; d.rec_area = b.rec_area; d.rec_wsol = b.rec_wsol; d.rec_psol = b.rec_psol;
-  d.rec_term = b.rec_term; d.tgt_off = b.tgt_off; d.tgt_ops = b.tgt_ops;
-  for (int f = 0; f < 6; f++) {
-    d.bctype[f] = b.bctype[f];
-    for (int q = 0; q < 3; q++) d.fnv[f][q] = b.fnv[f][q];
-  }
+  if (b.f32)
+    fill_view(b, b.dev32, scratch);
+  else
+    fill_view(b, b.dev, scratch);
   return MGE_OK;
 }
 
@@ -504,7 +602,9 @@ int mge_init(const mge_params* prm, int device, mge_ctx** out) {
   *out = nullptr;
   if (prm->nlevel < 1 || prm->nlevel > MGE_MAX_LEVEL || prm->mstage < 1 || prm->mstage > MGE_MAX_STAGE)
     return MGE_EBADCFG;
-  if (prm->distype != MGE_DIS_CENTRAL || prm->eqntype != MGE_EQN_EULER) return MGE_EBADCFG;
+  if (prm->distype != MGE_DIS_CENTRAL && prm->distype != MGE_DIS_ROE1 && prm->distype != MGE_DIS_ROE2)
+    return MGE_EBADCFG;
+  if (prm->eqntype != MGE_EQN_EULER && prm->eqntype != MGE_EQN_NS) return MGE_EBADCFG;
   if (prm->dissip != MGE_DISSIP_SCALAR && prm->dissip != MGE_DISSIP_MATRIX) return MGE_EBADCFG;
   if (prm->irs_variant != 0) return MGE_EBADCFG;
   mge_ctx* c = new mge_ctx();
@@ -522,7 +622,12 @@ int mge_init(const mge_params* prm, int device, mge_ctx** out) {
   }
   c->lv.resize(prm->nlevel);
   build_phys(c);
-  if (const char* e = getenv("MGE_COOP_MAX_CELLS")) c->coop_max_cells = atoll(e);
+  if (const char* e = getenv("MGE_COOP_MAX_CELLS")) {
+    c->coop_max_cells = atoll(e);
+    c->tune_path = false;  // an explicit threshold fixes the launch form
+  }
+  if (const char* e = getenv("MGE_AUTOTUNE")) c->autotune = atoi(e) != 0;
+  if (const char* e = getenv("MGE_COOP_MAX_CTAS")) c->coop_max_ctas = atoi(e);
   *out = c;
   return MGE_OK;
 }
@@ -535,6 +640,7 @@ void mge_destroy(mge_ctx* c) {
     if (g) cudaGraphExecDestroy(g);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->ev_done) cudaEventDestroy(c->ev_done);
   for (void* q : c->allocs) cudaFree(q);
   if (c->scratch) cudaFree(c->scratch);
   if (c->d_err) cudaFree(c->d_err);
@@ -644,16 +750,117 @@ int mge_commit(mge_ctx* c) {
     if (L.empty()) return fail(c, MGE_EBADCFG, "commit: a level has no block");
     for (Block& b : L) maxN = std::max(maxN, b.N);
   }
-  // scratch: H(1) F(15) fp(3) efs(15) dfs(15) = 49 fields of the largest block
-  int rc = dalloc(c, &c->scratch, (size_t)49 * maxN);
+  init_kernel_attributes();
+  // scratch: H(1) F(15) fp(3) efs(15) dfs(15) = 49 fields of the largest block,
+  // + vt(4) vfs(15) for Navier-Stokes
+  const size_t nsc = c->prm.eqntype == MGE_EQN_NS ? 68 : 49;
+  int rc = dalloc(c, &c->scratch, nsc * maxN);
   if (rc) return rc;
   c->allocs.pop_back();  // freed separately
-  for (auto& L : c->lv)
-    for (Block& b : L)
+  const bool mixed = c->prm.precision == MGE_PREC_MIXED;
+  for (size_t l = 0; l < c->lv.size(); l++)
+    for (Block& b : c->lv[l]) {
+      // mixed: coarse levels in FP32; the finest keeps FP64 state and residual,
+      // with its time step and residual smoothing in FP32 arithmetic
+      b.f32 = mixed && (l + 1 < c->lv.size());
+      b.aux32 = mixed && !b.f32;
+      b.esz = b.f32 ? 4 : 8;
+      b.use_coop = (long long)b.nx * b.ny * b.nz <= c->coop_max_cells;
       if ((rc = commit_block(c, b, c->scratch))) return rc;
+    }
   // the set-up copies ran on the legacy stream; order them before the context stream
   CK(cudaDeviceSynchronize());
   c->committed = true;
+  return MGE_OK;
+}
+
+static void free_stream_start(mge_ctx* c, Block& b) {  // init_flow.f90:46-96
+  enqueue_simple(c, b, 3);
+  enqueue_simple(c, b, 0);
+  enqueue_simple(c, b, 4);
+  enqueue_simple(c, b, 2);
+}
+
+// Autotuner: per block, time the two line-sweep variants of each direction
+// and the two launch forms of one timestep + euler update (one cooperative
+// launch, or one launch per phase) on the free-stream state, keep the faster,
+// and cache the choice by block shape and precision for later contexts.
+struct TuneKey {
+  int nx, ny, nz, f32, aux32, rec;
+  bool operator<(const TuneKey& o) const {
+    return std::tie(nx, ny, nz, f32, aux32, rec) < std::tie(o.nx, o.ny, o.nz, o.f32, o.aux32, o.rec);
+  }
+};
+struct TuneVal {
+  bool coop;
+  int irs[3];
+};
+static std::map<TuneKey, TuneVal> g_tune;
+static std::mutex g_tune_mu;
+
+static int autotune_block(mge_ctx* c, Block& b, bool tune_path) {
+  TuneKey key{b.nx, b.ny, b.nz, (int)b.f32, (int)b.aux32, b.recs.empty() ? 0 : 1};
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) {
+      if (tune_path) b.use_coop = it->second.coop;
+      for (int d = 0; d < 3; d++) b.irs_var[d] = it->second.irs[d];
+      return MGE_OK;
+    }
+  }
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  auto time_it = [&](auto&& fn, int reps) -> float {
+    fn();
+    cudaEventRecord(e0, c->stream);
+    for (int r = 0; r < reps; r++) fn();
+    cudaEventRecord(e1, c->stream);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    return ms;
+  };
+  if (c->prm.smoo > 0.0) {
+    for (int d = 0; d < 3; d++) {
+      float best = 1e30f;
+      int bv = 0;
+      for (int v = 0; v < 2; v++) {
+        int var[3] = {0, 0, 0};
+        var[d] = v;
+        float t = time_it([&] {
+          with_dev(b, [&](auto& D) {
+            using T = typename std::remove_reference_t<decltype(D)>::value_type;
+            launch_irs_part<T>(d, D, c->P, b.tabs, c->stream, b.aux32, var);
+          });
+        }, 3);
+        if (t < best) {
+          best = t;
+          bv = v;
+        }
+      }
+      b.irs_var[d] = bv;
+    }
+    free_stream_start(c, b);  // the timed sweeps ended in an update: restore the start state
+  }
+  if (tune_path) {
+    float tc = 1e30f, tp = 1e30f;
+    b.use_coop = true;
+    tc = time_it([&] { enqueue_euler(c, b, b.level, b.level, false, false, 0, false, true); }, 2);
+    cudaError_t e = cudaGetLastError();
+    b.use_coop = false;
+    tp = time_it([&] { enqueue_euler(c, b, b.level, b.level, false, false, 0, false, true); }, 2);
+    b.use_coop = (e == cudaSuccess) && tc < tp;
+    free_stream_start(c, b);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  CK(cudaGetLastError());
+  int rc = check_err(c);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune[key] = TuneVal{b.use_coop, {b.irs_var[0], b.irs_var[1], b.irs_var[2]}};
   return MGE_OK;
 }
 
@@ -661,23 +868,110 @@ int mge_init_flow(mge_ctx* c) {  // init_flow.f90:46-96
   if (!c || !c->committed) return MGE_EBADCFG;
   CK(cudaSetDevice(c->device));
   for (auto& L : c->lv)
+    for (Block& b : L) free_stream_start(c, b);
+  CK(cudaGetLastError());
+  int rc = check_err(c);
+  if (rc || !c->autotune) return rc;
+  for (auto& L : c->lv)
     for (Block& b : L) {
-      launch_init_free<double>(b.dev, c->P, c->stream);
-      launch_depvars_all<double>(b.dev, c->P, c->stream);
-      launch_cutcell<double>(b.dev, c->P, c->d_err, c->stream);
-      launch_bcond<double>(b.dev, c->P, c->stream);
+      const bool tune_path = c->tune_path && (long long)b.nx * b.ny * b.nz <= 2000000;
+      if ((rc = autotune_block(c, b, tune_path))) return rc;
     }
+  return MGE_OK;
+}
+
+// free one allocation made by dalloc
+static void dfree(mge_ctx* c, void* p, size_t bytes) {
+  if (!p) return;
+  auto it = std::find(c->allocs.begin(), c->allocs.end(), p);
+  if (it != c->allocs.end()) c->allocs.erase(it);
+  cudaFree(p);
+  c->bytes -= std::min(c->bytes, bytes);
+}
+
+// Switch a context between the plain FP64 and the mixed form in place: coarse
+// blocks change their storage (state converted, scratch fields re-zeroed),
+// the finest block toggles its FP32 time step and smoothing.
+int mge_set_precision(mge_ctx* c, int precision) {
+  if (!c || !c->committed || (precision != MGE_PREC_FP64 && precision != MGE_PREC_MIXED)) return MGE_EBADCFG;
+  CK(cudaSetDevice(c->device));
+  CK(cudaStreamSynchronize(c->stream));
+  const bool mixed = precision == MGE_PREC_MIXED;
+  for (size_t l = 0; l < c->lv.size(); l++)
+    for (Block& b : c->lv[l]) {
+      const bool f32 = mixed && (l + 1 < c->lv.size());
+      b.aux32 = mixed && !f32;
+      if (f32 == b.f32) continue;
+      const size_t oes = b.esz, nes = f32 ? 4 : 8;
+      const long long N = b.N;
+      const int nma = std::max((int)b.recs.size(), 1);
+      struct F { void** p; long long n; bool keep; };
+      F fields[] = {{&b.w, 5 * N, true},  {&b.p, N, true},        {&b.ws, 5 * N, true},   {&b.wn, 5 * N, false},
+                    {&b.dw, 5 * N, false}, {&b.fw, 5 * N, false}, {&b.wr, 5 * N, false}, {&b.qf, 5 * N, false},
+                    {&b.vdtim, N, false}, {&b.lam, N, false},     {&b.rec_wsol, 5LL * nma, true},
+                    {&b.rec_psol, nma, true}, {&b.rec_term, 50LL * nma, false}};
+      for (F& f : fields) {
+        void* np = nullptr;
+        int rc = valloc(c, &np, (size_t)f.n, nes);
+        if (rc) return rc;
+        if (f.keep) launch_convert(*f.p, oes == 4, np, nes == 4, f.n, c->stream);
+        CK(cudaStreamSynchronize(c->stream));
+        dfree(c, *f.p, (size_t)f.n * oes);
+        *f.p = np;
+      }
+      b.f32 = f32;
+      b.esz = nes;
+      if (b.f32)
+        fill_view(b, b.dev32, c->scratch);
+      else
+        fill_view(b, b.dev, c->scratch);
+    }
+  for (cudaGraphExec_t& g : c->graphs)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+  c->prm.precision = precision;
   CK(cudaGetLastError());
   return check_err(c);
+}
+
+int mge_tuned(mge_ctx* c, int level, int serial, int* coop, int* irs3) {
+  Block* b = getb(c, level, serial);
+  if (!b) return MGE_ENOTFOUND;
+  if (coop) *coop = b->use_coop ? 1 : 0;
+  if (irs3)
+    for (int d = 0; d < 3; d++) irs3[d] = b->irs_var[d];
+  return MGE_OK;
 }
 
 int mge_upload_state(mge_ctx* c, int level, int serial, const double* w) {
   Block* b = getb(c, level, serial);
   if (!b || !c->committed) return MGE_ENOTFOUND;
   CK(cudaSetDevice(c->device));
-  CK(cudaMemcpyAsync(b->w, w, 5 * b->N * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-  launch_depvars_all<double>(b->dev, c->P, c->stream);
+  if (b->f32) {
+    std::vector<float> t(5 * b->N);
+    for (long long q = 0; q < 5 * b->N; q++) t[q] = (float)w[q];
+    CK(cudaMemcpyAsync(b->w, t.data(), t.size() * 4, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+  } else {
+    CK(cudaMemcpyAsync(b->w, w, 5 * b->N * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  }
+  enqueue_simple(c, *b, 0);
   return check_err(c);
+}
+
+// copy len values of a state field (double, or float when the block is FP32) to host doubles
+static int copy_out(mge_ctx* c, const Block& b, const void* src, size_t len, bool typed, double* out) {
+  if (!len) return MGE_OK;
+  if (typed && b.f32) {
+    std::vector<float> t(len);
+    CK(cudaMemcpy(t.data(), src, len * 4, cudaMemcpyDeviceToHost));
+    for (size_t q = 0; q < len; q++) out[q] = (double)t[q];
+  } else {
+    CK(cudaMemcpy(out, src, len * sizeof(double), cudaMemcpyDeviceToHost));
+  }
+  return MGE_OK;
 }
 
 int mge_download_state(mge_ctx* c, int level, int serial, double* w, double* p) {
@@ -685,8 +979,9 @@ int mge_download_state(mge_ctx* c, int level, int serial, double* w, double* p) 
   if (!b || !c->committed) return MGE_ENOTFOUND;
   CK(cudaSetDevice(c->device));
   CK(cudaStreamSynchronize(c->stream));
-  if (w) CK(cudaMemcpy(w, b->w, 5 * b->N * sizeof(double), cudaMemcpyDeviceToHost));
-  if (p) CK(cudaMemcpy(p, b->p, b->N * sizeof(double), cudaMemcpyDeviceToHost));
+  int rc = MGE_OK;
+  if (w && (rc = copy_out(c, *b, b->w, 5 * b->N, true, w))) return rc;
+  if (p && (rc = copy_out(c, *b, b->p, b->N, true, p))) return rc;
   return MGE_OK;
 }
 
@@ -697,8 +992,9 @@ int mge_download_field(mge_ctx* c, int level, int serial, const char* name, doub
   CK(cudaStreamSynchronize(c->stream));
   std::string n(name);
   const long long N = b->N;
-  double* src = nullptr;
+  const void* src = nullptr;
   size_t len = 0;
+  bool typed = true;
   if (n == "w") { src = b->w; len = 5 * N; }
   else if (n == "p") { src = b->p; len = N; }
   else if (n == "dw") { src = b->dw; len = 5 * N; }
@@ -711,11 +1007,10 @@ int mge_download_field(mge_ctx* c, int level, int serial, const char* name, doub
   else if (n == "lam") { src = b->lam; len = N; }
   else if (n == "wsol") { src = b->rec_wsol; len = 5 * b->recs.size(); }
   else if (n == "psol") { src = b->rec_psol; len = b->recs.size(); }
-  else if (n == "dtim") { src = b->dtim; len = 1; }
+  else if (n == "dtim") { src = b->dtim; len = 1; typed = false; }
   if (src) {
     if (count < len) return fail(c, MGE_EBADCFG, "download_field: buffer too small");
-    if (len) CK(cudaMemcpy(out, src, len * sizeof(double), cudaMemcpyDeviceToHost));
-    return MGE_OK;
+    return copy_out(c, *b, src, len, typed, out);
   }
   if (n == "blank" || n == "marker") {
     if (count < (size_t)N) return fail(c, MGE_EBADCFG, "download_field: buffer too small");
@@ -802,7 +1097,10 @@ int mge_forces_compute(mge_ctx* c, int level, const mge_solve_opts* o, mge_force
   const double ctr[3] = {o ? o->moment_center[0] : 0.0, o ? o->moment_center[1] : 0.0, o ? o->moment_center[2] : 0.0};
   for (Block& b : c->lv[level - 1]) {
     if (b.recs.empty()) continue;
-    launch_forces<double>(b.dev, b.origin, b.h, ctr, b.forces, c->stream);
+    with_dev(b, [&](auto& D) {
+      using T = typename std::remove_reference_t<decltype(D)>::value_type;
+      launch_forces<T>(D, b.origin, b.h, ctr, b.forces, c->stream);
+    });
     double h6[8];
     CK(cudaMemcpyAsync(h6, b.forces, 6 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
@@ -895,6 +1193,111 @@ int mge_cycle(mge_ctx* c, int mlvl, int ncyc, double* max_res) {
 
 double mge_last_cycle_ms(const mge_ctx* c) { return c ? c->last_cycle_ms : 0.0; }
 
+// ------------------------------------------------ asynchronous cycles (many cases in flight)
+int mge_cycle_async(mge_ctx* c, int mlvl) {
+  if (!c || !c->committed || mlvl < 1 || mlvl > (int)c->lv.size()) return MGE_EBADCFG;
+  if (c->pending_mlvl) return fail(c, MGE_EBADCFG, "cycle_async: a cycle is already in flight");
+  CK(cudaSetDevice(c->device));
+  int rc = launch_cycle_graph(c, mlvl);
+  if (rc) return rc;
+  auto& fin = c->lv[mlvl - 1];
+  for (size_t q = 0; q < fin.size() && q < 64; q++)
+    CK(cudaMemcpyAsync(c->h_rt + q, fin[q].rt_cur, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaMemcpyAsync(c->h_err, c->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+  if (!c->ev_done) CK(cudaEventCreateWithFlags(&c->ev_done, cudaEventDisableTiming));
+  CK(cudaEventRecord(c->ev_done, c->stream));
+  c->pending_mlvl = mlvl;
+  return MGE_OK;
+}
+
+int mge_cycle_poll(mge_ctx* c, int ncyc, double* max_res) {
+  if (!c || !c->pending_mlvl || !max_res) return MGE_EBADCFG;
+  CK(cudaSetDevice(c->device));
+  cudaError_t e = cudaEventQuery(c->ev_done);
+  if (e == cudaErrorNotReady) return 1;
+  if (e != cudaSuccess) return cuda_fail(c, e, "cycle_poll");
+  const int mlvl = c->pending_mlvl;
+  c->pending_mlvl = 0;
+  unsigned w = *c->h_err;
+  if (w) {
+    cudaMemset(c->d_err, 0, sizeof(unsigned));
+    if (w & ERR_NEGPRESS) return fail(c, MGE_ENEGPRESS, "timestep: negative or NaN c^2 (timestep.f90:45-48)");
+    if (w & ERR_ZERORHO) return fail(c, MGE_EZERORHO, "efluxb: zero density at a cut cell (efluxb.f90:61-64)");
+    if (w & ERR_NAN) return fail(c, MGE_ENAN, "bc_cutcell: wsol is NaN (bc_cutcell.f90:147-156)");
+  }
+  auto& fin = c->lv[mlvl - 1];
+  double mr = 1000.0;
+  for (size_t q = 0; q < fin.size() && q < 64; q++) {
+    double r = c->h_rt[q];
+    if (ncyc >= 0) {
+      if ((int)fin[q].rtrms.size() <= ncyc) fin[q].rtrms.resize(ncyc + 1, 0.0);
+      fin[q].rtrms[ncyc] = r;
+    }
+    if (r < mr) mr = r;
+    if (r != r) return fail(c, MGE_ENAN, "NaN residual (solver.f90:180)");
+  }
+  *max_res = mr;
+  float ms = 0.f;
+  if (cudaEventElapsedTime(&ms, c->ev0, c->ev1) == cudaSuccess) c->last_cycle_ms = ms;
+  return MGE_OK;
+}
+
+int mge_prolong_async(mge_ctx* c, int mlvl) {
+  if (!c || !c->committed || mlvl < 1 || mlvl >= (int)c->lv.size()) return MGE_EBADCFG;
+  if (c->pending_mlvl) return fail(c, MGE_EBADCFG, "prolong_async: a cycle is in flight");
+  CK(cudaSetDevice(c->device));
+  enqueue_movfin(c, mlvl + 1, mlvl);  // FMG prolongation, solver.f90:256-259
+  CK(cudaGetLastError());
+  return MGE_OK;
+}
+
+int mge_device_mem(int device, size_t* free_bytes, size_t* total_bytes) {
+  int prev = 0;
+  if (cudaGetDevice(&prev) != cudaSuccess) return MGE_ECUDA;
+  if (cudaSetDevice(device) != cudaSuccess) return MGE_ECUDA;
+  size_t f = 0, t = 0;
+  cudaError_t e = cudaMemGetInfo(&f, &t);
+  cudaSetDevice(prev);
+  if (e != cudaSuccess) return MGE_ECUDA;
+  if (free_bytes) *free_bytes = f;
+  if (total_bytes) *total_bytes = t;
+  return MGE_OK;
+}
+
+int mge_set_coop_ctas(mge_ctx* c, int max_ctas) {
+  if (!c) return MGE_EBADCFG;
+  c->coop_max_ctas = max_ctas < 0 ? 0 : max_ctas;
+  for (cudaGraphExec_t& g : c->graphs)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+  return MGE_OK;
+}
+
+int mge_coop_trace(mge_ctx* c, int level, double* us_out, int nout) {
+  Block* bp = getb(c, level, 1);
+  if (!bp || !c->committed || !us_out || nout < 1) return MGE_EBADCFG;
+  CK(cudaSetDevice(c->device));
+  unsigned long long* d = nullptr;
+  CK(cudaMalloc(&d, 256 * sizeof(unsigned long long)));
+  CK(cudaMemset(d, 0, 256 * sizeof(unsigned long long)));
+  bool keep = bp->use_coop;
+  bp->use_coop = true;
+  c->coop_trace = d;
+  enqueue_euler(c, *bp, level, level, false, false, 0, true, true);
+  c->coop_trace = nullptr;
+  bp->use_coop = keep;
+  CK(cudaStreamSynchronize(c->stream));
+  unsigned long long h[256];
+  cudaError_t e = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return cuda_fail(c, e, "coop trace");
+  int n = (int)h[255];
+  for (int q = 0; q < nout; q++) us_out[q] = (q < n) ? (double)(h[1 + q] - h[q]) * 1e-3 : 0.0;
+  return n;
+}
+
 long long mge_launch_count(const mge_ctx* c) { return c ? c->launches : 0; }
 
 int mge_kernel_times(mge_ctx* c, int level, int reps, double* ms_out, int nout) {
@@ -923,7 +1326,10 @@ int mge_kernel_times(mge_ctx* c, int level, int reps, double* ms_out, int nout) 
   int rc = MGE_OK;
   for (int r = 0; r < reps && !rc; r++) {
     rc = timed(0, [&] { enqueue_timestep(c, b); });
-    launch_save_wn<double>(b.dev, c->stream);
+    with_dev(b, [&](auto& D) {
+      using T = typename std::remove_reference_t<decltype(D)>::value_type;
+      launch_save_wn<T>(D, c->stream);
+    });
     for (int m = 1; m <= P.mstage && !rc; m++) {
       StageArgs A;
       A.m = m;
@@ -937,14 +1343,30 @@ int mge_kernel_times(mge_ctx* c, int level, int reps, double* ms_out, int nout) 
       A.irs = (m % 2 != 0) && P.smoo > 0.0;
       A.vt = P.vt;
       for (int part = 0; part < 4 && !rc; part++)
-        rc = timed(1 + part, [&] { launch_stage_part<double>(part, b.dev, c->P, A, c->d_err, c->stream); });
+        rc = timed(1 + part, [&] {
+          with_dev(b, [&](auto& D) {
+            using T = typename std::remove_reference_t<decltype(D)>::value_type;
+            launch_stage_part<T>(part, D, c->P, A, c->d_err, c->stream);
+          });
+        });
       if (A.irs)
         for (int part = 0; part < 3 && !rc; part++)
-          rc = timed(5 + part, [&] { launch_irs_part<double>(part, b.dev, c->P, b.tabs, c->stream); });
-      if (!rc) rc = timed(8, [&] { launch_cutcell<double>(b.dev, c->P, c->d_err, c->stream); });
-      if (!rc) rc = timed(9, [&] { launch_bcond<double>(b.dev, c->P, c->stream); });
+          rc = timed(5 + part, [&] {
+            with_dev(b, [&](auto& D) {
+              using T = typename std::remove_reference_t<decltype(D)>::value_type;
+              launch_irs_part<T>(part, D, c->P, b.tabs, c->stream, b.aux32, b.irs_var);
+            });
+          });
+      if (!rc) rc = timed(8, [&] { enqueue_simple(c, b, 4); });
+      if (!rc) rc = timed(9, [&] { enqueue_simple(c, b, 2); });
     }
-    if (!rc) rc = timed(10, [&] { launch_rtrms<double>(b.dev, c->P, P.vt, b.rt_partial, b.npart, b.rt_cur, c->stream); });
+    if (!rc)
+      rc = timed(10, [&] {
+        with_dev(b, [&](auto& D) {
+          using T = typename std::remove_reference_t<decltype(D)>::value_type;
+          launch_rtrms<T>(D, c->P, P.vt, b.rt_partial, b.npart, b.rt_cur, c->stream);
+        });
+      });
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -973,6 +1395,10 @@ int mge_solve(mge_ctx* c, const mge_solve_opts* o, double* hist, int hist_len, i
       if (mlvl == nlevel) {
         if (hist && nfin < hist_len) hist[nfin] = max_res;
         nfin++;
+        // mixed form: FP32 coarse corrections stall near an eps32-sized residual
+        // drop; refine to FP64 once the drop reaches refine_drop
+        if (c->prm.precision == MGE_PREC_MIXED && o && o->refine_drop > 0.0 && max_res <= o->refine_drop * ini_res)
+          if ((rc = mge_set_precision(c, MGE_PREC_FP64))) return rc;
       }
       if (mlvl > 1) {  // convergence (solver.f90:237-239); the single-grid level runs all its cycles
         double drop = P.conv_drop > 0.0 ? P.conv_drop : 1.0e6;

@@ -108,7 +108,7 @@ class Cycle:
         self._chk(self._fn("get_rtrms")(self.ctx, level, serial, ncyc, C.byref(out)), "get_rtrms")
         return out.value
 
-    def solve(self, max_cycles_total=0, hist_len=100000, use_graph=1):
+    def solve(self, max_cycles_total=0, hist_len=100000, use_graph=1, refine_drop=0.0):
         hist = np.zeros(hist_len, dtype=np.float64)
         nd = C.c_int(0)
         fo = A.MgeForces()
@@ -117,6 +117,7 @@ class Cycle:
         o.ref_area = self.case.ref_area
         o.moment_center[:] = (0.0, 0.0, 0.0)
         o.use_graph = use_graph
+        o.refine_drop = refine_drop
         self._chk(self._fn("solve")(self.ctx, C.byref(o), hist.ctypes.data_as(C.POINTER(C.c_double)), hist_len,
                                     C.byref(nd), C.byref(fo)), "solve")
         return hist[: min(nd.value, hist_len)].copy(), nd.value, fo

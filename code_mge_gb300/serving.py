@@ -1,0 +1,356 @@
+"""Continuous-batching solve service and batched sweep over the C-ABI.
+
+Requests (geometry, grid size, Mach, angle, residual-drop tolerance) arrive
+over time.  Each admitted request becomes one resident case (one mge_ctx: its
+whole multigrid hierarchy stays in HBM until it converges).  Admission is
+gated by free device memory.  Every in-flight case advances by asynchronous
+multigrid cycles (mge_cycle_async / mge_cycle_poll) on its own stream, so the
+cycles of all admitted cases overlap on the GPU; a request that arrives
+while others run is admitted as soon as memory frees up.  A case follows the
+reference's full-multigrid schedule (solver.f90:119-259): mcyc cycles per
+coarse FMG level, then cycles on the finest level until its residual has
+dropped by the requested factor.
+
+The scheduler is independent of the GPU: ``FakeBackend`` drives it in the
+CPU tests; ``GpuBackend`` runs it on libmge_gpu.
+"""
+import ctypes as C
+import heapq
+import math
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _abi as A
+from . import cases as K
+
+
+# --------------------------------------------------------------------- requests
+@dataclass
+class Request:
+    rid: int
+    geometry: str          # "sphere", "ellipsoid", "cylinder"
+    n: int                 # finest cells per axis (slab: n x n x 2)
+    mach: float
+    alpha_deg: float = 0.0
+    tol: float = 1e-8      # converged when residual <= tol * first residual of the finest level
+    precision: int = A.MGE_PREC_MIXED
+    arrival: float = 0.0
+    semi: tuple = (1.0, 0.7, 0.5)
+    max_cycles: int = 2000
+    refine_drop: float = 1e-6  # mixed form: switch to FP64 at this residual drop
+    # results
+    t_admit: float = None
+    t_done: float = None
+    cycles: int = 0
+    residual: float = None
+    drop: float = None
+    cd: float = None
+    cl: float = None
+    error: str = None
+
+    @property
+    def latency(self):
+        return None if self.t_done is None else self.t_done - self.arrival
+
+
+def build_case(r: Request):
+    """The synthetic case of a request (3 levels, W-cycle, JST, 5-stage RK)."""
+    nlevel = 3 if r.n >= 32 else 2
+    if r.geometry == "sphere":
+        c = K.sphere_box(n=r.n, nlevel=nlevel, extent=6.0, mach=r.mach, mgtype=2, alpha_deg=r.alpha_deg,
+                         precision=r.precision)
+    elif r.geometry == "ellipsoid":
+        c = K.ellipsoid_box(n=r.n, semi=r.semi, nlevel=nlevel, extent=4.0 * max(r.semi), mach=r.mach,
+                            alpha_deg=r.alpha_deg, mgtype=2, precision=r.precision)
+    elif r.geometry == "cylinder":
+        c = K.cylinder_slab(n=r.n, span=2, nlevel=nlevel, extent=8.0, mach=r.mach, alpha_deg=r.alpha_deg,
+                            precision=r.precision)
+    else:
+        raise ValueError(r.geometry)
+    for L in range(nlevel - 1):
+        c.prm.mcyc[L] = 10
+    c.prm.mcyc[nlevel - 1] = r.max_cycles
+    return c
+
+
+def case_bytes(case):
+    """Device bytes a case holds (fields, records, stage scratch)."""
+    fine = max(s.dims[0] * s.dims[1] * s.dims[2] for L in case.levels for s in L)
+    mixed = case.prm.precision == A.MGE_PREC_MIXED
+    tot = 49 * 8 * fine
+    for li, L in enumerate(case.levels):
+        esz = 4 if (mixed and li + 1 < len(case.levels)) else 8
+        for s in L:
+            n = s.dims[0] * s.dims[1] * s.dims[2]
+            tot += n * (38 * esz + 3 + 4) + s.arrays["nmir"] * 512
+    return int(tot * 1.05) + (8 << 20)
+
+
+# --------------------------------------------------------------------- backends
+class GpuBackend:
+    """One mge_ctx per case, advanced with asynchronous cycles."""
+
+    def __init__(self, device=0, coop_ctas=32):
+        from .runtime import load_library
+        self.lib = load_library()
+        self.device = device
+        self.coop_ctas = coop_ctas
+
+    def free_memory(self):
+        f, t = C.c_size_t(), C.c_size_t()
+        if self.lib.mge_device_mem(self.device, C.byref(f), C.byref(t)) != 0:
+            raise RuntimeError("mge_device_mem failed")
+        return f.value
+
+    def open(self, case):
+        from .runtime import Cycle
+        cyc = Cycle(case, lib=self.lib, device=self.device)
+        if self.coop_ctas:
+            self.lib.mge_set_coop_ctas(cyc.ctx, self.coop_ctas)
+        return cyc
+
+    def launch(self, h, mlvl):
+        return self.lib.mge_cycle_async(h.ctx, mlvl)
+
+    def poll(self, h, ncyc):
+        out = C.c_double()
+        rc = self.lib.mge_cycle_poll(h.ctx, ncyc, C.byref(out))
+        return rc, out.value
+
+    def prolong(self, h, mlvl):
+        return self.lib.mge_prolong_async(h.ctx, mlvl)
+
+    def refine(self, h):
+        return self.lib.mge_set_precision(h.ctx, A.MGE_PREC_FP64)
+
+    def finish(self, h):
+        f = h.forces()
+        return f.cd, f.cl
+
+    def close(self, h):
+        h.close()
+
+
+class FakeBackend:
+    """Deterministic stand-in used by the CPU tests: each case's residual falls
+    geometrically per cycle; a cycle completes after `latency` polls."""
+
+    def __init__(self, free_bytes=1 << 34, rate=0.7, latency=2):
+        self.free = free_bytes
+        self.rate = rate
+        self.latency = latency
+        self.launched = 0
+
+    def free_memory(self):
+        return self.free
+
+    def open(self, case):
+        self.free -= case_bytes(case)
+        return {"case": case, "res": 1.0, "busy": 0, "bytes": case_bytes(case)}
+
+    def launch(self, h, mlvl):
+        h["busy"] = self.latency
+        self.launched += 1
+        return 0
+
+    def poll(self, h, ncyc):
+        h["busy"] -= 1
+        if h["busy"] > 0:
+            return 1, 0.0
+        h["res"] *= self.rate
+        return 0, h["res"]
+
+    def prolong(self, h, mlvl):
+        return 0
+
+    def refine(self, h):
+        h["refined"] = True
+        return 0
+
+    def finish(self, h):
+        return 0.5 + 0.01 * h["case"].prm.rm, 0.0
+
+    def close(self, h):
+        self.free += h["bytes"]
+
+
+# --------------------------------------------------------------------- scheduler
+@dataclass
+class _Slot:
+    req: Request
+    case: object
+    handle: object
+    nlevel: int
+    mlvl: int = 1
+    ncyc: int = 0
+    ini: float = None
+    inflight: bool = False
+    cycles_fine: int = 0
+    refined: bool = False
+
+
+class Server:
+    """Continuous batching: admit while memory allows, keep every admitted case
+    cycling, retire cases as they converge."""
+
+    def __init__(self, backend, reserve_bytes=2 << 30, max_active=64, clock=time.perf_counter):
+        self.be = backend
+        self.reserve = reserve_bytes
+        self.max_active = max_active
+        self.clock = clock
+        self.queue = []           # (arrival, rid, request) min-heap
+        self.active = []
+        self.done = []
+        self.peak_active = 0
+        self.cases = {}
+
+    def submit(self, r: Request):
+        heapq.heappush(self.queue, (r.arrival, r.rid, r))
+
+    def _admit(self, now):
+        while self.queue and self.queue[0][0] <= now and len(self.active) < self.max_active:
+            r = self.queue[0][2]
+            case = self.cases.get(r.rid) or build_case(r)
+            need = case_bytes(case)
+            if self.active and self.be.free_memory() - need < self.reserve:
+                return  # wait for memory to free up (FIFO: no overtaking)
+            heapq.heappop(self.queue)
+            try:
+                h = self.be.open(case)
+            except Exception as e:  # admission failed (out of memory): retry later unless nothing is running
+                if not self.active:
+                    r.error = str(e)
+                    r.t_done = now
+                    self.done.append(r)
+                    continue
+                heapq.heappush(self.queue, (r.arrival, r.rid, r))
+                return
+            r.t_admit = self.clock()
+            self.active.append(_Slot(r, case, h, case.prm.nlevel))
+            self.peak_active = max(self.peak_active, len(self.active))
+
+    def _advance(self, s: _Slot):
+        """Launch the next cycle of a slot (or finish it); returns False when retired."""
+        prm = s.case.prm
+        if s.mlvl < s.nlevel and s.ncyc >= prm.mcyc[s.mlvl - 1]:
+            self.be.prolong(s.handle, s.mlvl)        # FMG step to the next finer level
+            s.mlvl += 1
+            s.ncyc = 0
+        s.ncyc += 1
+        rc = self.be.launch(s.handle, s.mlvl)
+        if rc != 0:
+            self._retire(s, "cycle launch failed (%d)" % rc)
+            return False
+        s.inflight = True
+        return True
+
+    def _retire(self, s: _Slot, err=None):
+        r = s.req
+        if err is None:
+            try:
+                r.cd, r.cl = self.be.finish(s.handle)
+            except Exception as e:
+                err = str(e)
+        r.error = err
+        r.cycles = s.cycles_fine
+        r.t_done = self.clock()
+        self.be.close(s.handle)
+        self.active.remove(s)
+        self.done.append(r)
+
+    def step(self):
+        """One scheduler pass; returns True while work remains."""
+        now = self.clock()
+        self._admit(now)
+        progressed = False
+        for s in list(self.active):
+            if not s.inflight:
+                self._advance(s)
+                progressed = True
+                continue
+            rc, res = self.be.poll(s.handle, s.ncyc)
+            if rc == 1:
+                continue
+            s.inflight = False
+            progressed = True
+            if rc != 0:
+                self._retire(s, "cycle failed (%s)" % A.error_name(rc))
+                continue
+            if s.mlvl == s.nlevel:
+                s.cycles_fine += 1
+                if s.ncyc == 1:
+                    s.ini = res
+                s.req.residual = res
+                s.req.drop = res / s.ini if s.ini else None
+                if (s.req.precision == A.MGE_PREC_MIXED and not s.refined and s.ini
+                        and s.req.refine_drop > 0.0 and res <= s.req.refine_drop * s.ini):
+                    if self.be.refine(s.handle) != 0:
+                        self._retire(s, "precision refinement failed")
+                        continue
+                    s.refined = True
+                if (s.ini and res <= s.req.tol * s.ini) or s.cycles_fine >= s.req.max_cycles or res != res:
+                    self._retire(s)
+                    continue
+            self._advance(s)
+        return bool(self.active or self.queue), progressed
+
+    def run(self, idle_sleep=50e-6, deadline=None):
+        while True:
+            more, progressed = self.step()
+            if not more:
+                break
+            if deadline is not None and self.clock() > deadline:
+                break
+            if not progressed:
+                time.sleep(idle_sleep)
+        return self.done
+
+
+def poisson_requests(rate, duration, seed=20261204, sizes=(64, 256), mach=(0.1, 0.8), tol=1e-8,
+                     precision=A.MGE_PREC_MIXED, max_cycles=2000):
+    """Poisson arrivals (rate per second) over `duration` seconds; geometry
+    uniform over sphere / ellipsoid / cylinder slab, n a multiple of 8 in
+    [sizes], Mach uniform in [mach]."""
+    rng = np.random.default_rng(seed)
+    t, out, rid = 0.0, [], 0
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t > duration:
+            break
+        g = ["sphere", "ellipsoid", "cylinder"][int(rng.integers(0, 3))]
+        n = int(8 * rng.integers(sizes[0] // 8, sizes[1] // 8 + 1))
+        out.append(Request(rid, g, n, float(rng.uniform(*mach)), float(rng.uniform(-5.0, 10.0)) if g != "sphere" else 0.0,
+                           tol=tol, precision=precision, arrival=t,
+                           semi=tuple(float(x) for x in rng.uniform(0.5, 2.0, 3)), max_cycles=max_cycles))
+        rid += 1
+    return out
+
+
+def batched_sweep_requests(count=64, seed=20261203, sizes=(32, 48, 64, 96, 128), precision=A.MGE_PREC_MIXED,
+                           tol=1e-8, max_cycles=2000):
+    """The batched sweep: `count` ellipsoid cases with seeded sizes, semi-axes,
+    Mach and angle of attack, all present at t = 0."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for q in range(count):
+        n = int(rng.choice(sizes))
+        semi = tuple(float(x) for x in rng.uniform(0.5, 2.0, 3))
+        out.append(Request(q, "ellipsoid", n, float(rng.uniform(0.2, 0.8)), float(rng.uniform(-5.0, 10.0)),
+                           tol=tol, precision=precision, arrival=0.0, semi=semi, max_cycles=max_cycles))
+    return out
+
+
+def summarize(done, t_wall):
+    ok = [r for r in done if r.error is None]
+    lat = np.array([r.latency for r in ok]) if ok else np.zeros(0)
+    return {
+        "requests": len(done),
+        "completed": len(ok),
+        "failed": len(done) - len(ok),
+        "solves_per_s": len(ok) / t_wall if t_wall > 0 else None,
+        "p50_s": float(np.percentile(lat, 50)) if lat.size else None,
+        "p99_s": float(np.percentile(lat, 99)) if lat.size else None,
+        "wall_s": t_wall,
+    }

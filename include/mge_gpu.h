@@ -138,6 +138,7 @@ typedef struct mge_solve_opts {
   double ref_area;                /* reference area for Cl/Cd */
   double moment_center[3];
   int    use_graph;               /* capture the multigrid cycle in a CUDA graph */
+  double refine_drop;             /* mixed form: switch to FP64 once the residual has dropped by this factor (0: never) */
 } mge_solve_opts;
 
 typedef struct mge_ctx mge_ctx;
@@ -192,6 +193,39 @@ int mge_solve(mge_ctx* ctx, const mge_solve_opts* opts, double* rtrms_hist,
  * FMG level mlvl, replayed from a CUDA graph captured on the first call for
  * that level; *max_res receives the residual of the cycle (solver.f90:164-176). */
 int mge_cycle(mge_ctx* ctx, int mlvl, int ncyc, double* max_res);
+
+/* Asynchronous form of mge_cycle for driving many cases at once: enqueue one
+ * cycle (and the read-back of its residual) on the context's stream and
+ * return; mge_cycle_poll returns 1 while it runs, then MGE_OK with *max_res
+ * (or the error of the cycle).  mge_prolong_async enqueues the FMG
+ * prolongation from level mlvl to mlvl+1 (solver.f90:256-259). */
+int mge_cycle_async(mge_ctx* ctx, int mlvl);
+int mge_cycle_poll(mge_ctx* ctx, int ncyc, double* max_res);
+int mge_prolong_async(mge_ctx* ctx, int mlvl);
+
+/* Switch a committed context between MGE_PREC_FP64 and MGE_PREC_MIXED in
+ * place (the coarse levels' state is converted; graphs are re-captured).  The
+ * mixed form's FP32 coarse corrections carry rounding of the size of the
+ * coarse truncation error, so its residual stalls near a 1e-7 drop; switching
+ * to FP64 there finishes the solve at FP64 accuracy. */
+int mge_set_precision(mge_ctx* ctx, int precision);
+
+/* Launch forms the autotuner chose for a block at mge_init_flow: *coop = 1
+ * when timestep + euler run as one cooperative launch; irs3[d] = 1 when the
+ * direction-d line sweeps use shared-memory tiles. */
+int mge_tuned(mge_ctx* ctx, int level, int serial, int* coop, int* irs3);
+
+/* Free and total memory of a device (admission control of the serving loop). */
+int mge_device_mem(int device, size_t* free_bytes, size_t* total_bytes);
+
+/* Cap the grid of the one-launch euler of small blocks (0: all resident
+ * blocks), so that cases running side by side can share the GPU. */
+int mge_set_coop_ctas(mge_ctx* ctx, int max_ctas);
+
+/* Profiling hook: one timestep + euler update of (level, 1) as a single
+ * cooperative launch, recording the device time of every phase between its
+ * grid-wide barriers into us_out (microseconds); returns the phase count. */
+int mge_coop_trace(mge_ctx* ctx, int level, double* us_out, int nout);
 
 /* Device time (CUDA events on the context's stream) of the last mge_cycle. */
 double mge_last_cycle_ms(const mge_ctx* ctx);

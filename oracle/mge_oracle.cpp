@@ -1101,14 +1101,382 @@ int bc_cutcell(mgeo_ctx* c, OBlock& b) {
   return MGE_OK;
 }
 
+/* ------------------------------------------------------------------ Roe and viscous fluxes
+ * The reference selects these with distype 'r1'/'r2' and eqntype 'n'
+ * (euler.f90:137-210) but their sources (roepak, viscpak) are not part of
+ * its tree, so this build defines them from the published methods:
+ *  - Roe's approximate Riemann solver (P. L. Roe, J. Comput. Phys. 43, 1981)
+ *    with Harten's entropy fix (A. Harten, J. Comput. Phys. 49, 1983),
+ *    split like the JST scheme: the central part 0.5*(F(U_L)+F(U_R)).s goes
+ *    to dw, the upwind part 0.5*cdis(m)*|s|*|A|(U_R-U_L) to fw;
+ *  - 'r2': MUSCL reconstruction of (rho,u,v,w,p) with the van Albada
+ *    limiter, first order on any face whose 4-cell stencil touches a blanked
+ *    cell;
+ *  - laminar viscous flux with face gradients from central differences (the
+ *    normal one across the face, tangential ones averaged over the two
+ *    cells), Stokes stresses and Fourier heat flux, scaled by cdis(m) and
+ *    added to fw before the dissipation (euler.f90:157-181);
+ *  - cut-cell walls: the wall face of each record is replaced, for the Roe
+ *    dissipation by the flux to the ghost state (wsol,psol), for the viscous
+ *    flux by the no-slip adiabatic wall flux (normal gradients only, zero
+ *    heat flux).
+ */
+struct Prim {
+  double r, u[3], p;
+};
+inline Prim to_prim(const double* w, double p) {
+  Prim q;
+  q.r = w[0];
+  for (int a = 0; a < 3; a++) q.u[a] = w[1 + a] / w[0];
+  q.p = p;
+  return q;
+}
+inline void to_cons(double gamma, const Prim& q, double* w) {
+  w[0] = q.r;
+  for (int a = 0; a < 3; a++) w[1 + a] = q.r * q.u[a];
+  w[4] = q.p / (gamma - 1.0) + 0.5 * q.r * (q.u[0] * q.u[0] + q.u[1] * q.u[1] + q.u[2] * q.u[2]);
+}
+// van Albada limited slope of two one-sided differences
+// van Albada's limited slope (van Albada, van Leer & Roberts 1982) in its
+// smooth form with e2 = eps^2; no cut-off at a*b <= 0, which with e2 > 0
+// would make the slope jump by up to b/3 when a changes sign
+inline double van_albada(double a, double b, double e2) {
+  return ((b * b + e2) * a + (a * a + e2) * b) / (a * a + b * b + 2.0 * e2);
+}
+// upwind dissipation 0.5*|s|*|A_roe|(U_R-U_L) along axis d with Harten's fix
+void roe_dissipation(const mge_params& P, int d, double S, const double* wl, double pl, const double* wr, double pr,
+                     double* out) {
+  const double g = P.gamma;
+  double ul[3], ur[3];
+  for (int a = 0; a < 3; a++) {
+    ul[a] = wl[1 + a] / wl[0];
+    ur[a] = wr[1 + a] / wr[0];
+  }
+  double hl = (wl[4] + pl) / wl[0], hr = (wr[4] + pr) / wr[0];
+  double rt = std::sqrt(wr[0] / wl[0]);
+  double rh = rt * wl[0];
+  double uh[3];
+  for (int a = 0; a < 3; a++) uh[a] = (ul[a] + rt * ur[a]) / (1.0 + rt);
+  double hh = (hl + rt * hr) / (1.0 + rt);
+  double q2 = uh[0] * uh[0] + uh[1] * uh[1] + uh[2] * uh[2];
+  double c2 = (g - 1.0) * (hh - 0.5 * q2);
+  double ch = std::sqrt(fmax_(c2, 1e-300));
+  double un = uh[d];
+  double dr = wr[0] - wl[0], dp = pr - pl, dun = ur[d] - ul[d];
+  double du[3] = {ur[0] - ul[0], ur[1] - ul[1], ur[2] - ul[2]};
+  double delta = P.epsentr * (std::fabs(un) + ch);
+  auto fix = [&](double lam) {
+    double a = std::fabs(lam);
+    return (a < delta && delta > 0.0) ? (lam * lam + delta * delta) / (2.0 * delta) : a;
+  };
+  double l1 = fix(un - ch), l2 = fix(un), l5 = fix(un + ch);
+  double a1 = (dp - rh * ch * dun) / (2.0 * c2);
+  double a2 = dr - dp / c2;
+  double a5 = (dp + rh * ch * dun) / (2.0 * c2);
+  double sh[3];
+  for (int a = 0; a < 3; a++) sh[a] = rh * (du[a] - (a == d ? dun : 0.0));
+  double k1[5], k5[5];
+  k1[0] = 1.0;
+  k5[0] = 1.0;
+  for (int a = 0; a < 3; a++) {
+    k1[1 + a] = uh[a] - (a == d ? ch : 0.0);
+    k5[1 + a] = uh[a] + (a == d ? ch : 0.0);
+  }
+  k1[4] = hh - ch * un;
+  k5[4] = hh + ch * un;
+  double res[5];
+  res[0] = l1 * a1 * k1[0] + l2 * a2 + l5 * a5 * k5[0];
+  for (int a = 0; a < 3; a++) res[1 + a] = l1 * a1 * k1[1 + a] + l2 * (a2 * uh[a] + sh[a]) + l5 * a5 * k5[1 + a];
+  res[4] = l1 * a1 * k1[4] + l2 * (a2 * 0.5 * q2 + (uh[0] * sh[0] + uh[1] * sh[1] + uh[2] * sh[2])) + l5 * a5 * k5[4];
+  for (int v = 0; v < 5; v++) out[v] = 0.5 * S * res[v];
+}
+
+// left/right states of face q (between q-1 and q) along axis d at (i,j,k) = cell q
+void face_states(mgeo_ctx* c, OBlock& b, int d, int i, int j, int k, int order, double* wl, double* pl, double* wr,
+                 double* pr) {
+  const mge_params& P = c->prm;
+  int e[3] = {0, 0, 0};
+  e[d] = 1;
+  auto W = [&](int o, int v) { return b.W(i + o * e[0], j + o * e[1], k + o * e[2], v); };
+  auto PP = [&](int o) { return b.P(i + o * e[0], j + o * e[1], k + o * e[2]); };
+  auto BLK = [&](int o) { return b.BL(i + o * e[0], j + o * e[1], k + o * e[2]); };
+  for (int v = 0; v < 5; v++) {
+    wl[v] = W(-1, v);
+    wr[v] = W(0, v);
+  }
+  *pl = PP(-1);
+  *pr = PP(0);
+  if (order < 2) return;
+  const int q = d == 0 ? i : (d == 1 ? j : k);
+  const int lq = d == 0 ? b.il : (d == 1 ? b.jl : b.kl);
+  if (q - 2 < 0 || q + 1 > lq + 2) return;
+  if (BLK(-2) == 0 || BLK(-1) == 0 || BLK(0) == 0 || BLK(1) == 0) return;  // first order next to the body
+  double wt[4][5], pt[4];
+  for (int o = -2; o <= 1; o++) {
+    for (int v = 0; v < 5; v++) wt[o + 2][v] = W(o, v);
+    pt[o + 2] = PP(o);
+  }
+  Prim m2 = to_prim(wt[0], pt[0]), m1 = to_prim(wt[1], pt[1]), z0 = to_prim(wt[2], pt[2]), p1 = to_prim(wt[3], pt[3]);
+  const double u0n = std::sqrt(P.u0 * P.u0 + P.v0 * P.v0 + P.w0 * P.w0);
+  const double ref[5] = {P.rho0, u0n, u0n, u0n, P.p0};
+  auto lim = [&](double a, double bb, int kq) {
+    double e2 = 1e-6 * ref[kq] * ref[kq] / (P.limfac > 0.0 ? P.limfac : 1.0);
+    return van_albada(a, bb, e2);
+  };
+  auto comp = [&](const Prim& x, int kq) { return kq == 0 ? x.r : (kq == 4 ? x.p : x.u[kq - 1]); };
+  Prim L = m1, R = z0;
+  for (int kq = 0; kq < 5; kq++) {
+    double dm = comp(m1, kq) - comp(m2, kq), d0 = comp(z0, kq) - comp(m1, kq), dp = comp(p1, kq) - comp(z0, kq);
+    double sl = 0.5 * lim(dm, d0, kq), sr = 0.5 * lim(d0, dp, kq);
+    if (kq == 0) { L.r = m1.r + sl; R.r = z0.r - sr; }
+    else if (kq == 4) { L.p = m1.p + sl; R.p = z0.p - sr; }
+    else { L.u[kq - 1] = m1.u[kq - 1] + sl; R.u[kq - 1] = z0.u[kq - 1] - sr; }
+  }
+  if (L.r <= 0.0 || R.r <= 0.0 || L.p <= 0.0 || R.p <= 0.0) return;  // keep first order where the reconstruction fails
+  to_cons(P.gamma, L, wl);
+  to_cons(P.gamma, R, wr);
+  *pl = L.p;
+  *pr = R.p;
+}
+
+// Roe scheme: central part into dw (with efluxb at walls), upwind part into fw
+int roe_fluxes(mgeo_ctx* c, OBlock& b, int istage) {
+  const mge_params& P = c->prm;
+  const int order = P.distype == MGE_DIS_ROE2 ? 2 : 1;
+  const size_t N = b.N;
+  const double cd = P.cdis[istage - 1];
+  int rc;
+  if (order == 1) {
+    rc = eflux(c, b);  // the central part of Roe's flux with cell states is eflux's
+    if (rc) return rc;
+  } else {
+    std::vector<double> E(15 * N, 0.0);
+    const double* sv[3] = {b.si, b.sj, b.sk};
+    for (int d = 0; d < 3; d++) {
+      int lo[3] = {2, 2, 2}, hi[3] = {b.il, b.jl, b.kl};
+      hi[d] += 1;
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+      for (int k = lo[2]; k <= hi[2]; k++)
+        for (int j = lo[1]; j <= hi[1]; j++)
+          for (int i = lo[0]; i <= hi[0]; i++) {
+            double wl[5], wr[5], pl, pr, f1[5], f2[5];
+            face_states(c, b, d, i, j, k, 2, wl, &pl, wr, &pr);
+            ceflux(wr, pr, sv[d], f1);
+            ceflux(wl, pl, sv[d], f2);
+            for (int v = 0; v < 5; v++) E[(d * 5 + v) * N + b.I(i, j, k)] = 0.5 * (f1[v] + f2[v]);
+          }
+    }
+    const size_t st[3] = {1, b.Pi, b.Pi * b.Pj};
+    for (int k = 2; k <= b.kl; k++)
+      for (int j = 2; j <= b.jl; j++)
+        for (int i = 2; i <= b.il; i++) {
+          size_t q = b.I(i, j, k);
+          for (int v = 0; v < 5; v++) {
+            double a = E[(0 * 5 + v) * N + q] - E[(0 * 5 + v) * N + q + st[0]];
+            a = a + E[(1 * 5 + v) * N + q] - E[(1 * 5 + v) * N + q + st[1]];
+            a = a + E[(2 * 5 + v) * N + q] - E[(2 * 5 + v) * N + q + st[2]];
+            b.dw[v * N + q] = a;
+          }
+        }
+    // walls: efluxb's replacement of the wall face (efluxb.f90:30-114)
+    for (size_t m = 0; m < b.z.size(); m++) {
+      ORec& t = b.z[m];
+      int D = t.zz - 1, i = t.ccid[0], j = t.ccid[1], k = t.ccid[2];
+      if (std::fabs(b.W(i, j, k, 0)) < 1.0e-8) return fail(c, MGE_EZERORHO, "zero density at a cut cell");
+      const double* sc = sv[D];
+      double wc[5], wn[5], f1[5], f2[5], f3[5];
+      getw(b, i, j, k, wc);
+      ceflux(wc, b.P(i, j, k), sc, f1);
+      ceflux(t.wsol, t.psol, sc, f2);
+      int di = D == 0, dj = D == 1, dk = D == 2;
+      size_t q = b.I(i, j, k), qn = b.I(i + di, j + dj, k + dk);
+      for (int v = 0; v < 5; v++) b.dw[v * N + q] = b.dw[v * N + q] - (E[(D * 5 + v) * N + q] - E[(D * 5 + v) * N + qn]);
+      bool plus = t.faceid >= 4;
+      int s = plus ? -1 : 1;
+      getw(b, i + s * di, j + s * dj, k + s * dk, wn);
+      ceflux(wn, b.P(i + s * di, j + s * dj, k + s * dk), sc, f3);
+      for (int v = 0; v < 5; v++) {
+        double fs = 0.5 * (f1[v] + f2[v]), fa = 0.5 * (f1[v] + f3[v]);
+        b.dw[v * N + q] = b.dw[v * N + q] + (plus ? fa : fs) - (plus ? fs : fa);
+      }
+    }
+  }
+  if (cd <= 0.0) return MGE_OK;
+  // upwind dissipation faces
+  std::vector<double> D(15 * N, 0.0);
+  const double Sd[3] = {std::fabs(b.si[0]), std::fabs(b.sj[1]), std::fabs(b.sk[2])};
+  for (int d = 0; d < 3; d++) {
+    int lo[3] = {2, 2, 2}, hi[3] = {b.il, b.jl, b.kl};
+    hi[d] += 1;
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+    for (int k = lo[2]; k <= hi[2]; k++)
+      for (int j = lo[1]; j <= hi[1]; j++)
+        for (int i = lo[0]; i <= hi[0]; i++) {
+          double wl[5], wr[5], pl, pr, o[5];
+          face_states(c, b, d, i, j, k, order, wl, &pl, wr, &pr);
+          roe_dissipation(P, d, Sd[d], wl, pl, wr, pr, o);
+          for (int v = 0; v < 5; v++) D[(d * 5 + v) * N + b.I(i, j, k)] = cd * o[v];
+        }
+  }
+  const size_t st[3] = {1, b.Pi, b.Pi * b.Pj};
+  for (int d = 0; d < 3; d++)
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+    for (int k = 2; k <= b.kl; k++)
+      for (int j = 2; j <= b.jl; j++)
+        for (int i = 2; i <= b.il; i++) {
+          size_t q = b.I(i, j, k);
+          for (int v = 0; v < 5; v++)
+            b.fw[v * N + q] = b.fw[v * N + q] + (D[(d * 5 + v) * N + q] - D[(d * 5 + v) * N + q + st[d]]);
+        }
+  // walls: the wall face's upwind flux taken to the ghost state
+  for (size_t m = 0; m < b.z.size(); m++) {
+    ORec& t = b.z[m];
+    int d = t.zz - 1, i = t.ccid[0], j = t.ccid[1], k = t.ccid[2];
+    size_t q = b.I(i, j, k);
+    bool plus = t.faceid >= 4;
+    double wc[5], o[5], X[5], Z[5];
+    getw(b, i, j, k, wc);
+    if (plus) {
+      roe_dissipation(P, d, Sd[d], wc, b.P(i, j, k), t.wsol, t.psol, o);
+      for (int v = 0; v < 5; v++) {
+        X[v] = -D[(d * 5 + v) * N + q + st[d]];
+        Z[v] = -(cd * o[v]);
+      }
+    } else {
+      roe_dissipation(P, d, Sd[d], t.wsol, t.psol, wc, b.P(i, j, k), o);
+      for (int v = 0; v < 5; v++) {
+        X[v] = D[(d * 5 + v) * N + q];
+        Z[v] = cd * o[v];
+      }
+    }
+    for (int v = 0; v < 5; v++) {
+      b.fw[v * N + q] = b.fw[v * N + q] - X[v];
+      b.fw[v * N + q] = b.fw[v * N + q] + Z[v];
+    }
+  }
+  return MGE_OK;
+}
+
+// laminar viscous flux through the face of cell q along d (euler.f90:137-181, this build's definition)
+void visc_face(const mge_params& P, OBlock& b, const std::vector<double>& vel, const std::vector<double>& tem, int d,
+               int i, int j, int k, double S, double* out) {
+  const size_t N = b.N;
+  int e[3] = {0, 0, 0};
+  e[d] = 1;
+  size_t qR = b.I(i, j, k), qL = b.I(i - e[0], j - e[1], k - e[2]);
+  double g[4][3];  // d(u,v,w,T)/dx_t
+  for (int a = 0; a < 4; a++) {
+    const double* f = a < 3 ? &vel[a * N] : tem.data();
+    for (int t = 0; t < 3; t++) {
+      if (t == d) {
+        g[a][t] = (f[qR] - f[qL]) / b.h[d];
+      } else {
+        int o[3] = {0, 0, 0};
+        o[t] = 1;
+        size_t rp = b.I(i + o[0], j + o[1], k + o[2]), rm = b.I(i - o[0], j - o[1], k - o[2]);
+        size_t lp = b.I(i - e[0] + o[0], j - e[1] + o[1], k - e[2] + o[2]);
+        size_t lm = b.I(i - e[0] - o[0], j - e[1] - o[1], k - e[2] - o[2]);
+        g[a][t] = ((f[rp] - f[rm]) + (f[lp] - f[lm])) / (4.0 * b.h[t]);
+      }
+    }
+  }
+  const double mu = P.viscl;
+  const double kt = mu * P.gamma * P.gas_const / ((P.gamma - 1.0) * P.prlmean);
+  double div = g[0][0] + g[1][1] + g[2][2];
+  double tau[3];
+  for (int a = 0; a < 3; a++) tau[a] = mu * (g[a][d] + g[d][a]) - (a == d ? (2.0 / 3.0) * mu * div : 0.0);
+  double uf[3];
+  for (int a = 0; a < 3; a++) uf[a] = 0.5 * (vel[a * N + qL] + vel[a * N + qR]);
+  out[0] = 0.0;
+  for (int a = 0; a < 3; a++) out[1 + a] = S * tau[a];
+  out[4] = S * ((uf[0] * tau[0] + uf[1] * tau[1] + uf[2] * tau[2]) + kt * g[3][d]);
+}
+
+// no-slip adiabatic wall face of a record: normal gradients to the mirror state only
+void visc_wall(const mge_params& P, OBlock& b, const ORec& t, double S, double* out) {
+  int d = t.zz - 1;
+  bool plus = t.faceid >= 4;
+  double u[3], ug[3], qb[3] = {t.qb[0], t.qb[1], t.qb[2]};
+  for (int a = 0; a < 3; a++) {
+    u[a] = b.W(t.ccid[0], t.ccid[1], t.ccid[2], 1 + a) / b.W(t.ccid[0], t.ccid[1], t.ccid[2], 0);
+    ug[a] = 2.0 * qb[a] - u[a];
+  }
+  double gn[3];
+  for (int a = 0; a < 3; a++) gn[a] = plus ? (ug[a] - u[a]) / b.h[d] : (u[a] - ug[a]) / b.h[d];
+  const double mu = P.viscl;
+  double tau[3];
+  for (int a = 0; a < 3; a++) tau[a] = (a == d) ? (4.0 / 3.0) * mu * gn[a] : mu * gn[a];
+  out[0] = 0.0;
+  for (int a = 0; a < 3; a++) out[1 + a] = S * tau[a];
+  out[4] = S * (qb[0] * tau[0] + qb[1] * tau[1] + qb[2] * tau[2]);
+}
+
+int vflux_all(mgeo_ctx* c, OBlock& b, int istage) {
+  const mge_params& P = c->prm;
+  const double cd = P.cdis[istage - 1];
+  const size_t N = b.N;
+  std::vector<double> vel(3 * N), tem(N);
+  for (size_t q = 0; q < N; q++) {  // euler.f90:140-154
+    double w0 = b.w[q];
+    for (int a = 0; a < 3; a++) vel[a * N + q] = b.w[(1 + a) * N + q] / w0;
+    tem[q] = b.p[q] / (w0 * P.gas_const);
+    if (b.blank[q] == 0) {
+      for (int a = 0; a < 3; a++) vel[a * N + q] = 0.0;
+      tem[q] = 0.0;
+    }
+  }
+  const double Sd[3] = {std::fabs(b.si[0]), std::fabs(b.sj[1]), std::fabs(b.sk[2])};
+  const size_t st[3] = {1, b.Pi, b.Pi * b.Pj};
+  std::vector<double> V(15 * N, 0.0);
+  for (int d = 0; d < 3; d++) {
+    int hi[3] = {b.il, b.jl, b.kl};
+    hi[d] += 1;
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+    for (int k = 2; k <= hi[2]; k++)
+      for (int j = 2; j <= hi[1]; j++)
+        for (int i = 2; i <= hi[0]; i++) {
+          double o[5];
+          visc_face(P, b, vel, tem, d, i, j, k, Sd[d], o);
+          for (int v = 0; v < 5; v++) V[(d * 5 + v) * N + b.I(i, j, k)] = cd * o[v];
+        }
+  }
+  for (int d = 0; d < 3; d++)
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+    for (int k = 2; k <= b.kl; k++)
+      for (int j = 2; j <= b.jl; j++)
+        for (int i = 2; i <= b.il; i++) {
+          size_t q = b.I(i, j, k);
+          for (int v = 0; v < 5; v++)
+            b.fw[v * N + q] = b.fw[v * N + q] + (V[(d * 5 + v) * N + q] - V[(d * 5 + v) * N + q + st[d]]);
+        }
+  for (size_t m = 0; m < b.z.size(); m++) {  // walls, record order
+    const ORec& t = b.z[m];
+    int d = t.zz - 1;
+    size_t q = b.I(t.ccid[0], t.ccid[1], t.ccid[2]);
+    bool plus = t.faceid >= 4;
+    double o[5], X[5], Z[5];
+    visc_wall(P, b, t, Sd[d], o);
+    for (int v = 0; v < 5; v++) {
+      if (plus) {
+        X[v] = -V[(d * 5 + v) * N + q + st[d]];
+        Z[v] = -(cd * o[v]);
+      } else {
+        X[v] = V[(d * 5 + v) * N + q];
+        Z[v] = cd * o[v];
+      }
+      b.fw[v * N + q] = b.fw[v * N + q] - X[v];
+      b.fw[v * N + q] = b.fw[v * N + q] + Z[v];
+    }
+  }
+  return MGE_OK;
+}
+
 /* ------------------------------------------------------------------ euler.f90:1-462 */
 int euler(mgeo_ctx* c, OBlock& b, int itime, int ncyc, int mgl, int mlvl, bool lres, bool lfir, int nstage_limit) {
   (void)itime;
   const mge_params& P = c->prm;
   const size_t N = b.N;
   const double fcoll = 1.0;
-  if (P.distype != MGE_DIS_CENTRAL)
-    return fail(c, MGE_EBADCFG, "the oracle restates the central scheme (distype 'c') only");
   if (lfir) b.ws = b.w;  // euler.f90:75-77
 #pragma omp parallel for num_threads(g_threads) schedule(static)
   for (int k = 2; k <= b.kl; k++)
@@ -1129,12 +1497,23 @@ int euler(mgeo_ctx* c, OBlock& b, int itime, int ncyc, int mgl, int mlvl, bool l
             for (int v = 0; v < 5; v++) b.FW(i, j, k, v) = b.FW(i, j, k, v) * f;
     }
     int rc;
-    if (P.cdis[m - 1] > 0.0) {
-      rc = dflux(c, b, m);
+    if (P.eqntype == MGE_EQN_NS && P.cdis[m - 1] > 0.0) {  // euler.f90:137-182
+      rc = vflux_all(c, b, m);
       if (rc) return rc;
     }
-    rc = eflux(c, b);
-    if (rc) return rc;
+    if (P.distype == MGE_DIS_CENTRAL) {
+      if (P.cdis[m - 1] > 0.0) {
+        rc = dflux(c, b, m);
+        if (rc) return rc;
+      }
+      rc = eflux(c, b);
+      if (rc) return rc;
+    } else if (P.distype == MGE_DIS_ROE1 || P.distype == MGE_DIS_ROE2) {
+      rc = roe_fluxes(c, b, m);
+      if (rc) return rc;
+    } else {
+      return fail(c, MGE_EBADCFG, "distype should be c/r1/r2 (euler.f90:212-214)");
+    }
 #pragma omp parallel for num_threads(g_threads) schedule(static)
     for (int k = 2; k <= b.kl; k++)
       for (int j = 2; j <= b.jl; j++)

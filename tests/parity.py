@@ -25,7 +25,7 @@ def exact_fraction(a, b):
     return float(np.mean(a == b)) if a.size else 1.0
 
 
-PATHS = ("coop", "phases")
+PATHS = ("coop", "phases", "tuned")
 
 
 def set_path(path):
@@ -34,7 +34,9 @@ def set_path(path):
     import os
     if path == "phases":
         os.environ["MGE_COOP_MAX_CELLS"] = "0"
-    else:
+    elif path == "coop":
+        os.environ["MGE_COOP_MAX_CELLS"] = str(10 ** 9)
+    else:  # "tuned": the autotuner chooses
         os.environ.pop("MGE_COOP_MAX_CELLS", None)
 
 
@@ -70,7 +72,7 @@ def compare(g, o, name, level, rtol=RTOL, phys_only=True):
 
 
 def small_cylinder(**kw):
-    a = dict(n=32, span=2, nlevel=2, extent=4.0, mcyc_fine=4)
+    a = dict(n=32, span=2, nlevel=2, extent=4.0, mcyc_fine=4, mach=0.3)
     a.update(kw)
     return K.cylinder_slab(**a)
 

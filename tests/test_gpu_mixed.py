@@ -1,0 +1,70 @@
+"""Mixed precision: FP32 coarse levels, FP32 time step and residual smoothing
+on the finest level, FP64 finest residual, update, norm and forces.  The
+multigrid then acts as a defect correction: the converged answer must match
+the FP64 plain solve (and hence the FP64 oracle) to the stated tolerance."""
+import numpy as np
+import pytest
+
+from code_mge_gb300 import _abi as A
+from code_mge_gb300 import cases as K
+
+pytestmark = pytest.mark.gpu
+
+CD_TOL = 1e-6   # |dCd| of the converged mixed solve against the FP64 plain one
+
+
+def _solve(case, precision, cycles):
+    from code_mge_gb300.runtime import Cycle
+    case.prm.precision = precision
+    case.prm.conv_drop = 1e8       # converge to an 8-decade residual drop (or `cycles`)
+    case.prm.mcyc[case.prm.nlevel - 1] = cycles
+    g = Cycle(case)
+    # mixed: FP32 coarse corrections until a 1e-6 drop, then FP64 to the end
+    hist, n, f = g.solve(refine_drop=1e-6 if precision == A.MGE_PREC_MIXED else 0.0)
+    w = g.field("w", case.prm.nlevel)
+    g.close()
+    return hist, f, w
+
+
+@pytest.mark.parametrize("mk,cycles", [
+    (lambda: K.sphere_box(n=24, nlevel=3, extent=4.0, radius=0.7, mgtype=2), 3000),
+    (lambda: K.cylinder_slab(n=48, span=2, nlevel=3, extent=6.0, mach=0.3, smoo=0.6), 3000),
+])
+def test_mixed_converges_to_the_fp64_answer(gpulib, mk, cycles):
+    c1, c2 = mk(), mk()
+    for c in (c1, c2):
+        for L in range(c.prm.nlevel - 1):
+            c.prm.mcyc[L] = 5
+    h64, f64, w64 = _solve(c1, A.MGE_PREC_FP64, cycles)
+    h32, f32, w32 = _solve(c2, A.MGE_PREC_MIXED, cycles)
+    # both reach the 8-decade drop; the mixed answer keeps FP64 accuracy
+    assert h64[-1] / h64[0] < 1e-8
+    assert h32[-1] / h32[0] < 1e-8
+    assert abs(f32.cd - f64.cd) <= CD_TOL
+    assert abs(f32.cl - f64.cl) <= CD_TOL
+    assert np.max(np.abs(w32 - w64)) / np.max(np.abs(w64)) < 1e-6
+
+
+def test_mixed_levels_precision(gpulib):
+    from code_mge_gb300.runtime import Cycle
+    case = K.sphere_box(n=16, nlevel=2, extent=3.0, radius=0.7, mgtype=1, precision=A.MGE_PREC_MIXED)
+    g = Cycle(case)
+    g.solve()
+    wc = g.field("w", 1)
+    wf = g.field("w", 2)
+    # coarse level values are FP32-representable, the finest level is not restricted to them
+    assert np.array_equal(wc, wc.astype(np.float32).astype(np.float64))
+    assert not np.array_equal(wf, wf.astype(np.float32).astype(np.float64))
+
+
+def test_precision_switch_round_trip(gpulib):
+    from code_mge_gb300.runtime import Cycle
+    case = K.sphere_box(n=16, nlevel=2, extent=3.0, radius=0.7, mgtype=1)
+    g = Cycle(case)
+    g.solve()
+    w1 = g.field("w", 1).copy()
+    assert gpulib.mge_set_precision(g.ctx, A.MGE_PREC_MIXED) == 0
+    assert np.array_equal(g.field("w", 1), w1.astype(np.float32).astype(np.float64))
+    assert gpulib.mge_set_precision(g.ctx, A.MGE_PREC_FP64) == 0
+    r = g.cycle(2)
+    assert np.isfinite(r)

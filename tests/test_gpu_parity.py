@@ -19,6 +19,12 @@ CASES = {
     "sphere_global_dt": lambda: small_sphere(cfl=1.5),
     "ellipsoid_noirs": lambda: K.ellipsoid_box(n=16, nlevel=2, semi=(0.9, 0.6, 0.5), extent=2.5, alpha_deg=5.0,
                                                smoo=0.0, mcyc_fine=4),
+    # Navier-Stokes and Roe (this build's definitions, the reference's sources being absent)
+    "cylinder_ns": lambda: small_cylinder(eqntype=A.MGE_EQN_NS, reynolds=40.0, mach=0.2),
+    "cylinder_roe1": lambda: small_cylinder(distype=A.MGE_DIS_ROE1),
+    "sphere_roe2": lambda: small_sphere(distype=A.MGE_DIS_ROE2),
+    "cylinder_ns_roe2": lambda: small_cylinder(eqntype=A.MGE_EQN_NS, distype=A.MGE_DIS_ROE2, reynolds=40.0,
+                                               mach=0.2),
 }
 
 
@@ -160,6 +166,14 @@ def test_mixed_paths_in_one_hierarchy(gpulib):
         o = OracleCycle(case)
     finally:
         os.environ.pop("MGE_COOP_MAX_CELLS", None)
+    from code_mge_gb300.runtime import load_library
+    import ctypes as C
+    lib = load_library()
+    for L, expect in ((1, 1), (2, 1), (3, 0)):
+        coop = C.c_int(-1)
+        irs = (C.c_int * 3)()
+        assert lib.mge_tuned(g.ctx, L, 1, C.byref(coop), irs) == 0
+        assert coop.value == expect
     hg, _, _ = g.solve()
     ho, _, _ = o.solve()
     assert np.max(np.abs(hg - ho) / np.abs(ho)) <= 1e-11
