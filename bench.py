@@ -45,10 +45,17 @@ UNIT = "cell-updates/s"
 # 5-variable fields of 40 B): smoothing stages 11 fields, non-smoothing
 # stages 4 fields, 17 B of scalars per stage, 56 B for the time step.
 BYTES_PER_CELL_UPDATE_IRS = (11 + 4 + 11 + 4 + 11) * 40 + 5 * 17 + 56   # 1,781
-# Compulsory bytes per cell of one k_face launch as designed: reads the
-# per-cell fluxes F (15), sensors (3), w(1:4)+H (5) and lambda (1), writes
-# the convective and dissipative face fluxes (15 + 15): 54 doubles.
-BYTES_PER_CELL_FACE = 54 * 8
+# Compulsory bytes per cell of one k_face launch as designed.  A stage with
+# dissipation reads the per-cell fluxes F (15), sensors (3), w(1:4)+H (5) and
+# lambda (1) and writes the convective and dissipative face fluxes (15 + 15):
+# 54 doubles.  A stage without it reads F and writes the convective face
+# fluxes: 30 doubles.  mge_kernel_times averages over the 5 stages.
+FACE_DOUBLES_DISSIP, FACE_DOUBLES_PLAIN = 54, 30
+
+
+def face_bytes_per_cell(prm):
+    on = sum(1 for m in range(prm.mstage) if prm.cdis[m] > 0.0)
+    return 8.0 * (on * FACE_DOUBLES_DISSIP + (prm.mstage - on) * FACE_DOUBLES_PLAIN) / prm.mstage
 LAUNCHES_PER_UPDATE = {"timestep": 1, "prep": 5, "face": 5, "rec": 5, "combine": 5, "irs_i": 3, "irs_j": 3,
                        "irs_k_update": 3, "cutcell": 5, "bcond": 5, "rtrms": 1}
 
@@ -62,14 +69,17 @@ def workload_case(precision="fp64", n=192):
 def run_profile(args):
     """Short run for the ncu captures: set up the workload, one warm cycle,
     then one timed update of the finest level through the per-kernel path."""
+    import torch
     from code_mge_gb300.runtime import Cycle, load_library
     lib = load_library()
-    n = 96 if args.workload == "sphere96" else 192
+    n = int(args.workload[len("sphere"):])
     case = workload_case(args.precision, n=n)
     cyc = Cycle(case)
     cyc.cycle(case.prm.nlevel, ncyc=1)
     ms = np.zeros(len(A.KERNEL_KINDS))
+    torch.cuda.nvtx.range_push("profiled")  # one finest-level update, kernel by kernel
     lib.mge_kernel_times(cyc.ctx, case.prm.nlevel, 1, ms.ctypes.data_as(C.POINTER(C.c_double)), len(ms))
+    torch.cuda.nvtx.range_pop()
     print(json.dumps({"profile_run": args.workload, "kernel_ms": dict(zip(A.KERNEL_KINDS, ms.tolist()))}))
     cyc.close()
     return 0
@@ -225,9 +235,11 @@ def run_gpu(args):
     n_launch0 = lib.mge_launch_count(cyc.ctx)
     t0 = time.perf_counter()
     res = []
+    torch.cuda.nvtx.range_push("timed")  # lets a profiler select the timed steps
     for q in range(args.steps):
         res.append(cyc.cycle(L, ncyc=args.warmup + q + 1))
         dev_ms += lib.mge_last_cycle_ms(cyc.ctx)
+    torch.cuda.nvtx.range_pop()
     barrier()
     wall = time.perf_counter() - t0
     clocks = sampler.stop()
@@ -266,10 +278,7 @@ def run_gpu(args):
     ncell = case.finest_cells
     dims = sp.dims
     face_cells = (dims[0] - 3) * (dims[1] - 3) * (dims[2] - 3)
-    if dom == "face":
-        alg = BYTES_PER_CELL_FACE * face_cells
-    else:
-        alg = BYTES_PER_CELL_FACE * face_cells
+    alg = face_bytes_per_cell(case.prm) * face_cells
     achieved = alg / (kt["face"] * 1e-3) / 1e9 if kt["face"] > 0 else 0.0
     traffic = None
     tf = os.path.join(ROOT, "profiles", "ncu_traffic.json")
@@ -304,6 +313,7 @@ def run_gpu(args):
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(w_np.nbytes), "d2h_bytes_per_step": 8},
             "gpu_launches": None,
             "roofline": {"bound": "hbm", "kernel": "k_face", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "algorithmic_bytes_per_launch": alg, "launch_ms": kt["face"],
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": pkind,
                          "note": "GB300 FP64 issue rate, not HBM, bounds these kernels"},
             "whole_update_hbm": {"achieved_gbs": whole_update_gbs, "frac": whole_update_gbs / peak,
@@ -396,7 +406,7 @@ def main():
     ap.add_argument("--duration", type=float, default=300.0)
     ap.add_argument("--drain", type=float, default=120.0)
     ap.add_argument("--coop-ctas", type=int, default=32)
-    ap.add_argument("--workload", default="sphere192", choices=["sphere192", "sphere96"])
+    ap.add_argument("--workload", default="sphere192", choices=["sphere192", "sphere128", "sphere96"])
     ap.add_argument("--profile", action="store_true", help="short run for ncu captures")
     args = ap.parse_args()
     if args.profile:

@@ -54,6 +54,7 @@ module mge_gpu_mod
     integer(c_int) :: max_cycles_total
     real(c_double) :: ref_area, moment_center(3)
     integer(c_int) :: use_graph
+    real(c_double) :: refine_drop             ! mixed form: FP64 from this residual drop on (0: never)
   end type mge_solve_opts
 
   interface
@@ -143,6 +144,25 @@ module mge_gpu_mod
       integer(c_int), value :: hist_len
       integer(c_int), intent(out) :: cycles_done
       type(mge_forces), intent(out) :: forces
+    end function
+    integer(c_int) function mge_set_precision(ctx, precision) bind(C, name="mge_set_precision")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: precision
+    end function
+    integer(c_int) function mge_forces_compute(ctx, level, opts, forces) bind(C, name="mge_forces_compute")
+      import :: c_int, c_ptr, mge_solve_opts, mge_forces
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: level
+      type(mge_solve_opts), intent(in) :: opts
+      type(mge_forces), intent(out) :: forces
+    end function
+    integer(c_int) function mge_residual_norm_noalloc(dw_rho, vdtim, blank, nx, ny, nz, cfl, vt, dtim, &
+        norm_out, stream) bind(C, name="mge_residual_norm_noalloc")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: dw_rho, vdtim, blank, norm_out, stream   ! device pointers
+      integer(c_int), value :: nx, ny, nz, vt
+      real(c_double), value :: cfl, dtim
     end function
   end interface
 
