@@ -85,6 +85,18 @@ def run_profile(args):
     return 0
 
 
+def launch_plan(lib, cyc, nlevel):
+    """The launch forms the autotuner chose, as MGE_TUNE_PLAN takes them:
+    level:CIJK (C cooperative euler, I/J/K line-sweep form per direction)."""
+    out = []
+    for L in range(1, nlevel + 1):
+        coop = C.c_int(0)
+        irs = (C.c_int * 3)()
+        lib.mge_tuned(cyc.ctx, L, 1, C.byref(coop), irs)
+        out.append("%d:%d%d%d%d" % (L, coop.value, irs[0], irs[1], irs[2]))
+    return ",".join(out)
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -220,6 +232,10 @@ def run_gpu(args):
     cu = S.cell_updates_per_cycle(case)
     L = case.prm.nlevel
     cyc = Cycle(case, device=dev)
+    plan = launch_plan(lib, cyc, L)
+    if args.plan_out and rank == 0:
+        with open(args.plan_out, "w") as fh:
+            fh.write(plan + "\n")
     for q in range(args.warmup):
         cyc.cycle(L, ncyc=q + 1)
 
@@ -307,6 +323,7 @@ def run_gpu(args):
                                    "IRS 0.6, 4-level W-cycle; step = 1 W-cycle", "cells_finest": ncell,
                        "cell_updates_per_step": cu, "precision": args.precision,
                        "parallelism": "replicas" if world > 1 else "single GPU",
+                       "launch_plan": plan,
                        "l2": "fields of 301 MB each exceed the 129 MB L2 (no flush needed)"},
             "wall_ms_per_step": 1e3 * wall / args.steps,
             "residual_last": res[-1] if res else None,
@@ -339,12 +356,11 @@ def run_pattern(args):
         sizes = tuple(int(x) for x in args.sizes.split(","))
         reqs = SV.batched_sweep_requests(args.cases, sizes=sizes, precision=A.MGE_PREC_MIXED, tol=args.tol,
                                          max_cycles=args.max_cycles)
-        for r in reqs:
-            r.arrival = 0.0
         srv = SV.Server(SV.GpuBackend(coop_ctas=args.coop_ctas), max_active=args.cases)
-        for r in reqs:
-            srv.submit(r)
         t0 = time.perf_counter()
+        for r in reqs:
+            r.arrival = t0
+            srv.submit(r)
         done = srv.run()
         tb = time.perf_counter() - t0
         batched = SV.summarize(done, tb)
@@ -352,17 +368,28 @@ def run_pattern(args):
         plain, t0 = [], time.perf_counter()
         for r in SV.batched_sweep_requests(args.cases, sizes=sizes, precision=A.MGE_PREC_FP64, tol=args.tol,
                                            max_cycles=args.max_cycles):
+            r.arrival = t0
             one = SV.Server(SV.GpuBackend(coop_ctas=0), max_active=1)
             one.submit(r)
             plain += one.run()
         tp = time.perf_counter() - t0
         serial = SV.summarize(plain, tp)
         mix = {r.rid: r for r in done}
-        dcd = [abs(mix[r.rid].cd - r.cd) for r in plain if r.error is None and mix[r.rid].error is None]
+        both = [r for r in plain if r.error is None and mix[r.rid].error is None
+                and r.converged and mix[r.rid].converged]
+        dcd = [abs(mix[r.rid].cd - r.cd) for r in both]
+        per_case = [{"rid": r.rid, "n": r.n, "mach": round(r.mach, 4), "alpha_deg": round(r.alpha_deg, 3),
+                     "semi": [round(x, 3) for x in r.semi],
+                     "fp64": {"cycles": r.cycles, "converged": r.converged, "cd": r.cd, "error": r.error},
+                     "mixed": {"cycles": mix[r.rid].cycles, "fp64_from_cycle": mix[r.rid].refined_at,
+                               "converged": mix[r.rid].converged, "cd": mix[r.rid].cd, "error": mix[r.rid].error},
+                     "abs_dcd": (abs(mix[r.rid].cd - r.cd) if r.cd is not None and mix[r.rid].cd is not None
+                                 else None)} for r in plain]
         line = {"pattern": "batched sweep", "metric": "converged solves/s", "unit": "solves/s",
                 "value": batched["solves_per_s"], "baseline_fp64_serial": serial["solves_per_s"],
                 "speedup": batched["solves_per_s"] / serial["solves_per_s"] if serial["solves_per_s"] else None,
-                "max_abs_dcd_vs_fp64": max(dcd) if dcd else None, "cases": args.cases,
+                "max_abs_dcd_vs_fp64": max(dcd) if dcd else None, "dcd_cases": len(dcd), "cases": args.cases,
+                "per_case": per_case,
                 "config": {"sizes": sizes, "tol_drop": args.tol, "levels": 3, "cycle": "W",
                            "precision": "FP32 coarse / FP64 fine", "seed": 20261203},
                 "batched": batched, "fp64_serial": serial, "peak_active": srv.peak_active}
@@ -408,6 +435,7 @@ def main():
     ap.add_argument("--coop-ctas", type=int, default=32)
     ap.add_argument("--workload", default="sphere192", choices=["sphere192", "sphere128", "sphere96"])
     ap.add_argument("--profile", action="store_true", help="short run for ncu captures")
+    ap.add_argument("--plan-out", default=None, help="write the tuned launch plan (MGE_TUNE_PLAN form) here")
     args = ap.parse_args()
     if args.profile:
         return run_profile(args)

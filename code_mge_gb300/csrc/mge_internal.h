@@ -41,6 +41,7 @@ struct DevBlock {
   T* dfs;                   // 15N dissipative face flux
   T* vt;                    // 4N velocity and temperature (Navier-Stokes)
   T* vfs;                   // 15N viscous face flux (Navier-Stokes)
+  T* eps;                   // 3N smoothing coefficients eps_x,y,z (psmoo variant only, else null)
   // metric (uniform, axis-aligned face vectors)
   double s[3];              // si[0], sj[1], sk[2]
   double hx, hy, hz;        // cell sizes (viscous gradients)
@@ -89,6 +90,7 @@ struct PhysParams {
   double smoo;
   int vt;                   // global time step
   int distype;              // MGE_DIS_* (0 central, 1 Roe first order, 2 Roe MUSCL)
+  int irs_kind;             // 0 psmoo_old (what euler calls), 1 psmoo + progon3
   double viscl, kt, gas_const, prlmean;  // laminar viscosity, heat conductivity, R, Pr
   double cfac;              // viscous weight of the time step (timestep.f90:119-125)
   double epsentr;           // Harten entropy fix

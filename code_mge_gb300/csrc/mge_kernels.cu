@@ -127,6 +127,25 @@ __device__ __forceinline__ unsigned long long body_timestep(const DevBlock<T>& b
     b.vdtim[c] = (T)vd;
     b.lam[c] = (T)lsum;
   }
+  if (b.eps && P.smoo > 0.0) {
+    // coefficients of the psmoo variant, timestep.f90:286-309; the radii of
+    // blanked cells are zero there (timestep.f90:212-223), so their ratios
+    // are 0/0 and the NaN-ignoring min/max give eps = smoo
+    const bool bl = b.blank[c] == 0;
+    const TC zi = bl ? TC(0) : ri, zj = bl ? TC(0) : rj, zk = bl ? TC(0) : rk;
+    const TC smoo = (TC)P.smoo;
+    const TC cflrat = sqrt(TC(1) + TC(4) * smoo);
+    auto coef = [&](TC ra, TC rb, TC rc) -> TC {  // ra: this direction's radius
+      TC reval = rb / ra + rc / ra;
+      TC q = cflrat / (TC(1) + TC(0.0625) * reval);
+      TC ex = TC(0.25) * (q * q - TC(1));
+      ex = fmin(smoo, ex);
+      return fmax(TC(0), ex);
+    };
+    b.eps[c] = (T)coef(zi, zj, zk);
+    b.eps[N + c] = (T)coef(zj, zk, zi);
+    b.eps[2 * N + c] = (T)coef(zk, zi, zj);
+  }
   return mine;
 }
 
@@ -238,7 +257,7 @@ __device__ __forceinline__ void body_prep(const DevBlock<T>& b, const PhysParams
 
 // dflux_matrix, dflux.f90:283-339, with general face vector ss
 template <typename T>
-__device__ void dflux_matrix(T gamma, const T* u1, const T* u2, const T* dw, const T* ss, T* ff) {
+__device__ __noinline__ void dflux_matrix(T gamma, const T* u1, const T* u2, const T* dw, const T* ss, T* ff) {
   T gam1 = gamma - T(1), epsn = T(1), epsl = T(1);
   T rr = T(0.5) * (u1[0] + u2[0]);
   T us[3];
@@ -281,7 +300,7 @@ __device__ __forceinline__ T van_albada(T a, T b, T e2) {
 }
 
 template <typename T>
-__device__ void roe_diss(const PhysParams& P, int d, T S, const T* wl, T pl, const T* wr, T pr, T* out) {
+__device__ __noinline__ void roe_diss(const PhysParams& P, int d, T S, const T* wl, T pl, const T* wr, T pr, T* out) {
   const T g = (T)P.gamma;
   T ul[3], ur[3];
   for (int a = 0; a < 3; a++) {
@@ -329,7 +348,7 @@ __device__ void roe_diss(const PhysParams& P, int d, T S, const T* wl, T pl, con
 
 // face q (between q-1 and q) along D at cell c: cell states, MUSCL when order 2
 template <typename T, int D>
-__device__ void face_states(const DevBlock<T>& b, const PhysParams& P, long long c, int q, int order, T* wl, T* pl,
+__device__ __noinline__ void face_states(const DevBlock<T>& b, const PhysParams& P, long long c, int q, int order, T* wl, T* pl,
                             T* wr, T* pr) {
   const long long N = b.N;
   const long long st = D == 0 ? 1 : (D == 1 ? (long long)b.Pi : (long long)b.Pi * b.Pj);
@@ -385,7 +404,7 @@ __device__ __forceinline__ void ceflux_gen(int D, const T* w, T p, T s, T* f) {
 
 // laminar viscous flux through face q along D (at cell c), times S
 template <typename T, int D>
-__device__ void visc_face(const DevBlock<T>& b, const PhysParams& P, long long c, T S, T* out) {
+__device__ __noinline__ void visc_face(const DevBlock<T>& b, const PhysParams& P, long long c, T S, T* out) {
   const long long N = b.N;
   const long long st[3] = {1, (long long)b.Pi, (long long)b.Pi * b.Pj};
   const long long cl = c - st[D];
@@ -966,23 +985,53 @@ __device__ __forceinline__ void body_irs(const DevBlock<T>& b, const IrsTables& 
     }
     prev = x;
   }
-  for (int q = 3; q <= l; q++) {
-    long long c = c0 + q * st;
-    TC x = (TC)d[c];
-    if (b.blank[c] != 0) {
-      x = mdiv(x - bb * prev, (TC)tb.e1[q], (TC)tb.e1r[q]);
-      d[c] = (T)x;
-    }
-    prev = x;
+  // The recurrence is serial, its loads are not: each chunk of K cells is
+  // loaded before any of it is solved, so one memory latency is paid per
+  // chunk instead of per cell.  Every cell is read once and written once
+  // after its own read, so the order of results is unchanged.
+  constexpr int K = 8;
+  TC xb[K], pb[K], rb[K];
+  unsigned char bk[K];
+  for (int q0 = 3; q0 <= l; q0 += K) {
+#pragma unroll
+    for (int u = 0; u < K; u++)
+      if (q0 + u <= l) {
+        const long long c = c0 + (q0 + u) * st;
+        xb[u] = (TC)d[c];
+        bk[u] = b.blank[c];
+        pb[u] = (TC)tb.e1[q0 + u];
+        rb[u] = (TC)tb.e1r[q0 + u];
+      }
+#pragma unroll
+    for (int u = 0; u < K; u++)
+      if (q0 + u <= l) {
+        TC x = xb[u];
+        if (bk[u] != 0) {
+          x = mdiv(x - bb * prev, pb[u], rb[u]);
+          d[c0 + (q0 + u) * st] = (T)x;
+        }
+        prev = x;
+      }
   }
-  for (int q = l - 1; q >= 2; q--) {
-    long long c = c0 + q * st;
-    TC x = (TC)d[c];
-    if (b.blank[c] != 0) {
-      x = x - (TC)tb.e2[q] * prev;
-      d[c] = (T)x;
-    }
-    prev = x;
+  for (int q0 = l - 1; q0 >= 2; q0 -= K) {
+#pragma unroll
+    for (int u = 0; u < K; u++)
+      if (q0 - u >= 2) {
+        const long long c = c0 + (q0 - u) * st;
+        xb[u] = (TC)d[c];
+        bk[u] = b.blank[c];
+        pb[u] = (TC)tb.e2[q0 - u];
+      }
+#pragma unroll
+    for (int u = 0; u < K; u++)
+      if (q0 - u >= 2) {
+        TC x = xb[u];
+        if (bk[u] != 0) {
+          x = x - pb[u] * prev;
+          d[c0 + (q0 - u) * st] = (T)x;
+        }
+        prev = x;
+      }
   }
 }
 
@@ -1077,6 +1126,112 @@ size_t irs_smem_bytes(int len) {
 }
 
 // update after smoothing, euler.f90:381-399 (steady: lam = 1)
+// --------------------------------------------------------------- psmoo + progon3 (irs_variant 1)
+// psmoo.f90:1-95 with progon3.f90:41-60: per-cell coefficients eps from the
+// time step, aa = 1+2eps, bb = cc = -eps with the end couplings zeroed
+// (psmoo.f90:49-50), solved by progon3's forward/backward recurrences.  One
+// thread per line carries all five variables: the coefficient recurrences v
+// and w do not depend on the variable and are formed once.  The recurrences
+// pass through the stage scratch F, dead between the residual pass and the
+// next stage: slot q of a line holds progon3's v(q), w(q), u(q,1:5) on the
+// way forward and s(q-1), t(q-1,1:5) on the way back.
+template <typename T, int D>
+__device__ __forceinline__ void line_of(const DevBlock<T>& b, long long ln, long long& c0, long long& st, int& l) {
+  if (D == 0) {
+    int j = 2 + (int)(ln % b.ny), k = 2 + (int)(ln / b.ny);
+    c0 = cidx(b.Pi, b.Pj, 0, j, k);
+    st = 1;
+    l = b.il;
+  } else if (D == 1) {
+    int i = 2 + (int)(ln % b.nx), k = 2 + (int)(ln / b.nx);
+    c0 = cidx(b.Pi, b.Pj, i, 0, k);
+    st = b.Pi;
+    l = b.jl;
+  } else {
+    int i = 2 + (int)(ln % b.nx), j = 2 + (int)(ln / b.nx);
+    c0 = cidx(b.Pi, b.Pj, i, j, 0);
+    st = (long long)b.Pi * b.Pj;
+    l = b.kl;
+  }
+}
+
+template <typename T, typename TC, int D>
+__device__ __noinline__ void body_psmoo_line(const DevBlock<T>& b, long long ln) {
+  const long long N = b.N;
+  long long c0, st;
+  int l;
+  line_of<T, D>(b, ln, c0, st, l);
+  const T* eps = b.eps + (long long)D * N;
+  T* Sv = b.F;          // v forward, s backward
+  T* Sw = b.F + N;      // w forward
+  T* Su = b.F + 2 * N;  // u(1:5) forward, t(1:5) backward
+  // forward: equation i = 1..n sits at cell q = i+1 = 2..l (n = l-1)
+  TC v = TC(0), w = TC(1), u[5];
+#pragma unroll
+  for (int x = 0; x < 5; x++) u[x] = TC(0);
+  for (int q = 2; q <= l; q++) {
+    const long long c = c0 + q * st;
+    const TC e = (TC)eps[c];
+    const TC a = TC(1) + TC(2) * e;
+    const TC bq = (q == l) ? TC(0) : -e;
+    const TC cq = (q == 2) ? TC(0) : -e;
+    const TC z = TC(1) / (a + cq * v);
+    v = -bq * z;
+#pragma unroll
+    for (int x = 0; x < 5; x++) u[x] = (-cq * u[x] + (TC)b.dw[x * N + c]) * z;
+    w = -cq * w * z;
+    if (q < l) {  // v(n+1), w(n+1), u(n+1) are never read back
+      Sv[c] = (T)v;
+      Sw[c] = (T)w;
+#pragma unroll
+      for (int x = 0; x < 5; x++) Su[x * N + c] = (T)u[x];
+    }
+  }
+  // backward: s(i) = v(i+1) s(i+1) + w(i+1), t likewise, i = n-1..1, read
+  // from slot i+1 and stored back there; s(n-1), t(n-1) are kept for x(n)
+  // (zero when n = 1, progon3's s(0), t(0))
+  TC s = TC(1), t[5], shi = TC(0), thi[5];
+#pragma unroll
+  for (int x = 0; x < 5; x++) t[x] = thi[x] = TC(0);
+  for (int q = l - 1; q >= 2; q--) {
+    const long long c = c0 + q * st;
+    const TC vv = (TC)Sv[c], ww = (TC)Sw[c];
+    s = vv * s + ww;
+#pragma unroll
+    for (int x = 0; x < 5; x++) t[x] = vv * t[x] + (TC)Su[x * N + c];
+    Sv[c] = (T)s;
+#pragma unroll
+    for (int x = 0; x < 5; x++) Su[x * N + c] = (T)t[x];
+    if (q == l - 1) {
+      shi = s;
+#pragma unroll
+      for (int x = 0; x < 5; x++) thi[x] = t[x];
+    }
+  }
+  // x(n) at cell l, then x(i) = s(i) x(n) + t(i) at cells 2..l-1
+  const long long cl = c0 + l * st;
+  const TC el = (TC)eps[cl];
+  const TC an = TC(1) + TC(2) * el, bn = TC(0), cn = (l == 2) ? TC(0) : -el;
+  const TC den = an + bn * s + cn * shi;
+  TC xn[5];
+#pragma unroll
+  for (int x = 0; x < 5; x++) xn[x] = ((TC)b.dw[x * N + cl] - bn * t[x] - cn * thi[x]) / den;
+  for (int q = 2; q <= l - 1; q++) {
+    const long long c = c0 + q * st;
+    const TC sv = (TC)Sv[c];
+#pragma unroll
+    for (int x = 0; x < 5; x++) b.dw[x * N + c] = (T)(sv * xn[x] + (TC)Su[x * N + c]);
+  }
+#pragma unroll
+  for (int x = 0; x < 5; x++) b.dw[x * N + cl] = (T)xn[x];
+}
+
+template <typename T, typename TC, int D>
+__global__ void k_psmoo_line(DevBlock<T> b) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < irs_lines<T, D>(b)) body_psmoo_line<T, TC, D>(b, t);
+}
+
 template <typename T>
 __device__ __forceinline__ void body_update(const DevBlock<T>& b, const PhysParams& P, long long t) {
   int i = 2 + (int)(t % b.nx);
@@ -1146,12 +1301,6 @@ __device__ void body_cutcell(const DevBlock<T>& b, const PhysParams& P, unsigned
 // --------------------------------------------------------------- face boundary conditions
 // One launch per face in the order 1..6 of bcond.f90:16-39: later faces read
 // and overwrite ghost cells that earlier faces wrote.
-template <typename T>
-__device__ __forceinline__ long long bc_face_items(const DevBlock<T>& b, int face) {
-  const int ax = (face - 1) % 3;
-  return (long long)((ax == 0 ? b.jb : b.ib) + 1) * ((ax == 2 ? b.jb : b.kb) + 1);
-}
-
 template <typename T>
 __device__ void body_bc_face(const DevBlock<T>& b, const PhysParams& P, int face, long long t) {
   const int ax = (face - 1) % 3;
@@ -1262,6 +1411,58 @@ __device__ void body_bc_face(const DevBlock<T>& b, const PhysParams& P, int face
     b.p[d2] = b.p[p2];
     b.p[d1] = b.p[p1];
   }
+}
+
+// bcond.f90:16-42 applies the faces 1..6 one after the other over their
+// whole tangential range, so a later face overwrites the edge and corner
+// ghosts of an earlier one and reads what the earlier one wrote.  The same
+// result comes from three passes over all faces at once, by the number of
+// ghost coordinates among a ghost cell's two tangential ones (0: face
+// ghosts, 1: edges, 2: corners), each cell written only by its last writer,
+// the highest-numbered face (with a boundary condition) whose axis is a
+// ghost axis of the cell.  That writer reads cells with one ghost axis fewer,
+// whose own writers all come before it, so every read sees the value the
+// sequential order leaves there.
+template <typename T>
+__device__ __forceinline__ long long bc_pass_items(const DevBlock<T>& b) {
+  const long long s0 = (long long)(b.jb + 1) * (b.kb + 1), s1 = (long long)(b.ib + 1) * (b.kb + 1),
+                  s2 = (long long)(b.ib + 1) * (b.jb + 1);
+  return 2 * (s0 + s1 + s2);
+}
+
+template <typename T>
+__device__ __forceinline__ void body_bc_pass(const DevBlock<T>& b, const PhysParams& P, int pass, long long t) {
+  const long long sz[3] = {(long long)(b.jb + 1) * (b.kb + 1), (long long)(b.ib + 1) * (b.kb + 1),
+                           (long long)(b.ib + 1) * (b.jb + 1)};
+  int face = 1;
+  while (face < 6 && t >= sz[(face - 1) % 3]) {
+    t -= sz[(face - 1) % 3];
+    face++;
+  }
+  if (b.bctype[face - 1] == 0) return;
+  const int ax = (face - 1) % 3;
+  const int na = (ax == 0 ? b.jb : b.ib) + 1;
+  const int t1 = (int)(t % na), t2 = (int)(t / na);
+  const int ta = ax == 0 ? 1 : 0, tb = ax == 2 ? 1 : 2;  // tangential axes of t1, t2
+  const int lim[3] = {b.il, b.jl, b.kl};
+  int deg = 0;
+  bool last = true;
+  auto tangential = [&](int a, int q) {
+    const int g = q <= 1 ? a + 1 : (q > lim[a] ? a + 4 : 0);  // the face whose ghosts hold q
+    if (g) {
+      deg++;
+      if (g > face && b.bctype[g - 1] != 0) last = false;
+    }
+  };
+  tangential(ta, t1);
+  tangential(tb, t2);
+  if (deg == pass && last) body_bc_face(b, P, face, t);
+}
+
+template <typename T>
+__global__ void k_bc_pass(DevBlock<T> b, PhysParams P, int pass) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < bc_pass_items(b)) body_bc_pass(b, P, pass, t);
 }
 
 // bc_corner.f90:23-157 in one block: three dependent phases
@@ -1654,12 +1855,6 @@ __global__ void k_cutcell(DevBlock<T> b, PhysParams P, unsigned* err) {
   int m = blockIdx.x * blockDim.x + threadIdx.x;
   body_cutcell(b, P, err, m);
 }
-template <typename T>
-__global__ void k_bc_face(DevBlock<T> b, PhysParams P, int face) {
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < bc_face_items(b, face)) body_bc_face(b, P, face, t);
-}
-
 // =============================================================== one euler update in one launch
 // For the small coarse grids of the multigrid hierarchy every phase of
 // euler.f90 is latency-bound, so one cooperative kernel runs them all with a
@@ -1727,7 +1922,14 @@ __global__ void __launch_bounds__(256, 2) k_euler_coop(DevBlock<T> b, PhysParams
     for (long long t = gt; t < ncell; t += gs) body_combine<T, true>(b, P, A, E.err, t);
     g.sync();
     if (E.lres) return;
-    if (A.irs) {
+    if (A.irs && P.irs_kind == 1) {
+      for (long long t = gt; t < irs_lines<T, 0>(b); t += gs) body_psmoo_line<T, TA, 0>(b, t);
+      g.sync();
+      for (long long t = gt; t < irs_lines<T, 1>(b); t += gs) body_psmoo_line<T, TA, 1>(b, t);
+      g.sync();
+      for (long long t = gt; t < irs_lines<T, 2>(b); t += gs) body_psmoo_line<T, TA, 2>(b, t);
+      g.sync();
+    } else if (A.irs) {
       const TA bb = (TA)(-P.smoo);
       for (long long t = gt; t < 5 * irs_lines<T, 0>(b); t += gs) body_irs<T, TA, 0>(b, E.tab[0], bb, t);
       g.sync();
@@ -1740,10 +1942,9 @@ __global__ void __launch_bounds__(256, 2) k_euler_coop(DevBlock<T> b, PhysParams
     g.sync();
     for (long long t = gt; t < b.nmir; t += gs) body_cutcell(b, P, E.err, (int)t);
     g.sync();
-    for (int f = 1; f <= 6; f++) {
-      if (b.bctype[f - 1] == 0) continue;
-      const long long nf = bc_face_items(b, f);
-      for (long long t = gt; t < nf; t += gs) body_bc_face(b, P, f, t);
+    for (int pass = 0; pass < 3; pass++) {
+      const long long nf = bc_pass_items(b);
+      for (long long t = gt; t < nf; t += gs) body_bc_pass(b, P, pass, t);
       g.sync();
     }
     if (blockIdx.x == 0) body_corner(b, P);
@@ -1810,11 +2011,25 @@ void launch_irs_dir(const DevBlock<T>& b, const IrsTables& tb, TC bb, cudaStream
   }
 }
 
+template <typename T>
+long long irs_lines_h(const DevBlock<T>& b, int D) {
+  return D == 0 ? (long long)b.ny * b.nz : (D == 1 ? (long long)b.nx * b.nz : (long long)b.nx * b.ny);
+}
+
 template <typename T, typename TC>
 void launch_irs_part_t(int part, const DevBlock<T>& b, const PhysParams& P, const IrsTables* tab, cudaStream_t s,
                        const int* variant) {
   const TC bb = (TC)(-P.smoo);
   const long long ncell = (long long)b.nx * b.ny * b.nz;
+  if (P.irs_kind == 1) {  // psmoo + progon3: one thread per line
+    if (part == 0) k_psmoo_line<T, TC, 0><<<nblk(irs_lines_h(b, 0), 128), 128, 0, s>>>(b);
+    if (part == 1) k_psmoo_line<T, TC, 1><<<nblk(irs_lines_h(b, 1), 128), 128, 0, s>>>(b);
+    if (part == 2) {
+      k_psmoo_line<T, TC, 2><<<nblk(irs_lines_h(b, 2), 128), 128, 0, s>>>(b);
+      k_update<T><<<nblk(ncell, TPB), TPB, 0, s>>>(b, P);
+    }
+    return;
+  }
   if (part == 0) launch_irs_dir<T, TC, 0>(b, tab[0], bb, s, variant ? variant[0] : 0);
   if (part == 1) launch_irs_dir<T, TC, 1>(b, tab[1], bb, s, variant ? variant[1] : 0);
   if (part == 2) {
@@ -1845,12 +2060,9 @@ void launch_cutcell(const DevBlock<T>& b, const PhysParams& P, unsigned* err, cu
 
 template <typename T>
 void launch_bcond(const DevBlock<T>& b, const PhysParams& P, cudaStream_t s) {
-  for (int f = 1; f <= 6; f++) {
-    if (b.bctype[f - 1] == 0) continue;
-    int ax = (f - 1) % 3;
-    long long n = (long long)((ax == 0 ? b.jb : b.ib) + 1) * ((ax == 2 ? b.jb : b.kb) + 1);
-    k_bc_face<T><<<nblk(n, TPB), TPB, 0, s>>>(b, P, f);
-  }
+  const long long n = 2LL * ((long long)(b.jb + 1) * (b.kb + 1) + (long long)(b.ib + 1) * (b.kb + 1) +
+                             (long long)(b.ib + 1) * (b.jb + 1));
+  for (int pass = 0; pass < 3; pass++) k_bc_pass<T><<<nblk(n, TPB), TPB, 0, s>>>(b, P, pass);
   k_bc_corner<T><<<1, 512, 0, s>>>(b, P);
 }
 

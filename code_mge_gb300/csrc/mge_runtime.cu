@@ -54,6 +54,7 @@ struct Block {
   size_t esz = 8;
   void *w = nullptr, *p = nullptr, *wn = nullptr, *ws = nullptr, *dw = nullptr, *fw = nullptr, *wr = nullptr,
        *qf = nullptr, *vdtim = nullptr, *lam = nullptr;
+  void* eps = nullptr;  // 3N psmoo coefficients (irs_variant 1 only)
   double* dtim = nullptr;
   uint8_t *blank = nullptr, *marker = nullptr;
   int32_t* cutmap = nullptr;
@@ -105,6 +106,7 @@ struct mge_ctx {
   cudaEvent_t ev_done = nullptr;         // end of an asynchronous cycle
   bool autotune = true;                  // tune launch forms at init_flow
   bool tune_path = true;                 // ... including cooperative vs per-phase euler
+  std::string plan;                      // fixed launch forms per level (MGE_TUNE_PLAN), instead of tuning
   int pending_mlvl = 0;                  // level of the cycle in flight (0: none)
   unsigned long long* coop_trace = nullptr;
 };
@@ -350,6 +352,7 @@ void build_phys(mge_ctx* c) {
   Q.smoo = P.smoo;
   Q.vt = P.vt;
   Q.distype = P.distype;
+  Q.irs_kind = P.irs_variant;
   Q.viscl = P.viscl;
   Q.gas_const = P.gas_const;
   Q.prlmean = P.prlmean;
@@ -396,6 +399,7 @@ void fill_view(Block& b, DevBlock<T>& d, void* scratch) {
   d.w = (T*)b.w; d.p = (T*)b.p; d.wn = (T*)b.wn; d.ws = (T*)b.ws; d.dw = (T*)b.dw; d.fw = (T*)b.fw;
   d.wr = (T*)b.wr; d.qf = (T*)b.qf; d.vdtim = (T*)b.vdtim; d.lam = (T*)b.lam; d.dtim = b.dtim;
   d.blank = b.blank; d.marker = b.marker; d.cutmap = b.cutmap;
+  d.eps = (T*)b.eps;
   T* sc = (T*)scratch;
   d.H = sc;
   d.F = sc + N;
@@ -434,6 +438,7 @@ int commit_block(mge_ctx* c, Block& b, double* scratch) {
       (rc = valloc(c, &b.lam, N, es)) || (rc = dalloc(c, &b.dtim, 1)) || (rc = dalloc(c, &b.blank, N)) ||
       (rc = dalloc(c, &b.marker, N)) || (rc = dalloc(c, &b.cutmap, N)))
     return rc;
+  if (c->prm.irs_variant == 1 && (rc = valloc(c, &b.eps, 3 * N, es))) return rc;
   CK(cudaMemset(b.marker, 0, N));
   std::vector<uint8_t> bl(N);
   for (long long q = 0; q < N; q++) bl[q] = b.blank_h[q] != 0 ? 1 : 0;
@@ -606,7 +611,7 @@ int mge_init(const mge_params* prm, int device, mge_ctx** out) {
     return MGE_EBADCFG;
   if (prm->eqntype != MGE_EQN_EULER && prm->eqntype != MGE_EQN_NS) return MGE_EBADCFG;
   if (prm->dissip != MGE_DISSIP_SCALAR && prm->dissip != MGE_DISSIP_MATRIX) return MGE_EBADCFG;
-  if (prm->irs_variant != 0) return MGE_EBADCFG;
+  if (prm->irs_variant != 0 && prm->irs_variant != 1) return MGE_EBADCFG;
   mge_ctx* c = new mge_ctx();
   c->prm = *prm;
   c->device = device;
@@ -628,6 +633,7 @@ int mge_init(const mge_params* prm, int device, mge_ctx** out) {
   }
   if (const char* e = getenv("MGE_AUTOTUNE")) c->autotune = atoi(e) != 0;
   if (const char* e = getenv("MGE_COOP_MAX_CTAS")) c->coop_max_ctas = atoi(e);
+  if (const char* e = getenv("MGE_TUNE_PLAN")) c->plan = e;
   *out = c;
   return MGE_OK;
 }
@@ -786,9 +792,9 @@ static void free_stream_start(mge_ctx* c, Block& b) {  // init_flow.f90:46-96
 // launch, or one launch per phase) on the free-stream state, keep the faster,
 // and cache the choice by block shape and precision for later contexts.
 struct TuneKey {
-  int nx, ny, nz, f32, aux32, rec;
+  int nx, ny, nz, f32, aux32, rec, scheme;  // scheme: smoothing variant, equations, flux
   bool operator<(const TuneKey& o) const {
-    return std::tie(nx, ny, nz, f32, aux32, rec) < std::tie(o.nx, o.ny, o.nz, o.f32, o.aux32, o.rec);
+    return std::tie(nx, ny, nz, f32, aux32, rec, scheme) < std::tie(o.nx, o.ny, o.nz, o.f32, o.aux32, o.rec, o.scheme);
   }
 };
 struct TuneVal {
@@ -799,7 +805,9 @@ static std::map<TuneKey, TuneVal> g_tune;
 static std::mutex g_tune_mu;
 
 static int autotune_block(mge_ctx* c, Block& b, bool tune_path) {
-  TuneKey key{b.nx, b.ny, b.nz, (int)b.f32, (int)b.aux32, b.recs.empty() ? 0 : 1};
+  const mge_params& prm = c->prm;
+  TuneKey key{b.nx, b.ny, b.nz, (int)b.f32, (int)b.aux32, b.recs.empty() ? 0 : 1,
+              100 * prm.irs_variant + 10 * prm.eqntype + prm.distype};
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune.find(key);
@@ -822,7 +830,7 @@ static int autotune_block(mge_ctx* c, Block& b, bool tune_path) {
     cudaEventElapsedTime(&ms, e0, e1);
     return ms;
   };
-  if (c->prm.smoo > 0.0) {
+  if (c->prm.smoo > 0.0 && c->prm.irs_variant == 0) {  // the psmoo variant has one form
     for (int d = 0; d < 3; d++) {
       float best = 1e30f;
       int bv = 0;
@@ -871,9 +879,30 @@ int mge_init_flow(mge_ctx* c) {  // init_flow.f90:46-96
     for (Block& b : L) free_stream_start(c, b);
   CK(cudaGetLastError());
   int rc = check_err(c);
-  if (rc || !c->autotune) return rc;
-  for (auto& L : c->lv)
-    for (Block& b : L) {
+  if (rc) return rc;
+  // a fixed plan "level:CIJK,..." (C = 1 cooperative euler, I/J/K = line-sweep
+  // form per direction) replaces tuning for the levels it names, so that a
+  // run can repeat the launch forms another run chose
+  std::vector<bool> fixed(c->lv.size(), false);
+  for (size_t pos = 0; pos < c->plan.size();) {
+    size_t end = c->plan.find(',', pos);
+    if (end == std::string::npos) end = c->plan.size();
+    const std::string item = c->plan.substr(pos, end - pos);
+    pos = end + 1;
+    const size_t colon = item.find(':');
+    if (colon == std::string::npos || item.size() != colon + 5) return fail(c, MGE_EBADCFG, "MGE_TUNE_PLAN: bad item " + item);
+    const int lvl = atoi(item.substr(0, colon).c_str());
+    if (lvl < 1 || lvl > (int)c->lv.size()) return fail(c, MGE_EBADCFG, "MGE_TUNE_PLAN: bad level " + item);
+    for (Block& b : c->lv[lvl - 1]) {
+      b.use_coop = item[colon + 1] == '1';
+      for (int d = 0; d < 3; d++) b.irs_var[d] = item[colon + 2 + d] == '1' ? 1 : 0;
+    }
+    fixed[lvl - 1] = true;
+  }
+  if (!c->autotune) return MGE_OK;
+  for (size_t l = 0; l < c->lv.size(); l++)
+    for (Block& b : c->lv[l]) {
+      if (fixed[l]) continue;
       const bool tune_path = c->tune_path && (long long)b.nx * b.ny * b.nz <= 2000000;
       if ((rc = autotune_block(c, b, tune_path))) return rc;
     }
@@ -909,8 +938,9 @@ int mge_set_precision(mge_ctx* c, int precision) {
       F fields[] = {{&b.w, 5 * N, true},  {&b.p, N, true},        {&b.ws, 5 * N, true},   {&b.wn, 5 * N, false},
                     {&b.dw, 5 * N, false}, {&b.fw, 5 * N, false}, {&b.wr, 5 * N, false}, {&b.qf, 5 * N, false},
                     {&b.vdtim, N, false}, {&b.lam, N, false},     {&b.rec_wsol, 5LL * nma, true},
-                    {&b.rec_psol, nma, true}, {&b.rec_term, 50LL * nma, false}};
+                    {&b.rec_psol, nma, true}, {&b.rec_term, 50LL * nma, false}, {&b.eps, 3 * N, false}};
       for (F& f : fields) {
+        if (!*f.p) continue;  // not allocated for this context
         void* np = nullptr;
         int rc = valloc(c, &np, (size_t)f.n, nes);
         if (rc) return rc;
@@ -1005,6 +1035,7 @@ int mge_download_field(mge_ctx* c, int level, int serial, const char* name, doub
   else if (n == "qf") { src = b->qf; len = 5 * N; }
   else if (n == "vdtim") { src = b->vdtim; len = N; }
   else if (n == "lam") { src = b->lam; len = N; }
+  else if (n == "eps" && b->eps) { src = b->eps; len = 3 * N; }
   else if (n == "wsol") { src = b->rec_wsol; len = 5 * b->recs.size(); }
   else if (n == "psol") { src = b->rec_psol; len = b->recs.size(); }
   else if (n == "dtim") { src = b->dtim; len = 1; typed = false; }

@@ -138,7 +138,7 @@ class Cycle:
         sp = self.spec(level, serial)
         P = sp.dims
         N = P[0] * P[1] * P[2]
-        nvar = 5 if name in ("w", "dw", "fw", "wn", "ws", "wr", "qf") else 1
+        nvar = 5 if name in ("w", "dw", "fw", "wn", "ws", "wr", "qf") else (3 if name == "eps" else 1)
         if name in ("wsol", "psol"):
             nm = sp.arrays["nmir"]
             n = 5 * nm if name == "wsol" else nm
@@ -154,7 +154,7 @@ class Cycle:
         out = np.zeros(nvar * N, dtype=np.float64)
         self._chk(self._fn("download_field")(self.ctx, level, serial, name.encode(),
                                              out.ctypes.data_as(C.POINTER(C.c_double)), out.size), "download")
-        shp = (nvar, P[2], P[1], P[0]) if nvar == 5 else (P[2], P[1], P[0])
+        shp = (nvar, P[2], P[1], P[0]) if nvar > 1 else (P[2], P[1], P[0])
         return out.reshape(shp)
 
     def upload(self, w, level, serial=1):

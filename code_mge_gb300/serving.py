@@ -48,6 +48,8 @@ class Request:
     drop: float = None
     cd: float = None
     cl: float = None
+    converged: bool = False  # retired on the residual drop (not on max_cycles)
+    refined_at: int = None   # finest cycle of the switch to FP64 (mixed form)
     error: str = None
 
     @property
@@ -290,7 +292,14 @@ class Server:
                         self._retire(s, "precision refinement failed")
                         continue
                     s.refined = True
-                if (s.ini and res <= s.req.tol * s.ini) or s.cycles_fine >= s.req.max_cycles or res != res:
+                    s.req.refined_at = s.cycles_fine
+                    if s.req.tol >= s.req.refine_drop:
+                        # the drop counts only once an FP64 cycle confirms it
+                        self._advance(s)
+                        continue
+                conv = bool(s.ini) and res <= s.req.tol * s.ini
+                if conv or s.cycles_fine >= s.req.max_cycles or res != res:
+                    s.req.converged = conv
                     self._retire(s)
                     continue
             self._advance(s)
@@ -344,12 +353,14 @@ def batched_sweep_requests(count=64, seed=20261203, sizes=(32, 48, 64, 96, 128),
 
 def summarize(done, t_wall):
     ok = [r for r in done if r.error is None]
+    conv = [r for r in ok if r.converged]
     lat = np.array([r.latency for r in ok]) if ok else np.zeros(0)
     return {
         "requests": len(done),
         "completed": len(ok),
+        "converged": len(conv),
         "failed": len(done) - len(ok),
-        "solves_per_s": len(ok) / t_wall if t_wall > 0 else None,
+        "solves_per_s": len(conv) / t_wall if t_wall > 0 else None,
         "p50_s": float(np.percentile(lat, 50)) if lat.size else None,
         "p99_s": float(np.percentile(lat, 99)) if lat.size else None,
         "wall_s": t_wall,

@@ -1935,6 +1935,15 @@ int mgeo_download_field(mgeo_ctx* c, int level, int serial, const char* name, do
     std::memcpy(out, src->data(), src->size() * sizeof(double));
     return MGE_OK;
   }
+  if (n == "eps") {  // epsx, epsy, epsz of the psmoo variant
+    if (count < 3 * b->N) return fail(c, MGE_EBADCFG, "download_field: buffer too small");
+    for (size_t q = 0; q < b->N; q++) {
+      out[q] = b->epsx[q];
+      out[b->N + q] = b->epsy[q];
+      out[2 * b->N + q] = b->epsz[q];
+    }
+    return MGE_OK;
+  }
   if (n == "lam") {
     if (count < b->N) return MGE_EBADCFG;
     for (size_t q = 0; q < b->N; q++) out[q] = b->radi[q] + b->radj[q] + b->radk[q];

@@ -25,6 +25,9 @@ CASES = {
     "sphere_roe2": lambda: small_sphere(distype=A.MGE_DIS_ROE2),
     "cylinder_ns_roe2": lambda: small_cylinder(eqntype=A.MGE_EQN_NS, distype=A.MGE_DIS_ROE2, reynolds=40.0,
                                                mach=0.2),
+    # psmoo + progon3 (variable coefficients) in place of psmoo_old
+    "sphere_psmoo": lambda: small_sphere(irs_variant=1),
+    "cylinder_psmoo": lambda: small_cylinder(irs_variant=1),
 }
 
 
@@ -46,6 +49,8 @@ def test_timestep(gpulib, name):
     o.timestep(L)
     compare(g, o, "vdtim", L)
     compare(g, o, "lam", L)
+    if g.case.prm.irs_variant == 1:
+        compare(g, o, "eps", L)
     assert abs(g.field("dtim", L) - o.field("dtim", L)) <= RTOL * abs(o.field("dtim", L))
 
 

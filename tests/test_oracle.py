@@ -109,6 +109,49 @@ def test_psmoo_old_inverts_the_constant_tridiagonal_operators():
     np.testing.assert_allclose(back, raw, rtol=0, atol=1e-12 * np.abs(raw).max())
 
 
+def test_psmoo_inverts_the_variable_tridiagonal_operators():
+    # psmoo + progon3 (psmoo.f90:1-95): per-cell eps from the time step,
+    # aa = 1+2eps, bb = cc = -eps with the end couplings zeroed; the smoothed
+    # residual solves Tx Ty Tz applied in reverse
+    rng = np.random.default_rng(11)
+    case = K.free_stream_box(n=(9, 7, 5), nlevel=1, mach=0.5, smoo=0.0)
+    sp = case.levels[0][0]
+    case.prm.irs_variant = 1
+    w = None
+    outs, eps = {}, None
+    for smoo in (0.0, 0.6):
+        case.prm.smoo = smoo
+        o = OracleCycle(case)
+        if w is None:
+            w = o.field("w", 1).copy()
+            w[0] *= 1.0 + 0.05 * rng.standard_normal(w[0].shape)
+            w[1] += 0.2 * rng.standard_normal(w[1].shape)
+            w[4] *= 1.0 + 0.05 * rng.standard_normal(w[4].shape)
+        o.upload(w, 1)
+        o.timestep(1)
+        if smoo > 0:
+            eps = physical(o.field("eps", 1), sp)
+        o.euler_partial(1, 1)
+        outs[smoo] = physical(o.field("dw", 1), sp)
+    raw, sm = outs[0.0], outs[0.6]
+    assert 0.0 < eps.min() and eps.max() <= 0.6 and eps.std() > 0  # variable coefficients
+    nx, ny, nz = sp.n
+
+    def apply(e, x, axis):
+        # (T x)_q = (1+2e_q) x_q - e_q x_{q+1} - e_q x_{q-1}, no coupling past the ends
+        x = np.moveaxis(x, axis, -1)
+        e = np.moveaxis(e, axis - 1, -1)
+        y = (1.0 + 2.0 * e) * x
+        y[..., :-1] -= e[..., :-1] * x[..., 1:]
+        y[..., 1:] -= e[..., 1:] * x[..., :-1]
+        return np.moveaxis(y, -1, axis)
+
+    back = apply(eps[2], sm, 1)      # undo the k sweep (axis of k in [v, k, j, i])
+    back = apply(eps[1], back, 2)    # then j
+    back = apply(eps[0], back, 3)    # then i
+    np.testing.assert_allclose(back, raw, rtol=0, atol=1e-12 * np.abs(raw).max())
+
+
 def test_transfers_reproduce_linear_fields():
     case = K.sphere_box(n=16, nlevel=2, extent=2.0, radius=0.01)
     o = OracleCycle(case)

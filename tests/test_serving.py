@@ -29,8 +29,9 @@ def test_scheduler_completes_all_requests_in_fifo_admission():
     # from the first finest-level residual takes 10 more cycles (11 in all)
     assert all(r.cycles == 11 for r in done)
     assert srv.peak_active > 1   # requests overlapped
+    assert all(r.converged for r in done)
     st = S.summarize(done, 1.0)
-    assert st["completed"] == 9 and st["p99_s"] >= st["p50_s"]
+    assert st["completed"] == 9 and st["converged"] == 9 and st["p99_s"] >= st["p50_s"]
 
 
 def test_admission_is_gated_by_free_memory():
