@@ -39,6 +39,7 @@ struct DevBlock {
   T* fp;                    // 3N pressure sensor [dir]
   T* efs;                   // 15N convective face flux [dir][var] at the upper cell of the face
   T* dfs;                   // 15N dissipative face flux
+  T* dlt;                   // 15N differences w(q)-w(q-1) along each direction [dir][var], enthalpy in var 5
   T* vt;                    // 4N velocity and temperature (Navier-Stokes)
   T* vfs;                   // 15N viscous face flux (Navier-Stokes)
   T* eps;                   // 3N smoothing coefficients eps_x,y,z (psmoo variant only, else null)

@@ -30,6 +30,7 @@
 #include <algorithm>
 #include <cstring>
 
+#include "exact_ops.cuh"
 #include "mge_internal.h"
 
 namespace cg = cooperative_groups;
@@ -232,23 +233,37 @@ __device__ __forceinline__ void body_prep(const DevBlock<T>& b, const PhysParams
     F[3 * N] = f3;
     F[4 * N] = f4;
   }
+  if (dissip_on && P.distype == 0) {
+    // the differences the dissipation faces take (dflux.f90:95-99), once per
+    // cell instead of once per face; the neighbour's enthalpy is formed
+    // again with the same addition
+    const long long sts[3] = {1, (long long)b.Pi, (long long)b.Pi * b.Pj};
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      const long long cn = c - sts[d];
+      T* Dl = b.dlt + (long long)(d * 5) * N + c;
+#pragma unroll
+      for (int v = 0; v < 4; v++) Dl[v * N] = w[v] - b.w[v * N + cn];
+      Dl[4 * N] = Hc - (b.w[4 * N + cn] + b.p[cn]);
+    }
+  }
   if (dissip_on) {
     const long long pl = (long long)b.Pi * b.Pj;
     // i: abs(p(i-1) +2p(i) +p(i+1)), dflux.f90:71-76
     {
-      T pm = b.p[c - 1], pp = b.p[c + 1], p2 = T(2) * p;
+      T pm = b.p[c - 1], pp = b.p[c + 1], p2 = mul2(p);
       T pb = fabs(pm + p2 + pp);
       b.fp[c] = (pb > T(0)) ? fabs(pm - p2 + pp) / pb : T(0);
     }
     // j: abs(p(j+1) +2p(j) +p(j-1)), dflux.f90:131-136
     {
-      T pm = b.p[c - b.Pi], pp = b.p[c + b.Pi], p2 = T(2) * p;
+      T pm = b.p[c - b.Pi], pp = b.p[c + b.Pi], p2 = mul2(p);
       T pb = fabs(pp + p2 + pm);
       b.fp[N + c] = (pb > T(0)) ? fabs(pp - p2 + pm) / pb : T(0);
     }
     // k: abs(p(k-1) +2p(k) +p(k+1)), dflux.f90:188-193
     {
-      T pm = b.p[c - pl], pp = b.p[c + pl], p2 = T(2) * p;
+      T pm = b.p[c - pl], pp = b.p[c + pl], p2 = mul2(p);
       T pb = fabs(pm + p2 + pp);
       b.fp[2 * N + c] = (pb > T(0)) ? fabs(pm - p2 + pp) / pb : T(0);
     }
@@ -475,7 +490,7 @@ __device__ __forceinline__ void face_dir(const DevBlock<T>& b, const PhysParams&
   // convective: efs(q) = 0.5*(F(q) + F(q-1))
   const T* F = b.F + (long long)(D * 5) * N;
 #pragma unroll
-  for (int v = 0; v < 5; v++) E[v * N + c] = T(0.5) * (F[v * N + c] + F[v * N + c - st]);
+  for (int v = 0; v < 5; v++) E[v * N + c] = mulhalf(F[v * N + c] + F[v * N + c - st]);
   if (!dissip_on) return;
   // dissipation face q (dflux.f90:87-111)
   const T* fpd = b.fp + (long long)D * N;
@@ -483,35 +498,28 @@ __device__ __forceinline__ void face_dir(const DevBlock<T>& b, const PhysParams&
   T f_m1 = fpd[c - st];
   T f_0 = fpd[c];
   T f_p1 = (q + 1 == bq) ? T(0) : fpd[c + st];
-  T ep = fmaxT(fmaxT(fmaxT(f_m2, f_m1), f_0), f_p1);
+  // the sensors are >= +0: their maximum and the comparison below are taken
+  // on the bit patterns (exact_ops.cuh)
+  T ep = max_nonneg(max_nonneg(max_nonneg(f_m2, f_m1), f_0), f_p1);
   // lambda at ghost cells equals the adjacent physical cell (timestep.f90:227-282)
   long long cm = (q - 1 < 2) ? c : c - st;
   long long cp = (q > lq) ? c - st : c;
-  T lam = T(0.5) * (b.lam[cm] + b.lam[cp]);
+  T lam = mulhalf(b.lam[cm] + b.lam[cp]);
   T dis2 = (T)P.vis2 * ep;
   T dis4 = (T)P.vis4;
-  dis4 = fdimT(dis4, dis2);
+  dis4 = gt_nonneg(dis4, dis2) ? dis4 - dis2 : T(0);
   dis2 = dis2 * cd;
   dis4 = dis4 * cd;
-  // diw(q) = w(q)-w(q-1); diw(1) = diw(2); diw(ib) = diw(ie)
-  T wq[4][5];  // w at q-2, q-1, q, q+1 (enthalpy in slot 4)
-  const int lo = (q - 2 >= 0) ? 0 : 1;
-  const int hi = (q + 1 <= bq) ? 3 : 2;
-#pragma unroll
-  for (int a = 0; a < 4; a++) {
-    if (a < lo || a > hi) continue;
-    long long ca = c + (a - 2) * st;
-#pragma unroll
-    for (int v = 0; v < 4; v++) wq[a][v] = b.w[v * N + ca];
-    wq[a][4] = b.H[ca];
-  }
+  // diw(q) = w(q)-w(q-1), formed once per cell by the prep pass;
+  // diw(1) = diw(2); diw(ib) = diw(ie)
+  const T* Dl = b.dlt + (long long)(D * 5) * N;
   T out[5];
 #pragma unroll
   for (int v = 0; v < 5; v++) {
-    T d0 = wq[2][v] - wq[1][v];
-    T dm = (q - 1 == 1) ? d0 : wq[1][v] - wq[0][v];
-    T dp = (q + 1 == bq) ? d0 : wq[3][v] - wq[2][v];
-    T t3 = dp - T(2) * d0 + dm;
+    T d0 = Dl[v * N + c];
+    T dm = (q - 1 == 1) ? d0 : Dl[v * N + c - st];
+    T dp = (q + 1 == bq) ? d0 : Dl[v * N + c + st];
+    T t3 = dp - mul2(d0) + dm;
     out[v] = dis2 * d0 - dis4 * t3;
   }
   if (!P.matrix) {
@@ -520,8 +528,15 @@ __device__ __forceinline__ void face_dir(const DevBlock<T>& b, const PhysParams&
   } else {
     T ss[3] = {T(0), T(0), T(0)};
     ss[D] = (T)b.s[D];
-    T ff[5];
-    dflux_matrix((T)P.gamma, wq[1], wq[2], out, ss, ff);
+    T ff[5], wq1[5], wq2[5];  // w at q-1 and q, enthalpy in slot 4
+#pragma unroll
+    for (int v = 0; v < 4; v++) {
+      wq1[v] = b.w[v * N + c - st];
+      wq2[v] = b.w[v * N + c];
+    }
+    wq1[4] = b.H[c - st];
+    wq2[4] = b.H[c];
+    dflux_matrix((T)P.gamma, wq1, wq2, out, ss, ff);
 #pragma unroll
     for (int v = 0; v < 5; v++) out[v] = ff[v];
   }

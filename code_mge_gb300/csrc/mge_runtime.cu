@@ -406,8 +406,9 @@ void fill_view(Block& b, DevBlock<T>& d, void* scratch) {
   d.fp = sc + 16 * N;
   d.efs = sc + 19 * N;
   d.dfs = sc + 34 * N;
-  d.vt = sc + 49 * N;
-  d.vfs = sc + 53 * N;
+  d.dlt = sc + 49 * N;
+  d.vt = sc + 64 * N;
+  d.vfs = sc + 68 * N;
   d.hx = b.h[0];
   d.hy = b.h[1];
   d.hz = b.h[2];
@@ -757,9 +758,9 @@ int mge_commit(mge_ctx* c) {
     for (Block& b : L) maxN = std::max(maxN, b.N);
   }
   init_kernel_attributes();
-  // scratch: H(1) F(15) fp(3) efs(15) dfs(15) = 49 fields of the largest block,
-  // + vt(4) vfs(15) for Navier-Stokes
-  const size_t nsc = c->prm.eqntype == MGE_EQN_NS ? 68 : 49;
+  // scratch: H(1) F(15) fp(3) efs(15) dfs(15) dlt(15) = 64 fields of the
+  // largest block, + vt(4) vfs(15) for Navier-Stokes
+  const size_t nsc = c->prm.eqntype == MGE_EQN_NS ? 83 : 64;
   int rc = dalloc(c, &c->scratch, nsc * maxN);
   if (rc) return rc;
   c->allocs.pop_back();  // freed separately

@@ -81,7 +81,7 @@ def case_bytes(case):
     """Device bytes a case holds (fields, records, stage scratch)."""
     fine = max(s.dims[0] * s.dims[1] * s.dims[2] for L in case.levels for s in L)
     mixed = case.prm.precision == A.MGE_PREC_MIXED
-    tot = 49 * 8 * fine
+    tot = 64 * 8 * fine
     for li, L in enumerate(case.levels):
         esz = 4 if (mixed and li + 1 < len(case.levels)) else 8
         for s in L:
