@@ -60,7 +60,6 @@ struct DevBlock {
   const double* rec_area;   // [nmir] wall-face area
   T* rec_wsol;              // [nmir][5]
   T* rec_psol;              // [nmir]
-  T* rec_term;              // [nmir][50] stage terms of efluxb/dfluxb and the viscous wall
   const int32_t* tgt_off;   // [ntgt+1]
   const int32_t* tgt_ops;   // op = 2*m + role (0: cut cell, 1: neighbour)
   int bctype[6];

@@ -559,9 +559,10 @@ __device__ __forceinline__ void body_face(const DevBlock<T>& b, const PhysParams
 }
 
 // --------------------------------------------------------------- stage: cut-cell record terms
-// rec_term layout per record (40 values): [0,5) efluxb subtrahend,
+// Terms of one record (rec_terms fills 50 values): [0,5) efluxb subtrahend,
 // [5,10) first addend, [10,15) second addend, [15,20) X0, [20,25) Z0,
-// [25,30) X1, [30,35) Z1 (dfluxb: fw(t) = fw(t) - X; fw(t) = fw(t) + Z).
+// [25,30) X1, [30,35) Z1 (dfluxb: fw(t) = fw(t) - X; fw(t) = fw(t) + Z),
+// [40,45) and [45,50) the viscous wall face (NS).
 template <typename T>
 __device__ __forceinline__ void ceflux_axis(int D, const T* w, T p, T s, T* f) {
   T f0 = w[1 + D] * s;
@@ -791,15 +792,11 @@ __device__ __noinline__ void rec_terms(const DevBlock<T>& b, const PhysParams& P
 }
 
 // --------------------------------------------------------------- stage: combine + update
-template <typename T>
-__global__ void k_rec(DevBlock<T> b, PhysParams P, int dissip_on, T cd, unsigned* err) {
-  int m = blockIdx.x * blockDim.x + threadIdx.x;
-  if (m < b.nmir) rec_terms(b, P, dissip_on, cd, err, m, b.rec_term + 50LL * m);
-}
-
-// INLINE_REC: compute each record's terms here (one-launch euler) instead of
-// reading them from the record pass (per-phase launches)
-template <typename T, bool INLINE_REC>
+// Each cut-cell record's wall terms are formed here, by the thread of every
+// cell the record acts on.  Those threads read w and p of neighbouring cells,
+// so with records present the update cannot be done in this pass
+// (DEFER_UPDATE: the caller runs body_update after a barrier).
+template <typename T, bool DEFER_UPDATE>
 __device__ __forceinline__ void body_combine(const DevBlock<T>& b, const PhysParams& P, const StageArgs& A,
                                              unsigned* err, long long t) {
   const int nxl = b.nx, nyl = b.ny;
@@ -843,17 +840,11 @@ __device__ __forceinline__ void body_combine(const DevBlock<T>& b, const PhysPar
         vis[v] = a;
       }
       if (tg >= 0) {
-        T Rv[INLINE_REC ? 50 : 1];
+        T R[50];
         for (int o = b.tgt_off[tg]; o < b.tgt_off[tg + 1]; o++) {
           const int op = b.tgt_ops[o];
           if (op & 1) continue;
-          const T* R;
-          if (INLINE_REC) {
-            rec_terms(b, P, A.dissip_on, (T)A.cd, err, op >> 1, Rv);
-            R = Rv;
-          } else {
-            R = b.rec_term + 50LL * (op >> 1);
-          }
+          rec_terms(b, P, A.dissip_on, (T)A.cd, err, op >> 1, R);
 #pragma unroll
           for (int v = 0; v < 5; v++) {
             vis[v] = vis[v] - R[40 + v];
@@ -877,16 +868,10 @@ __device__ __forceinline__ void body_combine(const DevBlock<T>& b, const PhysPar
   if (tg >= 0) {
     // cut-cell wall faces, this cell's records in record order: efluxb on dw
     // (efluxb.f90:72-110) and dfluxb on fw (dfluxb.f90:47-420)
-    T Rl[INLINE_REC ? 50 : 1];
+    T R[50];
     for (int o = b.tgt_off[tg]; o < b.tgt_off[tg + 1]; o++) {
       const int op = b.tgt_ops[o];
-      const T* R;
-      if (INLINE_REC) {
-        rec_terms(b, P, A.dissip_on, (T)A.cd, err, op >> 1, Rl);
-        R = Rl;
-      } else {
-        R = b.rec_term + 50LL * (op >> 1);
-      }
+      rec_terms(b, P, A.dissip_on, (T)A.cd, err, op >> 1, R);
       if (!(op & 1)) {
 #pragma unroll
         for (int v = 0; v < 5; v++) {
@@ -937,9 +922,7 @@ __device__ __forceinline__ void body_combine(const DevBlock<T>& b, const PhysPar
   T de = mdiv((T)A.fn * vd, (T)b.vol, (T)b.rvol);
 #pragma unroll
   for (int v = 0; v < 5; v++) dwv[v] = de * dwv[v];
-  if (A.irs || INLINE_REC) {
-    // with the record terms computed inline, other threads of this pass
-    // still read w and p of this cell: the update waits for the barrier
+  if (A.irs || DEFER_UPDATE) {
 #pragma unroll
     for (int v = 0; v < 5; v++) b.dw[v * N + c] = dwv[v];
     return;
@@ -1480,9 +1463,17 @@ __global__ void k_bc_pass(DevBlock<T> b, PhysParams P, int pass) {
   if (t < bc_pass_items(b)) body_bc_pass(b, P, pass, t);
 }
 
-// bc_corner.f90:23-157 in one block: three dependent phases
+// bc_corner.f90:23-157: three dependent phases, each a set of independent
+// items (phase 0: edges along k and j, phase 1: edges along i, phase 2: the
+// eight corners); no item of a phase reads a cell another item of the same
+// phase writes
 template <typename T>
-__device__ void body_corner(const DevBlock<T>& b, const PhysParams& P) {
+__device__ __forceinline__ int corner_items(const DevBlock<T>& b, int phase) {
+  return phase == 0 ? 4 * (b.kl - 1) + 4 * (b.jl - 1) : (phase == 1 ? 4 * (b.ib + 1) : 8);
+}
+
+template <typename T>
+__device__ void body_corner_item(const DevBlock<T>& b, const PhysParams& P, int phase, int t) {
   const long long N = b.N;
   const int il = b.il, jl = b.jl, kl = b.kl, ie = b.ie, je = b.je, ke = b.ke;
   const T gamma = (T)P.gamma;
@@ -1495,8 +1486,7 @@ __device__ void body_corner(const DevBlock<T>& b, const PhysParams& P) {
     }
     b.p[d] = depvars(gamma, wv);
   };
-  // phase A: edges along k (k = 2..kl) and along j (j = 2..jl)
-  for (int t = threadIdx.x; t < 4 * (kl - 1) + 4 * (jl - 1); t += blockDim.x) {
+  if (phase == 0) {  // edges along k (k = 2..kl) and along j (j = 2..jl)
     if (t < 4 * (kl - 1)) {
       int k = 2 + t / 4, e = t % 4;
       if (e == 0) set3(C3(1, 1, k), C3(2, 1, k), C3(1, 2, k), C3(2, 2, k));
@@ -1511,22 +1501,15 @@ __device__ void body_corner(const DevBlock<T>& b, const PhysParams& P) {
       else if (e == 2) set3(C3(1, j, ke), C3(2, j, ke), C3(1, j, kl), C3(2, j, kl));
       else set3(C3(ie, j, ke), C3(il, j, ke), C3(ie, j, kl), C3(il, j, kl));
     }
-  }
-  __syncthreads();
-  // phase B: edges along i (i = 0..ib)
-  for (int t = threadIdx.x; t < 4 * (b.ib + 1); t += blockDim.x) {
+  } else if (phase == 1) {  // edges along i (i = 0..ib)
     int i = t / 4, e = t % 4;
     if (e == 0) set3(C3(i, 1, 1), C3(i, 1, 2), C3(i, 2, 1), C3(i, 2, 2));
     else if (e == 1) set3(C3(i, 1, ke), C3(i, 2, ke), C3(i, 1, kl), C3(i, 2, kl));
     else if (e == 2) set3(C3(i, je, 1), C3(i, je, 1), C3(i, jl, 2), C3(i, jl, 2));  // bc_corner.f90:120 as written
     else set3(C3(i, je, ke), C3(i, jl, ke), C3(i, je, kl), C3(i, jl, kl));
-  }
-  __syncthreads();
-  // phase C: the 8 corners
-  if (threadIdx.x < 8) {
-    int e = threadIdx.x;
+  } else {  // the 8 corners; each reads only edge cells
     long long d, a, bq, cq, dq;
-    switch (e) {
+    switch (t) {
       case 0: d = C3(1, 1, 1); a = C3(2, 1, 1); bq = C3(1, 2, 1); cq = C3(1, 1, 2); dq = C3(2, 2, 2); break;
       case 1: d = C3(1, 1, ke); a = C3(2, 1, ke); bq = C3(1, 2, ke); cq = C3(1, 1, kl); dq = C3(2, 2, kl); break;
       case 2: d = C3(1, je, 1); a = C3(2, je, 1); bq = C3(1, jl, 1); cq = C3(1, je, 2); dq = C3(2, jl, 2); break;
@@ -1537,18 +1520,37 @@ __device__ void body_corner(const DevBlock<T>& b, const PhysParams& P) {
       default: d = C3(ie, je, ke); a = C3(il, je, ke); bq = C3(ie, jl, ke); cq = C3(ie, je, kl); dq = C3(il, jl, kl); break;
     }
     T wv[5];
-    for (int v = 0; v < 5; v++)
+    for (int v = 0; v < 5; v++) {
       wv[v] = (b.w[v * N + a] + b.w[v * N + bq] + b.w[v * N + cq]) * T(2) / T(3) - b.w[v * N + dq];
-    // all eight read only edge cells, so the writes can follow the reads
-    __syncwarp(0xffu);
-    for (int v = 0; v < 5; v++) b.w[v * N + d] = wv[v];
+      b.w[v * N + d] = wv[v];
+    }
     b.p[d] = depvars(gamma, wv);
   }
 }
 
 template <typename T>
-__global__ void k_bc_corner(DevBlock<T> b, PhysParams P) {
-  body_corner(b, P);
+__global__ void k_bc_corner(DevBlock<T> b, PhysParams P, int phase) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < corner_items(b, phase)) body_corner_item(b, P, phase, t);
+}
+
+// the whole of bcond.f90 in one cooperative launch: the three face passes and
+// the three corner phases with a grid barrier between them
+template <typename T>
+__global__ void __launch_bounds__(256, 2) k_bcond_coop(DevBlock<T> b, PhysParams P) {
+  cg::grid_group g = cg::this_grid();
+  const long long gt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long gs = (long long)gridDim.x * blockDim.x;
+  const long long nf = bc_pass_items(b);
+  for (int pass = 0; pass < 3; pass++) {
+    for (long long t = gt; t < nf; t += gs) body_bc_pass(b, P, pass, t);
+    g.sync();
+  }
+  for (int phase = 0; phase < 3; phase++) {
+    const int n = corner_items(b, phase);
+    for (long long t = gt; t < n; t += gs) body_corner_item(b, P, phase, (int)t);
+    if (phase < 2) g.sync();
+  }
 }
 
 // --------------------------------------------------------------- residual norm (euler.f90:431-447)
@@ -1846,14 +1848,35 @@ __global__ void k_prep(DevBlock<T> b, PhysParams P, int dissip_on) {
   if (t < (long long)b.ie * b.je * b.ke) body_prep(b, P, dissip_on, t);
 }
 template <typename T>
-__global__ void k_face(DevBlock<T> b, PhysParams P, int dissip_on, T cd) {
+__global__ void __launch_bounds__(256, 3) k_face(DevBlock<T> b, PhysParams P, int dissip_on, T cd) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t < (long long)(b.ie - 1) * (b.je - 1) * (b.ke - 1)) body_face(b, P, dissip_on, cd, t);
 }
+// a stage without dissipation of the central scheme: only the convective
+// face fluxes efs(q) = 0.5*(F(q) + F(q-1)), the same expression as face_dir,
+// in a kernel small enough to keep the memory system busy
 template <typename T>
+__global__ void __launch_bounds__(256) k_face_conv(DevBlock<T> b) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int ex = b.ie - 1, ey = b.je - 1;
+  if (t >= (long long)ex * ey * (b.ke - 1)) return;
+  const int i = 2 + (int)(t % ex), j = 2 + (int)((t / ex) % ey), k = 2 + (int)(t / ((long long)ex * ey));
+  const long long N = b.N, c = cidx(b.Pi, b.Pj, i, j, k);
+  const bool on[3] = {j <= b.jl && k <= b.kl, i <= b.il && k <= b.kl, i <= b.il && j <= b.jl};
+  const long long sts[3] = {1, (long long)b.Pi, (long long)b.Pi * b.Pj};
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    if (!on[d]) continue;
+    const T* F = b.F + (long long)(d * 5) * N;
+    T* E = b.efs + (long long)(d * 5) * N;
+#pragma unroll
+    for (int v = 0; v < 5; v++) E[v * N + c] = mulhalf(F[v * N + c] + F[v * N + c - sts[d]]);
+  }
+}
+template <typename T, bool INLINE_REC>
 __global__ void k_combine(DevBlock<T> b, PhysParams P, StageArgs A, unsigned* err) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < (long long)b.nx * b.ny * b.nz) body_combine<T, false>(b, P, A, err, t);
+  if (t < (long long)b.nx * b.ny * b.nz) body_combine<T, INLINE_REC>(b, P, A, err, t);
 }
 template <typename T, typename TC, int D>
 __global__ void k_irs(DevBlock<T> b, IrsTables tb, TC bb) {
@@ -1962,8 +1985,11 @@ __global__ void __launch_bounds__(256, 2) k_euler_coop(DevBlock<T> b, PhysParams
       for (long long t = gt; t < nf; t += gs) body_bc_pass(b, P, pass, t);
       g.sync();
     }
-    if (blockIdx.x == 0) body_corner(b, P);
-    g.sync();
+    for (int phase = 0; phase < 3; phase++) {
+      const int n = corner_items(b, phase);
+      for (long long t = gt; t < n; t += gs) body_corner_item(b, P, phase, (int)t);
+      g.sync();
+    }
   }
   if (E.rt) {
     for (int part = blockIdx.x; part < E.npart; part += gridDim.x)
@@ -1995,12 +2021,23 @@ void launch_stage_part(int part, const DevBlock<T>& b, const PhysParams& P, cons
     k_prep<T><<<nblk(n1, TPB), TPB, 0, s>>>(b, P, A.dissip_on);
   } else if (part == 1) {
     long long n2 = (long long)(b.ie - 1) * (b.je - 1) * (b.ke - 1);
-    k_face<T><<<nblk(n2, TPB), TPB, 0, s>>>(b, P, A.dissip_on, (T)A.cd);
+    if (!A.dissip_on && P.distype == 0)
+      k_face_conv<T><<<nblk(n2, TPB), TPB, 0, s>>>(b);
+    else
+      k_face<T><<<nblk(n2, TPB), TPB, 0, s>>>(b, P, A.dissip_on, (T)A.cd);
   } else if (part == 2) {
-    if (b.nmir > 0) k_rec<T><<<nblk(b.nmir, 128), 128, 0, s>>>(b, P, A.dissip_on, (T)A.cd, err);
+    // the record terms are formed inside the combine pass (below): a separate
+    // launch over a few hundred records would be pure latency
   } else if (part == 3) {
     long long n3 = (long long)b.nx * b.ny * b.nz;
-    k_combine<T><<<nblk(n3, TPB), TPB, 0, s>>>(b, P, A, err);
+    if (b.nmir > 0) {
+      // with the record terms computed in place, other threads of the pass
+      // read w and p of a cell's neighbours, so the update is a launch of its own
+      k_combine<T, true><<<nblk(n3, TPB), TPB, 0, s>>>(b, P, A, err);
+      if (!A.irs && !A.lres) k_update<T><<<nblk(n3, TPB), TPB, 0, s>>>(b, P);
+    } else {
+      k_combine<T, false><<<nblk(n3, TPB), TPB, 0, s>>>(b, P, A, err);
+    }
   }
 }
 
@@ -2077,8 +2114,29 @@ template <typename T>
 void launch_bcond(const DevBlock<T>& b, const PhysParams& P, cudaStream_t s) {
   const long long n = 2LL * ((long long)(b.jb + 1) * (b.kb + 1) + (long long)(b.ib + 1) * (b.kb + 1) +
                              (long long)(b.ib + 1) * (b.jb + 1));
+  // one cooperative launch when every block it needs fits on the device at once
+  static int resident[64] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev >= 0 && dev < 64 && resident[dev] == 0) {
+    int nsm = 0, per = 0, coop = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_bcond_coop<T>, TPB, 0);
+    resident[dev] = (coop && per > 0) ? nsm * per : -1;
+  }
+  const int grid = (dev >= 0 && dev < 64) ? resident[dev] : -1;
+  if (grid > 0) {
+    const int need = (int)std::max<long long>(1, std::min<long long>(nblk(n, TPB), grid));
+    DevBlock<T> bb = b;
+    PhysParams pp = P;
+    void* args[] = {&bb, &pp};
+    if (cudaLaunchCooperativeKernel((void*)k_bcond_coop<T>, need, TPB, args, 0, s) == cudaSuccess) return;
+    cudaGetLastError();
+  }
   for (int pass = 0; pass < 3; pass++) k_bc_pass<T><<<nblk(n, TPB), TPB, 0, s>>>(b, P, pass);
-  k_bc_corner<T><<<1, 512, 0, s>>>(b, P);
+  for (int phase = 0; phase < 3; phase++)
+    k_bc_corner<T><<<phase == 2 ? 1 : nblk(4LL * (b.ib + b.jl + b.kl + 2), TPB), TPB, 0, s>>>(b, P, phase);
 }
 
 template <typename T>

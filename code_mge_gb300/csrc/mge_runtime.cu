@@ -60,7 +60,7 @@ struct Block {
   int32_t* cutmap = nullptr;
   int32_t *rec_i = nullptr, *rec_cloud = nullptr, *tgt_off = nullptr, *tgt_ops = nullptr;
   double *rec_coef = nullptr, *rec_nvec = nullptr, *rec_qb = nullptr, *rec_area = nullptr;
-  void *rec_wsol = nullptr, *rec_psol = nullptr, *rec_term = nullptr;
+  void *rec_wsol = nullptr, *rec_psol = nullptr;
   double* irs = nullptr;
   IrsTables tabs[3];
   double *rt_partial = nullptr, *rt_cur = nullptr, *forces = nullptr;
@@ -422,7 +422,7 @@ void fill_view(Block& b, DevBlock<T>& d, void* scratch) {
   d.m0 = b.m0;
   d.rec_i = b.rec_i; d.rec_cloud = b.rec_cloud; d.rec_coef = b.rec_coef; d.rec_nvec = b.rec_nvec;
   d.rec_qb = b.rec_qb; d.rec_area = b.rec_area; d.rec_wsol = (T*)b.rec_wsol; d.rec_psol = (T*)b.rec_psol;
-  d.rec_term = (T*)b.rec_term; d.tgt_off = b.tgt_off; d.tgt_ops = b.tgt_ops;
+  d.tgt_off = b.tgt_off; d.tgt_ops = b.tgt_ops;
   for (int f = 0; f < 6; f++) {
     d.bctype[f] = b.bctype[f];
     for (int q = 0; q < 3; q++) d.fnv[f][q] = b.fnv[f][q];
@@ -477,8 +477,7 @@ int commit_block(mge_ctx* c, Block& b, double* scratch) {
   if ((rc = dalloc(c, &b.rec_i, 8 * nma)) || (rc = dalloc(c, &b.rec_cloud, 24 * nma)) ||
       (rc = dalloc(c, &b.rec_coef, 8 * nma)) || (rc = dalloc(c, &b.rec_nvec, 3 * nma)) ||
       (rc = dalloc(c, &b.rec_qb, 3 * nma)) || (rc = dalloc(c, &b.rec_area, nma)) ||
-      (rc = valloc(c, &b.rec_wsol, 5 * nma, es)) || (rc = valloc(c, &b.rec_psol, nma, es)) ||
-      (rc = valloc(c, &b.rec_term, 50 * nma, es)))
+      (rc = valloc(c, &b.rec_wsol, 5 * nma, es)) || (rc = valloc(c, &b.rec_psol, nma, es)))
     return rc;
   CK(cudaMemcpy(b.rec_i, ri.data(), ri.size() * 4, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(b.rec_cloud, rcl.data(), rcl.size() * 4, cudaMemcpyHostToDevice));
@@ -939,7 +938,7 @@ int mge_set_precision(mge_ctx* c, int precision) {
       F fields[] = {{&b.w, 5 * N, true},  {&b.p, N, true},        {&b.ws, 5 * N, true},   {&b.wn, 5 * N, false},
                     {&b.dw, 5 * N, false}, {&b.fw, 5 * N, false}, {&b.wr, 5 * N, false}, {&b.qf, 5 * N, false},
                     {&b.vdtim, N, false}, {&b.lam, N, false},     {&b.rec_wsol, 5LL * nma, true},
-                    {&b.rec_psol, nma, true}, {&b.rec_term, 50LL * nma, false}, {&b.eps, 3 * N, false}};
+                    {&b.rec_psol, nma, true}, {&b.eps, 3 * N, false}};
       for (F& f : fields) {
         if (!*f.p) continue;  // not allocated for this context
         void* np = nullptr;
