@@ -60,6 +60,7 @@ struct DevBlock {
   const double* rec_area;   // [nmir] wall-face area
   T* rec_wsol;              // [nmir][5]
   T* rec_psol;              // [nmir]
+  T* rec_wall;              // [nmir][25] wall-side terms of the current stage (rec_wall_terms)
   const int32_t* tgt_off;   // [ntgt+1]
   const int32_t* tgt_ops;   // op = 2*m + role (0: cut cell, 1: neighbour)
   int bctype[6];
@@ -130,7 +131,8 @@ template <typename T> int launch_euler_coop(const DevBlock<T>& b, const PhysPara
 template <typename T> void launch_timestep(const DevBlock<T>& b, const PhysParams& P, unsigned* err, cudaStream_t s,
                                            bool aux32 = false);
 template <typename T> void launch_stage(const DevBlock<T>& b, const PhysParams& P, const StageArgs& A, unsigned* err,
-                                        cudaStream_t s);
+                                        cudaStream_t s, cudaStream_t side = nullptr, cudaEvent_t fork = nullptr,
+                                        cudaEvent_t join = nullptr);
 template <typename T> void launch_irs(const DevBlock<T>& b, const PhysParams& P, const IrsTables* tab, cudaStream_t s,
                                       bool aux32 = false, const int* variant = nullptr);
 template <typename T> void launch_stage_part(int part, const DevBlock<T>& b, const PhysParams& P, const StageArgs& A,

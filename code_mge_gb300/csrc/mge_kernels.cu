@@ -559,10 +559,17 @@ __device__ __forceinline__ void body_face(const DevBlock<T>& b, const PhysParams
 }
 
 // --------------------------------------------------------------- stage: cut-cell record terms
-// Terms of one record (rec_terms fills 50 values): [0,5) efluxb subtrahend,
-// [5,10) first addend, [10,15) second addend, [15,20) X0, [20,25) Z0,
-// [25,30) X1, [30,35) Z1 (dfluxb: fw(t) = fw(t) - X; fw(t) = fw(t) + Z),
-// [40,45) and [45,50) the viscous wall face (NS).
+// A record's corrections take dense face fluxes out and wall fluxes in.  The
+// wall side depends only on the state (w, p, H, lambda, wsol, psol), not on
+// this stage's face fluxes, so the record pass (rec_wall_terms) runs beside
+// the face pass, and the combine pass takes the dense side from efs/dfs/vfs
+// itself.  rec_wall holds per record (25 values):
+//   [0,5)   efluxb first addend, [5,10) second addend (efluxb.f90:72-110)
+//   [10,15) viscous wall stress term (NS)
+//   [15,20) dfluxb Z0: fs1 - fs2 (JST) or the Roe wall flux
+//   [20,25) dfluxb fs1 (solid on the + side) or fs2 (solid on the - side)
+// With X the dense differences, dfluxb.f90 applies fw(t) = fw(t) - X and then
+// fw(t) = fw(t) + Z at the cut cell (X0, Z0) and at its neighbour (X1, Z1).
 template <typename T>
 __device__ __forceinline__ void ceflux_axis(int D, const T* w, T p, T s, T* f) {
   T f0 = w[1 + D] * s;
@@ -576,8 +583,8 @@ __device__ __forceinline__ void ceflux_axis(int D, const T* w, T p, T s, T* f) {
 }
 
 template <typename T>
-__device__ __noinline__ void rec_terms(const DevBlock<T>& b, const PhysParams& P, int dissip_on, T cd, unsigned* err,
-                                       int m, T* R) {
+__device__ void rec_wall_terms(const DevBlock<T>& b, const PhysParams& P, int dissip_on, T cd, unsigned* err, int m) {
+  T* W = b.rec_wall + 25LL * m;
   const long long N = b.N;
   const int* ri = b.rec_i + 8 * m;
   int i = ri[0], j = ri[1], k = ri[2], id = ri[3], zz = ri[4];
@@ -595,7 +602,6 @@ __device__ __noinline__ void rec_terms(const DevBlock<T>& b, const PhysParams& P
   T f1[5], f2[5], f3[5];
   ceflux_axis<T>(D, wc, b.p[c], s, f1);
   ceflux_axis<T>(D, wsol, psol, s, f2);
-  const T* E = b.efs + (long long)(D * 5) * N;
   const bool plus = (id >= 4);  // solid on the + side
   long long cn = plus ? c - st : c + st;
   T wnb[5];
@@ -604,14 +610,11 @@ __device__ __noinline__ void rec_terms(const DevBlock<T>& b, const PhysParams& P
   for (int v = 0; v < 5; v++) {
     T fs = T(0.5) * (f1[v] + f2[v]);
     T fa = T(0.5) * (f1[v] + f3[v]);
-    R[v] = E[v * N + c] - E[v * N + c + st];
-    R[5 + v] = plus ? fa : fs;
-    R[10 + v] = plus ? fs : fa;
+    W[v] = plus ? fa : fs;
+    W[5 + v] = plus ? fs : fa;
   }
   if (!dissip_on) return;
-  const long long qn = plus ? c + st : c;  // the wall face's upper cell
   if (P.eqn_ns) {  // no-slip adiabatic wall face: normal gradients to the mirror state only
-    const T* V = b.vfs + (long long)(D * 5) * N;
     T u[3], ug[3], qbv[3] = {(T)b.rec_qb[3 * m], (T)b.rec_qb[3 * m + 1], (T)b.rec_qb[3 * m + 2]};
     const double hh[3] = {b.hx, b.hy, b.hz};
     for (int a = 0; a < 3; a++) {
@@ -628,33 +631,22 @@ __device__ __noinline__ void rec_terms(const DevBlock<T>& b, const PhysParams& P
     o[0] = T(0);
     for (int a = 0; a < 3; a++) o[1 + a] = S * tau[a];
     o[4] = S * (qbv[0] * tau[0] + qbv[1] * tau[1] + qbv[2] * tau[2]);
-    for (int v = 0; v < 5; v++) {
-      R[40 + v] = plus ? -V[v * N + qn] : V[v * N + qn];
-      R[45 + v] = plus ? -(cd * o[v]) : cd * o[v];
-    }
+    for (int v = 0; v < 5; v++) W[10 + v] = plus ? -(cd * o[v]) : cd * o[v];
   }
   if (P.distype != 0) {  // Roe: the wall face's upwind flux taken to the ghost state
-    const T* Dd = b.dfs + (long long)(D * 5) * N;
     T o[5];
     const T S = (T)fabs(b.s[D]);
     if (plus)
       roe_diss<T>(P, D, S, wc, b.p[c], wsol, psol, o);
     else
       roe_diss<T>(P, D, S, wsol, psol, wc, b.p[c], o);
-    for (int v = 0; v < 5; v++) {
-      R[15 + v] = plus ? -Dd[v * N + qn] : Dd[v * N + qn];
-      R[20 + v] = plus ? -(cd * o[v]) : cd * o[v];
-      R[25 + v] = T(0);
-      R[30 + v] = T(0);
-    }
+    for (int v = 0; v < 5; v++) W[15 + v] = plus ? -(cd * o[v]) : cd * o[v];
     return;
   }
   // dfluxb.f90:29-423; w(:,5) is the enthalpy here
   wsol[4] = wsol[4] + psol;
-  const T* Dd = b.dfs + (long long)(D * 5) * N;
   auto pp = [&](int a) -> T { return b.p[c + a * st]; };
   auto ww = [&](int a, int v) -> T { return v < 4 ? b.w[v * N + c + a * st] : b.H[c + a * st]; };
-  auto dd = [&](int a, int v) -> T { return Dd[v * N + c + a * st]; };
   auto lamc = [&](int a) -> T {
     // lambda with the ghost-copy rule of timestep.f90:227-282 along the record axis
     int q = (D == 0 ? i : (D == 1 ? j : k)) + a;
@@ -676,10 +668,6 @@ __device__ __noinline__ void rec_terms(const DevBlock<T>& b, const PhysParams& P
     dis4 = dis4 * cd;
   };
   if (plus) {
-    for (int v = 0; v < 5; v++) {
-      R[15 + v] = dd(0, v) - dd(1, v);
-      R[25 + v] = dd(-1, v) - dd(0, v);
-    }
     if (D == 0) {
       fp[0] = fabs(pp(-2) - T(2) * pp(-1) + pp(0)) / fabs(pp(-2) + T(2) * pp(-1) + pp(0));
       fp[1] = fabs(pp(-1) - T(2) * pp(0) + psol) / fabs(pp(-1) + T(2) * pp(0) + psol);
@@ -731,14 +719,10 @@ __device__ __noinline__ void rec_terms(const DevBlock<T>& b, const PhysParams& P
       for (int v = 0; v < 5; v++) fs1[v] = tmp[v];
     }
     for (int v = 0; v < 5; v++) {
-      R[20 + v] = fs1[v] - fs2[v];
-      R[30 + v] = dd(-1, v) - fs1[v];
+      W[15 + v] = fs1[v] - fs2[v];
+      W[20 + v] = fs1[v];
     }
   } else {
-    for (int v = 0; v < 5; v++) {
-      R[15 + v] = dd(0, v) - dd(1, v);
-      R[25 + v] = dd(1, v) - dd(2, v);
-    }
     fp[0] = fabs(pp(1) - T(2) * pp(0) + psol) / fabs(pp(1) + T(2) * pp(0) + psol);
     fp[1] = fabs(pp(2) - T(2) * pp(1) + pp(0)) / fabs(pp(2) + T(2) * pp(1) + pp(0));
     if (pos + 3 <= lim)
@@ -785,18 +769,33 @@ __device__ __noinline__ void rec_terms(const DevBlock<T>& b, const PhysParams& P
       for (int v = 0; v < 5; v++) fs1[v] = tmp[v];
     }
     for (int v = 0; v < 5; v++) {
-      R[20 + v] = fs1[v] - fs2[v];
-      R[30 + v] = fs2[v] - dd(2, v);
+      W[15 + v] = fs1[v] - fs2[v];
+      W[20 + v] = fs2[v];
     }
   }
 }
 
+template <typename T>
+__global__ void k_rec_wall(DevBlock<T> b, PhysParams P, int dissip_on, T cd, unsigned* err) {
+  int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m < b.nmir) rec_wall_terms(b, P, dissip_on, cd, err, m);
+}
+
+// the record's geometry: cell, axis stride, solid side
+template <typename T>
+__device__ __forceinline__ void rec_geom(const DevBlock<T>& b, int m, long long& c, long long& st, int& D, bool& plus) {
+  const int* ri = b.rec_i + 8 * m;
+  D = ri[4] - 1;
+  st = D == 0 ? 1 : (D == 1 ? (long long)b.Pi : (long long)b.Pi * b.Pj);
+  c = cidx(b.Pi, b.Pj, ri[0], ri[1], ri[2]);
+  plus = ri[3] >= 4;
+}
+
 // --------------------------------------------------------------- stage: combine + update
-// Each cut-cell record's wall terms are formed here, by the thread of every
-// cell the record acts on.  Those threads read w and p of neighbouring cells,
-// so with records present the update cannot be done in this pass
-// (DEFER_UPDATE: the caller runs body_update after a barrier).
-template <typename T, bool DEFER_UPDATE>
+// The cut-cell records act here in record order on the cell they touch: the
+// dense face pair out, the wall pair in, from this stage's face fluxes and
+// the record pass's wall terms (rec_wall_terms).
+template <typename T>
 __device__ __forceinline__ void body_combine(const DevBlock<T>& b, const PhysParams& P, const StageArgs& A,
                                              unsigned* err, long long t) {
   const int nxl = b.nx, nyl = b.ny;
@@ -840,15 +839,22 @@ __device__ __forceinline__ void body_combine(const DevBlock<T>& b, const PhysPar
         vis[v] = a;
       }
       if (tg >= 0) {
-        T R[50];
         for (int o = b.tgt_off[tg]; o < b.tgt_off[tg + 1]; o++) {
           const int op = b.tgt_ops[o];
           if (op & 1) continue;
-          rec_terms(b, P, A.dissip_on, (T)A.cd, err, op >> 1, R);
+          const int m = op >> 1;
+          long long cm, st;
+          int D;
+          bool plus;
+          rec_geom(b, m, cm, st, D, plus);
+          const T* V = b.vfs + (long long)(D * 5) * N;
+          const T* Wm = b.rec_wall + 25LL * m;
+          const long long qn = plus ? cm + st : cm;  // the wall face's upper cell
 #pragma unroll
           for (int v = 0; v < 5; v++) {
-            vis[v] = vis[v] - R[40 + v];
-            vis[v] = vis[v] + R[45 + v];
+            const T x = plus ? -V[v * N + qn] : V[v * N + qn];
+            vis[v] = vis[v] - x;
+            vis[v] = vis[v] + Wm[10 + v];
           }
         }
       }
@@ -868,23 +874,45 @@ __device__ __forceinline__ void body_combine(const DevBlock<T>& b, const PhysPar
   if (tg >= 0) {
     // cut-cell wall faces, this cell's records in record order: efluxb on dw
     // (efluxb.f90:72-110) and dfluxb on fw (dfluxb.f90:47-420)
-    T R[50];
     for (int o = b.tgt_off[tg]; o < b.tgt_off[tg + 1]; o++) {
       const int op = b.tgt_ops[o];
-      rec_terms(b, P, A.dissip_on, (T)A.cd, err, op >> 1, R);
-      if (!(op & 1)) {
+      const int m = op >> 1;
+      long long cm, st;
+      int D;
+      bool plus;
+      rec_geom(b, m, cm, st, D, plus);
+      const T* Wm = b.rec_wall + 25LL * m;
+      if (!(op & 1)) {  // efluxb on the cut cell: the dense face pair out, the wall pair in
+        const T* E = b.efs + (long long)(D * 5) * N;
 #pragma unroll
         for (int v = 0; v < 5; v++) {
-          dwv[v] = dwv[v] - R[v];
-          dwv[v] = dwv[v] + R[5 + v] - R[10 + v];
+          const T x = E[v * N + cm] - E[v * N + cm + st];
+          dwv[v] = dwv[v] - x;
+          dwv[v] = dwv[v] + Wm[v] - Wm[5 + v];
         }
       }
       if (A.dissip_on) {
-        const T* Rd = R + ((op & 1) ? 25 : 15);
+        const T* Dd = b.dfs + (long long)(D * 5) * N;
+        auto dd = [&](int a, int v) -> T { return Dd[v * N + cm + a * st]; };
 #pragma unroll
         for (int v = 0; v < 5; v++) {
-          fwv[v] = fwv[v] - Rd[v];
-          fwv[v] = fwv[v] + Rd[5 + v];
+          T x, z;
+          if (P.distype != 0) {  // Roe wall: the dense face out, the ghost-state flux in (neighbour: zeros)
+            const long long qn = plus ? cm + st : cm;
+            x = (op & 1) ? T(0) : (plus ? -Dd[v * N + qn] : Dd[v * N + qn]);
+            z = (op & 1) ? T(0) : Wm[15 + v];
+          } else if (!(op & 1)) {  // dfluxb X0, Z0
+            x = dd(0, v) - dd(1, v);
+            z = Wm[15 + v];
+          } else if (plus) {  // dfluxb X1, Z1, solid on the + side
+            x = dd(-1, v) - dd(0, v);
+            z = dd(-1, v) - Wm[20 + v];
+          } else {  // solid on the - side
+            x = dd(1, v) - dd(2, v);
+            z = Wm[20 + v] - dd(2, v);
+          }
+          fwv[v] = fwv[v] - x;
+          fwv[v] = fwv[v] + z;
         }
       }
     }
@@ -922,7 +950,7 @@ __device__ __forceinline__ void body_combine(const DevBlock<T>& b, const PhysPar
   T de = mdiv((T)A.fn * vd, (T)b.vol, (T)b.rvol);
 #pragma unroll
   for (int v = 0; v < 5; v++) dwv[v] = de * dwv[v];
-  if (A.irs || DEFER_UPDATE) {
+  if (A.irs) {
 #pragma unroll
     for (int v = 0; v < 5; v++) b.dw[v * N + c] = dwv[v];
     return;
@@ -1873,10 +1901,10 @@ __global__ void __launch_bounds__(256) k_face_conv(DevBlock<T> b) {
     for (int v = 0; v < 5; v++) E[v * N + c] = mulhalf(F[v * N + c] + F[v * N + c - sts[d]]);
   }
 }
-template <typename T, bool INLINE_REC>
+template <typename T>
 __global__ void k_combine(DevBlock<T> b, PhysParams P, StageArgs A, unsigned* err) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < (long long)b.nx * b.ny * b.nz) body_combine<T, INLINE_REC>(b, P, A, err, t);
+  if (t < (long long)b.nx * b.ny * b.nz) body_combine<T>(b, P, A, err, t);
 }
 template <typename T, typename TC, int D>
 __global__ void k_irs(DevBlock<T> b, IrsTables tb, TC bb) {
@@ -1956,8 +1984,9 @@ __global__ void __launch_bounds__(256, 2) k_euler_coop(DevBlock<T> b, PhysParams
     for (long long t = gt; t < nprep; t += gs) body_prep(b, P, A.dissip_on, t);
     g.sync();
     for (long long t = gt; t < nface; t += gs) body_face(b, P, A.dissip_on, (T)A.cd, t);
+    for (long long t = gt; t < b.nmir; t += gs) rec_wall_terms(b, P, A.dissip_on, (T)A.cd, E.err, (int)t);
     g.sync();
-    for (long long t = gt; t < ncell; t += gs) body_combine<T, true>(b, P, A, E.err, t);
+    for (long long t = gt; t < ncell; t += gs) body_combine<T>(b, P, A, E.err, t);
     g.sync();
     if (E.lres) return;
     if (A.irs && P.irs_kind == 1) {
@@ -1976,8 +2005,10 @@ __global__ void __launch_bounds__(256, 2) k_euler_coop(DevBlock<T> b, PhysParams
       for (long long t = gt; t < 5 * irs_lines<T, 2>(b); t += gs) body_irs<T, TA, 2>(b, E.tab[2], bb, t);
       g.sync();
     }
-    for (long long t = gt; t < ncell; t += gs) body_update(b, P, t);
-    g.sync();
+    if (A.irs) {
+      for (long long t = gt; t < ncell; t += gs) body_update(b, P, t);
+      g.sync();
+    }
     for (long long t = gt; t < b.nmir; t += gs) body_cutcell(b, P, E.err, (int)t);
     g.sync();
     for (int pass = 0; pass < 3; pass++) {
@@ -2026,24 +2057,32 @@ void launch_stage_part(int part, const DevBlock<T>& b, const PhysParams& P, cons
     else
       k_face<T><<<nblk(n2, TPB), TPB, 0, s>>>(b, P, A.dissip_on, (T)A.cd);
   } else if (part == 2) {
-    // the record terms are formed inside the combine pass (below): a separate
-    // launch over a few hundred records would be pure latency
+    if (b.nmir > 0) k_rec_wall<T><<<nblk(b.nmir, 64), 64, 0, s>>>(b, P, A.dissip_on, (T)A.cd, err);
   } else if (part == 3) {
     long long n3 = (long long)b.nx * b.ny * b.nz;
-    if (b.nmir > 0) {
-      // with the record terms computed in place, other threads of the pass
-      // read w and p of a cell's neighbours, so the update is a launch of its own
-      k_combine<T, true><<<nblk(n3, TPB), TPB, 0, s>>>(b, P, A, err);
-      if (!A.irs && !A.lres) k_update<T><<<nblk(n3, TPB), TPB, 0, s>>>(b, P);
-    } else {
-      k_combine<T, false><<<nblk(n3, TPB), TPB, 0, s>>>(b, P, A, err);
-    }
+    k_combine<T><<<nblk(n3, TPB), TPB, 0, s>>>(b, P, A, err);
   }
 }
 
+// One stage.  With a side stream and two events, the record pass runs on the
+// side stream beside the face pass (it needs only the prep pass's output);
+// the combine pass waits for both.
 template <typename T>
-void launch_stage(const DevBlock<T>& b, const PhysParams& P, const StageArgs& A, unsigned* err, cudaStream_t s) {
-  for (int part = 0; part < 4; part++) launch_stage_part<T>(part, b, P, A, err, s);
+void launch_stage(const DevBlock<T>& b, const PhysParams& P, const StageArgs& A, unsigned* err, cudaStream_t s,
+                  cudaStream_t side, cudaEvent_t fork, cudaEvent_t join) {
+  launch_stage_part<T>(0, b, P, A, err, s);
+  const bool beside = b.nmir > 0 && side && fork && join;
+  if (beside) {
+    cudaEventRecord(fork, s);
+    cudaStreamWaitEvent(side, fork, 0);
+    launch_stage_part<T>(2, b, P, A, err, side);
+    cudaEventRecord(join, side);
+  } else {
+    launch_stage_part<T>(2, b, P, A, err, s);
+  }
+  launch_stage_part<T>(1, b, P, A, err, s);
+  if (beside) cudaStreamWaitEvent(s, join, 0);
+  launch_stage_part<T>(3, b, P, A, err, s);
 }
 
 // the line-sweep variant: 0 = one thread per (line, variable) in global
@@ -2288,7 +2327,8 @@ void launch_forces(const DevBlock<T>& b, const double* origin, const double* h, 
 // explicit instantiations
 #define MGE_INST(T)                                                                                              \
   template void launch_timestep<T>(const DevBlock<T>&, const PhysParams&, unsigned*, cudaStream_t, bool);       \
-  template void launch_stage<T>(const DevBlock<T>&, const PhysParams&, const StageArgs&, unsigned*, cudaStream_t); \
+  template void launch_stage<T>(const DevBlock<T>&, const PhysParams&, const StageArgs&, unsigned*, cudaStream_t,     \
+                                cudaStream_t, cudaEvent_t, cudaEvent_t);                                               \
   template void launch_stage_part<T>(int, const DevBlock<T>&, const PhysParams&, const StageArgs&, unsigned*,       \
                                      cudaStream_t);                                                             \
   template void launch_irs_part<T>(int, const DevBlock<T>&, const PhysParams&, const IrsTables*, cudaStream_t,    \

@@ -60,7 +60,7 @@ struct Block {
   int32_t* cutmap = nullptr;
   int32_t *rec_i = nullptr, *rec_cloud = nullptr, *tgt_off = nullptr, *tgt_ops = nullptr;
   double *rec_coef = nullptr, *rec_nvec = nullptr, *rec_qb = nullptr, *rec_area = nullptr;
-  void *rec_wsol = nullptr, *rec_psol = nullptr;
+  void *rec_wsol = nullptr, *rec_psol = nullptr, *rec_wall = nullptr;
   double* irs = nullptr;
   IrsTables tabs[3];
   double *rt_partial = nullptr, *rt_cur = nullptr, *forces = nullptr;
@@ -86,6 +86,8 @@ struct mge_ctx {
   mge_params prm;
   int device = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t side = nullptr;                 // record pass beside the face pass
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   std::vector<std::vector<Block>> lv;
   std::string err;
   unsigned* d_err = nullptr;
@@ -225,7 +227,7 @@ void enqueue_euler(mge_ctx* c, Block& b, int mgl, int mlvl, bool lres, bool lfir
     launch_save_wn<T>(D, c->stream);
     for (int m = 1; m <= mstage; m++) {
       StageArgs A = stage_args(P, m, mgl, mlvl, lres, lfir);
-      launch_stage<T>(D, c->P, A, c->d_err, c->stream);
+      launch_stage<T>(D, c->P, A, c->d_err, c->stream, c->side, c->ev_fork, c->ev_join);
       if (lres) return;
       if (A.irs) launch_irs<T>(D, c->P, b.tabs, c->stream, b.aux32, b.irs_var);
       launch_cutcell<T>(D, c->P, c->d_err, c->stream);
@@ -422,7 +424,7 @@ void fill_view(Block& b, DevBlock<T>& d, void* scratch) {
   d.m0 = b.m0;
   d.rec_i = b.rec_i; d.rec_cloud = b.rec_cloud; d.rec_coef = b.rec_coef; d.rec_nvec = b.rec_nvec;
   d.rec_qb = b.rec_qb; d.rec_area = b.rec_area; d.rec_wsol = (T*)b.rec_wsol; d.rec_psol = (T*)b.rec_psol;
-  d.tgt_off = b.tgt_off; d.tgt_ops = b.tgt_ops;
+  d.rec_wall = (T*)b.rec_wall; d.tgt_off = b.tgt_off; d.tgt_ops = b.tgt_ops;
   for (int f = 0; f < 6; f++) {
     d.bctype[f] = b.bctype[f];
     for (int q = 0; q < 3; q++) d.fnv[f][q] = b.fnv[f][q];
@@ -477,7 +479,8 @@ int commit_block(mge_ctx* c, Block& b, double* scratch) {
   if ((rc = dalloc(c, &b.rec_i, 8 * nma)) || (rc = dalloc(c, &b.rec_cloud, 24 * nma)) ||
       (rc = dalloc(c, &b.rec_coef, 8 * nma)) || (rc = dalloc(c, &b.rec_nvec, 3 * nma)) ||
       (rc = dalloc(c, &b.rec_qb, 3 * nma)) || (rc = dalloc(c, &b.rec_area, nma)) ||
-      (rc = valloc(c, &b.rec_wsol, 5 * nma, es)) || (rc = valloc(c, &b.rec_psol, nma, es)))
+      (rc = valloc(c, &b.rec_wsol, 5 * nma, es)) || (rc = valloc(c, &b.rec_psol, nma, es)) ||
+      (rc = valloc(c, &b.rec_wall, 25 * nma, es)))
     return rc;
   CK(cudaMemcpy(b.rec_i, ri.data(), ri.size() * 4, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(b.rec_cloud, rcl.data(), rcl.size() * 4, cudaMemcpyHostToDevice));
@@ -617,6 +620,9 @@ int mge_init(const mge_params* prm, int device, mge_ctx** out) {
   c->device = device;
   cudaError_t e = cudaSetDevice(device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaMalloc(&c->d_err, sizeof(unsigned));
   if (e == cudaSuccess) e = cudaMemset(c->d_err, 0, sizeof(unsigned));
   if (e == cudaSuccess) e = cudaMallocHost(&c->h_err, sizeof(unsigned));
@@ -647,6 +653,9 @@ void mge_destroy(mge_ctx* c) {
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->ev_done) cudaEventDestroy(c->ev_done);
+  if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+  if (c->ev_join) cudaEventDestroy(c->ev_join);
+  if (c->side) cudaStreamDestroy(c->side);
   for (void* q : c->allocs) cudaFree(q);
   if (c->scratch) cudaFree(c->scratch);
   if (c->d_err) cudaFree(c->d_err);
@@ -938,7 +947,7 @@ int mge_set_precision(mge_ctx* c, int precision) {
       F fields[] = {{&b.w, 5 * N, true},  {&b.p, N, true},        {&b.ws, 5 * N, true},   {&b.wn, 5 * N, false},
                     {&b.dw, 5 * N, false}, {&b.fw, 5 * N, false}, {&b.wr, 5 * N, false}, {&b.qf, 5 * N, false},
                     {&b.vdtim, N, false}, {&b.lam, N, false},     {&b.rec_wsol, 5LL * nma, true},
-                    {&b.rec_psol, nma, true}, {&b.eps, 3 * N, false}};
+                    {&b.rec_psol, nma, true}, {&b.rec_wall, 25LL * nma, false}, {&b.eps, 3 * N, false}};
       for (F& f : fields) {
         if (!*f.p) continue;  // not allocated for this context
         void* np = nullptr;
