@@ -45,17 +45,20 @@ UNIT = "cell-updates/s"
 # 5-variable fields of 40 B): smoothing stages 11 fields, non-smoothing
 # stages 4 fields, 17 B of scalars per stage, 56 B for the time step.
 BYTES_PER_CELL_UPDATE_IRS = (11 + 4 + 11 + 4 + 11) * 40 + 5 * 17 + 56   # 1,781
-# Compulsory bytes per cell of one k_face launch as designed.  A stage with
-# dissipation reads the per-cell fluxes F (15), sensors (3), w(1:4)+H (5) and
-# lambda (1) and writes the convective and dissipative face fluxes (15 + 15):
-# 54 doubles.  A stage without it reads F and writes the convective face
-# fluxes: 30 doubles.  mge_kernel_times averages over the 5 stages.
-FACE_DOUBLES_DISSIP, FACE_DOUBLES_PLAIN = 54, 30
-
-
-def face_bytes_per_cell(prm):
-    on = sum(1 for m in range(prm.mstage) if prm.cdis[m] > 0.0)
-    return 8.0 * (on * FACE_DOUBLES_DISSIP + (prm.mstage - on) * FACE_DOUBLES_PLAIN) / prm.mstage
+# The roofline kernel is k_face on a stage with dissipation (stage 1), one
+# thread per cell of [2..ie]^3.  Compulsory bytes per cell: it reads the
+# per-cell fluxes F (15), sensors (3), the differences w(q)-w(q-1) (15) and
+# lambda (1), and writes the convective and dissipative face fluxes (15 + 15):
+# 64 doubles.
+FACE_DOUBLES_DISSIP = 64
+# From one ncu capture of that launch on the 128^3 sphere (2,146,689 cells):
+# DRAM read + write 1,111.8 MB = 517.9 B per cell, and 118.2 FP64
+# instructions (DADD + DMUL, no DFMA under --fmad=false) per cell.  Traffic
+# scales with the cells a launch covers.
+FACE_DRAM_BYTES_PER_CELL = 517.9
+FACE_FP64_PER_CELL = 118.2
+FP64_LANES_PER_SM_CYCLE = 2      # GB300: 2 FP64 thread-operations per SM per cycle
+GB300_SMS = 152
 LAUNCHES_PER_UPDATE = {"timestep": 1, "prep": 5, "face": 5, "rec": 5, "combine": 5, "irs_i": 3, "irs_j": 3,
                        "irs_k_update": 3, "cutcell": 5, "bcond": 5, "rtrms": 1}
 
@@ -284,9 +287,11 @@ def run_gpu(args):
     e2e = R.whole_job_rate(args.steps * cu, e2e_s)
 
     # per-kernel device times (CUDA events on the library stream), finest level
-    ms = np.zeros(len(A.KERNEL_KINDS))
+    nk = len(A.KERNEL_KINDS)
+    ms = np.zeros(nk + case.prm.mstage)
     lib.mge_kernel_times(cyc.ctx, L, 2, ms.ctypes.data_as(C.POINTER(C.c_double)), len(ms))
     kt = {k: float(ms[q]) for q, k in enumerate(A.KERNEL_KINDS)}
+    face_stage_ms = [float(x) for x in ms[nk:]]
     share = {k: kt[k] * LAUNCHES_PER_UPDATE[k] for k in kt}
     tot = sum(share.values()) or 1.0
     dom = max(share, key=share.get)
@@ -294,15 +299,13 @@ def run_gpu(args):
     ncell = case.finest_cells
     dims = sp.dims
     face_cells = (dims[0] - 3) * (dims[1] - 3) * (dims[2] - 3)
-    alg = face_bytes_per_cell(case.prm) * face_cells
-    achieved = alg / (kt["face"] * 1e-3) / 1e9 if kt["face"] > 0 else 0.0
-    traffic = None
-    tf = os.path.join(ROOT, "profiles", "ncu_traffic.json")
-    if os.path.exists(tf):
-        try:
-            traffic = json.load(open(tf)).get("k_face_bytes_per_launch_192")
-        except Exception:
-            traffic = None
+    t_face = face_stage_ms[0]                      # stage 1: dissipation on
+    alg = 8.0 * FACE_DOUBLES_DISSIP * face_cells
+    achieved = alg / (t_face * 1e-3) / 1e9 if t_face > 0 else 0.0
+    traffic = FACE_DRAM_BYTES_PER_CELL * face_cells
+    clk = (clocks.get("sm_mhz") or 2070.0) * 1e6
+    fp64_peak = FP64_LANES_PER_SM_CYCLE * GB300_SMS * clk
+    fp64_achieved = FACE_FP64_PER_CELL * face_cells / (t_face * 1e-3) if t_face > 0 else 0.0
     upd_ms = sum(kt[k] * LAUNCHES_PER_UPDATE[k] for k in kt)
     whole_update_gbs = BYTES_PER_CELL_UPDATE_IRS * ncell / (upd_ms * 1e-3) / 1e9 if upd_ms > 0 else 0.0
 
@@ -329,10 +332,15 @@ def run_gpu(args):
             "residual_last": res[-1] if res else None,
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(w_np.nbytes), "d2h_bytes_per_step": 8},
             "gpu_launches": None,
-            "roofline": {"bound": "hbm", "kernel": "k_face", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "algorithmic_bytes_per_launch": alg, "launch_ms": kt["face"],
-                         "frac": achieved / peak, "traffic": traffic, "peak_kind": pkind,
-                         "note": "GB300 FP64 issue rate, not HBM, bounds these kernels"},
+            "roofline": {"bound": "hbm", "kernel": "k_face (stage 1, dissipation on)", "achieved": achieved,
+                         "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                         "algorithmic_bytes_per_launch": alg, "launch_ms": t_face, "peak_kind": pkind,
+                         "note": "the FP64 issue rate, not HBM, bounds this kernel: see fp64_roofline"},
+            "fp64_roofline": {"kernel": "k_face (stage 1)", "achieved": fp64_achieved / 1e12,
+                              "peak": fp64_peak / 1e12, "unit": "T FP64 instr/s", "frac": fp64_achieved / fp64_peak,
+                              "fp64_per_cell": FACE_FP64_PER_CELL,
+                              "peak_basis": "2 FP64 thread-ops per SM per cycle x 152 SMs x median SM clock"},
+            "face_stage_ms": face_stage_ms,
             "whole_update_hbm": {"achieved_gbs": whole_update_gbs, "frac": whole_update_gbs / peak,
                                  "bytes_per_cell_update": BYTES_PER_CELL_UPDATE_IRS},
             "kernel_ms": kt, "kernel_share": {k: share[k] / tot for k in share}, "dominant_kernel": dom,

@@ -1347,7 +1347,7 @@ int mge_kernel_times(mge_ctx* c, int level, int reps, double* ms_out, int nout) 
   Block& b = *bp;
   const mge_params& P = c->prm;
   const int NK = 11;
-  double tot[NK] = {0};
+  double tot[NK] = {0}, face_stage[MGE_MAX_STAGE] = {0};
   int cnt[NK] = {0};
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
@@ -1382,13 +1382,16 @@ int mge_kernel_times(mge_ctx* c, int level, int reps, double* ms_out, int nout) 
       A.lres = 0;
       A.irs = (m % 2 != 0) && P.smoo > 0.0;
       A.vt = P.vt;
-      for (int part = 0; part < 4 && !rc; part++)
+      for (int part = 0; part < 4 && !rc; part++) {
+        const double before = tot[1 + part];
         rc = timed(1 + part, [&] {
           with_dev(b, [&](auto& D) {
             using T = typename std::remove_reference_t<decltype(D)>::value_type;
             launch_stage_part<T>(part, D, c->P, A, c->d_err, c->stream);
           });
         });
+        if (part == 1) face_stage[m - 1] += tot[2] - before;
+      }
       if (A.irs)
         for (int part = 0; part < 3 && !rc; part++)
           rc = timed(5 + part, [&] {
@@ -1412,6 +1415,7 @@ int mge_kernel_times(mge_ctx* c, int level, int reps, double* ms_out, int nout) 
   cudaEventDestroy(e1);
   if (rc) return rc;
   for (int q = 0; q < NK && q < nout; q++) ms_out[q] = cnt[q] ? tot[q] / cnt[q] : 0.0;
+  for (int m = 0; m < P.mstage && NK + m < nout; m++) ms_out[NK + m] = face_stage[m] / reps;
   return check_err(c);
 }
 

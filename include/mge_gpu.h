@@ -236,8 +236,9 @@ long long mge_launch_count(const mge_ctx* ctx);
 /* Profiling hook: run one timestep + full euler update on (level, 1) `reps`
  * times outside any graph, timing each kernel kind with CUDA events; writes
  * the average ms per launch of {timestep, prep, face, rec, combine, irs_i,
- * irs_j, irs_k_update, cutcell, bcond, rtrms} into ms_out[0..10].  Advances
- * the state of that level. */
+ * irs_j, irs_k_update, cutcell, bcond, rtrms} into ms_out[0..10] ("rec" is
+ * the cut-cell wall-term pass), and, when nout allows, the face pass of stage
+ * m into ms_out[10 + m].  Advances the state of that level. */
 int mge_kernel_times(mge_ctx* ctx, int level, int reps, double* ms_out, int nout);
 
 /* Residual norm rtrms (the quantity of euler.f90:431-447) of one block from
