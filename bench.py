@@ -309,6 +309,17 @@ def run_gpu(args):
     upd_ms = sum(kt[k] * LAUNCHES_PER_UPDATE[k] for k in kt)
     whole_update_gbs = BYTES_PER_CELL_UPDATE_IRS * ncell / (upd_ms * 1e-3) / 1e9 if upd_ms > 0 else 0.0
 
+    # solution output of the finest level (upload_solut.f90:203-237) through
+    # the C-ABI: device kernel, device-to-host copy of the 7 variables
+    prm = case.prm
+    p_tot = prm.p0 * (1.0 + 0.2 * prm.rm ** 2) ** 3.5
+    sol = np.zeros(7 * ncell)
+    nval = C.c_int(0)
+    t0 = time.perf_counter()
+    rc = lib.mge_upload_solut(cyc.ctx, L, 1, p_tot, sol.ctypes.data_as(C.POINTER(C.c_double)), sol.size,
+                              C.byref(nval))
+    solut_ms = 1e3 * (time.perf_counter() - t0) if rc == 0 else None
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         dt = time_cpu_oracle(case, threads=1, cycles=1)
@@ -341,6 +352,7 @@ def run_gpu(args):
                               "fp64_per_cell": FACE_FP64_PER_CELL,
                               "peak_basis": "2 FP64 thread-ops per SM per cycle x 152 SMs x median SM clock"},
             "face_stage_ms": face_stage_ms,
+            "upload_solut": {"ms": solut_ms, "cells": ncell, "d2h_bytes": int(sol.nbytes), "nval": nval.value},
             "whole_update_hbm": {"achieved_gbs": whole_update_gbs, "frac": whole_update_gbs / peak,
                                  "bytes_per_cell_update": BYTES_PER_CELL_UPDATE_IRS},
             "kernel_ms": kt, "kernel_share": {k: share[k] / tot for k in share}, "dominant_kernel": dom,

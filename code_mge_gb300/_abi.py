@@ -150,6 +150,7 @@ SIGNATURES = [
     ("get_rtrms", _i, [_vp, _i, _i, _i, _pd]),
     ("solve", _i, [_vp, C.POINTER(MgeSolveOpts), _pd, _i, C.POINTER(_i), C.POINTER(MgeForces)]),
     ("forces_compute", _i, [_vp, _i, C.POINTER(MgeSolveOpts), C.POINTER(MgeForces)]),
+    ("upload_solut", _i, [_vp, _i, _i, _d, _pd, C.c_size_t, C.POINTER(_i)]),
 ]
 
 # entry points only the product library has (mge_init also takes the device)
@@ -175,6 +176,10 @@ PRODUCT_ONLY = [
     ("set_precision", _i, [_vp, _i]),
     ("device_mem", _i, [_i, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
     ("residual_norm_noalloc", _i, [_vp, _vp, _vp, _i, _i, _i, _d, _i, _d, _vp, _vp]),
+    ("write_restart", _i, [_vp, C.c_char_p, C.POINTER(_i), _i]),
+    ("read_restart", _i, [_vp, C.c_char_p, C.POINTER(_i), _i]),
+    ("restart_format", C.c_longlong, [_i, _i, _i, _i, _pd, C.c_char_p, C.c_longlong]),
+    ("restart_parse", C.c_longlong, [C.c_char_p, C.c_longlong, _i, _i, _i, _i, _pd]),
 ]
 KERNEL_KINDS = ["timestep", "prep", "face", "rec", "combine", "irs_i", "irs_j", "irs_k_update", "cutcell", "bcond",
                 "rtrms"]
@@ -187,6 +192,7 @@ HEADER_SYMBOLS = [
     "mge_movfin", "mge_bc_overlap", "mge_get_rtrms", "mge_solve", "mge_forces_compute",
     "mge_cycle", "mge_cycle_async", "mge_cycle_poll", "mge_prolong_async", "mge_set_coop_ctas", "mge_device_mem", "mge_tuned", "mge_set_precision",
     "mge_coop_trace", "mge_last_cycle_ms", "mge_launch_count", "mge_kernel_times", "mge_residual_norm_noalloc", "mge_euler_partial", "mge_device_bytes", "mge_sync",
+    "mge_upload_solut", "mge_write_restart", "mge_read_restart", "mge_restart_format", "mge_restart_parse",
 ]
 
 

@@ -1,6 +1,6 @@
 """In-tree build of libmge_gpu.so for sm_103a (no CPU fallback exists).
 
-Two translation units are compiled in parallel with nvcc and linked into
+The sources are compiled in parallel with nvcc and linked into
 code_mge_gb300/_build/libmge_gpu.so.  The plain FP64 kernels are compiled
 with --fmad=false so that no multiply-add is contracted: each expression
 rounds exactly as the reference's Fortran evaluates it.
@@ -15,7 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libmge_gpu.so")
 ROOT = os.path.dirname(HERE)
-SOURCES = ["mge_kernels.cu", "mge_runtime.cu", "mge_noalloc.cu"]
+SOURCES = ["mge_kernels.cu", "mge_runtime.cu", "mge_noalloc.cu", "mge_restart.cpp"]
 HEADERS = ["mge_internal.h", "exact_ops.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "--fmad=false", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
@@ -39,7 +39,7 @@ def build(force=False, verbose=False):
     objs, jobs = [], []
     for s in SOURCES:
         src = os.path.join(CSRC, s)
-        obj = os.path.join(OUT_DIR, s.replace(".cu", ".o"))
+        obj = os.path.join(OUT_DIR, os.path.splitext(s)[0] + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + hdrs):
             jobs.append([_nvcc()] + ARCH + NVCC_FLAGS + ["-c", src, "-o", obj])

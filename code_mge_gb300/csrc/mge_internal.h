@@ -139,6 +139,8 @@ template <typename T> void launch_stage_part(int part, const DevBlock<T>& b, con
                                              unsigned* err, cudaStream_t s);
 template <typename T> void launch_irs_part(int part, const DevBlock<T>& b, const PhysParams& P, const IrsTables* tab,
                                            cudaStream_t s, bool aux32 = false, const int* variant = nullptr);
+template <typename T> void launch_solut(const DevBlock<T>& b, const PhysParams& P, double rm, double p_tot, int ns,
+                                        double* out, cudaStream_t s);
 template <typename T> void launch_cutcell(const DevBlock<T>& b, const PhysParams& P, unsigned* err, cudaStream_t s);
 template <typename T> void launch_bcond(const DevBlock<T>& b, const PhysParams& P, cudaStream_t s);
 template <typename T> void launch_rtrms(const DevBlock<T>& b, const PhysParams& P, int vt, double* partial,

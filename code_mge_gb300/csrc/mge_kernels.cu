@@ -1832,6 +1832,42 @@ __global__ void k_embed(DevBlock<TF> f, DevBlock<TC> c, Xfer X, double gamma) {
   f.p[q] = depvars((TF)gamma, wv);
 }
 
+// upload_solut.f90:203-237: the cell-centre output variables of the physical
+// cells, solut(2:il,2:jl,2:kl,1:nval) in Fortran order (nval 7, or 11 with
+// the NS energy and three zero gradients); the expressions in the
+// reference's order, in FP64 whatever the block's storage
+template <typename T>
+__global__ void k_solut(DevBlock<T> b, double gamma, double p0, double rm, double p_tot, int ns, double* out) {
+  const long long ncell = (long long)b.nx * b.ny * b.nz;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ncell) return;
+  const int i = 2 + (int)(t % b.nx), j = 2 + (int)((t / b.nx) % b.ny), k = 2 + (int)(t / ((long long)b.nx * b.ny));
+  const long long N = b.N, c = cidx(b.Pi, b.Pj, i, j, k);
+  const double rr = (double)b.w[c];
+  const double uu = (double)b.w[N + c] / rr;
+  const double vv = (double)b.w[2 * N + c] / rr;
+  const double ww = (double)b.w[3 * N + c] / rr;
+  const double re = (double)b.w[4 * N + c];
+  const double qq = 0.5 * (uu * uu + vv * vv + ww * ww) * rr;
+  double pp = (gamma - 1.0) * (re > qq ? re - qq : 0.0);  // dim(re, qq)
+  const double mm = sqrt((uu * uu + vv * vv + ww * ww) / gamma / pp * rr);
+  const double ptloss = pp * pow(1.0 + 0.2 * mm * mm, 3.5) / p_tot - 1.0;
+  pp = (pp / p0 - 1.0) * 2.0 / (gamma * rm * rm);
+  out[t] = rr;
+  out[ncell + t] = uu;
+  out[2 * ncell + t] = vv;
+  out[3 * ncell + t] = ww;
+  out[4 * ncell + t] = pp;
+  out[5 * ncell + t] = mm;
+  out[6 * ncell + t] = ptloss;
+  if (ns) {
+    out[7 * ncell + t] = re / rr;
+    out[8 * ncell + t] = 0.0;
+    out[9 * ncell + t] = 0.0;
+    out[10 * ncell + t] = 0.0;
+  }
+}
+
 // wall forces from the records (new): 7 sums, fixed order within one block
 template <typename T>
 __global__ void k_forces(DevBlock<T> b, double ox, double oy, double oz, double hx, double hy, double hz, double cx,
@@ -2033,6 +2069,14 @@ __global__ void __launch_bounds__(256, 2) k_euler_coop(DevBlock<T> b, PhysParams
 
 // =============================================================== launchers
 constexpr int TPB = 256;
+
+template <typename T>
+void launch_solut(const DevBlock<T>& b, const PhysParams& P, double rm, double p_tot, int ns, double* out,
+                  cudaStream_t s) {
+  const long long n = (long long)b.nx * b.ny * b.nz;
+  k_solut<T><<<nblk(n, TPB), TPB, 0, s>>>(b, P.gamma, P.p0, rm, p_tot, ns, out);
+}
+
 
 template <typename T>
 void launch_timestep(const DevBlock<T>& b, const PhysParams& P, unsigned* err, cudaStream_t s, bool aux32) {
@@ -2327,6 +2371,7 @@ void launch_forces(const DevBlock<T>& b, const double* origin, const double* h, 
 // explicit instantiations
 #define MGE_INST(T)                                                                                              \
   template void launch_timestep<T>(const DevBlock<T>&, const PhysParams&, unsigned*, cudaStream_t, bool);       \
+  template void launch_solut<T>(const DevBlock<T>&, const PhysParams&, double, double, int, double*, cudaStream_t); \
   template void launch_stage<T>(const DevBlock<T>&, const PhysParams&, const StageArgs&, unsigned*, cudaStream_t,     \
                                 cudaStream_t, cudaEvent_t, cudaEvent_t);                                               \
   template void launch_stage_part<T>(int, const DevBlock<T>&, const PhysParams&, const StageArgs&, unsigned*,       \

@@ -89,6 +89,7 @@ struct mge_ctx {
   cudaStream_t side = nullptr;                 // record pass beside the face pass
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   std::vector<std::vector<Block>> lv;
+  std::vector<std::pair<int, int>> order;  // (level, serial) in mge_add_block order
   std::string err;
   unsigned* d_err = nullptr;
   unsigned* h_err = nullptr;  // pinned
@@ -753,6 +754,7 @@ int mge_add_block(mge_ctx* c, const mge_block_desc* d, int level, int serial) {
       if (e != ax) fa *= d->h[e];
     t.area = d->area ? d->area[m] : fa;
   }
+  c->order.emplace_back(level, serial);
   return MGE_OK;
 }
 
@@ -1127,6 +1129,81 @@ int mge_get_rtrms(mge_ctx* c, int level, int serial, int ncyc, double* out) {
   Block* b = getb(c, level, serial);
   if (!b || !out) return MGE_ENOTFOUND;
   *out = (ncyc >= 0 && ncyc < (int)b->rtrms.size()) ? b->rtrms[ncyc] : 0.0;
+  return MGE_OK;
+}
+
+// upload_solut.f90:203-237 on the device: the output variables of one block's
+// physical cells, computed in the stage scratch and copied to the caller
+int mge_upload_solut(mge_ctx* c, int level, int serial, double p_tot, double* solut, size_t count, int* nval_out) {
+  Block* b = getb(c, level, serial);
+  if (!b || !c->committed) return MGE_ENOTFOUND;
+  const int ns = c->prm.eqntype == MGE_EQN_NS ? 1 : 0;
+  const int nval = ns ? 11 : 7;
+  if (nval_out) *nval_out = nval;
+  const size_t ncell = (size_t)b->nx * b->ny * b->nz;
+  if (!solut || count < nval * ncell) return fail(c, MGE_EBADCFG, "upload_solut: buffer too small");
+  CK(cudaSetDevice(c->device));
+  // the scratch holds at least 64 fields of the largest block: room for 11
+  with_dev(*b, [&](auto& D) {
+    using T = typename std::remove_reference_t<decltype(D)>::value_type;
+    launch_solut<T>(D, c->P, c->prm.rm, p_tot, ns, c->scratch, c->stream);
+  });
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(solut, c->scratch, nval * ncell * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return check_err(c);
+}
+
+// write_solut / read_solut (wsolut.f90:49-92, rsolut.f90:1-41): every block
+// of the context, in mge_add_block order, as the reference's restart text.
+// codes[q] is the block code of the q-th block added (ncodes = 0: 1, 2, ...).
+int mge_write_restart(mge_ctx* c, const char* path, const int* codes, int ncodes) {
+  if (!c || !c->committed || !path) return MGE_EBADCFG;
+  if (ncodes != 0 && (ncodes != (int)c->order.size() || !codes)) return fail(c, MGE_EBADCFG, "write_restart: codes");
+  FILE* f = std::fopen(path, "w");
+  if (!f) return fail(c, MGE_EBADCFG, std::string("write_restart: cannot open ") + path);
+  int rc = MGE_OK;
+  std::vector<double> w, p;
+  std::vector<char> text;
+  for (size_t q = 0; q < c->order.size() && !rc; q++) {
+    Block* b = getb(c, c->order[q].first, c->order[q].second);
+    w.resize(5 * b->N);
+    p.resize(b->N);
+    rc = mge_download_state(c, c->order[q].first, c->order[q].second, w.data(), p.data());
+    if (rc) break;
+    const int code = ncodes ? codes[q] : (int)q + 1;
+    const long long need = mge_restart_format(code, b->ib, b->jb, b->kb, w.data(), nullptr, 0);
+    text.resize((size_t)need + 1);
+    mge_restart_format(code, b->ib, b->jb, b->kb, w.data(), text.data(), need + 1);
+    if (std::fwrite(text.data(), 1, (size_t)need, f) != (size_t)need) rc = fail(c, MGE_EBADCFG, "write_restart: write");
+  }
+  std::fclose(f);
+  return rc;
+}
+
+int mge_read_restart(mge_ctx* c, const char* path, const int* codes, int ncodes) {
+  if (!c || !c->committed || !path) return MGE_EBADCFG;
+  if (ncodes != 0 && (ncodes != (int)c->order.size() || !codes)) return fail(c, MGE_EBADCFG, "read_restart: codes");
+  FILE* f = std::fopen(path, "r");
+  if (!f) return fail(c, MGE_EBADCFG, std::string("read_restart: cannot open ") + path);
+  std::string text;
+  char chunk[1 << 16];
+  size_t got;
+  while ((got = std::fread(chunk, 1, sizeof chunk, f)) > 0) text.append(chunk, got);
+  std::fclose(f);
+  long long pos = 0;
+  std::vector<double> w;
+  for (size_t q = 0; q < c->order.size(); q++) {
+    Block* b = getb(c, c->order[q].first, c->order[q].second);
+    w.resize(5 * b->N);
+    const int code = ncodes ? codes[q] : (int)q + 1;
+    const long long used =
+        mge_restart_parse(text.data() + pos, (long long)text.size() - pos, code, b->ib, b->jb, b->kb, w.data());
+    if (used < 0) return fail(c, MGE_EBADCFG, "read_restart: inconsistent file dof & grid dimension (rsolut.f90:27-32)");
+    pos += used;
+    int rc = mge_upload_state(c, c->order[q].first, c->order[q].second, w.data());
+    if (rc) return rc;
+  }
   return MGE_OK;
 }
 

@@ -157,6 +157,30 @@ module mge_gpu_mod
       type(mge_solve_opts), intent(in) :: opts
       type(mge_forces), intent(out) :: forces
     end function
+    integer(c_int) function mge_upload_solut(ctx, level, serial, p_tot, solut, count, nval_out) &
+        bind(C, name="mge_upload_solut")
+      import :: c_int, c_ptr, c_double, c_size_t
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: level, serial
+      real(c_double), value :: p_tot
+      real(c_double), intent(out) :: solut(*)        ! solut(2:il,2:jl,2:kl,1:nval)
+      integer(c_size_t), value :: count
+      integer(c_int), intent(out) :: nval_out
+    end function
+    integer(c_int) function mge_write_restart(ctx, path, codes, ncodes) bind(C, name="mge_write_restart")
+      import :: c_int, c_ptr, c_char
+      type(c_ptr), value :: ctx
+      character(kind=c_char), intent(in) :: path(*)  ! NUL-terminated
+      integer(c_int), intent(in) :: codes(*)
+      integer(c_int), value :: ncodes
+    end function
+    integer(c_int) function mge_read_restart(ctx, path, codes, ncodes) bind(C, name="mge_read_restart")
+      import :: c_int, c_ptr, c_char
+      type(c_ptr), value :: ctx
+      character(kind=c_char), intent(in) :: path(*)
+      integer(c_int), intent(in) :: codes(*)
+      integer(c_int), value :: ncodes
+    end function
     integer(c_int) function mge_residual_norm_noalloc(dw_rho, vdtim, blank, nx, ny, nz, cfl, vt, dtim, &
         norm_out, stream) bind(C, name="mge_residual_norm_noalloc")
       import :: c_int, c_ptr, c_double

@@ -257,6 +257,34 @@ int mge_residual_norm_noalloc(const double* dw_rho, const double* vdtim, const i
                               int nx, int ny, int nz, double cfl, int vt, double dtim,
                               double* norm_out, void* stream);
 
+/* upload_solut.f90:203-237 (blk2mgrid.f90:14-26 calls it per block): the
+ * cell-centre output variables rho, u, v, w, cp, mach, pt-loss of the
+ * physical cells (Navier-Stokes adds the energy and three zero gradients),
+ * computed on the device in FP64 and copied into
+ * solut(2:il,2:jl,2:kl,1:nval), Fortran order.  *nval_out = 7 or 11;
+ * count >= nval*nx*ny*nz.  p_tot: the free-stream total pressure the
+ * reference's pt-loss is relative to. */
+int mge_upload_solut(mge_ctx* ctx, int level, int serial, double p_tot, double* solut,
+                     size_t count, int* nval_out);
+
+/* write_solut / read_solut (wsolut.f90:49-92, rsolut.f90:1-41): every block
+ * of the context, in mge_add_block order, as the reference's restart text:
+ * "(5I5)" code, low(1:4), upp(1:4), then "(5f16.7)" w(0:ib,0:jb,0:kb,1:5).
+ * codes[q] is the code of the q-th block added (ncodes = 0: codes 1..n).
+ * Reading checks each block's code and upper bounds (the reference stops on a
+ * mismatch: MGE_EBADCFG here) and uploads the state. */
+int mge_write_restart(mge_ctx* ctx, const char* path, const int* codes, int ncodes);
+int mge_read_restart(mge_ctx* ctx, const char* path, const int* codes, int ncodes);
+
+/* The same text for one block, without a context or a GPU: returns the bytes
+ * of the text (writing at most cap-1 of them and a NUL into buf when buf is
+ * not null); and the parse of one block from text, returning the bytes it
+ * consumed or a negative MGE_E* code. */
+long long mge_restart_format(int code, int ib, int jb, int kb, const double* w, char* buf,
+                             long long cap);
+long long mge_restart_parse(const char* text, long long len, int code, int ib, int jb, int kb,
+                            double* w);
+
 /* Cut-cell wall force integration on the finest level (R-FORCE, new). */
 int mge_forces_compute(mge_ctx* ctx, int level, const mge_solve_opts* opts,
                        mge_forces* out);

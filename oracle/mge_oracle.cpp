@@ -2007,6 +2007,52 @@ int mgeo_get_rtrms(mgeo_ctx* c, int level, int serial, int ncyc, double* out) {
   return MGE_OK;
 }
 
+/* upload_solut.f90:203-237 (called per block by blk2mgrid.f90:14-26): the
+   cell-centre output variables rho, u, v, w, cp, mach, pt-loss (NS adds the
+   energy re/rr and three zero gradients) of the physical cells, as
+   solut(2:il,2:jl,2:kl,1:nval) in Fortran order */
+int mgeo_upload_solut(mgeo_ctx* c, int level, int serial, double p_tot, double* out, size_t count, int* nval_out) {
+  OBlock* b = getb(c, level, serial);
+  if (!b) return MGE_ENOTFOUND;
+  const mge_params& P = c->prm;
+  const bool ns = P.eqntype == MGE_EQN_NS;
+  const int nval = ns ? 11 : 7;
+  if (nval_out) *nval_out = nval;
+  const size_t nx = b->il - 1, ny = b->jl - 1, nz = b->kl - 1, ncell = nx * ny * nz;
+  if (!out || count < nval * ncell) return MGE_EBADCFG;
+  const double gamma = P.gamma;
+  for (int k = 2; k <= b->kl; k++)
+    for (int j = 2; j <= b->jl; j++)
+      for (int i = 2; i <= b->il; i++) {
+        const size_t q = b->I(i, j, k);
+        const double rr = b->w[q];
+        const double uu = b->w[b->N + q] / rr;
+        const double vv = b->w[2 * b->N + q] / rr;
+        const double ww = b->w[3 * b->N + q] / rr;
+        const double re = b->w[4 * b->N + q];
+        const double qq = 0.5 * (uu * uu + vv * vv + ww * ww) * rr;
+        double pp = (gamma - 1.0) * fdim_(re, qq);
+        const double mm = std::sqrt((uu * uu + vv * vv + ww * ww) / gamma / pp * rr);
+        const double ptloss = pp * std::pow(1.0 + 0.2 * mm * mm, 3.5) / p_tot - 1.0;
+        pp = (pp / P.p0 - 1.0) * 2.0 / (gamma * P.rm * P.rm);
+        const size_t t = (i - 2) + nx * ((j - 2) + ny * (size_t)(k - 2));
+        out[t] = rr;
+        out[ncell + t] = uu;
+        out[2 * ncell + t] = vv;
+        out[3 * ncell + t] = ww;
+        out[4 * ncell + t] = pp;
+        out[5 * ncell + t] = mm;
+        out[6 * ncell + t] = ptloss;
+        if (ns) {
+          out[7 * ncell + t] = re / rr;
+          out[8 * ncell + t] = 0.0;
+          out[9 * ncell + t] = 0.0;
+          out[10 * ncell + t] = 0.0;
+        }
+      }
+  return MGE_OK;
+}
+
 int mgeo_forces_compute(mgeo_ctx* c, int level, const mge_solve_opts* o, mge_forces* out) {
   if (level < 1 || level > (int)c->lv.size()) return MGE_ENOTFOUND;
   double F[3] = {0, 0, 0}, M[3] = {0, 0, 0};
