@@ -77,6 +77,8 @@ class MgeParams(C.Structure):
         ("nlevel", _i),
         ("mcyc", _i * MGE_MAX_LEVEL),
         ("conv_drop", _d),
+        ("execmode", _i),
+        ("dtstep", _d),
     ]
 
 
@@ -151,6 +153,7 @@ SIGNATURES = [
     ("solve", _i, [_vp, C.POINTER(MgeSolveOpts), _pd, _i, C.POINTER(_i), C.POINTER(MgeForces)]),
     ("forces_compute", _i, [_vp, _i, C.POINTER(MgeSolveOpts), C.POINTER(MgeForces)]),
     ("upload_solut", _i, [_vp, _i, _i, _d, _pd, C.c_size_t, C.POINTER(_i)]),
+    ("time_advance", _i, [_vp, C.POINTER(_i)]),
 ]
 
 # entry points only the product library has (mge_init also takes the device)
@@ -193,6 +196,7 @@ HEADER_SYMBOLS = [
     "mge_cycle", "mge_cycle_async", "mge_cycle_poll", "mge_prolong_async", "mge_set_coop_ctas", "mge_device_mem", "mge_tuned", "mge_set_precision",
     "mge_coop_trace", "mge_last_cycle_ms", "mge_launch_count", "mge_kernel_times", "mge_residual_norm_noalloc", "mge_euler_partial", "mge_device_bytes", "mge_sync",
     "mge_upload_solut", "mge_write_restart", "mge_read_restart", "mge_restart_format", "mge_restart_parse",
+    "mge_time_advance",
 ]
 
 

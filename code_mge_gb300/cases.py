@@ -251,7 +251,7 @@ def params(mach, alpha_deg=0.0, beta_deg=0.0, gamma=1.4, cfl=-2.8, vis2=0.5, vis
            cstp=(0.25, 1.0 / 6.0, 0.375, 0.5, 1.0), cdis=(1.0, 0.0, 0.56, 0.0, 0.44), mgtype=1,
            nlevel=3, mcyc=None, eqntype=A.MGE_EQN_EULER, distype=A.MGE_DIS_CENTRAL,
            dissip=A.MGE_DISSIP_SCALAR, precision=A.MGE_PREC_FP64, irs_variant=0, conv_drop=1.0e6,
-           reynolds=None, prandtl=0.72, limfac=5.0, epsentr=0.05):
+           reynolds=None, prandtl=0.72, limfac=5.0, epsentr=0.05, execmode=0, dtstep=None):
     """mge_params as input_param.f90:17-114 derives them from a job sheet."""
     p = A.MgeParams()
     p.mstage = len(cstp)
@@ -297,6 +297,10 @@ def params(mach, alpha_deg=0.0, beta_deg=0.0, gamma=1.4, cfl=-2.8, vis2=0.5, vis
     for q in range(nlevel):
         p.mcyc[q] = int(mc[q])
     p.conv_drop = conv_drop
+    # unsteady dual time stepping: dtstep non-dimensional; the reference's
+    # default for NS is u0/ref_leng/5 (input_param.f90:93-96)
+    p.execmode = execmode
+    p.dtstep = dtstep if dtstep is not None else (p.u0 / ref_leng / 5.0 if execmode == 1 else 0.0)
     return p
 
 

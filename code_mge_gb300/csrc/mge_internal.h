@@ -22,6 +22,8 @@ struct DevBlock {
   T* w;                     // 5N conservative variables
   T* p;                     // N pressure
   T* wn;                    // 5N state at the start of euler
+  T* w1;                    // 5N state of the previous physical time step (unsteady only, else null)
+  T* w2;                    // 5N state of the one before
   T* ws;                    // 5N state saved on first coarse entry
   T* dw;                    // 5N residual
   T* fw;                    // 5N blended dissipation
@@ -78,6 +80,7 @@ struct StageArgs {
   int lres;
   int irs;          // odd stage with smoo > 0: defer the update to the line sweeps
   int vt;
+  int tmode;        // unsteady source term: 0 none, 1 first step (itime 1), 2 BDF2 (itime > 1)
 };
 
 struct PhysParams {
@@ -92,6 +95,8 @@ struct PhysParams {
   int vt;                   // global time step
   int distype;              // MGE_DIS_* (0 central, 1 Roe first order, 2 Roe MUSCL)
   int irs_kind;             // 0 psmoo_old (what euler calls), 1 psmoo + progon3
+  int unsteady;             // execmode 1: dual time stepping
+  double dtstep;            // physical time step
   double viscl, kt, gas_const, prlmean;  // laminar viscosity, heat conductivity, R, Pr
   double cfac;              // viscous weight of the time step (timestep.f90:119-125)
   double epsentr;           // Harten entropy fix
@@ -134,11 +139,13 @@ template <typename T> void launch_stage(const DevBlock<T>& b, const PhysParams& 
                                         cudaStream_t s, cudaStream_t side = nullptr, cudaEvent_t fork = nullptr,
                                         cudaEvent_t join = nullptr);
 template <typename T> void launch_irs(const DevBlock<T>& b, const PhysParams& P, const IrsTables* tab, cudaStream_t s,
-                                      bool aux32 = false, const int* variant = nullptr);
+                                      bool aux32 = false, const int* variant = nullptr,
+                                      const StageArgs* A = nullptr);
 template <typename T> void launch_stage_part(int part, const DevBlock<T>& b, const PhysParams& P, const StageArgs& A,
                                              unsigned* err, cudaStream_t s);
 template <typename T> void launch_irs_part(int part, const DevBlock<T>& b, const PhysParams& P, const IrsTables* tab,
-                                           cudaStream_t s, bool aux32 = false, const int* variant = nullptr);
+                                           cudaStream_t s, bool aux32 = false, const int* variant = nullptr,
+                                           const StageArgs* A = nullptr);
 template <typename T> void launch_solut(const DevBlock<T>& b, const PhysParams& P, double rm, double p_tot, int ns,
                                         double* out, cudaStream_t s);
 template <typename T> void launch_cutcell(const DevBlock<T>& b, const PhysParams& P, unsigned* err, cudaStream_t s);

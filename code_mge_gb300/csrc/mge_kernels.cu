@@ -118,6 +118,10 @@ __device__ __forceinline__ unsigned long long body_timestep(const DevBlock<T>& b
   TC dpj = fabs((pjp - p2 + pjm) / (pjp + p2 + pjm + plim));
   TC dpk = fabs((pkp - p2 + pkm) / (pkp + p2 + pkm + plim));
   TC r = TC(1) / (TC(1) + fminT((TC)P.dimcfl, TC(2) * (dpi + dpj + dpk)));
+  if (P.unsteady) {  // timestep.f90:85-99,180-190: at most 2*dtstep/(3*cfl)
+    const TC dtime = (TC(2) * (TC)P.dtstep) / (TC(3) * (TC)P.cfl);
+    fict = fict < dtime ? fict : dtime;
+  }
   TC vd = fict * r;
   double vdd = (double)vd;
   if (vdd >= 0.0) mine = (unsigned long long)__double_as_longlong(vdd);
@@ -792,6 +796,16 @@ __device__ __forceinline__ void rec_geom(const DevBlock<T>& b, int m, long long&
 }
 
 // --------------------------------------------------------------- stage: combine + update
+// euler.f90:320-331,387-391: the unsteady mode's factor lam = 1 + 3*de/(2*dtstep)
+// with de = fn*vdtim (or fn*dtim), dividing the coarse-level residual and the
+// finest level's update
+template <typename T>
+__device__ __forceinline__ T unsteady_lam(const DevBlock<T>& b, const PhysParams& P, const StageArgs& A, long long c) {
+  const T vd = A.vt ? (T)(*b.dtim) : b.vdtim[c];
+  const T de = (T)A.fn * vd;
+  return T(1) + ((de * T(3)) / T(2)) / (T)P.dtstep;
+}
+
 // The cut-cell records act here in record order on the cell they touch: the
 // dense face pair out, the wall pair in, from this stage's face fluxes and
 // the record pass's wall terms (rec_wall_terms).
@@ -923,6 +937,15 @@ __device__ __forceinline__ void body_combine(const DevBlock<T>& b, const PhysPar
   }
 #pragma unroll
   for (int v = 0; v < 5; v++) dwv[v] = dwv[v] + fwv[v];
+  if (A.tmode) {  // euler.f90:249-275: BDF2, or the first step's (halved) BDF1
+    const T f = (T(0.5) * (T)b.vol) / (T)P.dtstep;
+#pragma unroll
+    for (int v = 0; v < 5; v++) {
+      const T wv = b.w[v * N + c], w1 = b.w1[v * N + c];
+      const T d = A.tmode == 2 ? (T(3) * wv - T(4) * w1) + b.w2[v * N + c] : wv - w1;
+      dwv[v] = dwv[v] + f * d;
+    }
+  }
   if (A.forcing) {  // euler.f90:294-318
 #pragma unroll
     for (int v = 0; v < 5; v++) {
@@ -935,6 +958,11 @@ __device__ __forceinline__ void body_combine(const DevBlock<T>& b, const PhysPar
         q = b.qf[v * N + c];
       }
       dwv[v] = dwv[v] + q;
+    }
+    if (P.unsteady) {
+      const T lam = unsteady_lam(b, P, A, c), rl = T(1) / lam;
+#pragma unroll
+      for (int v = 0; v < 5; v++) dwv[v] = mdiv(dwv[v], lam, rl);
     }
   }
   const T bl = (T)b.blank[c];
@@ -955,11 +983,13 @@ __device__ __forceinline__ void body_combine(const DevBlock<T>& b, const PhysPar
     for (int v = 0; v < 5; v++) b.dw[v * N + c] = dwv[v];
     return;
   }
-  // update, euler.f90:381-399 (steady: lam = 1)
+  // update, euler.f90:381-399 (steady: lam = 1, and dw/1 is dw)
   T wv[5];
+  const bool ulam = P.unsteady && !A.forcing;
+  const T lam = ulam ? unsteady_lam(b, P, A, c) : T(1), rl = ulam ? T(1) / lam : T(1);
 #pragma unroll
   for (int v = 0; v < 5; v++) {
-    wv[v] = b.wn[v * N + c] - dwv[v];
+    wv[v] = b.wn[v * N + c] - (ulam ? mdiv(dwv[v], lam, rl) : dwv[v]);
     b.w[v * N + c] = wv[v];
     b.dw[v * N + c] = dwv[v];
   }
@@ -1259,16 +1289,20 @@ __global__ void k_psmoo_line(DevBlock<T> b) {
 }
 
 template <typename T>
-__device__ __forceinline__ void body_update(const DevBlock<T>& b, const PhysParams& P, long long t) {
+__device__ __forceinline__ void body_update(const DevBlock<T>& b, const PhysParams& P, const StageArgs& A,
+                                            long long t) {
   int i = 2 + (int)(t % b.nx);
   int j = 2 + (int)((t / b.nx) % b.ny);
   int k = 2 + (int)(t / ((long long)b.nx * b.ny));
   const long long N = b.N;
   const long long c = cidx(b.Pi, b.Pj, i, j, k);
   T wv[5];
+  const bool ulam = P.unsteady && !A.forcing;
+  const T lam = ulam ? unsteady_lam(b, P, A, c) : T(1), rl = ulam ? T(1) / lam : T(1);
 #pragma unroll
   for (int v = 0; v < 5; v++) {
-    wv[v] = b.wn[v * N + c] - b.dw[v * N + c];
+    const T d = b.dw[v * N + c];
+    wv[v] = b.wn[v * N + c] - (ulam ? mdiv(d, lam, rl) : d);
     b.w[v * N + c] = wv[v];
   }
   b.p[c] = depvars((T)P.gamma, wv);
@@ -1948,9 +1982,9 @@ __global__ void k_irs(DevBlock<T> b, IrsTables tb, TC bb) {
   if (t < 5 * irs_lines<T, D>(b)) body_irs<T, TC, D>(b, tb, bb, t);
 }
 template <typename T>
-__global__ void k_update(DevBlock<T> b, PhysParams P) {
+__global__ void k_update(DevBlock<T> b, PhysParams P, StageArgs A) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < (long long)b.nx * b.ny * b.nz) body_update(b, P, t);
+  if (t < (long long)b.nx * b.ny * b.nz) body_update(b, P, A, t);
 }
 template <typename T>
 __global__ void k_cutcell(DevBlock<T> b, PhysParams P, unsigned* err) {
@@ -2042,7 +2076,7 @@ __global__ void __launch_bounds__(256, 2) k_euler_coop(DevBlock<T> b, PhysParams
       g.sync();
     }
     if (A.irs) {
-      for (long long t = gt; t < ncell; t += gs) body_update(b, P, t);
+      for (long long t = gt; t < ncell; t += gs) body_update(b, P, A, t);
       g.sync();
     }
     for (long long t = gt; t < b.nmir; t += gs) body_cutcell(b, P, E.err, (int)t);
@@ -2153,7 +2187,10 @@ long long irs_lines_h(const DevBlock<T>& b, int D) {
 
 template <typename T, typename TC>
 void launch_irs_part_t(int part, const DevBlock<T>& b, const PhysParams& P, const IrsTables* tab, cudaStream_t s,
-                       const int* variant) {
+                       const int* variant, const StageArgs* A) {
+  StageArgs Au;  // the update's stage (steady without one: lam = 1)
+  memset(&Au, 0, sizeof(Au));
+  if (A) Au = *A;
   const TC bb = (TC)(-P.smoo);
   const long long ncell = (long long)b.nx * b.ny * b.nz;
   if (P.irs_kind == 1) {  // psmoo + progon3: one thread per line
@@ -2161,7 +2198,7 @@ void launch_irs_part_t(int part, const DevBlock<T>& b, const PhysParams& P, cons
     if (part == 1) k_psmoo_line<T, TC, 1><<<nblk(irs_lines_h(b, 1), 128), 128, 0, s>>>(b);
     if (part == 2) {
       k_psmoo_line<T, TC, 2><<<nblk(irs_lines_h(b, 2), 128), 128, 0, s>>>(b);
-      k_update<T><<<nblk(ncell, TPB), TPB, 0, s>>>(b, P);
+      k_update<T><<<nblk(ncell, TPB), TPB, 0, s>>>(b, P, Au);
     }
     return;
   }
@@ -2169,23 +2206,23 @@ void launch_irs_part_t(int part, const DevBlock<T>& b, const PhysParams& P, cons
   if (part == 1) launch_irs_dir<T, TC, 1>(b, tab[1], bb, s, variant ? variant[1] : 0);
   if (part == 2) {
     launch_irs_dir<T, TC, 2>(b, tab[2], bb, s, variant ? variant[2] : 0);
-    k_update<T><<<nblk(ncell, TPB), TPB, 0, s>>>(b, P);
+    k_update<T><<<nblk(ncell, TPB), TPB, 0, s>>>(b, P, Au);
   }
 }
 
 template <typename T>
 void launch_irs_part(int part, const DevBlock<T>& b, const PhysParams& P, const IrsTables* tab, cudaStream_t s,
-                     bool aux32, const int* variant) {
+                     bool aux32, const int* variant, const StageArgs* A) {
   if (aux32)
-    launch_irs_part_t<T, float>(part, b, P, tab, s, variant);
+    launch_irs_part_t<T, float>(part, b, P, tab, s, variant, A);
   else
-    launch_irs_part_t<T, T>(part, b, P, tab, s, variant);
+    launch_irs_part_t<T, T>(part, b, P, tab, s, variant, A);
 }
 
 template <typename T>
 void launch_irs(const DevBlock<T>& b, const PhysParams& P, const IrsTables* tab, cudaStream_t s, bool aux32,
-                const int* variant) {
-  for (int part = 0; part < 3; part++) launch_irs_part<T>(part, b, P, tab, s, aux32, variant);
+                const int* variant, const StageArgs* A) {
+  for (int part = 0; part < 3; part++) launch_irs_part<T>(part, b, P, tab, s, aux32, variant, A);
 }
 
 template <typename T>
@@ -2377,11 +2414,11 @@ void launch_forces(const DevBlock<T>& b, const double* origin, const double* h, 
   template void launch_stage_part<T>(int, const DevBlock<T>&, const PhysParams&, const StageArgs&, unsigned*,       \
                                      cudaStream_t);                                                             \
   template void launch_irs_part<T>(int, const DevBlock<T>&, const PhysParams&, const IrsTables*, cudaStream_t,    \
-                                   bool, const int*);                                                           \
+                                   bool, const int*, const StageArgs*);                                         \
   template int launch_euler_coop<T>(const DevBlock<T>&, const PhysParams&, const EulerLaunch&, int, cudaStream_t,  \
                                     bool);                                                                      \
   template void launch_irs<T>(const DevBlock<T>&, const PhysParams&, const IrsTables*, cudaStream_t, bool,       \
-                              const int*);                                                                      \
+                              const int*, const StageArgs*);                                                    \
   template void launch_cutcell<T>(const DevBlock<T>&, const PhysParams&, unsigned*, cudaStream_t);              \
   template void launch_bcond<T>(const DevBlock<T>&, const PhysParams&, cudaStream_t);                           \
   template void launch_rtrms<T>(const DevBlock<T>&, const PhysParams&, int, double*, int, double*, cudaStream_t); \

@@ -52,6 +52,7 @@ struct Block {
   bool use_coop = false;   // run timestep + euler as one cooperative launch
   int irs_var[3] = {0, 0, 0};  // line-sweep variant per direction (autotuned)
   size_t esz = 8;
+  void *w1 = nullptr, *w2 = nullptr;  // previous physical time steps (unsteady only)
   void *w = nullptr, *p = nullptr, *wn = nullptr, *ws = nullptr, *dw = nullptr, *fw = nullptr, *wr = nullptr,
        *qf = nullptr, *vdtim = nullptr, *lam = nullptr;
   void* eps = nullptr;  // 3N psmoo coefficients (irs_variant 1 only)
@@ -90,6 +91,7 @@ struct mge_ctx {
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   std::vector<std::vector<Block>> lv;
   std::vector<std::pair<int, int>> order;  // (level, serial) in mge_add_block order
+  int itime = 0;                           // physical time step counter (unsteady mode)
   std::string err;
   unsigned* d_err = nullptr;
   unsigned* h_err = nullptr;  // pinned
@@ -175,8 +177,9 @@ void enqueue_timestep(mge_ctx* c, Block& b) {
   });
 }
 
-StageArgs stage_args(const mge_params& P, int m, int mgl, int mlvl, bool lres, bool lfir) {
+StageArgs stage_args(const mge_params& P, int m, int mgl, int mlvl, bool lres, bool lfir, int itime) {
   StageArgs A;
+  std::memset(&A, 0, sizeof(A));
   A.m = m;
   A.fn = P.cstp[m - 1] * P.cfl;
   A.cd = P.cdis[m - 1];
@@ -187,14 +190,17 @@ StageArgs stage_args(const mge_params& P, int m, int mgl, int mlvl, bool lres, b
   A.lres = lres;
   A.irs = (m % 2 != 0) && P.smoo > 0.0 && !lres;
   A.vt = P.vt;
+  // euler.f90:249-275: the transient source needs itime >= 1 (none in the first physical step)
+  A.tmode = P.execmode == 1 ? (itime > 1 ? 2 : (itime == 1 ? 1 : 0)) : 0;
   return A;
 }
 
 // timestep.f90 (optionally) followed by euler.f90:1-462 on one block;
 // nstage_limit > 0 stops after that stage (parity probes)
 void enqueue_euler(mge_ctx* c, Block& b, int mgl, int mlvl, bool lres, bool lfir, int nstage_limit, bool rt,
-                   bool with_timestep = false) {
+                   bool with_timestep = false, int itime = -1) {
   const mge_params& P = c->prm;
+  if (itime < 0) itime = c->itime;
   const int mstage = (nstage_limit > 0) ? std::min(P.mstage, nstage_limit) : P.mstage;
   const bool want_rt = rt && (nstage_limit <= 0 || nstage_limit >= P.mstage) && !lres;
   if (b.use_coop) {
@@ -205,7 +211,7 @@ void enqueue_euler(mge_ctx* c, Block& b, int mgl, int mlvl, bool lres, bool lfir
     L.lfir = lfir;
     L.lres = lres;
     L.rt = want_rt;
-    for (int m = 1; m <= mstage; m++) L.st[m - 1] = stage_args(P, m, mgl, mlvl, lres, lfir);
+    for (int m = 1; m <= mstage; m++) L.st[m - 1] = stage_args(P, m, mgl, mlvl, lres, lfir, itime);
     for (int d = 0; d < 3; d++) L.tab[d] = b.tabs[d];
     L.rt_partial = b.rt_partial;
     L.npart = b.npart;
@@ -227,10 +233,10 @@ void enqueue_euler(mge_ctx* c, Block& b, int mgl, int mlvl, bool lres, bool lfir
     if (lfir) launch_copy_ws<T>(D, c->stream);
     launch_save_wn<T>(D, c->stream);
     for (int m = 1; m <= mstage; m++) {
-      StageArgs A = stage_args(P, m, mgl, mlvl, lres, lfir);
+      StageArgs A = stage_args(P, m, mgl, mlvl, lres, lfir, itime);
       launch_stage<T>(D, c->P, A, c->d_err, c->stream, c->side, c->ev_fork, c->ev_join);
       if (lres) return;
-      if (A.irs) launch_irs<T>(D, c->P, b.tabs, c->stream, b.aux32, b.irs_var);
+      if (A.irs) launch_irs<T>(D, c->P, b.tabs, c->stream, b.aux32, b.irs_var, &A);
       launch_cutcell<T>(D, c->P, c->d_err, c->stream);
       launch_bcond<T>(D, c->P, c->stream);
     }
@@ -356,6 +362,8 @@ void build_phys(mge_ctx* c) {
   Q.vt = P.vt;
   Q.distype = P.distype;
   Q.irs_kind = P.irs_variant;
+  Q.unsteady = P.execmode == 1;
+  Q.dtstep = P.dtstep;
   Q.viscl = P.viscl;
   Q.gas_const = P.gas_const;
   Q.prlmean = P.prlmean;
@@ -400,6 +408,7 @@ void fill_view(Block& b, DevBlock<T>& d, void* scratch) {
   d.il = b.il; d.jl = b.jl; d.kl = b.kl; d.ie = b.ie; d.je = b.je; d.ke = b.ke; d.ib = b.ib; d.jb = b.jb; d.kb = b.kb;
   d.Pi = b.Pi; d.Pj = b.Pj; d.N = N;
   d.w = (T*)b.w; d.p = (T*)b.p; d.wn = (T*)b.wn; d.ws = (T*)b.ws; d.dw = (T*)b.dw; d.fw = (T*)b.fw;
+  d.w1 = (T*)b.w1; d.w2 = (T*)b.w2;
   d.wr = (T*)b.wr; d.qf = (T*)b.qf; d.vdtim = (T*)b.vdtim; d.lam = (T*)b.lam; d.dtim = b.dtim;
   d.blank = b.blank; d.marker = b.marker; d.cutmap = b.cutmap;
   d.eps = (T*)b.eps;
@@ -443,6 +452,7 @@ int commit_block(mge_ctx* c, Block& b, double* scratch) {
       (rc = dalloc(c, &b.marker, N)) || (rc = dalloc(c, &b.cutmap, N)))
     return rc;
   if (c->prm.irs_variant == 1 && (rc = valloc(c, &b.eps, 3 * N, es))) return rc;
+  if (c->prm.execmode == 1 && ((rc = valloc(c, &b.w1, 5 * N, es)) || (rc = valloc(c, &b.w2, 5 * N, es)))) return rc;
   CK(cudaMemset(b.marker, 0, N));
   std::vector<uint8_t> bl(N);
   for (long long q = 0; q < N; q++) bl[q] = b.blank_h[q] != 0 ? 1 : 0;
@@ -616,6 +626,7 @@ int mge_init(const mge_params* prm, int device, mge_ctx** out) {
   if (prm->eqntype != MGE_EQN_EULER && prm->eqntype != MGE_EQN_NS) return MGE_EBADCFG;
   if (prm->dissip != MGE_DISSIP_SCALAR && prm->dissip != MGE_DISSIP_MATRIX) return MGE_EBADCFG;
   if (prm->irs_variant != 0 && prm->irs_variant != 1) return MGE_EBADCFG;
+  if (prm->execmode != 0 && (prm->execmode != 1 || !(prm->dtstep > 0.0))) return MGE_EBADCFG;
   mge_ctx* c = new mge_ctx();
   c->prm = *prm;
   c->device = device;
@@ -796,6 +807,10 @@ static void free_stream_start(mge_ctx* c, Block& b) {  // init_flow.f90:46-96
   enqueue_simple(c, b, 0);
   enqueue_simple(c, b, 4);
   enqueue_simple(c, b, 2);
+  if (b.w1) {  // init_flow.f90:79-86: the previous time steps start equal to w
+    cudaMemcpyAsync(b.w1, b.w, 5 * b.N * b.esz, cudaMemcpyDeviceToDevice, c->stream);
+    cudaMemcpyAsync(b.w2, b.w, 5 * b.N * b.esz, cudaMemcpyDeviceToDevice, c->stream);
+  }
 }
 
 // Autotuner: per block, time the two line-sweep variants of each direction
@@ -888,6 +903,7 @@ int mge_init_flow(mge_ctx* c) {  // init_flow.f90:46-96
   CK(cudaSetDevice(c->device));
   for (auto& L : c->lv)
     for (Block& b : L) free_stream_start(c, b);
+  c->itime = 0;
   CK(cudaGetLastError());
   int rc = check_err(c);
   if (rc) return rc;
@@ -949,7 +965,8 @@ int mge_set_precision(mge_ctx* c, int precision) {
       F fields[] = {{&b.w, 5 * N, true},  {&b.p, N, true},        {&b.ws, 5 * N, true},   {&b.wn, 5 * N, false},
                     {&b.dw, 5 * N, false}, {&b.fw, 5 * N, false}, {&b.wr, 5 * N, false}, {&b.qf, 5 * N, false},
                     {&b.vdtim, N, false}, {&b.lam, N, false},     {&b.rec_wsol, 5LL * nma, true},
-                    {&b.rec_psol, nma, true}, {&b.rec_wall, 25LL * nma, false}, {&b.eps, 3 * N, false}};
+                    {&b.rec_psol, nma, true}, {&b.rec_wall, 25LL * nma, false}, {&b.eps, 3 * N, false},
+                    {&b.w1, 5 * N, true},     {&b.w2, 5 * N, true}};
       for (F& f : fields) {
         if (!*f.p) continue;  // not allocated for this context
         void* np = nullptr;
@@ -1047,6 +1064,8 @@ int mge_download_field(mge_ctx* c, int level, int serial, const char* name, doub
   else if (n == "vdtim") { src = b->vdtim; len = N; }
   else if (n == "lam") { src = b->lam; len = N; }
   else if (n == "eps" && b->eps) { src = b->eps; len = 3 * N; }
+  else if (n == "w1" && b->w1) { src = b->w1; len = 5 * N; }
+  else if (n == "w2" && b->w2) { src = b->w2; len = 5 * N; }
   else if (n == "wsol") { src = b->rec_wsol; len = 5 * b->recs.size(); }
   else if (n == "psol") { src = b->rec_psol; len = b->recs.size(); }
   else if (n == "dtim") { src = b->dtim; len = 1; typed = false; }
@@ -1073,13 +1092,13 @@ int mge_timestep(mge_ctx* c, int level, int serial) {
   return check_err(c);
 }
 
-static int euler_common(mge_ctx* c, int level, int serial, int ncyc, int mgl, int mlvl, int lres, int lfir,
-                        int nstage) {
+static int euler_common(mge_ctx* c, int level, int serial, int itime, int ncyc, int mgl, int mlvl, int lres,
+                        int lfir, int nstage) {
   Block* b = getb(c, level, serial);
   if (!b || !c->committed) return MGE_ENOTFOUND;
   CK(cudaSetDevice(c->device));
   const bool full = !lres && (nstage <= 0 || nstage >= c->prm.mstage);
-  enqueue_euler(c, *b, mgl, mlvl, lres != 0, lfir != 0, nstage, full);
+  enqueue_euler(c, *b, mgl, mlvl, lres != 0, lfir != 0, nstage, full, false, itime < 0 ? 0 : itime);
   CK(cudaGetLastError());
   int rc = check_err(c);
   if (rc) return rc;
@@ -1093,14 +1112,12 @@ static int euler_common(mge_ctx* c, int level, int serial, int ncyc, int mgl, in
 }
 
 int mge_euler(mge_ctx* c, int level, int serial, int itime, int ncyc, int mgl, int mlvl, int lres, int lfir) {
-  (void)itime;
-  return euler_common(c, level, serial, ncyc, mgl, mlvl, lres, lfir, 0);
+  return euler_common(c, level, serial, itime, ncyc, mgl, mlvl, lres, lfir, 0);
 }
 
 int mge_euler_partial(mge_ctx* c, int level, int serial, int itime, int ncyc, int mgl, int mlvl, int lres, int lfir,
                       int nstage) {
-  (void)itime;
-  return euler_common(c, level, serial, ncyc, mgl, mlvl, lres, lfir, nstage);
+  return euler_common(c, level, serial, itime, ncyc, mgl, mlvl, lres, lfir, nstage);
 }
 
 int mge_movco(mge_ctx* c, int mgl) {
@@ -1207,6 +1224,23 @@ int mge_read_restart(mge_ctx* c, const char* path, const int* codes, int ncodes)
   return MGE_OK;
 }
 
+// solver.f90:263-276,286: the end of a physical time step of the unsteady
+// mode: w2 = w1, w1 = w on every block, and the step counter advances
+int mge_time_advance(mge_ctx* c, int* itime_out) {
+  if (!c || !c->committed) return MGE_EBADCFG;
+  if (c->prm.execmode != 1) return fail(c, MGE_EBADCFG, "time_advance: execmode is not 1");
+  CK(cudaSetDevice(c->device));
+  for (auto& L : c->lv)
+    for (Block& b : L) {
+      CK(cudaMemcpyAsync(b.w2, b.w1, 5 * b.N * b.esz, cudaMemcpyDeviceToDevice, c->stream));
+      CK(cudaMemcpyAsync(b.w1, b.w, 5 * b.N * b.esz, cudaMemcpyDeviceToDevice, c->stream));
+    }
+  CK(cudaStreamSynchronize(c->stream));
+  c->itime += 1;
+  if (itime_out) *itime_out = c->itime;
+  return MGE_OK;
+}
+
 int mge_forces_compute(mge_ctx* c, int level, const mge_solve_opts* o, mge_forces* out) {
   if (!c || !c->committed || level < 1 || level > (int)c->lv.size() || !out) return MGE_ENOTFOUND;
   CK(cudaSetDevice(c->device));
@@ -1240,12 +1274,16 @@ int mge_forces_compute(mge_ctx* c, int level, const mge_solve_opts* o, mge_force
   return MGE_OK;
 }
 
-static int launch_cycle_graph(mge_ctx* c, int mlvl) {
-  if ((int)c->graphs.size() < (int)c->lv.size() + 1) c->graphs.resize(c->lv.size() + 1, nullptr);
+static int launch_cycle_graph(mge_ctx* c, int mlvl_in) {
+  // one graph per FMG level and, in the unsteady mode, per form of the
+  // transient source (none, first step, BDF2): the stage arguments are baked in
+  const int tclass = c->prm.execmode == 1 ? std::min(c->itime, 2) : 0;
+  const int mlvl = mlvl_in + tclass * ((int)c->lv.size() + 1);
+  if ((int)c->graphs.size() < 3 * ((int)c->lv.size() + 1)) c->graphs.resize(3 * (c->lv.size() + 1), nullptr);
   if (!c->graphs[mlvl]) {
     cudaGraph_t g;
     CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-    enqueue_cycle(c, mlvl);
+    enqueue_cycle(c, mlvl_in);
     cudaError_t e = cudaStreamEndCapture(c->stream, &g);
     if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamEndCapture");
     e = cudaGraphInstantiate(&c->graphs[mlvl], g, 0);
@@ -1258,7 +1296,7 @@ static int launch_cycle_graph(mge_ctx* c, int mlvl) {
       cudaGraphNodeType t;
       if (cudaGraphNodeGetType(nodes[q], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) nk++;
     }
-    if ((int)c->graph_kernels.size() < (int)c->lv.size() + 1) c->graph_kernels.resize(c->lv.size() + 1, 0);
+    if ((int)c->graph_kernels.size() < (int)c->graphs.size()) c->graph_kernels.resize(c->graphs.size(), 0);
     c->graph_kernels[mlvl] = nk;
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return cuda_fail(c, e, "cudaGraphInstantiate");
@@ -1449,6 +1487,7 @@ int mge_kernel_times(mge_ctx* c, int level, int reps, double* ms_out, int nout) 
     });
     for (int m = 1; m <= P.mstage && !rc; m++) {
       StageArgs A;
+      std::memset(&A, 0, sizeof(A));
       A.m = m;
       A.fn = P.cstp[m - 1] * P.cfl;
       A.cd = P.cdis[m - 1];
@@ -1474,7 +1513,7 @@ int mge_kernel_times(mge_ctx* c, int level, int reps, double* ms_out, int nout) 
           rc = timed(5 + part, [&] {
             with_dev(b, [&](auto& D) {
               using T = typename std::remove_reference_t<decltype(D)>::value_type;
-              launch_irs_part<T>(part, D, c->P, b.tabs, c->stream, b.aux32, b.irs_var);
+              launch_irs_part<T>(part, D, c->P, b.tabs, c->stream, b.aux32, b.irs_var, &A);
             });
           });
       if (!rc) rc = timed(8, [&] { enqueue_simple(c, b, 4); });

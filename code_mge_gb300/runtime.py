@@ -122,6 +122,13 @@ class Cycle:
                                     C.byref(nd), C.byref(fo)), "solve")
         return hist[: min(nd.value, hist_len)].copy(), nd.value, fo
 
+    def time_advance(self):
+        """End of a physical time step of the unsteady mode (solver.f90:263-276):
+        w2 = w1, w1 = w; returns the new step counter."""
+        it = C.c_int(0)
+        self._chk(self._fn("time_advance")(self.ctx, C.byref(it)), "time_advance")
+        return it.value
+
     def forces(self, level=None):
         level = self.case.prm.nlevel if level is None else level
         o = A.MgeSolveOpts()
@@ -138,7 +145,7 @@ class Cycle:
         sp = self.spec(level, serial)
         P = sp.dims
         N = P[0] * P[1] * P[2]
-        nvar = 5 if name in ("w", "dw", "fw", "wn", "ws", "wr", "qf") else (3 if name == "eps" else 1)
+        nvar = 5 if name in ("w", "dw", "fw", "wn", "ws", "wr", "qf", "w1", "w2") else (3 if name == "eps" else 1)
         if name in ("wsol", "psol"):
             nm = sp.arrays["nmir"]
             n = 5 * nm if name == "wsol" else nm

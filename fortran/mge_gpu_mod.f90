@@ -30,6 +30,8 @@ module mge_gpu_mod
     integer(c_int) :: wall_adiabatic, irs_variant, precision, nlevel
     integer(c_int) :: mcyc(MGE_MAX_LEVEL)
     real(c_double) :: conv_drop
+    integer(c_int) :: execmode
+    real(c_double) :: dtstep
   end type mge_params
 
   type, bind(C) :: mge_block_desc
@@ -180,6 +182,11 @@ module mge_gpu_mod
       character(kind=c_char), intent(in) :: path(*)
       integer(c_int), intent(in) :: codes(*)
       integer(c_int), value :: ncodes
+    end function
+    integer(c_int) function mge_time_advance(ctx, itime_out) bind(C, name="mge_time_advance")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int), intent(out) :: itime_out
     end function
     integer(c_int) function mge_residual_norm_noalloc(dw_rho, vdtim, blank, nx, ny, nz, cfl, vt, dtim, &
         norm_out, stream) bind(C, name="mge_residual_norm_noalloc")

@@ -92,6 +92,8 @@ typedef struct mge_params {
   int    nlevel;                  /* number of multigrid levels */
   int    mcyc[MGE_MAX_LEVEL];     /* cycles per FMG level (mcyc) */
   double conv_drop;               /* exit when ini_res/max_res > conv_drop (1e6, solver.f90:238) */
+  int    execmode;                /* 0 steady, 1 unsteady dual time stepping (BDF2 in physical time) */
+  double dtstep;                  /* physical time step, non-dimensional (input_param.f90:90-96) */
 } mge_params;
 
 /*
@@ -275,6 +277,13 @@ int mge_upload_solut(mge_ctx* ctx, int level, int serial, double p_tot, double* 
  * mismatch: MGE_EBADCFG here) and uploads the state. */
 int mge_write_restart(mge_ctx* ctx, const char* path, const int* codes, int ncodes);
 int mge_read_restart(mge_ctx* ctx, const char* path, const int* codes, int ncodes);
+
+/* solver.f90:263-276,286, the end of a physical time step of the unsteady
+ * mode (execmode 1): w2 = w1, w1 = w on every block, and the step counter
+ * the following cycles use advances (*itime_out receives it).  The counter
+ * starts at 0 at mge_init_flow; the transient source of euler.f90:249-275
+ * applies from itime 1 on. */
+int mge_time_advance(mge_ctx* ctx, int* itime_out);
 
 /* The same text for one block, without a context or a GPU: returns the bytes
  * of the text (writing at most cap-1 of them and a NUL into buf when buf is

@@ -61,6 +61,7 @@ struct OBlock {
   int bctype[6] = {0, 0, 0, 0, 0, 0};
   double fnv[6][3] = {};
   std::vector<double> w, p, wn, ws, dw, fw, wr, qf, vdtim, radi, radj, radk, epsx, epsy, epsz;
+  std::vector<double> w1, w2;  // states of the two previous physical time steps (execmode 1)
   std::vector<int> blank, marker;
   std::vector<double> rtrms;
   double dtim = 10.0;
@@ -87,6 +88,7 @@ struct mgeo_ctx {
   std::string err;
   bool committed = false;
   int mirr_zero_warned = 0;
+  int itime = 0;  // physical time step counter of the unsteady mode (solver.f90:115,286)
 };
 
 namespace {
@@ -208,8 +210,13 @@ int timestep(mgeo_ctx* c, OBlock& b) {
           fict = b.vol / (ri + rj + rk + cfac * (rvi + rvj + rvk));  // timestep.f90:177-178
         else
           fict = b.vol / (ri + rj + rk);  // timestep.f90:85
-        // execmode == 0 (steady): vdtim = fict (timestep.f90:88-92)
+        // timestep.f90:85-99 (and 180-190 for NS): the steady local step, or
+        // in the unsteady mode at most 2*dtstep/(3*cfl)
         double vd = fict;
+        if (P.execmode == 1) {
+          const double dtime = 2.0 * P.dtstep / (3.0 * P.cfl);
+          vd = fmin_(fict, dtime);
+        }
         double pc = b.P(i, j, k);
         double pip = b.P(i + 1, j, k), pim = b.P(i - 1, j, k);
         double pjp = b.P(i, j + 1, k), pjm = b.P(i, j - 1, k);
@@ -1473,8 +1480,8 @@ int vflux_all(mgeo_ctx* c, OBlock& b, int istage) {
 
 /* ------------------------------------------------------------------ euler.f90:1-462 */
 int euler(mgeo_ctx* c, OBlock& b, int itime, int ncyc, int mgl, int mlvl, bool lres, bool lfir, int nstage_limit) {
-  (void)itime;
   const mge_params& P = c->prm;
+  const bool unsteady = P.execmode == 1;
   const size_t N = b.N;
   const double fcoll = 1.0;
   if (lfir) b.ws = b.w;  // euler.f90:75-77
@@ -1519,6 +1526,22 @@ int euler(mgeo_ctx* c, OBlock& b, int itime, int ncyc, int mgl, int mlvl, bool l
       for (int j = 2; j <= b.jl; j++)
         for (int i = 2; i <= b.il; i++)
           for (int v = 0; v < 5; v++) b.DW(i, j, k, v) = b.DW(i, j, k, v) + b.FW(i, j, k, v);
+    if (unsteady && itime >= 1) {  // euler.f90:249-275: BDF2, or the first step's (halved) BDF1
+      const double f = 0.5 * b.vol / P.dtstep;
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+      for (int k = 2; k <= b.kl; k++)
+        for (int j = 2; j <= b.jl; j++)
+          for (int i = 2; i <= b.il; i++) {
+            const size_t q = b.I(i, j, k);
+            for (int v = 0; v < 5; v++) {
+              const size_t x = v * N + q;
+              if (itime > 1)
+                b.dw[x] = b.dw[x] + f * (3.0 * b.w[x] - 4.0 * b.w1[x] + b.w2[x]);
+              else
+                b.dw[x] = b.dw[x] + f * (b.w[x] - b.w1[x]);
+            }
+          }
+    }
     if (mgl < mlvl) {  // euler.f90:294-318
       const bool first = lfir && m == 1;
 #pragma omp parallel for num_threads(g_threads) schedule(static)
@@ -1534,6 +1557,17 @@ int euler(mgeo_ctx* c, OBlock& b, int itime, int ncyc, int mgl, int mlvl, bool l
               b.dw[v * N + q] = b.dw[v * N + q] + b.qf[v * N + q];
             }
           }
+      if (unsteady) {  // euler.f90:320-331
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+        for (int k = 2; k <= b.kl; k++)
+          for (int j = 2; j <= b.jl; j++)
+            for (int i = 2; i <= b.il; i++) {
+              double de = fn * b.vdtim[b.I(i, j, k)];
+              if (P.vt == 1) de = fn * b.dtim;
+              const double lam = 1.0 + de * 3.0 / 2.0 / P.dtstep;
+              for (int v = 0; v < 5; v++) b.DW(i, j, k, v) = b.DW(i, j, k, v) / lam;
+            }
+      }
     }
 #pragma omp parallel for num_threads(g_threads) schedule(static)
     for (int k = 2; k <= b.kl; k++)
@@ -1557,7 +1591,12 @@ int euler(mgeo_ctx* c, OBlock& b, int itime, int ncyc, int mgl, int mlvl, bool l
     for (int k = 2; k <= b.kl; k++)
       for (int j = 2; j <= b.jl; j++)
         for (int i = 2; i <= b.il; i++) {
-          const double lam = 1.0;
+          double lam = 1.0;
+          if (unsteady && mgl == mlvl) {  // euler.f90:387-391
+            double de = fn * b.vdtim[b.I(i, j, k)];
+            if (P.vt == 1) de = fn * b.dtim;
+            lam = 1.0 + de * 3.0 / 2.0 / P.dtstep;
+          }
           for (int v = 0; v < 5; v++) b.W(i, j, k, v) = b.wn[v * N + b.I(i, j, k)] - b.DW(i, j, k, v) / lam;
           depvars_cell(P, b, i, j, k);
         }
@@ -1846,6 +1885,7 @@ int mgeo_add_block(mgeo_ctx* c, const mge_block_desc* d, int level, int serial) 
   b.parent = d->parent;
   const size_t N = b.N;
   b.w.assign(5 * N, 0.0); b.p.assign(N, 0.0); b.wn.assign(5 * N, 0.0); b.ws.assign(5 * N, 0.0);
+  if (c->prm.execmode == 1) { b.w1.assign(5 * N, 0.0); b.w2.assign(5 * N, 0.0); }  // make_flow.f90:38-39,60-61
   b.dw.assign(5 * N, 0.0); b.fw.assign(5 * N, 0.0); b.wr.assign(5 * N, 0.0); b.qf.assign(5 * N, 0.0);
   b.vdtim.assign(N, 0.0); b.radi.assign(N, 0.0); b.radj.assign(N, 0.0); b.radk.assign(N, 0.0);
   b.epsx.assign(N, 0.0); b.epsy.assign(N, 0.0); b.epsz.assign(N, 0.0);
@@ -1904,7 +1944,12 @@ int mgeo_init_flow(mgeo_ctx* c) {  // init_flow.f90:46-96 (free stream, no resta
       if (rc) return rc;
       rc = bcond(c, b);
       if (rc) return rc;
+      if (P.execmode == 1) {  // init_flow.f90:79-86
+        b.w1 = b.w;
+        b.w2 = b.w;
+      }
     }
+  c->itime = 0;
   return MGE_OK;
 }
 
@@ -1930,6 +1975,8 @@ int mgeo_download_field(mgeo_ctx* c, int level, int serial, const char* name, do
   else if (n == "wr") src = &b->wr;
   else if (n == "qf") src = &b->qf;
   else if (n == "vdtim") src = &b->vdtim;
+  else if (n == "w1" && !b->w1.empty()) src = &b->w1;
+  else if (n == "w2" && !b->w2.empty()) src = &b->w2;
   if (src) {
     if (count < src->size()) return MGE_EBADCFG;
     std::memcpy(out, src->data(), src->size() * sizeof(double));
@@ -2053,6 +2100,20 @@ int mgeo_upload_solut(mgeo_ctx* c, int level, int serial, double p_tot, double* 
   return MGE_OK;
 }
 
+/* solver.f90:263-276,286: the end of a physical time step of the unsteady
+   mode: w2 = w1, w1 = w on every block, and the step counter advances */
+int mgeo_time_advance(mgeo_ctx* c, int* itime_out) {
+  if (c->prm.execmode != 1) return fail(c, MGE_EBADCFG, "time_advance: execmode is not 1");
+  for (auto& L : c->lv)
+    for (OBlock& b : L) {
+      b.w2 = b.w1;
+      b.w1 = b.w;
+    }
+  c->itime += 1;
+  if (itime_out) *itime_out = c->itime;
+  return MGE_OK;
+}
+
 int mgeo_forces_compute(mgeo_ctx* c, int level, const mge_solve_opts* o, mge_forces* out) {
   if (level < 1 || level > (int)c->lv.size()) return MGE_ENOTFOUND;
   double F[3] = {0, 0, 0}, M[3] = {0, 0, 0};
@@ -2076,7 +2137,7 @@ static int oracle_cycle(mgeo_ctx* c, int mlvl, int ncyc, double* max_res_out, do
   const mge_params& P = c->prm;
   const int nlevel = (int)c->lv.size();
   std::vector<int> icyc(nlevel + 2, 0);
-  const int itime = 0;
+  const int itime = c->itime;
   int rc = 0;
   int mgl = mlvl;
   for (;;) {    // lopmg

@@ -50,6 +50,7 @@ int  mgeo_forces_compute(mgeo_ctx* ctx, int level, const mge_solve_opts* opts,
                          mge_forces* out);
 int  mgeo_upload_solut(mgeo_ctx* ctx, int level, int serial, double p_tot, double* solut,
                        size_t count, int* nval_out);
+int  mgeo_time_advance(mgeo_ctx* ctx, int* itime_out);
 /* threads used by the loops of the oracle (1 = the serial mgsol analogue) */
 void mgeo_set_threads(int n);
 int  mgeo_get_threads(void);

@@ -47,10 +47,13 @@ def pair(case, develop_cycles=0, path="coop"):
     o = OracleCycle(case)
     g = Cycle(case)
     if develop_cycles:
-        dev = OracleCycle(case)
-        dev.prm.mcyc[case.prm.nlevel - 1] = develop_cycles
+        # the context copies its parameters when it is made: set the cycle
+        # counts on a copy first
+        prm = type(case.prm).from_buffer_copy(case.prm)
+        prm.mcyc[case.prm.nlevel - 1] = develop_cycles
         for L in range(case.prm.nlevel - 1):
-            dev.prm.mcyc[L] = 1
+            prm.mcyc[L] = 1
+        dev = OracleCycle(case, prm=prm)
         dev.solve()
         for L in range(1, case.prm.nlevel + 1):
             w = dev.field("w", L)
