@@ -985,11 +985,16 @@ __device__ __forceinline__ void body_combine(const DevBlock<T>& b, const PhysPar
   }
   // update, euler.f90:381-399 (steady: lam = 1, and dw/1 is dw)
   T wv[5];
-  const bool ulam = P.unsteady && !A.forcing;
-  const T lam = ulam ? unsteady_lam(b, P, A, c) : T(1), rl = ulam ? T(1) / lam : T(1);
+  if (P.unsteady && !A.forcing) {
+    const T lam = unsteady_lam(b, P, A, c), rl = T(1) / lam;
+#pragma unroll
+    for (int v = 0; v < 5; v++) wv[v] = b.wn[v * N + c] - mdiv(dwv[v], lam, rl);
+  } else {
+#pragma unroll
+    for (int v = 0; v < 5; v++) wv[v] = b.wn[v * N + c] - dwv[v];
+  }
 #pragma unroll
   for (int v = 0; v < 5; v++) {
-    wv[v] = b.wn[v * N + c] - (ulam ? mdiv(dwv[v], lam, rl) : dwv[v]);
     b.w[v * N + c] = wv[v];
     b.dw[v * N + c] = dwv[v];
   }
@@ -1297,14 +1302,16 @@ __device__ __forceinline__ void body_update(const DevBlock<T>& b, const PhysPara
   const long long N = b.N;
   const long long c = cidx(b.Pi, b.Pj, i, j, k);
   T wv[5];
-  const bool ulam = P.unsteady && !A.forcing;
-  const T lam = ulam ? unsteady_lam(b, P, A, c) : T(1), rl = ulam ? T(1) / lam : T(1);
+  if (P.unsteady && !A.forcing) {
+    const T lam = unsteady_lam(b, P, A, c), rl = T(1) / lam;
 #pragma unroll
-  for (int v = 0; v < 5; v++) {
-    const T d = b.dw[v * N + c];
-    wv[v] = b.wn[v * N + c] - (ulam ? mdiv(d, lam, rl) : d);
-    b.w[v * N + c] = wv[v];
+    for (int v = 0; v < 5; v++) wv[v] = b.wn[v * N + c] - mdiv(b.dw[v * N + c], lam, rl);
+  } else {
+#pragma unroll
+    for (int v = 0; v < 5; v++) wv[v] = b.wn[v * N + c] - b.dw[v * N + c];
   }
+#pragma unroll
+  for (int v = 0; v < 5; v++) b.w[v * N + c] = wv[v];
   b.p[c] = depvars((T)P.gamma, wv);
 }
 
