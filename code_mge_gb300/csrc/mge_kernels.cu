@@ -31,6 +31,7 @@
 #include <cstring>
 
 #include "exact_ops.cuh"
+#include "fast_pow.cuh"
 #include "mge_internal.h"
 
 namespace cg = cooperative_groups;
@@ -1368,6 +1369,18 @@ __device__ void body_cutcell(const DevBlock<T>& b, const PhysParams& P, unsigned
 // --------------------------------------------------------------- face boundary conditions
 // One launch per face in the order 1..6 of bcond.f90:16-39: later faces read
 // and overwrite ghost cells that earlier faces wrote.
+// the far field's powers: the short forms for gamma = 1.4 in FP64 (fast_pow.cuh)
+__device__ __forceinline__ double pow_gm(const PhysParams& P, double x, double gm) {
+  if (P.gamma14) return pow_5_2(x);
+  return pow(x, gm);
+}
+__device__ __forceinline__ float pow_gm(const PhysParams&, float x, float gm) { return pow(x, gm); }
+__device__ __forceinline__ double pow_gamma(const PhysParams& P, double x, double gamma) {
+  if (P.gamma14) return pow_7_5(x);
+  return pow(x, gamma);
+}
+__device__ __forceinline__ float pow_gamma(const PhysParams&, float x, float gamma) { return pow(x, gamma); }
+
 template <typename T>
 __device__ void body_bc_face(const DevBlock<T>& b, const PhysParams& P, int face, long long t) {
   const int ax = (face - 1) % 3;
@@ -1419,7 +1432,7 @@ __device__ void body_bc_face(const DevBlock<T>& b, const PhysParams& P, int face
       T ci = T(0.25) * (gamma - T(1)) * (rpo - rmi);
       T si = (T)P.si_far;
       T cc = ci * ci / gamma;
-      T rhoi = pow(si * cc, gm);
+      T rhoi = pow_gm(P, si * cc, gm);
       T prei = rhoi * cc;
       out[0] = rhoi;
       out[1] = rhoi * vv[0];
@@ -1432,7 +1445,7 @@ __device__ void body_bc_face(const DevBlock<T>& b, const PhysParams& P, int face
       T rhoi = wp[0];
       T vv[3] = {wp[1] / rhoi, wp[2] / rhoi, wp[3] / rhoi};
       T prei = pph;
-      T si = pow(rhoi, gamma) / prei;
+      T si = pow_gamma(P, rhoi, gamma) / prei;
       T ci = sqrt(gamma * prei / rhoi);
       T rpo = vv[ax] * fnn + T(2) * ci / (gamma - T(1));
       T rmi = u0a * fnn - T(2) * (T)P.c0 / (gamma - T(1));
@@ -1440,7 +1453,7 @@ __device__ void body_bc_face(const DevBlock<T>& b, const PhysParams& P, int face
       ve[ax] = T(0.5) * (rpo + rmi) * fnn;
       T ce = T(0.25) * (gamma - T(1)) * (rpo - rmi);
       T cc = ce * ce / gamma;
-      T rhoe = pow(si * cc, gm);
+      T rhoe = pow_gm(P, si * cc, gm);
       T pe = rhoe * cc;
       out[0] = rhoe;
       out[1] = rhoe * ve[0];

@@ -363,6 +363,7 @@ void build_phys(mge_ctx* c) {
   Q.distype = P.distype;
   Q.irs_kind = P.irs_variant;
   Q.unsteady = P.execmode == 1;
+  Q.gamma14 = P.gamma == 1.4;
   Q.dtstep = P.dtstep;
   Q.viscl = P.viscl;
   Q.gas_const = P.gas_const;

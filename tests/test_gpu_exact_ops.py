@@ -21,3 +21,13 @@ def test_exact_ops_match_fp64(tmp_path):
     r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "mismatches 0 " in r.stdout
+
+
+def test_fast_powers_stay_within_three_ulp_of_pow(tmp_path):
+    # x^(5/2) and x^(7/5) of the far-field boundary (fast_pow.cuh) against
+    # CUDA's pow at the double exponents 1/(gamma-1) and gamma, gamma = 1.4
+    exe = str(tmp_path / "fast_pow_check")
+    subprocess.run([B._nvcc(), "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "--fmad=false", "-o", exe,
+                    os.path.join(HERE, "fast_pow_check.cu")], check=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
