@@ -9,24 +9,28 @@
 //   x^(5/2) = x^2 * sqrt(x)                       (three roundings)
 //   x^(7/5) = x * z,  z = (x^2)^(1/5)             (Newton's method for the
 //             fifth root, z <- (4z + x^2/z^4)/5, two steps from an FP32 seed)
-// Both stay within 2 ulp of the correctly rounded x^(5/2) and x^(7/5).  The
-// double exponents of the reference, gamma = 1.4 - 8.9e-17 and
-// 1/(gamma-1) = 2.5 + 5.6e-16, move the power by a relative e*|ln x|,
-// under 2 ulp for x in [1/3, 3]; in the far field x stays near 1 (s*c^2/gamma
-// is 1 in the free stream).  tests/test_gpu_exact_ops.py compares both with
-// CUDA's pow at those exponents.  Outside [1e-30, 1e30] they return pow itself.
+// The exponents the reference actually uses are doubles: gamma = 7/5 + dg and
+// 1/(gamma-1) = 5/2 + dm with dg = -8.9e-17 and dm = 4.4e-16.  x^(e+d) =
+// x^e * (1 + d*ln x + ...), and d*ln x is a few 1e-16 at most, so the factor
+// is applied as y + y*(d*ln x) with ln x to single precision.  Over
+// x in [1/10, 10] the result stays within 3 ulp of the correctly rounded
+// pow(x, e+d); tests/test_gpu_exact_ops.py allows 4 against CUDA's pow.
+// Outside [1e-30, 1e30] the functions return pow itself.
 #pragma once
 #include <cuda_runtime.h>
 
 namespace mge {
 
-__device__ __forceinline__ double pow_5_2(double x) {
-  if (!(x > 1e-30 && x < 1e30)) return pow(x, 2.5);
-  return (x * x) * sqrt(x);
+// x^(5/2 + d)
+__device__ __forceinline__ double pow_5_2(double x, double d) {
+  if (!(x > 1e-30 && x < 1e30)) return pow(x, 2.5 + d);
+  const double y = (x * x) * sqrt(x);
+  return y + y * (d * (double)logf((float)x));
 }
 
-__device__ __forceinline__ double pow_7_5(double x) {
-  if (!(x > 1e-30 && x < 1e30)) return pow(x, 1.4);
+// x^(7/5 + d)
+__device__ __forceinline__ double pow_7_5(double x, double d) {
+  if (!(x > 1e-30 && x < 1e30)) return pow(x, 1.4 + d);
   const double a = x * x;
   double z = (double)powf((float)x, 0.4f);  // x^(2/5) to single precision
 #pragma unroll
@@ -34,7 +38,8 @@ __device__ __forceinline__ double pow_7_5(double x) {
     const double z2 = z * z;
     z = (4.0 * z + a / (z2 * z2)) / 5.0;
   }
-  return x * z;
+  const double y = x * z;
+  return y + y * (d * (double)logf((float)x));
 }
 
 }  // namespace mge

@@ -96,6 +96,7 @@ struct PhysParams {
   int distype;              // MGE_DIS_* (0 central, 1 Roe first order, 2 Roe MUSCL)
   int irs_kind;             // 0 psmoo_old (what euler calls), 1 psmoo + progon3
   int gamma14;              // gamma is 1.4: the far field's powers take the short forms of fast_pow.cuh
+  double pow_dg, pow_dm;    // gamma - 7/5 and 1/(gamma-1) - 5/2 (the double exponents' offsets)
   int unsteady;             // execmode 1: dual time stepping
   double dtstep;            // physical time step
   double viscl, kt, gas_const, prlmean;  // laminar viscosity, heat conductivity, R, Pr

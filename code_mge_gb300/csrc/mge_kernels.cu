@@ -1371,12 +1371,12 @@ __device__ void body_cutcell(const DevBlock<T>& b, const PhysParams& P, unsigned
 // and overwrite ghost cells that earlier faces wrote.
 // the far field's powers: the short forms for gamma = 1.4 in FP64 (fast_pow.cuh)
 __device__ __forceinline__ double pow_gm(const PhysParams& P, double x, double gm) {
-  if (P.gamma14) return pow_5_2(x);
+  if (P.gamma14) return pow_5_2(x, P.pow_dm);
   return pow(x, gm);
 }
 __device__ __forceinline__ float pow_gm(const PhysParams&, float x, float gm) { return pow(x, gm); }
 __device__ __forceinline__ double pow_gamma(const PhysParams& P, double x, double gamma) {
-  if (P.gamma14) return pow_7_5(x);
+  if (P.gamma14) return pow_7_5(x, P.pow_dg);
   return pow(x, gamma);
 }
 __device__ __forceinline__ float pow_gamma(const PhysParams&, float x, float gamma) { return pow(x, gamma); }

@@ -364,6 +364,8 @@ void build_phys(mge_ctx* c) {
   Q.irs_kind = P.irs_variant;
   Q.unsteady = P.execmode == 1;
   Q.gamma14 = P.gamma == 1.4;
+  Q.pow_dg = std::fma(P.gamma, 5.0, -7.0) / 5.0;    // exact 5*gamma - 7, then /5
+  Q.pow_dm = Q.gm - 2.5;                            // exact: both near 2.5
   Q.dtstep = P.dtstep;
   Q.viscl = P.viscl;
   Q.gas_const = P.gas_const;

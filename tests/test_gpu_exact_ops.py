@@ -23,7 +23,7 @@ def test_exact_ops_match_fp64(tmp_path):
     assert "mismatches 0 " in r.stdout
 
 
-def test_fast_powers_stay_within_three_ulp_of_pow(tmp_path):
+def test_fast_powers_stay_within_four_ulp_of_pow(tmp_path):
     # x^(5/2) and x^(7/5) of the far-field boundary (fast_pow.cuh) against
     # CUDA's pow at the double exponents 1/(gamma-1) and gamma, gamma = 1.4
     exe = str(tmp_path / "fast_pow_check")
