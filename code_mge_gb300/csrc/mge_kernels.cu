@@ -25,6 +25,7 @@
 // 1990), so results stay bit-identical to IEEE a/b at a third of its cost.
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 
 #include <cooperative_groups.h>
 #include <algorithm>
@@ -2036,7 +2037,7 @@ __device__ __forceinline__ unsigned long long gtimer() {
 }
 
 template <typename T, typename TA>
-__global__ void __launch_bounds__(256, 2) k_euler_coop(DevBlock<T> b, PhysParams P, EulerArgs E) {
+__global__ void __launch_bounds__(256, 1) k_euler_coop(DevBlock<T> b, PhysParams P, EulerArgs E) {
   cg::grid_group g_ = cg::this_grid();
   int ntr = 0;
   struct Sync {
@@ -2256,16 +2257,21 @@ void launch_bcond(const DevBlock<T>& b, const PhysParams& P, cudaStream_t s) {
                              (long long)(b.ib + 1) * (b.jb + 1));
   // one cooperative launch when every block it needs fits on the device at once
   static int resident[64] = {0};
+  static int coop_env = -1;
+  if (coop_env < 0) {
+    const char* e = getenv("MGE_BCOND_COOP");
+    coop_env = (e && atoi(e) == 0) ? 0 : 1;
+  }
   int dev = 0;
   cudaGetDevice(&dev);
-  if (dev >= 0 && dev < 64 && resident[dev] == 0) {
+  if (coop_env && dev >= 0 && dev < 64 && resident[dev] == 0) {
     int nsm = 0, per = 0, coop = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_bcond_coop<T>, TPB, 0);
     resident[dev] = (coop && per > 0) ? nsm * per : -1;
   }
-  const int grid = (dev >= 0 && dev < 64) ? resident[dev] : -1;
+  const int grid = (coop_env && dev >= 0 && dev < 64) ? resident[dev] : -1;
   if (grid > 0) {
     const int need = (int)std::max<long long>(1, std::min<long long>(nblk(n, TPB), grid));
     DevBlock<T> bb = b;

@@ -39,7 +39,8 @@ class Request:
     arrival: float = 0.0
     semi: tuple = (1.0, 0.7, 0.5)
     max_cycles: int = 2000
-    refine_drop: float = 1e-6  # mixed form: switch to FP64 at this residual drop
+    refine_drop: float = 1e-6  # mixed form: switch to FP64 at this residual drop ...
+    refine_stall: int = 40     # ... or once the residual has not improved by 5 % for this many cycles
     # results
     t_admit: float = None
     t_done: float = None
@@ -139,11 +140,12 @@ class FakeBackend:
     """Deterministic stand-in used by the CPU tests: each case's residual falls
     geometrically per cycle; a cycle completes after `latency` polls."""
 
-    def __init__(self, free_bytes=1 << 34, rate=0.7, latency=2):
+    def __init__(self, free_bytes=1 << 34, rate=0.7, latency=2, floor32=0.0):
         self.free = free_bytes
         self.rate = rate
         self.latency = latency
         self.launched = 0
+        self.floor32 = floor32     # mixed form: the residual stalls here until refined
 
     def free_memory(self):
         return self.free
@@ -161,7 +163,10 @@ class FakeBackend:
         h["busy"] -= 1
         if h["busy"] > 0:
             return 1, 0.0
-        h["res"] *= self.rate
+        nxt = h["res"] * self.rate
+        if h["case"].prm.precision == A.MGE_PREC_MIXED and not h.get("refined"):
+            nxt = max(nxt, self.floor32)
+        h["res"] = nxt
         return 0, h["res"]
 
     def prolong(self, h, mlvl):
@@ -191,6 +196,8 @@ class _Slot:
     inflight: bool = False
     cycles_fine: int = 0
     refined: bool = False
+    best: float = None         # best finest-level residual so far, and the cycle it came at
+    best_at: int = 0
 
 
 class Server:
@@ -286,8 +293,13 @@ class Server:
                     s.ini = res
                 s.req.residual = res
                 s.req.drop = res / s.ini if s.ini else None
+                if s.best is None or res < 0.95 * s.best:
+                    s.best, s.best_at = res, s.cycles_fine
+                # FP32 coarse corrections stall near eps32 * |tau|: switch to
+                # FP64 at the set drop, or as soon as the residual stops falling
+                stalled = s.req.refine_stall > 0 and s.cycles_fine - s.best_at >= s.req.refine_stall
                 if (s.req.precision == A.MGE_PREC_MIXED and not s.refined and s.ini
-                        and s.req.refine_drop > 0.0 and res <= s.req.refine_drop * s.ini):
+                        and ((s.req.refine_drop > 0.0 and res <= s.req.refine_drop * s.ini) or stalled)):
                     if self.be.refine(s.handle) != 0:
                         self._retire(s, "precision refinement failed")
                         continue

@@ -47,6 +47,20 @@ def test_admission_is_gated_by_free_memory():
     assert be.free == int(2.5 * one)  # every case released its memory
 
 
+def test_mixed_case_refines_when_its_residual_stalls():
+    # the fake's mixed residual stops at 1e-4 until the case switches to FP64
+    be = S.FakeBackend(rate=0.5, latency=1, floor32=1e-4)
+    srv = S.Server(be, reserve_bytes=0, clock=FakeClock())
+    r = S.Request(0, "sphere", 16, 0.5, tol=1e-8, max_cycles=500, refine_drop=1e-9, refine_stall=20)
+    srv.submit(r)
+    (d,) = srv.run(idle_sleep=0)
+    assert d.converged and d.refined_at is not None
+    # the coarse FMG cycles already halve the fake residual 10 times: the
+    # floor is reached in the 4th finest cycle, the stall is seen 20 later
+    assert d.refined_at == 24
+    assert d.cycles < 80
+
+
 def test_poisson_and_sweep_generators_are_seeded():
     a = S.poisson_requests(4.0, 10.0)
     b = S.poisson_requests(4.0, 10.0)
