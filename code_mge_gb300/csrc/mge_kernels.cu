@@ -2125,6 +2125,23 @@ __global__ void __launch_bounds__(256, 1) k_euler_coop(DevBlock<T> b, PhysParams
 // =============================================================== launchers
 constexpr int TPB = 256;
 
+// Threads per block for n work items: 256, halved down to 32 while the grid
+// would not give every SM two blocks.  The stage kernels are bound by the FP64
+// pipe of the SMs they run on, so on the small coarse levels spreading the
+// cells over all SMs is worth more than wide blocks.
+inline int tpb_for(long long n) {
+  static int nsm = 0;
+  if (!nsm) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0) nsm = 152;
+  }
+  int t = TPB;
+  while (t > 32 && n < (long long)t * nsm * 2) t >>= 1;
+  return t;
+}
+#define LAUNCH_N(n) nblk((n), tpb_for(n)), tpb_for(n)
+
 template <typename T>
 void launch_solut(const DevBlock<T>& b, const PhysParams& P, double rm, double p_tot, int ns, double* out,
                   cudaStream_t s) {
@@ -2138,9 +2155,9 @@ void launch_timestep(const DevBlock<T>& b, const PhysParams& P, unsigned* err, c
   long long n = (long long)b.nx * b.ny * b.nz;
   k_dtim_reset<<<1, 32, 0, s>>>(b.dtim);
   if (aux32)
-    k_timestep<T, float><<<nblk(n, TPB), TPB, 0, s>>>(b, P, err);
+    k_timestep<T, float><<<LAUNCH_N(n), 0, s>>>(b, P, err);
   else
-    k_timestep<T, T><<<nblk(n, TPB), TPB, 0, s>>>(b, P, err);
+    k_timestep<T, T><<<LAUNCH_N(n), 0, s>>>(b, P, err);
 }
 
 template <typename T>
@@ -2148,18 +2165,18 @@ void launch_stage_part(int part, const DevBlock<T>& b, const PhysParams& P, cons
                        cudaStream_t s) {
   if (part == 0) {
     long long n1 = (long long)b.ie * b.je * b.ke;
-    k_prep<T><<<nblk(n1, TPB), TPB, 0, s>>>(b, P, A.dissip_on);
+    k_prep<T><<<LAUNCH_N(n1), 0, s>>>(b, P, A.dissip_on);
   } else if (part == 1) {
     long long n2 = (long long)(b.ie - 1) * (b.je - 1) * (b.ke - 1);
     if (!A.dissip_on && P.distype == 0)
-      k_face_conv<T><<<nblk(n2, TPB), TPB, 0, s>>>(b);
+      k_face_conv<T><<<LAUNCH_N(n2), 0, s>>>(b);
     else
-      k_face<T><<<nblk(n2, TPB), TPB, 0, s>>>(b, P, A.dissip_on, (T)A.cd);
+      k_face<T><<<LAUNCH_N(n2), 0, s>>>(b, P, A.dissip_on, (T)A.cd);
   } else if (part == 2) {
-    if (b.nmir > 0) k_rec_wall<T><<<nblk(b.nmir, 64), 64, 0, s>>>(b, P, A.dissip_on, (T)A.cd, err);
+    if (b.nmir > 0) k_rec_wall<T><<<LAUNCH_N(b.nmir), 0, s>>>(b, P, A.dissip_on, (T)A.cd, err);
   } else if (part == 3) {
     long long n3 = (long long)b.nx * b.ny * b.nz;
-    k_combine<T><<<nblk(n3, TPB), TPB, 0, s>>>(b, P, A, err);
+    k_combine<T><<<LAUNCH_N(n3), 0, s>>>(b, P, A, err);
   }
 }
 
@@ -2197,7 +2214,7 @@ void launch_irs_dir(const DevBlock<T>& b, const IrsTables& tb, TC bb, cudaStream
     const long long grid = 5 * ((lines + LT - 1) / LT);
     k_irs_smem<T, TC, D, LT><<<(unsigned)grid, LT, sm, s>>>(b, tb, bb);
   } else {
-    k_irs<T, TC, D><<<nblk(5 * lines, 128), 128, 0, s>>>(b, tb, bb);
+    k_irs<T, TC, D><<<LAUNCH_N(5 * lines), 0, s>>>(b, tb, bb);
   }
 }
 
@@ -2215,11 +2232,11 @@ void launch_irs_part_t(int part, const DevBlock<T>& b, const PhysParams& P, cons
   const TC bb = (TC)(-P.smoo);
   const long long ncell = (long long)b.nx * b.ny * b.nz;
   if (P.irs_kind == 1) {  // psmoo + progon3: one thread per line
-    if (part == 0) k_psmoo_line<T, TC, 0><<<nblk(irs_lines_h(b, 0), 128), 128, 0, s>>>(b);
-    if (part == 1) k_psmoo_line<T, TC, 1><<<nblk(irs_lines_h(b, 1), 128), 128, 0, s>>>(b);
+    if (part == 0) k_psmoo_line<T, TC, 0><<<LAUNCH_N(irs_lines_h(b, 0)), 0, s>>>(b);
+    if (part == 1) k_psmoo_line<T, TC, 1><<<LAUNCH_N(irs_lines_h(b, 1)), 0, s>>>(b);
     if (part == 2) {
-      k_psmoo_line<T, TC, 2><<<nblk(irs_lines_h(b, 2), 128), 128, 0, s>>>(b);
-      k_update<T><<<nblk(ncell, TPB), TPB, 0, s>>>(b, P, Au);
+      k_psmoo_line<T, TC, 2><<<LAUNCH_N(irs_lines_h(b, 2)), 0, s>>>(b);
+      k_update<T><<<LAUNCH_N(ncell), 0, s>>>(b, P, Au);
     }
     return;
   }
@@ -2227,7 +2244,7 @@ void launch_irs_part_t(int part, const DevBlock<T>& b, const PhysParams& P, cons
   if (part == 1) launch_irs_dir<T, TC, 1>(b, tab[1], bb, s, variant ? variant[1] : 0);
   if (part == 2) {
     launch_irs_dir<T, TC, 2>(b, tab[2], bb, s, variant ? variant[2] : 0);
-    k_update<T><<<nblk(ncell, TPB), TPB, 0, s>>>(b, P, Au);
+    k_update<T><<<LAUNCH_N(ncell), 0, s>>>(b, P, Au);
   }
 }
 
@@ -2248,41 +2265,44 @@ void launch_irs(const DevBlock<T>& b, const PhysParams& P, const IrsTables* tab,
 
 template <typename T>
 void launch_cutcell(const DevBlock<T>& b, const PhysParams& P, unsigned* err, cudaStream_t s) {
-  if (b.nmir > 0) k_cutcell<T><<<nblk(b.nmir, 128), 128, 0, s>>>(b, P, err);
+  if (b.nmir > 0) k_cutcell<T><<<LAUNCH_N(b.nmir), 0, s>>>(b, P, err);
 }
 
 template <typename T>
 void launch_bcond(const DevBlock<T>& b, const PhysParams& P, cudaStream_t s) {
   const long long n = 2LL * ((long long)(b.jb + 1) * (b.kb + 1) + (long long)(b.ib + 1) * (b.kb + 1) +
                              (long long)(b.ib + 1) * (b.jb + 1));
-  // one cooperative launch when every block it needs fits on the device at once
-  static int resident[64] = {0};
+  const int tpb = tpb_for(n);
+  // one cooperative launch when every block it needs fits on the device at
+  // once (residency per block size: 32, 64, 128, 256 threads)
+  static int resident[64][4] = {};
   static int coop_env = -1;
   if (coop_env < 0) {
     const char* e = getenv("MGE_BCOND_COOP");
     coop_env = (e && atoi(e) == 0) ? 0 : 1;
   }
+  const int ti = tpb == 32 ? 0 : (tpb == 64 ? 1 : (tpb == 128 ? 2 : 3));
   int dev = 0;
   cudaGetDevice(&dev);
-  if (coop_env && dev >= 0 && dev < 64 && resident[dev] == 0) {
+  if (coop_env && dev >= 0 && dev < 64 && resident[dev][ti] == 0) {
     int nsm = 0, per = 0, coop = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_bcond_coop<T>, TPB, 0);
-    resident[dev] = (coop && per > 0) ? nsm * per : -1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_bcond_coop<T>, tpb, 0);
+    resident[dev][ti] = (coop && per > 0) ? nsm * per : -1;
   }
-  const int grid = (coop_env && dev >= 0 && dev < 64) ? resident[dev] : -1;
+  const int grid = (coop_env && dev >= 0 && dev < 64) ? resident[dev][ti] : -1;
   if (grid > 0) {
-    const int need = (int)std::max<long long>(1, std::min<long long>(nblk(n, TPB), grid));
+    const int need = (int)std::max<long long>(1, std::min<long long>(nblk(n, tpb), grid));
     DevBlock<T> bb = b;
     PhysParams pp = P;
     void* args[] = {&bb, &pp};
-    if (cudaLaunchCooperativeKernel((void*)k_bcond_coop<T>, need, TPB, args, 0, s) == cudaSuccess) return;
+    if (cudaLaunchCooperativeKernel((void*)k_bcond_coop<T>, need, tpb, args, 0, s) == cudaSuccess) return;
     cudaGetLastError();
   }
-  for (int pass = 0; pass < 3; pass++) k_bc_pass<T><<<nblk(n, TPB), TPB, 0, s>>>(b, P, pass);
-  for (int phase = 0; phase < 3; phase++)
-    k_bc_corner<T><<<phase == 2 ? 1 : nblk(4LL * (b.ib + b.jl + b.kl + 2), TPB), TPB, 0, s>>>(b, P, phase);
+  for (int pass = 0; pass < 3; pass++) k_bc_pass<T><<<LAUNCH_N(n), 0, s>>>(b, P, pass);
+  const long long nc = 4LL * (b.ib + b.jl + b.kl + 2);  // covers the items of phases 0 and 1
+  for (int phase = 0; phase < 3; phase++) k_bc_corner<T><<<LAUNCH_N(phase == 2 ? 8 : nc), 0, s>>>(b, P, phase);
 }
 
 template <typename T>
@@ -2398,7 +2418,7 @@ void launch_collc(const DevBlock<TC>& c, const DevBlock<TF>& f, const int ratio[
     X.o[d] = offset[d];
   }
   long long n = (long long)(f.nx / ratio[0]) * (f.ny / ratio[1]) * (f.nz / ratio[2]);
-  k_collc<TC, TF><<<nblk(n, TPB), TPB, 0, s>>>(c, f, X, marker_c);
+  k_collc<TC, TF><<<LAUNCH_N(n), 0, s>>>(c, f, X, marker_c);
 }
 
 template <typename TF, typename TC>
@@ -2410,7 +2430,7 @@ void launch_addw(const DevBlock<TF>& f, const DevBlock<TC>& c, const int ratio[3
     X.o[d] = offset[d];
   }
   long long n = (long long)f.nx * f.ny * f.nz;
-  k_addw<TF, TC><<<nblk(n, TPB), TPB, 0, s>>>(f, c, X, fmg);
+  k_addw<TF, TC><<<LAUNCH_N(n), 0, s>>>(f, c, X, fmg);
 }
 
 template <typename TF, typename TC>
@@ -2421,7 +2441,7 @@ void launch_embed(const DevBlock<TF>& f, const DevBlock<TC>& c, const int ratio[
     X.r[d] = ratio[d];
     X.o[d] = offset[d];
   }
-  k_embed<TF, TC><<<nblk(f.N, TPB), TPB, 0, s>>>(f, c, X, P.gamma);
+  k_embed<TF, TC><<<LAUNCH_N(f.N), 0, s>>>(f, c, X, P.gamma);
 }
 
 template <typename T>
