@@ -2273,13 +2273,15 @@ void launch_bcond(const DevBlock<T>& b, const PhysParams& P, cudaStream_t s) {
   const long long n = 2LL * ((long long)(b.jb + 1) * (b.kb + 1) + (long long)(b.ib + 1) * (b.kb + 1) +
                              (long long)(b.ib + 1) * (b.jb + 1));
   const int tpb = tpb_for(n);
-  // one cooperative launch when every block it needs fits on the device at
-  // once (residency per block size: 32, 64, 128, 256 threads)
+  // Six launches (three face passes, three corner phases) measured a little
+  // faster inside the cycle graphs than one cooperative launch with grid
+  // barriers; MGE_BCOND_COOP=1 selects the cooperative form (when every block
+  // it needs fits on the device at once; residency per block size).
   static int resident[64][4] = {};
   static int coop_env = -1;
   if (coop_env < 0) {
     const char* e = getenv("MGE_BCOND_COOP");
-    coop_env = (e && atoi(e) == 0) ? 0 : 1;
+    coop_env = (e && atoi(e) == 1) ? 1 : 0;
   }
   const int ti = tpb == 32 ? 0 : (tpb == 64 ? 1 : (tpb == 128 ? 2 : 3));
   int dev = 0;
