@@ -2050,7 +2050,9 @@ __global__ void __launch_bounds__(256, 1) k_euler_coop(DevBlock<T> b, PhysParams
     }
   } g{g_, E.trace, ntr};
   if (E.trace && blockIdx.x == 0 && threadIdx.x == 0) E.trace[0] = gtimer();
-  const long long gt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  // items go round-robin over the blocks (item q to block q mod G), so that
+  // the few cells of a small level still spread over every SM's FP64 pipe
+  const long long gt = (long long)threadIdx.x * gridDim.x + blockIdx.x;
   const long long gs = (long long)gridDim.x * blockDim.x;
   const long long ncell = (long long)b.nx * b.ny * b.nz;
   if (E.do_timestep) {
@@ -2361,7 +2363,10 @@ int launch_euler_coop(const DevBlock<T>& b, const PhysParams& P, const EulerLaun
   int grid = aux32 ? coop_grid<T, float>(device) : coop_grid<T, T>(device);
   if (grid <= 0) return -1;
   long long work = (long long)(b.ie) * b.je * b.ke;
-  int need = (int)std::min<long long>((work + 255) / 256, (long long)grid);
+  static int nsm = 0;
+  if (!nsm && cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) nsm = 1;
+  // at least one block per SM: the kernel deals items round-robin over the blocks
+  int need = (int)std::min<long long>(std::max<long long>((work + 255) / 256, nsm), (long long)grid);
   if (L.max_ctas > 0 && need > L.max_ctas) need = L.max_ctas;
   if (need < 1) need = 1;
   EulerArgs E;
