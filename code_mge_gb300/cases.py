@@ -32,12 +32,30 @@ from . import _abi as A
 # --------------------------------------------------------------------- bodies
 @dataclass
 class Body:
-    kind: str                      # "cylinder" (axis z), "sphere", "ellipsoid", "none"
+    kind: str                      # "cylinder" (axis z), "sphere", "ellipsoid", "polygon", "none"
     center: tuple = (0.0, 0.0, 0.0)
     radius: float = 0.5
     semi: tuple = (0.5, 0.5, 0.5)  # ellipsoid semi-axes
+    poly: object = None            # polygon: (m, 2) section vertices across the span axis
+    span_axis: int = 1             # polygon: the axis it is extruded along
+
+    def _across(self, a, b, c):
+        """The two coordinates across the span axis."""
+        return [v for q, v in enumerate((a, b, c)) if q != self.span_axis]
 
     def inside(self, x, y, z):
+        if self.kind == "polygon":  # even-odd rule on the section
+            u, v = self._across(x, y, z)
+            u, v = np.broadcast_arrays(u, v)
+            res = np.zeros(u.shape, dtype=bool)
+            P = np.asarray(self.poly, dtype=np.float64)
+            for q in range(len(P)):
+                (u1, v1), (u2, v2) = P[q], P[(q + 1) % len(P)]
+                crosses = (v1 > v) != (v2 > v)
+                with np.errstate(divide="ignore", invalid="ignore"):
+                    ux = u1 + (v - v1) * (u2 - u1) / (v2 - v1)
+                res ^= crosses & (u < ux)
+            return res
         cx, cy, cz = self.center
         if self.kind == "cylinder":
             return (x - cx) ** 2 + (y - cy) ** 2 < self.radius ** 2
@@ -77,6 +95,32 @@ class Body:
             n = xw / s ** 2
             n = n / np.linalg.norm(n, axis=1)[:, None]
             return c + xw, n
+        if self.kind == "polygon":
+            # the nearest point of the section's edges; the outward normal
+            # points from the (inside) point to it, or along the edge normal
+            # for a point on the edge
+            keep = [a for a in range(3) if a != self.span_axis]
+            P = np.asarray(self.poly, dtype=np.float64)
+            A2, B2 = P, np.roll(P, -1, axis=0)
+            q2 = p[:, keep]
+            d = B2 - A2
+            t = np.einsum("mnk,nk->mn", q2[:, None, :] - A2[None], d) / np.maximum(np.sum(d * d, axis=1), 1e-300)
+            t = np.clip(t, 0.0, 1.0)
+            near = A2[None] + t[..., None] * d[None]
+            dist = np.linalg.norm(near - q2[:, None, :], axis=2)
+            e = np.argmin(dist, axis=1)
+            w2 = near[np.arange(len(p)), e]
+            g = w2 - q2
+            gl = np.linalg.norm(g, axis=1)
+            de = d[e]
+            en = np.stack([de[:, 1], -de[:, 0]], axis=1)
+            en = en / np.maximum(np.linalg.norm(en, axis=1), 1e-300)[:, None]
+            n2 = np.where(gl[:, None] > 1e-14, g / np.maximum(gl, 1e-300)[:, None], en)
+            xw = p.copy()
+            n = np.zeros_like(p)
+            xw[:, keep] = w2
+            n[:, keep] = n2
+            return xw, n
         raise ValueError(self.kind)
 
 
