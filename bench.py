@@ -63,8 +63,23 @@ LAUNCHES_PER_UPDATE = {"timestep": 1, "prep": 5, "face": 5, "rec": 5, "combine":
                        "irs_k_update": 3, "cutcell": 5, "bcond": 5, "rtrms": 1}
 
 
-def workload_case(precision="fp64", n=192):
+WORKLOADS = {
+    "sphere192": "sphere D=1 in 192^3 box [-10,10]^3, M=0.5, JST scalar, 5-stage RK, CFL 2.8, IRS 0.6, "
+                 "4-level W-cycle; step = 1 W-cycle",
+    "cylinder512ns": "laminar NS cylinder D=1, Re=40, M=0.2, 512x512x2 finest grid at h=D/96 with 3 coarser "
+                     "embedded levels (each doubling h and extent), Roe MUSCL + viscous fluxes, adiabatic no-slip "
+                     "cut-cell wall, 5-stage RK, CFL 2.8, IRS 0.6, 4-level V-cycle; step = 1 V-cycle",
+}
+
+
+GEOMETRY = {"sphere192": "sphere", "cylinder512ns": "cylinder"}
+
+
+def workload_case(precision="fp64", n=192, name="sphere192"):
     prec = A.MGE_PREC_MIXED if precision == "mixed" else A.MGE_PREC_FP64
+    if name == "cylinder512ns":
+        return K.cylinder_embedded(n=512, span=2, nlevel=4, h_fine=1.0 / 96.0, mach=0.2, mcyc_fine=200,
+                                   eqntype=A.MGE_EQN_NS, distype=A.MGE_DIS_ROE2, reynolds=40.0, precision=prec)
     return K.sphere_box(n=n, nlevel=4, extent=10.0, mach=0.5, mgtype=2, mcyc_fine=400, smoo=0.6,
                         precision=prec)
 
@@ -75,6 +90,8 @@ def run_profile(args):
     import torch
     from code_mge_gb300.runtime import Cycle, load_library
     lib = load_library()
+    if not args.workload.startswith("sphere"):
+        raise SystemExit("--profile takes a sphere workload")
     n = int(args.workload[len("sphere"):])
     case = workload_case(args.precision, n=n)
     cyc = Cycle(case)
@@ -192,7 +209,8 @@ def run_reference(args):
     if rank != 0:
         return 0
     threads = os.cpu_count() or 1
-    case = workload_case("fp64")
+    wl = args.workload if args.workload in WORKLOADS else "sphere192"
+    case = workload_case("fp64", name=wl)
     cu = S.cell_updates_per_cycle(case)
     from oracle.oracle import OracleCycle, set_threads
     set_threads(threads)
@@ -207,12 +225,11 @@ def run_reference(args):
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (analytic sphere geometry)",
-        "config": {"workload": "sphere D=1 in 192^3 box [-10,10]^3, M=0.5, JST scalar, 5-stage RK, CFL 2.8, "
-                               "IRS 0.6, 4-level W-cycle; step = 1 W-cycle", "cells_finest": 192 ** 3,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (analytic %s geometry)" % GEOMETRY[wl],
+        "config": {"workload": WORKLOADS[wl], "cells_finest": case.finest_cells,
                    "cell_updates_per_step": cu},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": "%d W-cycles of the 192^3 case, OpenMP over %d host threads" % (args.steps, threads)},
+                         "sample": "%d cycles of the same case, OpenMP over %d host threads" % (args.steps, threads)},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference (Fortran mgsol/pmgsol) cannot be built or run here; the timed CPU implementation is "
                 "the line-by-line C++ restatement of its algorithm",
@@ -231,7 +248,8 @@ def run_gpu(args):
     dev = local
     from code_mge_gb300.runtime import Cycle, load_library
     lib = load_library()
-    case = workload_case(args.precision)
+    wl = args.workload if args.workload in WORKLOADS else "sphere192"
+    case = workload_case(args.precision, name=wl)
     cu = S.cell_updates_per_cycle(case)
     L = case.prm.nlevel
     cyc = Cycle(case, device=dev)
@@ -302,10 +320,13 @@ def run_gpu(args):
     t_face = face_stage_ms[0]                      # stage 1: dissipation on
     alg = 8.0 * FACE_DOUBLES_DISSIP * face_cells
     achieved = alg / (t_face * 1e-3) / 1e9 if t_face > 0 else 0.0
-    traffic = FACE_DRAM_BYTES_PER_CELL * face_cells
+    # the measured per-cell traffic and FP64 count are those of the Euler JST
+    # face pass; other schemes get the bytes model only
+    jst = case.prm.eqntype == A.MGE_EQN_EULER and case.prm.distype == A.MGE_DIS_CENTRAL
+    traffic = FACE_DRAM_BYTES_PER_CELL * face_cells if jst else None
     clk = (clocks.get("sm_mhz") or 2070.0) * 1e6
     fp64_peak = FP64_LANES_PER_SM_CYCLE * GB300_SMS * clk
-    fp64_achieved = FACE_FP64_PER_CELL * face_cells / (t_face * 1e-3) if t_face > 0 else 0.0
+    fp64_achieved = FACE_FP64_PER_CELL * face_cells / (t_face * 1e-3) if (t_face > 0 and jst) else None
     upd_ms = sum(kt[k] * LAUNCHES_PER_UPDATE[k] for k in kt)
     whole_update_gbs = BYTES_PER_CELL_UPDATE_IRS * ncell / (upd_ms * 1e-3) / 1e9 if upd_ms > 0 else 0.0
 
@@ -324,7 +345,7 @@ def run_gpu(args):
     if rank == 0 and world == 1 and not args.no_cpu:
         dt = time_cpu_oracle(case, threads=1, cycles=1)
         cpu = {"value": cu / dt, "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": "1 W-cycle of the same 192^3 case on 1 host thread (%.1f s)" % dt}
+               "sample": "1 cycle of the same case on 1 host thread (%.1f s)" % dt}
     cyc.close()
     if rank == 0:
         line = {
@@ -332,13 +353,13 @@ def run_gpu(args):
             "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
             "dtype": "f64" if args.precision == "fp64" else "f64-fine/f32-coarse",
-            "data": "synthetic (analytic sphere geometry, free-stream start)",
-            "config": {"workload": "sphere D=1 in 192^3 box [-10,10]^3, M=0.5, JST scalar, 5-stage RK, CFL 2.8, "
-                                   "IRS 0.6, 4-level W-cycle; step = 1 W-cycle", "cells_finest": ncell,
+            "data": "synthetic (analytic %s geometry, free-stream start)" % GEOMETRY[wl],
+            "config": {"workload": WORKLOADS[wl], "cells_finest": ncell,
                        "cell_updates_per_step": cu, "precision": args.precision,
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "launch_plan": plan,
-                       "l2": "fields of 301 MB each exceed the 129 MB L2 (no flush needed)"},
+                       "l2": "finest fields of %.0f MB each exceed the 129 MB L2 (no flush needed)"
+                             % (5 * 8 * sp.dims[0] * sp.dims[1] * sp.dims[2] / 1e6)},
             "wall_ms_per_step": 1e3 * wall / args.steps,
             "residual_last": res[-1] if res else None,
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(w_np.nbytes), "d2h_bytes_per_step": 8},
@@ -453,7 +474,7 @@ def main():
     ap.add_argument("--duration", type=float, default=300.0)
     ap.add_argument("--drain", type=float, default=120.0)
     ap.add_argument("--coop-ctas", type=int, default=32)
-    ap.add_argument("--workload", default="sphere192", choices=["sphere192", "sphere128", "sphere96"])
+    ap.add_argument("--workload", default="sphere192", choices=["sphere192", "cylinder512ns", "sphere128", "sphere96"])
     ap.add_argument("--profile", action="store_true", help="short run for ncu captures")
     ap.add_argument("--plan-out", default=None, help="write the tuned launch plan (MGE_TUNE_PLAN form) here")
     args = ap.parse_args()
