@@ -51,6 +51,11 @@ BYTES_PER_CELL_UPDATE_IRS = (11 + 4 + 11 + 4 + 11) * 40 + 5 * 17 + 56   # 1,781
 # lambda (1), and writes the convective and dissipative face fluxes (15 + 15):
 # 64 doubles.
 FACE_DOUBLES_DISSIP = 64
+# The Roe + viscous face pass (MUSCL states from w and p, viscous stresses
+# from the cell-centred u, v, w, T) on such a stage reads w (5), p (1) and
+# the 4 viscous variables once per cell and writes the convective, upwind
+# and viscous face fluxes (15 + 15 + 15): 55 doubles.
+FACE_DOUBLES_ROE_NS = 55
 # From one ncu capture of that launch on the 128^3 sphere (2,146,689 cells):
 # DRAM read + write 1,111.8 MB = 517.9 B per cell, and 118.2 FP64
 # instructions (DADD + DMUL, no DFMA under --fmad=false) per cell.  Traffic
@@ -318,11 +323,11 @@ def run_gpu(args):
     dims = sp.dims
     face_cells = (dims[0] - 3) * (dims[1] - 3) * (dims[2] - 3)
     t_face = face_stage_ms[0]                      # stage 1: dissipation on
-    alg = 8.0 * FACE_DOUBLES_DISSIP * face_cells
-    achieved = alg / (t_face * 1e-3) / 1e9 if t_face > 0 else 0.0
     # the measured per-cell traffic and FP64 count are those of the Euler JST
-    # face pass; other schemes get the bytes model only
+    # face pass; the Roe + viscous pass gets its bytes model only
     jst = case.prm.eqntype == A.MGE_EQN_EULER and case.prm.distype == A.MGE_DIS_CENTRAL
+    alg = 8.0 * (FACE_DOUBLES_DISSIP if jst else FACE_DOUBLES_ROE_NS) * face_cells
+    achieved = alg / (t_face * 1e-3) / 1e9 if t_face > 0 else 0.0
     traffic = FACE_DRAM_BYTES_PER_CELL * face_cells if jst else None
     clk = (clocks.get("sm_mhz") or 2070.0) * 1e6
     fp64_peak = FP64_LANES_PER_SM_CYCLE * GB300_SMS * clk
@@ -367,11 +372,13 @@ def run_gpu(args):
             "roofline": {"bound": "hbm", "kernel": "k_face (stage 1, dissipation on)", "achieved": achieved,
                          "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                          "algorithmic_bytes_per_launch": alg, "launch_ms": t_face, "peak_kind": pkind,
-                         "note": "the FP64 issue rate, not HBM, bounds this kernel: see fp64_roofline"},
+                         "note": ("the FP64 issue rate, not HBM, bounds this kernel: see fp64_roofline" if jst else
+                                  "Roe + viscous face pass: 55 doubles per cell; its DRAM traffic is not captured")},
             "fp64_roofline": {"kernel": "k_face (stage 1)", "achieved": fp64_achieved / 1e12,
                               "peak": fp64_peak / 1e12, "unit": "T FP64 instr/s", "frac": fp64_achieved / fp64_peak,
                               "fp64_per_cell": FACE_FP64_PER_CELL,
-                              "peak_basis": "2 FP64 thread-ops per SM per cycle x 152 SMs x median SM clock"},
+                              "peak_basis": "2 FP64 thread-ops per SM per cycle x 152 SMs x median SM clock"}
+                             if fp64_achieved is not None else None,
             "face_stage_ms": face_stage_ms,
             "upload_solut": {"ms": solut_ms, "cells": ncell, "d2h_bytes": int(sol.nbytes), "nval": nval.value},
             "whole_update_hbm": {"achieved_gbs": whole_update_gbs, "frac": whole_update_gbs / peak,
@@ -385,6 +392,51 @@ def run_gpu(args):
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+    return 0
+
+
+def run_converge(args):
+    """One workload solved in FP64 and in the mixed form to a residual drop:
+    cycles, wall time, the final drop, Cl and Cd (pressure forces on the wall
+    records) and their differences, and for the cylinder the length of the
+    closed wake on y = 0.  The FP64 solve is the reference the mixed one is
+    measured against; the FP64 path itself matches the oracle to 1e-9 in Cd
+    on the cases the GPU tests solve."""
+    from code_mge_gb300.runtime import Cycle, load_library
+    load_library()
+    wl = args.workload if args.workload in WORKLOADS else "sphere192"
+    out = {}
+    for prec in ("fp64", "mixed"):
+        case = workload_case(prec, name=wl)
+        L = case.prm.nlevel
+        case.prm.conv_drop = 1.0 / args.tol
+        case.prm.mcyc[L - 1] = args.max_cycles
+        cyc = Cycle(case)
+        t0 = time.perf_counter()
+        hist, n, fo = cyc.solve(max_cycles_total=args.max_cycles,
+                                refine_drop=args.refine_drop if prec == "mixed" else 0.0)
+        wall = time.perf_counter() - t0
+        r = {"cycles": int(n), "wall_s": wall, "drop": float(hist[0] / hist[-1]) if len(hist) else None,
+             "converged": bool(len(hist) and hist[0] / hist[-1] > 1.0 / args.tol), "cd": fo.cd, "cl": fo.cl,
+             "residual_last": float(hist[-1]) if len(hist) else None}
+        if GEOMETRY[wl] == "cylinder":
+            levels = [(cyc.field("w", lv), cyc.spec(lv)) for lv in range(L, 0, -1)]
+            r["recirculation_length"] = K.recirculation_length(levels, radius=0.5)
+        cyc.close()
+        out[prec] = r
+    f, m = out["fp64"], out["mixed"]
+    line = {"pattern": "converge", "metric": "time to a %.0e residual drop, FP64 plain vs mixed" % args.tol,
+            "unit": "s", "value": m["wall_s"], "fp64_s": f["wall_s"],
+            "speedup": f["wall_s"] / m["wall_s"] if m["wall_s"] > 0 else None,
+            "abs_dcd": abs(m["cd"] - f["cd"]), "abs_dcl": abs(m["cl"] - f["cl"]),
+            "fp64": f, "mixed": m,
+            "config": {"workload": WORKLOADS[wl], "tol_drop": args.tol, "max_cycles_finest": args.max_cycles,
+                       "refine_drop": args.refine_drop,
+                       "forces": "pressure on the wall records; Cd over q_inf x reference area"}}
+    if "recirculation_length" in f:
+        a, b = f["recirculation_length"], m["recirculation_length"]
+        line["abs_d_recirculation_length"] = abs(a - b) if a is not None and b is not None else None
+    print(json.dumps(line), flush=True)
     return 0
 
 
@@ -465,7 +517,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--pattern", default=None, choices=["batched", "serving"])
+    ap.add_argument("--pattern", default=None, choices=["batched", "serving", "converge"])
+    ap.add_argument("--refine-drop", type=float, default=1e-5,
+                    help="mixed form: switch to FP64 once the residual has dropped by this factor")
     ap.add_argument("--cases", type=int, default=64)
     ap.add_argument("--sizes", default="32,48,64,96,128")
     ap.add_argument("--tol", type=float, default=1e-8)
@@ -480,6 +534,8 @@ def main():
     args = ap.parse_args()
     if args.profile:
         return run_profile(args)
+    if args.pattern == "converge":
+        return run_converge(args)
     if args.pattern:
         return run_pattern(args)
     if args.warmup < 3:

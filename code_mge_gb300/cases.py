@@ -446,6 +446,46 @@ def cylinder_embedded(n=512, span=2, nlevel=4, h_fine=1.0 / 96.0, mach=0.2, mcyc
     return Case("cylinder_embedded_%dx%dx%d" % (n, n, span), prm, levels, body, ref_area=span * h_fine)
 
 
+def recirculation_length(levels, radius=0.5):
+    """Length of the closed wake behind a cylinder whose axis is z, with the
+    free stream along +x: from the rear of the body (x = radius) along y = 0
+    to the first point where the span-averaged u = (rho u)/rho turns from
+    negative to non-negative, linear between cell centres.
+
+    ``levels`` lists (w, spec) pairs, finest first, with w shaped (5, k, j, i)
+    over the block's cells with their two ghost layers (as ``Cycle.field``
+    returns it).  Each x takes the finest level whose physical cells cover it.
+    Returns 0.0 when u is not negative just behind the body, and None when the
+    wake is still open at the last cell."""
+    xs, us, covered = [], [], -np.inf
+    for w, sp in levels:
+        nx, ny, nz = sp.n
+        hx, hy = sp.h[0], sp.h[1]
+        ox, oy = sp.origin[0], sp.origin[1]
+        yc = oy + (np.arange(ny) + 0.5) * hy
+        # the rows straddling y = 0 (one row when a cell centre lies on it)
+        jlo = int(np.searchsorted(yc, 0.0, side="right")) - 1
+        rows = [jlo] if abs(yc[jlo]) <= 1e-12 * hy else [jlo, jlo + 1]
+        ph = w[:, 2:nz + 2, 2:ny + 2, 2:nx + 2]
+        u = np.mean([ph[1, :, j, :] / ph[0, :, j, :] for j in rows], axis=0).mean(axis=0)
+        xc = ox + (np.arange(nx) + 0.5) * hx
+        keep = (xc > radius) & (xc > covered)
+        xs.append(xc[keep])
+        us.append(u[keep])
+        covered = max(covered, ox + nx * hx)
+    x, u = np.concatenate(xs), np.concatenate(us)
+    order = np.argsort(x)
+    x, u = x[order], u[order]
+    if len(x) == 0 or u[0] >= 0.0:
+        return 0.0
+    pos = np.nonzero(u >= 0.0)[0]
+    if len(pos) == 0:
+        return None
+    i = pos[0]
+    x0 = x[i - 1] + (0.0 - u[i - 1]) * (x[i] - x[i - 1]) / (u[i] - u[i - 1])
+    return float(x0 - radius)
+
+
 def free_stream_box(n=(12, 10, 8), nlevel=2, mach=0.5, bctype=(-20,) * 6, **kw):
     """No body: free-stream preservation case."""
     body = Body("none")
