@@ -48,6 +48,8 @@ struct DevBlock {
   // metric (uniform, axis-aligned face vectors)
   double s[3];              // si[0], sj[1], sk[2]
   double hx, hy, hz;        // cell sizes (viscous gradients)
+  double rh[3], r4h[3];     // RN(1/h) and RN(1/(4h)) per axis, for FP64 blocks
+  float rhf[3], r4hf[3];    // the same in single precision, of the single-precision h
   double sqrt_ds[3];        // sqrt(s*s) computed on the host
   double vol;
   double rvol;              // RN(1/vol)
@@ -103,6 +105,8 @@ struct PhysParams {
   double cfac;              // viscous weight of the time step (timestep.f90:119-125)
   double epsentr;           // Harten entropy fix
   double lim_e2[5];         // van Albada floor per primitive variable
+  double rgm1;              // RN(1/(gamma-1))
+  float rgm1f;              // RN(1/(gamma-1)) in single precision, of the single-precision gamma-1
 };
 
 // error word bits

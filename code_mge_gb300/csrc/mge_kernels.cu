@@ -50,6 +50,14 @@ __device__ __forceinline__ float mdiv(float a, float b, float y) {
   float r = fmaf(-q, b, a);
   return fmaf(r, y, q);
 }
+// reciprocals the host prepares once, RN(1/x) of the divisor x in the
+// block's precision, so that mdiv gives the correctly rounded quotient
+__device__ __forceinline__ double rcp_gm1(const PhysParams& P, double) { return P.rgm1; }
+__device__ __forceinline__ float rcp_gm1(const PhysParams& P, float) { return P.rgm1f; }
+__device__ __forceinline__ double rcp_h(const DevBlock<double>& b, int d) { return b.rh[d]; }
+__device__ __forceinline__ float rcp_h(const DevBlock<float>& b, int d) { return b.rhf[d]; }
+__device__ __forceinline__ double rcp_4h(const DevBlock<double>& b, int d) { return b.r4h[d]; }
+__device__ __forceinline__ float rcp_4h(const DevBlock<float>& b, int d) { return b.r4hf[d]; }
 template <typename T> __device__ __forceinline__ T fdimT(T a, T b) { return a > b ? a - b : T(0); }
 template <typename T> __device__ __forceinline__ T fmaxT(T a, T b) { return a > b ? a : b; }
 template <typename T> __device__ __forceinline__ T fminT(T a, T b) { return a < b ? a : b; }
@@ -221,23 +229,27 @@ __device__ __forceinline__ void body_prep(const DevBlock<T>& b, const PhysParams
     for (int a = 0; a < 3; a++) b.vt[a * N + c] = solid ? T(0) : mdiv(w[1 + a], w[0], y);
     b.vt[3 * N + c] = solid ? T(0) : p / (w[0] * (T)P.gas_const);
   }
+  // the MUSCL Roe faces take their central flux from the reconstructed
+  // states, not from the cell fluxes
+  if (P.distype != 2) {
 #pragma unroll
-  for (int d = 0; d < 3; d++) {
-    T s = (T)b.s[d];
-    T f0 = w[1 + d] * s;  // sum(w(2:4)*ss) with the two zero components dropped
-    T f1 = mdiv(f0 * w[1], w[0], y);
-    T f2 = mdiv(f0 * w[2], w[0], y);
-    T f3 = mdiv(f0 * w[3], w[0], y);
-    if (d == 0) f1 = f1 + p * s;
-    if (d == 1) f2 = f2 + p * s;
-    if (d == 2) f3 = f3 + p * s;
-    T f4 = mdiv(f0 * Hc, w[0], y);
-    T* F = b.F + (long long)(d * 5) * N + c;
-    F[0] = f0;
-    F[N] = f1;
-    F[2 * N] = f2;
-    F[3 * N] = f3;
-    F[4 * N] = f4;
+    for (int d = 0; d < 3; d++) {
+      T s = (T)b.s[d];
+      T f0 = w[1 + d] * s;  // sum(w(2:4)*ss) with the two zero components dropped
+      T f1 = mdiv(f0 * w[1], w[0], y);
+      T f2 = mdiv(f0 * w[2], w[0], y);
+      T f3 = mdiv(f0 * w[3], w[0], y);
+      if (d == 0) f1 = f1 + p * s;
+      if (d == 1) f2 = f2 + p * s;
+      if (d == 2) f3 = f3 + p * s;
+      T f4 = mdiv(f0 * Hc, w[0], y);
+      T* F = b.F + (long long)(d * 5) * N + c;
+      F[0] = f0;
+      F[N] = f1;
+      F[2 * N] = f2;
+      F[3 * N] = f3;
+      F[4 * N] = f4;
+    }
   }
   if (dissip_on && P.distype == 0) {
     // the differences the dissipation faces take (dflux.f90:95-99), once per
@@ -253,7 +265,7 @@ __device__ __forceinline__ void body_prep(const DevBlock<T>& b, const PhysParams
       Dl[4 * N] = Hc - (b.w[4 * N + cn] + b.p[cn]);
     }
   }
-  if (dissip_on) {
+  if (dissip_on && P.distype == 0) {  // the pressure sensors of the JST faces
     const long long pl = (long long)b.Pi * b.Pj;
     // i: abs(p(i-1) +2p(i) +p(i+1)), dflux.f90:71-76
     {
@@ -320,20 +332,24 @@ __device__ __forceinline__ T van_albada(T a, T b, T e2) {
   return ((b * b + e2) * a + (a * a + e2) * b) / (a * a + b * b + T(2) * e2);
 }
 
+// yl, yr: RN(1/wl[0]) and RN(1/wr[0]); every quotient below that shares a
+// divisor takes one reciprocal and mdiv, which rounds as the division does
 template <typename T>
-__device__ __noinline__ void roe_diss(const PhysParams& P, int d, T S, const T* wl, T pl, const T* wr, T pr, T* out) {
+__device__ __noinline__ void roe_diss(const PhysParams& P, int d, T S, const T* wl, T pl, const T* wr, T pr, T yl, T yr,
+                                      T* out) {
   const T g = (T)P.gamma;
   T ul[3], ur[3];
   for (int a = 0; a < 3; a++) {
-    ul[a] = wl[1 + a] / wl[0];
-    ur[a] = wr[1 + a] / wr[0];
+    ul[a] = mdiv(wl[1 + a], wl[0], yl);
+    ur[a] = mdiv(wr[1 + a], wr[0], yr);
   }
-  T hl = (wl[4] + pl) / wl[0], hr = (wr[4] + pr) / wr[0];
-  T rt = sqrt(wr[0] / wl[0]);
+  T hl = mdiv(wl[4] + pl, wl[0], yl), hr = mdiv(wr[4] + pr, wr[0], yr);
+  T rt = sqrt(mdiv(wr[0], wl[0], yl));
   T rh = rt * wl[0];
+  const T den = T(1) + rt, yden = T(1) / den;
   T uh[3];
-  for (int a = 0; a < 3; a++) uh[a] = (ul[a] + rt * ur[a]) / (T(1) + rt);
-  T hh = (hl + rt * hr) / (T(1) + rt);
+  for (int a = 0; a < 3; a++) uh[a] = mdiv(ul[a] + rt * ur[a], den, yden);
+  T hh = mdiv(hl + rt * hr, den, yden);
   T q2 = uh[0] * uh[0] + uh[1] * uh[1] + uh[2] * uh[2];
   T c2 = (g - T(1)) * (hh - T(0.5) * q2);
   T ch = sqrt(fmaxT(c2, (T)1e-300));
@@ -346,9 +362,10 @@ __device__ __noinline__ void roe_diss(const PhysParams& P, int d, T S, const T* 
     return (a < delta && delta > T(0)) ? (lam * lam + delta * delta) / (T(2) * delta) : a;
   };
   T l1 = fix(un - ch), l2 = fix(un), l5 = fix(un + ch);
-  T a1 = (dp - rh * ch * dun) / (T(2) * c2);
+  const T c22 = T(2) * c2, yc22 = T(1) / c22;
+  T a1 = mdiv(dp - rh * ch * dun, c22, yc22);
   T a2 = dr - dp / c2;
-  T a5 = (dp + rh * ch * dun) / (T(2) * c2);
+  T a5 = mdiv(dp + rh * ch * dun, c22, yc22);
   T sh[3];
   for (int a = 0; a < 3; a++) sh[a] = rh * (du[a] - (a == d ? dun : T(0)));
   T k1[5], k5[5];
@@ -386,9 +403,9 @@ __device__ __noinline__ void face_states(const DevBlock<T>& b, const PhysParams&
   T qv[4][5];  // primitive (rho,u,v,w,p) at q-2..q+1
   for (int o = 0; o < 4; o++) {
     long long co = c + (o - 2) * st;
-    T r = b.w[co];
+    T r = b.w[co], yr = T(1) / r;
     qv[o][0] = r;
-    for (int a = 0; a < 3; a++) qv[o][1 + a] = b.w[(1 + a) * N + co] / r;
+    for (int a = 0; a < 3; a++) qv[o][1 + a] = mdiv(b.w[(1 + a) * N + co], r, yr);
     qv[o][4] = b.p[co];
   }
   T L[5], R[5];
@@ -399,28 +416,29 @@ __device__ __noinline__ void face_states(const DevBlock<T>& b, const PhysParams&
     R[kq] = qv[2][kq] - T(0.5) * van_albada(d0, dp, e2);
   }
   if (L[0] <= T(0) || R[0] <= T(0) || L[4] <= T(0) || R[4] <= T(0)) return;
-  const T gm1 = (T)P.gamma - T(1);
+  const T gm1 = (T)P.gamma - T(1), rg = rcp_gm1(P, T(0));
   wl[0] = L[0];
   wr[0] = R[0];
   for (int a = 0; a < 3; a++) {
     wl[1 + a] = L[0] * L[1 + a];
     wr[1 + a] = R[0] * R[1 + a];
   }
-  wl[4] = L[4] / gm1 + T(0.5) * L[0] * (L[1] * L[1] + L[2] * L[2] + L[3] * L[3]);
-  wr[4] = R[4] / gm1 + T(0.5) * R[0] * (R[1] * R[1] + R[2] * R[2] + R[3] * R[3]);
+  wl[4] = mdiv(L[4], gm1, rg) + T(0.5) * L[0] * (L[1] * L[1] + L[2] * L[2] + L[3] * L[3]);
+  wr[4] = mdiv(R[4], gm1, rg) + T(0.5) * R[0] * (R[1] * R[1] + R[2] * R[2] + R[3] * R[3]);
   *pl = L[4];
   *pr = R[4];
 }
 
+// y = RN(1/w[0])
 template <typename T>
-__device__ __forceinline__ void ceflux_gen(int D, const T* w, T p, T s, T* f) {
+__device__ __forceinline__ void ceflux_gen(int D, const T* w, T p, T s, T y, T* f) {
   T f0 = w[1 + D] * s;
   f[0] = f0;
-  f[1] = f0 * w[1] / w[0];
-  f[2] = f0 * w[2] / w[0];
-  f[3] = f0 * w[3] / w[0];
+  f[1] = mdiv(f0 * w[1], w[0], y);
+  f[2] = mdiv(f0 * w[2], w[0], y);
+  f[3] = mdiv(f0 * w[3], w[0], y);
   f[1 + D] = f[1 + D] + p * s;
-  f[4] = f0 * (w[4] + p) / w[0];
+  f[4] = mdiv(f0 * (w[4] + p), w[0], y);
 }
 
 // laminar viscous flux through face q along D (at cell c), times S
@@ -435,9 +453,10 @@ __device__ __noinline__ void visc_face(const DevBlock<T>& b, const PhysParams& P
     const T* f = b.vt + (long long)a * N;
     for (int t = 0; t < 3; t++) {
       if (t == D)
-        g[a][t] = (f[c] - f[cl]) / (T)h[D];
+        g[a][t] = mdiv(f[c] - f[cl], (T)h[D], rcp_h(b, D));
       else
-        g[a][t] = ((f[c + st[t]] - f[c - st[t]]) + (f[cl + st[t]] - f[cl - st[t]])) / (T(4) * (T)h[t]);
+        g[a][t] = mdiv((f[c + st[t]] - f[c - st[t]]) + (f[cl + st[t]] - f[cl - st[t]]), T(4) * (T)h[t],
+                       rcp_4h(b, t));
     }
   }
   const T mu = (T)P.viscl, kt = (T)P.kt;
@@ -454,7 +473,10 @@ __device__ __noinline__ void visc_face(const DevBlock<T>& b, const PhysParams& P
 // --------------------------------------------------------------- stage: per-face pass
 // Thread (i,j,k) in [2..ie]x[2..je]x[2..ke] owns the lower face of cell
 // (i,j,k) in each direction whose tangential indices are physical.
-template <typename T, int D>
+// SCH: FACE_CENTRAL or FACE_ROE when the launch knows the scheme (each then
+// gets its own register allocation), FACE_ANY to test P.distype.
+enum { FACE_CENTRAL = 0, FACE_ROE = 1, FACE_ANY = 2 };
+template <typename T, int D, int SCH>
 __device__ __forceinline__ void face_dir(const DevBlock<T>& b, const PhysParams& P, int dissip_on, T cd, int i, int j,
                                          int k) {
   const long long N = b.N;
@@ -471,13 +493,15 @@ __device__ __forceinline__ void face_dir(const DevBlock<T>& b, const PhysParams&
 #pragma unroll
     for (int v = 0; v < 5; v++) V[v * N + c] = cd * o[v];
   }
-  if (P.distype != 0) {  // Roe: central part of the (reconstructed) states, upwind part into dfs
+  const bool roe = SCH == FACE_ROE || (SCH == FACE_ANY && P.distype != 0);
+  if (roe) {  // Roe: central part of the (reconstructed) states, upwind part into dfs
     T wl[5], wr[5], pl, pr;
     face_states<T, D>(b, P, c, q, P.distype == 2 ? 2 : 1, wl, &pl, wr, &pr);
+    const T yl = T(1) / wl[0], yr = T(1) / wr[0];
     if (P.distype == 2) {
       T f1[5], f2[5];
-      ceflux_gen<T>(D, wr, pr, (T)b.s[D], f1);
-      ceflux_gen<T>(D, wl, pl, (T)b.s[D], f2);
+      ceflux_gen<T>(D, wr, pr, (T)b.s[D], yr, f1);
+      ceflux_gen<T>(D, wl, pl, (T)b.s[D], yl, f2);
 #pragma unroll
       for (int v = 0; v < 5; v++) E[v * N + c] = T(0.5) * (f1[v] + f2[v]);
     } else {
@@ -487,7 +511,7 @@ __device__ __forceinline__ void face_dir(const DevBlock<T>& b, const PhysParams&
     }
     if (!dissip_on) return;
     T o[5];
-    roe_diss<T>(P, D, (T)fabs(b.s[D]), wl, pl, wr, pr, o);
+    roe_diss<T>(P, D, (T)fabs(b.s[D]), wl, pl, wr, pr, yl, yr, o);
     T* Df = b.dfs + (long long)(D * 5) * N;
 #pragma unroll
     for (int v = 0; v < 5; v++) Df[v * N + c] = cd * o[v];
@@ -552,16 +576,16 @@ __device__ __forceinline__ void face_dir(const DevBlock<T>& b, const PhysParams&
   (void)eq;
 }
 
-template <typename T>
+template <typename T, int SCH = FACE_ANY>
 __device__ __forceinline__ void body_face(const DevBlock<T>& b, const PhysParams& P, int dissip_on, T cd, long long t) {
   const int ex = b.ie - 1, ey = b.je - 1;  // 2..ie
   int i = 2 + (int)(t % ex);
   int j = 2 + (int)((t / ex) % ey);
   int k = 2 + (int)(t / ((long long)ex * ey));
   bool jp = j <= b.jl, kp = k <= b.kl, ip = i <= b.il;
-  if (jp && kp) face_dir<T, 0>(b, P, dissip_on, cd, i, j, k);
-  if (ip && kp) face_dir<T, 1>(b, P, dissip_on, cd, i, j, k);
-  if (ip && jp) face_dir<T, 2>(b, P, dissip_on, cd, i, j, k);
+  if (jp && kp) face_dir<T, 0, SCH>(b, P, dissip_on, cd, i, j, k);
+  if (ip && kp) face_dir<T, 1, SCH>(b, P, dissip_on, cd, i, j, k);
+  if (ip && jp) face_dir<T, 2, SCH>(b, P, dissip_on, cd, i, j, k);
 }
 
 // --------------------------------------------------------------- stage: cut-cell record terms
@@ -642,10 +666,11 @@ __device__ void rec_wall_terms(const DevBlock<T>& b, const PhysParams& P, int di
   if (P.distype != 0) {  // Roe: the wall face's upwind flux taken to the ghost state
     T o[5];
     const T S = (T)fabs(b.s[D]);
+    const T yc = T(1) / wc[0], ys = T(1) / wsol[0];
     if (plus)
-      roe_diss<T>(P, D, S, wc, b.p[c], wsol, psol, o);
+      roe_diss<T>(P, D, S, wc, b.p[c], wsol, psol, yc, ys, o);
     else
-      roe_diss<T>(P, D, S, wsol, psol, wc, b.p[c], o);
+      roe_diss<T>(P, D, S, wsol, psol, wc, b.p[c], ys, yc, o);
     for (int v = 0; v < 5; v++) W[15 + v] = plus ? -(cd * o[v]) : cd * o[v];
     return;
   }
@@ -1969,7 +1994,13 @@ __global__ void k_prep(DevBlock<T> b, PhysParams P, int dissip_on) {
 template <typename T>
 __global__ void __launch_bounds__(256, 3) k_face(DevBlock<T> b, PhysParams P, int dissip_on, T cd) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < (long long)(b.ie - 1) * (b.je - 1) * (b.ke - 1)) body_face(b, P, dissip_on, cd, t);
+  if (t < (long long)(b.ie - 1) * (b.je - 1) * (b.ke - 1)) body_face<T, FACE_CENTRAL>(b, P, dissip_on, cd, t);
+}
+// the Roe faces (MUSCL states, upwind flux, and the viscous flux with NS)
+template <typename T>
+__global__ void __launch_bounds__(256, 2) k_face_roe(DevBlock<T> b, PhysParams P, int dissip_on, T cd) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < (long long)(b.ie - 1) * (b.je - 1) * (b.ke - 1)) body_face<T, FACE_ROE>(b, P, dissip_on, cd, t);
 }
 // a stage without dissipation of the central scheme: only the convective
 // face fluxes efs(q) = 0.5*(F(q) + F(q-1)), the same expression as face_dir,
@@ -2172,8 +2203,10 @@ void launch_stage_part(int part, const DevBlock<T>& b, const PhysParams& P, cons
     long long n2 = (long long)(b.ie - 1) * (b.je - 1) * (b.ke - 1);
     if (!A.dissip_on && P.distype == 0)
       k_face_conv<T><<<LAUNCH_N(n2), 0, s>>>(b);
-    else
+    else if (P.distype == 0)
       k_face<T><<<LAUNCH_N(n2), 0, s>>>(b, P, A.dissip_on, (T)A.cd);
+    else
+      k_face_roe<T><<<LAUNCH_N(n2), 0, s>>>(b, P, A.dissip_on, (T)A.cd);
   } else if (part == 2) {
     if (b.nmir > 0) k_rec_wall<T><<<LAUNCH_N(b.nmir), 0, s>>>(b, P, A.dissip_on, (T)A.cd, err);
   } else if (part == 3) {

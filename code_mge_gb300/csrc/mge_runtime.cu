@@ -376,6 +376,8 @@ void build_phys(mge_ctx* c) {
   const double u0n = std::sqrt(P.u0 * P.u0 + P.v0 * P.v0 + P.w0 * P.w0);
   const double ref[5] = {P.rho0, u0n, u0n, u0n, P.p0};
   for (int q = 0; q < 5; q++) Q.lim_e2[q] = 1e-6 * ref[q] * ref[q] / (P.limfac > 0.0 ? P.limfac : 1.0);
+  Q.rgm1 = 1.0 / (P.gamma - 1.0);
+  Q.rgm1f = 1.0f / ((float)P.gamma - 1.0f);
 }
 
 // psmoo.f90:136-166 pivots for a line of l-1 unknowns (rows 2..l)
@@ -427,6 +429,12 @@ void fill_view(Block& b, DevBlock<T>& d, void* scratch) {
   d.hx = b.h[0];
   d.hy = b.h[1];
   d.hz = b.h[2];
+  for (int q = 0; q < 3; q++) {
+    d.rh[q] = 1.0 / b.h[q];
+    d.r4h[q] = 1.0 / (4.0 * b.h[q]);
+    d.rhf[q] = 1.0f / (float)b.h[q];
+    d.r4hf[q] = 1.0f / (4.0f * (float)b.h[q]);
+  }
   for (int q = 0; q < 3; q++) {
     d.s[q] = b.s[q];
     d.sqrt_ds[q] = std::sqrt(b.s[q] * b.s[q]);
