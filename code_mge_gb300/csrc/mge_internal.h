@@ -168,7 +168,7 @@ void launch_collc(const DevBlock<TC>& c, const DevBlock<TF>& f, const int ratio[
                   uint8_t* marker_c, cudaStream_t s);
 template <typename TF, typename TC>
 void launch_addw(const DevBlock<TF>& f, const DevBlock<TC>& c, const int ratio[3], const int offset[3], int fmg,
-                 cudaStream_t s);
+                 double* scratch, cudaStream_t s);
 template <typename TF, typename TC>
 void launch_embed(const DevBlock<TF>& f, const DevBlock<TC>& c, const int ratio[3], const int offset[3],
                   const PhysParams& P, cudaStream_t s);

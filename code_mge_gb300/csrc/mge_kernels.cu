@@ -209,6 +209,14 @@ template <typename T> __global__ void k_dtim_convert(double* src, T* dst) {
 // --------------------------------------------------------------- stage: per-cell pass
 // Box [1..ie]x[1..je]x[1..ke]: every cell whose flux or sensor a face needs.
 template <typename T>
+__device__ __forceinline__ T van_albada(T a, T b, T e2);
+
+// SLOPES: the MUSCL Roe form with the velocities of every cell already in
+// F[0..2] (k_prim): the limited slope of each primitive variable along each
+// direction goes to dlt[dir][var], once per cell.  A face takes the slope of
+// its lower cell for the left state and that of its upper cell for the right
+// state, the same van_albada(q(c)-q(c-1), q(c+1)-q(c)) it would form itself.
+template <typename T, bool SLOPES = false>
 __device__ __forceinline__ void body_prep(const DevBlock<T>& b, const PhysParams& P, int dissip_on, long long t) {
   const int ex = b.ie, ey = b.je;  // count = ie (cells 1..ie)
   int i = 1 + (int)(t % ex);
@@ -228,6 +236,26 @@ __device__ __forceinline__ void body_prep(const DevBlock<T>& b, const PhysParams
 #pragma unroll
     for (int a = 0; a < 3; a++) b.vt[a * N + c] = solid ? T(0) : mdiv(w[1 + a], w[0], y);
     b.vt[3 * N + c] = solid ? T(0) : p / (w[0] * (T)P.gas_const);
+  }
+  if (SLOPES) {
+    const long long sts[3] = {1, (long long)b.Pi, (long long)b.Pi * b.Pj};
+    // a face along d has physical tangential indices: only those cells need
+    // the slope along d
+    const bool ti = i >= 2 && i <= b.il, tj = j >= 2 && j <= b.jl, tk = k >= 2 && k <= b.kl;
+    const bool need[3] = {tj && tk, ti && tk, ti && tj};
+    auto prim = [&](long long q, int v) -> T {
+      return v == 0 ? b.w[q] : (v == 4 ? b.p[q] : b.F[(long long)(v - 1) * N + q]);
+    };
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      if (!need[d]) continue;
+#pragma unroll
+      for (int v = 0; v < 5; v++) {
+        const T q0 = prim(c, v);
+        const T dm = q0 - prim(c - sts[d], v), dp = prim(c + sts[d], v) - q0;
+        b.dlt[(long long)(d * 5 + v) * N + c] = van_albada(dm, dp, (T)P.lim_e2[v]);
+      }
+    }
   }
   // the MUSCL Roe faces take their central flux from the reconstructed
   // states, not from the cell fluxes
@@ -328,7 +356,10 @@ __device__ __noinline__ void dflux_matrix(T gamma, const T* u1, const T* u2, con
 template <typename T>
 __device__ __forceinline__ T van_albada(T a, T b, T e2) {
   // smooth form, no cut-off at a*b <= 0: with e2 > 0 a cut-off would make the
-  // slope jump by up to b/3 when a changes sign
+  // slope jump by up to b/3 when a changes sign.  Both differences zero (a
+  // uniform stretch) and e2 > 0: the numerator is e2*a + e2*b, a zero with
+  // the sign of a + b, and so is the quotient
+  if (a == T(0) && b == T(0) && e2 > T(0)) return a + b;
   return ((b * b + e2) * a + (a * a + e2) * b) / (a * a + b * b + T(2) * e2);
 }
 
@@ -430,6 +461,48 @@ __device__ __noinline__ void face_states(const DevBlock<T>& b, const PhysParams&
 }
 
 // y = RN(1/w[0])
+// face_states in the MUSCL form from the per-cell velocities (F[0..2]) and
+// limited slopes (dlt) of k_prim and the prep pass: the same values, with each
+// quotient and slope formed once per cell instead of once per face
+template <typename T, int D>
+__device__ __noinline__ void face_states_pre(const DevBlock<T>& b, const PhysParams& P, long long c, int q, T* wl, T* pl,
+                                             T* wr, T* pr) {
+  const long long N = b.N;
+  const long long st = D == 0 ? 1 : (D == 1 ? (long long)b.Pi : (long long)b.Pi * b.Pj);
+  const long long cm = c - st;
+  for (int v = 0; v < 5; v++) {
+    wl[v] = b.w[v * N + cm];
+    wr[v] = b.w[v * N + c];
+  }
+  *pl = b.p[cm];
+  *pr = b.p[c];
+  const int lq = D == 0 ? b.il : (D == 1 ? b.jl : b.kl);
+  if (q - 2 < 0 || q + 1 > lq + 2) return;
+  if (b.blank[c - 2 * st] == 0 || b.blank[cm] == 0 || b.blank[c] == 0 || b.blank[c + st] == 0) return;
+  const T* S = b.dlt + (long long)(D * 5) * N;
+  T L[5], R[5];
+  L[0] = wl[0] + T(0.5) * S[cm];
+  R[0] = wr[0] - T(0.5) * S[c];
+  for (int a = 0; a < 3; a++) {
+    L[1 + a] = b.F[(long long)a * N + cm] + T(0.5) * S[(long long)(1 + a) * N + cm];
+    R[1 + a] = b.F[(long long)a * N + c] - T(0.5) * S[(long long)(1 + a) * N + c];
+  }
+  L[4] = *pl + T(0.5) * S[4 * N + cm];
+  R[4] = *pr - T(0.5) * S[4 * N + c];
+  if (L[0] <= T(0) || R[0] <= T(0) || L[4] <= T(0) || R[4] <= T(0)) return;
+  const T gm1 = (T)P.gamma - T(1), rg = rcp_gm1(P, T(0));
+  wl[0] = L[0];
+  wr[0] = R[0];
+  for (int a = 0; a < 3; a++) {
+    wl[1 + a] = L[0] * L[1 + a];
+    wr[1 + a] = R[0] * R[1 + a];
+  }
+  wl[4] = mdiv(L[4], gm1, rg) + T(0.5) * L[0] * (L[1] * L[1] + L[2] * L[2] + L[3] * L[3]);
+  wr[4] = mdiv(R[4], gm1, rg) + T(0.5) * R[0] * (R[1] * R[1] + R[2] * R[2] + R[3] * R[3]);
+  *pl = L[4];
+  *pr = R[4];
+}
+
 template <typename T>
 __device__ __forceinline__ void ceflux_gen(int D, const T* w, T p, T s, T y, T* f) {
   T f0 = w[1 + D] * s;
@@ -496,7 +569,10 @@ __device__ __forceinline__ void face_dir(const DevBlock<T>& b, const PhysParams&
   const bool roe = SCH == FACE_ROE || (SCH == FACE_ANY && P.distype != 0);
   if (roe) {  // Roe: central part of the (reconstructed) states, upwind part into dfs
     T wl[5], wr[5], pl, pr;
-    face_states<T, D>(b, P, c, q, P.distype == 2 ? 2 : 1, wl, &pl, wr, &pr);
+    if (SCH == FACE_ROE && P.distype == 2)
+      face_states_pre<T, D>(b, P, c, q, wl, &pl, wr, &pr);
+    else
+      face_states<T, D>(b, P, c, q, P.distype == 2 ? 2 : 1, wl, &pl, wr, &pr);
     const T yl = T(1) / wl[0], yr = T(1) / wr[0];
     if (P.distype == 2) {
       T f1[5], f2[5];
@@ -1636,6 +1712,7 @@ __device__ void body_corner_item(const DevBlock<T>& b, const PhysParams& P, int 
   }
 }
 
+
 template <typename T>
 __global__ void k_bc_corner(DevBlock<T> b, PhysParams P, int phase) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1788,6 +1865,7 @@ __device__ __forceinline__ void trilinear_factor(double x, double y, double z, d
 
 struct Xfer {
   int r[3], o[3];
+  double rinv[3];  // 1/r when r is a power of two (x/r = x*(1/r) exactly), else 0
 };
 
 // collc.f90:58-158 for the coarse cells under one child
@@ -1819,7 +1897,7 @@ __global__ void k_collc(DevBlock<TC> c, DevBlock<TF> f, Xfer X, uint8_t* marker)
       for (int dj = 0; dj < 2; dj++)
         for (int di = 0; di < 2; di++) {
           long long fq = cidx(f.Pi, f.Pj, sh[0] + di, sh[1] + dj, sh[2] + dk);
-          double val = (double)f.dw[v * f.N + fq] / f.vol;
+          double val = mdiv((double)f.dw[v * f.N + fq], f.vol, f.rvol);
           acc = acc + val * fac[nn++];
         }
     c.wr[v * c.N + cc] = (TC)(acc * c.vol);
@@ -1843,7 +1921,8 @@ __device__ __forceinline__ bool fine_to_coarse(const Xfer& X, int ncp0, int ncp1
   int lc[3] = {lc0, lc1, lc2};
   double xi[3];
   for (int d = 0; d < 3; d++) {
-    double u = (double)X.o[d] + ((double)ic[d] - 1.5) / (double)X.r[d];
+    const double x = (double)ic[d] - 1.5;
+    double u = (double)X.o[d] + (X.rinv[d] > 0.0 ? x * X.rinv[d] : x / (double)X.r[d]);
     if (u < 0.0 || u >= (double)nc[d]) return false;
     int s = (int)floor(u + 1.5);
     if (s < 2) s = 2;
@@ -1855,9 +1934,20 @@ __device__ __forceinline__ bool fine_to_coarse(const Xfer& X, int ncp0, int ncp1
   return true;
 }
 
-// addw.f90:83-188: w_f = store_w + I(w_c - ws_c), or I(w_c) in the FMG step
+// the coarse correction w_c - ws_c of every coarse cell, formed once for the
+// 64 fine cells whose interpolation takes it (the same subtraction)
+template <typename TC>
+__global__ void k_addw_diff(DevBlock<TC> c, double* dc) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= c.N) return;
+#pragma unroll
+  for (int v = 0; v < 5; v++) dc[v * c.N + q] = (double)c.w[v * c.N + q] - (double)c.ws[v * c.N + q];
+}
+
+// addw.f90:83-188: w_f = store_w + I(w_c - ws_c), or I(w_c) in the FMG step;
+// dc holds w_c - ws_c (k_addw_diff) unless fmg
 template <typename TF, typename TC>
-__global__ void k_addw(DevBlock<TF> f, DevBlock<TC> c, Xfer X, int fmg) {
+__global__ void k_addw(DevBlock<TF> f, DevBlock<TC> c, Xfer X, int fmg, const double* dc) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long long)f.nx * f.ny * f.nz) return;
   int i = 2 + (int)(t % f.nx), j = 2 + (int)((t / f.nx) % f.ny), k = 2 + (int)(t / ((long long)f.nx * f.ny));
@@ -1873,8 +1963,7 @@ __global__ void k_addw(DevBlock<TF> f, DevBlock<TC> c, Xfer X, int fmg) {
       for (int dj = 0; dj < 2; dj++)
         for (int di = 0; di < 2; di++) {
           long long cq = cidx(c.Pi, c.Pj, sh[0] + di, sh[1] + dj, sh[2] + dk);
-          double val = (double)c.w[v * c.N + cq];
-          if (!fmg) val = val - (double)c.ws[v * c.N + cq];
+          double val = fmg ? (double)c.w[v * c.N + cq] : dc[v * c.N + cq];
           acc = acc + val * fac[nn++];
         }
     if (fmg)
@@ -1986,10 +2075,21 @@ __global__ void k_forces(DevBlock<T> b, double ox, double oy, double oz, double 
 }
 
 // =============================================================== one-launch-per-phase kernels
-template <typename T>
+template <typename T, bool SLOPES>
 __global__ void k_prep(DevBlock<T> b, PhysParams P, int dissip_on) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < (long long)b.ie * b.je * b.ke) body_prep(b, P, dissip_on, t);
+  if (t < (long long)b.ie * b.je * b.ke) body_prep<T, SLOPES>(b, P, dissip_on, t);
+}
+// the velocities of every cell, ghosts included, into F[0..2] for the MUSCL
+// Roe form (one reciprocal of the density and mdiv: the IEEE quotients)
+template <typename T>
+__global__ void k_prim(DevBlock<T> b) {
+  long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= b.N) return;
+  const long long N = b.N;
+  const T r = b.w[c], y = T(1) / r;
+#pragma unroll
+  for (int a = 0; a < 3; a++) b.F[(long long)a * N + c] = mdiv(b.w[(long long)(1 + a) * N + c], r, y);
 }
 template <typename T>
 __global__ void __launch_bounds__(256, 3) k_face(DevBlock<T> b, PhysParams P, int dissip_on, T cd) {
@@ -2198,7 +2298,12 @@ void launch_stage_part(int part, const DevBlock<T>& b, const PhysParams& P, cons
                        cudaStream_t s) {
   if (part == 0) {
     long long n1 = (long long)b.ie * b.je * b.ke;
-    k_prep<T><<<LAUNCH_N(n1), 0, s>>>(b, P, A.dissip_on);
+    if (P.distype == 2) {
+      k_prim<T><<<LAUNCH_N(b.N), 0, s>>>(b);
+      k_prep<T, true><<<LAUNCH_N(n1), 0, s>>>(b, P, A.dissip_on);
+    } else {
+      k_prep<T, false><<<LAUNCH_N(n1), 0, s>>>(b, P, A.dissip_on);
+    }
   } else if (part == 1) {
     long long n2 = (long long)(b.ie - 1) * (b.je - 1) * (b.ke - 1);
     if (!A.dissip_on && P.distype == 0)
@@ -2449,38 +2554,40 @@ void launch_init_free(const DevBlock<T>& b, const PhysParams& P, cudaStream_t s)
   k_init_free<T><<<nblk(b.N, TPB), TPB, 0, s>>>(b, P);
 }
 
-template <typename TC, typename TF>
-void launch_collc(const DevBlock<TC>& c, const DevBlock<TF>& f, const int ratio[3], const int offset[3],
-                  uint8_t* marker_c, cudaStream_t s) {
+// a transfer's ratio and offset; an exact reciprocal of a power-of-two ratio
+inline Xfer make_xfer(const int ratio[3], const int offset[3]) {
   Xfer X;
   for (int d = 0; d < 3; d++) {
     X.r[d] = ratio[d];
     X.o[d] = offset[d];
+    X.rinv[d] = (ratio[d] > 0 && (ratio[d] & (ratio[d] - 1)) == 0) ? 1.0 / (double)ratio[d] : 0.0;
   }
+  return X;
+}
+
+template <typename TC, typename TF>
+void launch_collc(const DevBlock<TC>& c, const DevBlock<TF>& f, const int ratio[3], const int offset[3],
+                  uint8_t* marker_c, cudaStream_t s) {
+  Xfer X = make_xfer(ratio, offset);
   long long n = (long long)(f.nx / ratio[0]) * (f.ny / ratio[1]) * (f.nz / ratio[2]);
   k_collc<TC, TF><<<LAUNCH_N(n), 0, s>>>(c, f, X, marker_c);
 }
 
 template <typename TF, typename TC>
 void launch_addw(const DevBlock<TF>& f, const DevBlock<TC>& c, const int ratio[3], const int offset[3], int fmg,
-                 cudaStream_t s) {
-  Xfer X;
-  for (int d = 0; d < 3; d++) {
-    X.r[d] = ratio[d];
-    X.o[d] = offset[d];
-  }
+                 double* scratch, cudaStream_t s) {
+  Xfer X = make_xfer(ratio, offset);
   long long n = (long long)f.nx * f.ny * f.nz;
-  k_addw<TF, TC><<<LAUNCH_N(n), 0, s>>>(f, c, X, fmg);
+  // the coarse corrections go to the stage scratch (at least 64 fields of
+  // the largest block), free between euler calls
+  if (!fmg) k_addw_diff<TC><<<LAUNCH_N(c.N), 0, s>>>(c, scratch);
+  k_addw<TF, TC><<<LAUNCH_N(n), 0, s>>>(f, c, X, fmg, scratch);
 }
 
 template <typename TF, typename TC>
 void launch_embed(const DevBlock<TF>& f, const DevBlock<TC>& c, const int ratio[3], const int offset[3],
                   const PhysParams& P, cudaStream_t s) {
-  Xfer X;
-  for (int d = 0; d < 3; d++) {
-    X.r[d] = ratio[d];
-    X.o[d] = offset[d];
-  }
+  Xfer X = make_xfer(ratio, offset);
   k_embed<TF, TC><<<LAUNCH_N(f.N), 0, s>>>(f, c, X, P.gamma);
 }
 
@@ -2521,7 +2628,7 @@ MGE_INST(float)
   template void launch_collc<TC, TF>(const DevBlock<TC>&, const DevBlock<TF>&, const int*, const int*, uint8_t*,   \
                                      cudaStream_t);                                                             \
   template void launch_addw<TF, TC>(const DevBlock<TF>&, const DevBlock<TC>&, const int*, const int*, int,          \
-                                    cudaStream_t);                                                              \
+                                    double*, cudaStream_t);                                                     \
   template void launch_embed<TF, TC>(const DevBlock<TF>&, const DevBlock<TC>&, const int*, const int*,              \
                                      const PhysParams&, cudaStream_t);
 MGE_XFER(double, double)

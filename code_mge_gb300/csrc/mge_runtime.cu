@@ -264,7 +264,7 @@ void enqueue_addw_embed(mge_ctx* c, Block& f, Block& pb, bool fmg, bool embed) {
         if (embed)
           launch_embed<TF, TC>(DF, DC, f.ratio, f.offset, c->P, c->stream);
         else
-          launch_addw<TF, TC>(DF, DC, f.ratio, f.offset, fmg ? 1 : 0, c->stream);
+          launch_addw<TF, TC>(DF, DC, f.ratio, f.offset, fmg ? 1 : 0, c->scratch, c->stream);
       }
     });
   });
