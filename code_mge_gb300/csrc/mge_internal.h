@@ -53,6 +53,7 @@ struct DevBlock {
   double sqrt_ds[3];        // sqrt(s*s) computed on the host
   double vol;
   double rvol;              // RN(1/vol)
+  float rvolf;              // RN(1/vol) in single precision, of the single-precision vol
   // cut-cell records
   int nmir;
   int m0;                   // first record with an empty cloud (nmir if none)

@@ -58,6 +58,8 @@ __device__ __forceinline__ double rcp_h(const DevBlock<double>& b, int d) { retu
 __device__ __forceinline__ float rcp_h(const DevBlock<float>& b, int d) { return b.rhf[d]; }
 __device__ __forceinline__ double rcp_4h(const DevBlock<double>& b, int d) { return b.r4h[d]; }
 __device__ __forceinline__ float rcp_4h(const DevBlock<float>& b, int d) { return b.r4hf[d]; }
+__device__ __forceinline__ double rcp_vol(const DevBlock<double>& b) { return b.rvol; }
+__device__ __forceinline__ float rcp_vol(const DevBlock<float>& b) { return b.rvolf; }
 template <typename T> __device__ __forceinline__ T fdimT(T a, T b) { return a > b ? a - b : T(0); }
 template <typename T> __device__ __forceinline__ T fmaxT(T a, T b) { return a > b ? a : b; }
 template <typename T> __device__ __forceinline__ T fminT(T a, T b) { return a < b ? a : b; }
@@ -92,13 +94,13 @@ __device__ __forceinline__ unsigned long long body_timestep(const DevBlock<T>& b
   const TC gamma = (TC)P.gamma;
   TC w0 = (TC)b.w[c], w1 = (TC)b.w[N + c], w2 = (TC)b.w[2 * N + c], w3 = (TC)b.w[3 * N + c];
   TC pc = (TC)b.p[c];
-  TC cc = gamma * pc / w0;
+  TC y = TC(1) / w0;
+  TC cc = mdiv(gamma * pc, w0, y);
   if (cc < TC(0) || cc != cc) {  // timestep.f90:45-48
     atomicOr(err, ERR_NEGPRESS);
     return mine;
   }
   cc = sqrt(fmaxT(cc, TC(0)));
-  TC y = TC(1) / w0;
   TC uu = mdiv(w1, w0, y), uv = mdiv(w2, w0, y), uw = mdiv(w3, w0, y);
   // face vectors are axis-aligned: |u.s| = |u_d s_d|, |s| precomputed
   TC ri = fabs(uu * (TC)b.s[0]) + cc * (TC)b.sqrt_ds[0];
@@ -123,11 +125,11 @@ __device__ __forceinline__ unsigned long long body_timestep(const DevBlock<T>& b
   TC pjp = (TC)b.p[c + b.Pi], pjm = (TC)b.p[c - b.Pi];
   long long pl = (long long)b.Pi * b.Pj;
   TC pkp = (TC)b.p[c + pl], pkm = (TC)b.p[c - pl];
-  TC p2 = TC(2) * pc;
+  TC p2 = mul2(pc);
   TC dpi = fabs((pip - p2 + pim) / (pip + p2 + pim + plim));
   TC dpj = fabs((pjp - p2 + pjm) / (pjp + p2 + pjm + plim));
   TC dpk = fabs((pkp - p2 + pkm) / (pkp + p2 + pkm + plim));
-  TC r = TC(1) / (TC(1) + fminT((TC)P.dimcfl, TC(2) * (dpi + dpj + dpk)));
+  TC r = TC(1) / (TC(1) + fminT((TC)P.dimcfl, mul2(dpi + dpj + dpk)));
   if (P.unsteady) {  // timestep.f90:85-99,180-190: at most 2*dtstep/(3*cfl)
     const TC dtime = (TC(2) * (TC)P.dtstep) / (TC(3) * (TC)P.cfl);
     fict = fict < dtime ? fict : dtime;
@@ -1078,7 +1080,7 @@ __device__ __forceinline__ void body_combine(const DevBlock<T>& b, const PhysPar
   }
   // time-step scaling, euler.f90:364-372: de = fn*vdtim/cellvolume
   T vd = A.vt ? (T)(*b.dtim) : b.vdtim[c];
-  T de = mdiv((T)A.fn * vd, (T)b.vol, (T)b.rvol);
+  T de = mdiv((T)A.fn * vd, (T)b.vol, rcp_vol(b));
 #pragma unroll
   for (int v = 0; v < 5; v++) dwv[v] = de * dwv[v];
   if (A.irs) {

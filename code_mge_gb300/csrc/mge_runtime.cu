@@ -441,6 +441,7 @@ void fill_view(Block& b, DevBlock<T>& d, void* scratch) {
   }
   d.vol = b.vol;
   d.rvol = 1.0 / b.vol;
+  d.rvolf = 1.0f / (float)b.vol;
   d.nmir = (int)b.recs.size();
   d.m0 = b.m0;
   d.rec_i = b.rec_i; d.rec_cloud = b.rec_cloud; d.rec_coef = b.rec_coef; d.rec_nvec = b.rec_nvec;
