@@ -418,7 +418,8 @@ def run_converge(args):
         wall = time.perf_counter() - t0
         r = {"cycles": int(n), "wall_s": wall, "drop": float(hist[0] / hist[-1]) if len(hist) else None,
              "converged": bool(len(hist) and hist[0] / hist[-1] > 1.0 / args.tol), "cd": fo.cd, "cl": fo.cl,
-             "residual_last": float(hist[-1]) if len(hist) else None}
+             "residual_last": float(hist[-1]) if len(hist) else None,
+             "residual_every_50": [float(x) for x in hist[::50]]}
         if GEOMETRY[wl] == "cylinder":
             levels = [(cyc.field("w", lv), cyc.spec(lv)) for lv in range(L, 0, -1)]
             r["recirculation_length"] = K.recirculation_length(levels, radius=0.5)
