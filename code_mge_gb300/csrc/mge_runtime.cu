@@ -67,6 +67,10 @@ struct Block {
   double *rt_partial = nullptr, *rt_cur = nullptr, *forces = nullptr;
   int npart = 1;
   int m0 = 0;
+  // every cloud cell of the records processed by bc_cutcell is physical, so
+  // bc_cutcell (reads those cells, writes only the records) and bcond
+  // (writes only ghost cells) touch disjoint data and may run concurrently
+  bool cut_beside_bcond = false;
   std::vector<double> rtrms;  // host history rtrms(ncyc)
   DevBlock<double> dev;       // view when !f32
   DevBlock<float> dev32;      // view when f32
@@ -237,8 +241,17 @@ void enqueue_euler(mge_ctx* c, Block& b, int mgl, int mlvl, bool lres, bool lfir
       launch_stage<T>(D, c->P, A, c->d_err, c->stream, c->side, c->ev_fork, c->ev_join);
       if (lres) return;
       if (A.irs) launch_irs<T>(D, c->P, b.tabs, c->stream, b.aux32, b.irs_var, &A);
-      launch_cutcell<T>(D, c->P, c->d_err, c->stream);
-      launch_bcond<T>(D, c->P, c->stream);
+      if (b.cut_beside_bcond && c->side) {  // disjoint data: the record pass beside the boundary passes
+        cudaEventRecord(c->ev_fork, c->stream);
+        cudaStreamWaitEvent(c->side, c->ev_fork, 0);
+        launch_cutcell<T>(D, c->P, c->d_err, c->side);
+        cudaEventRecord(c->ev_join, c->side);
+        launch_bcond<T>(D, c->P, c->stream);
+        cudaStreamWaitEvent(c->stream, c->ev_join, 0);
+      } else {
+        launch_cutcell<T>(D, c->P, c->d_err, c->stream);
+        launch_bcond<T>(D, c->P, c->stream);
+      }
     }
     if (want_rt) launch_rtrms<T>(D, c->P, P.vt, b.rt_partial, b.npart, b.rt_cur, c->stream);
   });
@@ -498,6 +511,13 @@ int commit_block(mge_ctx* c, Block& b, double* scratch) {
     }
     rar[m] = t.area;
   }
+  b.cut_beside_bcond = nm > 0;
+  for (int m = 0; m < nm && m < b.m0; m++)
+    for (int q = 0; q < b.recs[m].npoint; q++) {
+      const int* ijk = b.recs[m].ijk[q];
+      if (ijk[0] < 2 || ijk[0] > b.il || ijk[1] < 2 || ijk[1] > b.jl || ijk[2] < 2 || ijk[2] > b.kl)
+        b.cut_beside_bcond = false;
+    }
   const int nma = std::max(nm, 1);
   if ((rc = dalloc(c, &b.rec_i, 8 * nma)) || (rc = dalloc(c, &b.rec_cloud, 24 * nma)) ||
       (rc = dalloc(c, &b.rec_coef, 8 * nma)) || (rc = dalloc(c, &b.rec_nvec, 3 * nma)) ||
