@@ -231,11 +231,29 @@ void enqueue_euler(mge_ctx* c, Block& b, int mgl, int mlvl, bool lres, bool lfir
     if (rc == 0) return;
     cudaGetLastError();  // cooperative launch unavailable: fall through to per-phase launches
   }
-  if (with_timestep) enqueue_timestep(c, b);
+  // the time step (reads w, p; writes vdtim, lam, dtim) and the copies of w
+  // into ws and wn touch disjoint outputs: the copies run beside it
+  const bool copies_beside = with_timestep && c->side;
+  if (copies_beside) {
+    cudaEventRecord(c->ev_fork, c->stream);
+    cudaStreamWaitEvent(c->side, c->ev_fork, 0);
+    with_dev(b, [&](auto& D) {
+      using T = typename std::remove_reference_t<decltype(D)>::value_type;
+      if (lfir) launch_copy_ws<T>(D, c->side);
+      launch_save_wn<T>(D, c->side);
+    });
+    cudaEventRecord(c->ev_join, c->side);
+    enqueue_timestep(c, b);
+    cudaStreamWaitEvent(c->stream, c->ev_join, 0);
+  } else if (with_timestep) {
+    enqueue_timestep(c, b);
+  }
   with_dev(b, [&](auto& D) {
     using T = typename std::remove_reference_t<decltype(D)>::value_type;
-    if (lfir) launch_copy_ws<T>(D, c->stream);
-    launch_save_wn<T>(D, c->stream);
+    if (!copies_beside) {
+      if (lfir) launch_copy_ws<T>(D, c->stream);
+      launch_save_wn<T>(D, c->stream);
+    }
     for (int m = 1; m <= mstage; m++) {
       StageArgs A = stage_args(P, m, mgl, mlvl, lres, lfir, itime);
       launch_stage<T>(D, c->P, A, c->d_err, c->stream, c->side, c->ev_fork, c->ev_join);
