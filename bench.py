@@ -95,10 +95,10 @@ def run_profile(args):
     import torch
     from code_mge_gb300.runtime import Cycle, load_library
     lib = load_library()
-    if not args.workload.startswith("sphere"):
-        raise SystemExit("--profile takes a sphere workload")
-    n = int(args.workload[len("sphere"):])
-    case = workload_case(args.precision, n=n)
+    if args.workload in WORKLOADS and not args.workload.startswith("sphere"):
+        case = workload_case(args.precision, name=args.workload)
+    else:
+        case = workload_case(args.precision, n=int(args.workload[len("sphere"):]))
     cyc = Cycle(case)
     cyc.cycle(case.prm.nlevel, ncyc=1)
     ms = np.zeros(len(A.KERNEL_KINDS))
