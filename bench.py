@@ -57,10 +57,10 @@ FACE_DOUBLES_DISSIP = 64
 # and viscous face fluxes (15 + 15 + 15): 55 doubles.
 FACE_DOUBLES_ROE_NS = 55
 # From one ncu capture of that launch on the 128^3 sphere (2,146,689 cells):
-# DRAM read + write 1,111.8 MB = 517.9 B per cell, and 118.2 FP64
+# DRAM read + write 1,115.3 MB = 519.6 B per cell, and 118.2 FP64
 # instructions (DADD + DMUL, no DFMA under --fmad=false) per cell.  Traffic
 # scales with the cells a launch covers.
-FACE_DRAM_BYTES_PER_CELL = 517.9
+FACE_DRAM_BYTES_PER_CELL = 519.6
 FACE_FP64_PER_CELL = 118.2
 FP64_LANES_PER_SM_CYCLE = 2      # GB300: 2 FP64 thread-operations per SM per cycle
 GB300_SMS = 152
