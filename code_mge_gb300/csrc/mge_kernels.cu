@@ -2094,13 +2094,13 @@ __global__ void k_prim(DevBlock<T> b) {
   for (int a = 0; a < 3; a++) b.F[(long long)a * N + c] = mdiv(b.w[(long long)(1 + a) * N + c], r, y);
 }
 template <typename T>
-__global__ void __launch_bounds__(256, 3) k_face(DevBlock<T> b, PhysParams P, int dissip_on, T cd) {
+__global__ void __launch_bounds__(256, 4) k_face(DevBlock<T> b, PhysParams P, int dissip_on, T cd) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t < (long long)(b.ie - 1) * (b.je - 1) * (b.ke - 1)) body_face<T, FACE_CENTRAL>(b, P, dissip_on, cd, t);
 }
 // the Roe faces (MUSCL states, upwind flux, and the viscous flux with NS)
 template <typename T>
-__global__ void __launch_bounds__(256, 2) k_face_roe(DevBlock<T> b, PhysParams P, int dissip_on, T cd) {
+__global__ void __launch_bounds__(256, 3) k_face_roe(DevBlock<T> b, PhysParams P, int dissip_on, T cd) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t < (long long)(b.ie - 1) * (b.je - 1) * (b.ke - 1)) body_face<T, FACE_ROE>(b, P, dissip_on, cd, t);
 }
