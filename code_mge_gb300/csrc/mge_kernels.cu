@@ -2078,7 +2078,7 @@ __global__ void k_forces(DevBlock<T> b, double ox, double oy, double oz, double 
 
 // =============================================================== one-launch-per-phase kernels
 template <typename T, bool SLOPES>
-__global__ void k_prep(DevBlock<T> b, PhysParams P, int dissip_on) {
+__global__ void __launch_bounds__(256, SLOPES ? 3 : 6) k_prep(DevBlock<T> b, PhysParams P, int dissip_on) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t < (long long)b.ie * b.je * b.ke) body_prep<T, SLOPES>(b, P, dissip_on, t);
 }

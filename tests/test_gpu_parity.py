@@ -142,9 +142,17 @@ def test_graph_matches_stream(gpulib, path):
     assert np.array_equal(a.field("w", 3), b.field("w", 3))
 
 
+EMBEDDED = {
+    "jst": dict(mach=0.3),
+    # the scheme of the 512x512x2 NS cylinder workload: Roe MUSCL + viscous fluxes
+    "ns_roe2": dict(mach=0.2, eqntype=A.MGE_EQN_NS, distype=A.MGE_DIS_ROE2, reynolds=40.0),
+}
+
+
+@pytest.mark.parametrize("scheme", sorted(EMBEDDED))
 @pytest.mark.parametrize("path", PATHS)
-def test_embedded_levels(gpulib, path):
-    case = K.cylinder_embedded(n=24, span=2, nlevel=3, h_fine=0.1, mach=0.3, mcyc_fine=3)
+def test_embedded_levels(gpulib, path, scheme):
+    case = K.cylinder_embedded(n=24, span=2, nlevel=3, h_fine=0.1, mcyc_fine=3, **EMBEDDED[scheme])
     case.prm.mcyc[0] = 1
     case.prm.mcyc[1] = 1
     g, o = pair(case, path=path)
