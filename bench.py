@@ -397,9 +397,9 @@ def run_gpu(args):
 
 def run_converge(args):
     """One workload solved in FP64 and in the mixed form to a residual drop:
-    cycles, wall time, the final drop, Cl and Cd (pressure forces on the wall
-    records) and their differences, and for the cylinder the length of the
-    closed wake on y = 0.  The FP64 solve is the reference the mixed one is
+    cycles, wall time, the final drop, Cl and Cd (pressure on the wall
+    records, plus the wall's viscous stress with NS) and their differences,
+    and for the cylinder the length of the closed wake on y = 0.  The FP64 solve is the reference the mixed one is
     measured against; the FP64 path itself matches the oracle to 1e-9 in Cd
     on the cases the GPU tests solve."""
     from code_mge_gb300.runtime import Cycle, load_library
@@ -433,7 +433,8 @@ def run_converge(args):
             "fp64": f, "mixed": m,
             "config": {"workload": WORKLOADS[wl], "tol_drop": args.tol, "max_cycles_finest": args.max_cycles,
                        "refine_drop": args.refine_drop,
-                       "forces": "pressure on the wall records; Cd over q_inf x reference area"}}
+                       "forces": "pressure on the wall records, plus the no-slip wall stress with NS; "
+                                 "Cd over q_inf x reference area"}}
     if "recirculation_length" in f:
         a, b = f["recirculation_length"], m["recirculation_length"]
         line["abs_d_recirculation_length"] = abs(a - b) if a is not None and b is not None else None

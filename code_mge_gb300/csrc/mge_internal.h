@@ -174,7 +174,7 @@ template <typename TF, typename TC>
 void launch_embed(const DevBlock<TF>& f, const DevBlock<TC>& c, const int ratio[3], const int offset[3],
                   const PhysParams& P, cudaStream_t s);
 template <typename T> void launch_forces(const DevBlock<T>& b, const double* origin, const double* h,
-                                         const double* center, double* out7, cudaStream_t s);
+                                         const double* center, double mu, double* out7, cudaStream_t s);
 int rtrms_partials(long long ncells);
 void init_kernel_attributes();
 void launch_convert(const void* src, bool src32, void* dst, bool dst32, long long n, cudaStream_t s);

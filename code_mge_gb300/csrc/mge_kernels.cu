@@ -2039,10 +2039,13 @@ __global__ void k_solut(DevBlock<T> b, double gamma, double p0, double rm, doubl
   }
 }
 
-// wall forces from the records (new): 7 sums, fixed order within one block
+// wall forces from the records (new): 7 sums, fixed order within one block.
+// Pressure on each wall face and, when mu > 0 (NS), the wall's viscous
+// stress: the momentum the solver's wall flux (rec_wall_terms) gives the
+// fluid, with the opposite sign
 template <typename T>
 __global__ void k_forces(DevBlock<T> b, double ox, double oy, double oz, double hx, double hy, double hz, double cx,
-                         double cy, double cz, double* out) {
+                         double cy, double cz, double mu, double* out) {
   __shared__ double sh[7][256];
   double acc[7] = {0, 0, 0, 0, 0, 0, 0};
   const double org[3] = {ox, oy, oz}, h[3] = {hx, hy, hz}, ctr[3] = {cx, cy, cz};
@@ -2053,8 +2056,20 @@ __global__ void k_forces(DevBlock<T> b, double ox, double oy, double oz, double 
     long long c = cidx(b.Pi, b.Pj, ri[0], ri[1], ri[2]);
     double area = b.rec_area[m];
     double pw = 0.5 * ((double)b.p[c] + (double)b.rec_psol[m]);
-    double f[3] = {0, 0, 0};
-    f[ax] = pw * area * sgn;
+    double fv[3] = {0, 0, 0};
+    if (mu > 0.0) {  // visc_wall of rec_wall_terms, in FP64
+      const bool plus = ri[3] >= 4;
+      const double S = fabs(b.s[ax]), r0 = (double)b.w[c];
+      for (int a = 0; a < 3; a++) {
+        const double u = (double)b.w[(1 + a) * b.N + c] / r0;
+        const double ug = 2.0 * b.rec_qb[3 * m + a] - u;
+        const double gn = plus ? (ug - u) / h[ax] : (u - ug) / h[ax];
+        const double tau = (a == ax) ? (4.0 / 3.0) * mu * gn : mu * gn;
+        fv[a] = plus ? -(S * tau) : S * tau;
+      }
+    }
+    double f[3];
+    for (int d = 0; d < 3; d++) f[d] = (d == ax ? pw * area * sgn : 0.0) + fv[d];
     double xf[3];
     for (int d = 0; d < 3; d++) xf[d] = org[d] + ((double)ri[d] - 1.5) * h[d];
     xf[ax] = xf[ax] + sgn * 0.5 * h[ax];
@@ -2594,10 +2609,10 @@ void launch_embed(const DevBlock<TF>& f, const DevBlock<TC>& c, const int ratio[
 }
 
 template <typename T>
-void launch_forces(const DevBlock<T>& b, const double* origin, const double* h, const double* center, double* out7,
-                   cudaStream_t s) {
+void launch_forces(const DevBlock<T>& b, const double* origin, const double* h, const double* center, double mu,
+                   double* out7, cudaStream_t s) {
   k_forces<T><<<1, 256, 0, s>>>(b, origin[0], origin[1], origin[2], h[0], h[1], h[2], center[0], center[1], center[2],
-                                out7);
+                                mu, out7);
 }
 
 // explicit instantiations
@@ -2622,7 +2637,8 @@ void launch_forces(const DevBlock<T>& b, const double* origin, const double* h, 
   template void launch_save_wn<T>(const DevBlock<T>&, cudaStream_t);                                            \
   template void launch_copy_wn<T>(const DevBlock<T>&, cudaStream_t);                                            \
   template void launch_init_free<T>(const DevBlock<T>&, const PhysParams&, cudaStream_t);                       \
-  template void launch_forces<T>(const DevBlock<T>&, const double*, const double*, const double*, double*, cudaStream_t);
+  template void launch_forces<T>(const DevBlock<T>&, const double*, const double*, const double*, double, double*,  \
+                                 cudaStream_t);
 MGE_INST(double)
 MGE_INST(float)
 #undef MGE_INST

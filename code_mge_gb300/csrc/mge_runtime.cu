@@ -1300,7 +1300,8 @@ int mge_forces_compute(mge_ctx* c, int level, const mge_solve_opts* o, mge_force
     if (b.recs.empty()) continue;
     with_dev(b, [&](auto& D) {
       using T = typename std::remove_reference_t<decltype(D)>::value_type;
-      launch_forces<T>(D, b.origin, b.h, ctr, b.forces, c->stream);
+      launch_forces<T>(D, b.origin, b.h, ctr, c->prm.eqntype == MGE_EQN_NS ? c->prm.viscl : 0.0, b.forces,
+                       c->stream);
     });
     double h6[8];
     CK(cudaMemcpyAsync(h6, b.forces, 6 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));

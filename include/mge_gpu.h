@@ -127,7 +127,9 @@ typedef struct mge_block_desc {
   int    offset[3];               /* origin = parent origin + offset * h_parent */
 } mge_block_desc;
 
-/* Cut-cell wall forces (new: the reference has no Cl/Cd integrator) */
+/* Cut-cell wall forces (new: the reference has no Cl/Cd integrator): the
+ * pressure on every wall face of the records and, for Navier-Stokes, the
+ * wall's viscous stress as the solver's no-slip wall flux defines it. */
 typedef struct mge_forces {
   double force[3];
   double moment[3];
@@ -294,7 +296,8 @@ long long mge_restart_format(int code, int ib, int jb, int kb, const double* w, 
 long long mge_restart_parse(const char* text, long long len, int code, int ib, int jb, int kb,
                             double* w);
 
-/* Cut-cell wall force integration on the finest level (R-FORCE, new). */
+/* Cut-cell wall force integration on a level: pressure, plus the viscous
+ * wall stress for Navier-Stokes (new: no counterpart in the reference). */
 int mge_forces_compute(mge_ctx* ctx, int level, const mge_solve_opts* opts,
                        mge_forces* out);
 

@@ -1806,15 +1806,25 @@ int movfin(mgeo_ctx* c, int mgl, int mlvl) {  // movfin.f90:20-39
   return MGE_OK;
 }
 
-/* Wall forces from the cut-cell records (new; the reference has none). */
+/* Wall forces from the cut-cell records (new; the reference has none):
+   pressure on each wall face and, with NS, the wall's viscous stress.  The
+   body takes the momentum the solver's wall flux gives the fluid, with the
+   opposite sign: -(S*tau) for a solid on the + side, S*tau on the - side. */
 void forces_block(mgeo_ctx* c, OBlock& b, const mge_solve_opts* o, double* F, double* M) {
+  const double Sd[3] = {std::fabs(b.si[0]), std::fabs(b.sj[1]), std::fabs(b.sk[2])};
   for (const ORec& t : b.z) {
     int ax = t.zz - 1;
     double sgn = t.faceid >= 4 ? 1.0 : -1.0;
     double area = t.area;
     double pw = 0.5 * (b.P(t.ccid[0], t.ccid[1], t.ccid[2]) + t.psol);
-    double f[3] = {0, 0, 0};
-    f[ax] = pw * area * sgn;
+    double fv[3] = {0, 0, 0};
+    if (c->prm.eqntype == MGE_EQN_NS) {
+      double vo[5];
+      visc_wall(c->prm, b, t, Sd[ax], vo);
+      for (int d = 0; d < 3; d++) fv[d] = t.faceid >= 4 ? -vo[1 + d] : vo[1 + d];
+    }
+    double f[3];
+    for (int d = 0; d < 3; d++) f[d] = (d == ax ? pw * area * sgn : 0.0) + fv[d];
     double xf[3];
     int ic[3] = {t.ccid[0], t.ccid[1], t.ccid[2]};
     for (int d = 0; d < 3; d++) xf[d] = b.origin[d] + ((double)ic[d] - 1.5) * b.h[d];

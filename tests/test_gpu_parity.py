@@ -109,7 +109,7 @@ def test_transfer(gpulib, name, path):
 
 
 @pytest.mark.parametrize("path", PATHS)
-@pytest.mark.parametrize("name,mgtype", [("cylinder", 1), ("sphere", 2)])
+@pytest.mark.parametrize("name,mgtype", [("cylinder", 1), ("sphere", 2), ("cylinder_ns", 1)])
 def test_solve(gpulib, name, mgtype, path):
     case = CASES[name]()
     case.prm.mgtype = mgtype

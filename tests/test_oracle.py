@@ -200,3 +200,17 @@ def test_w_cycle_converges():
     assert n == 40
     assert hist[-1] < 0.05 * hist[0]
     assert np.isfinite(f.cd)
+
+
+def test_viscous_wall_stress_drags_the_body_at_free_stream():
+    """At the free-stream start the wall pressure is uniform, so the pressure
+    forces of the closed wall cancel; with NS the no-slip wall stress pulls
+    the body along the flow (+x), and nothing acts across it."""
+    from code_mge_gb300 import _abi as A
+    from parity import small_cylinder
+    euler = OracleCycle(small_cylinder(mach=0.2)).forces()
+    ns = OracleCycle(small_cylinder(mach=0.2, eqntype=A.MGE_EQN_NS, reynolds=40.0)).forces()
+    assert abs(euler.force[0]) < 1e-9 and abs(euler.force[1]) < 1e-9
+    assert ns.force[0] > 1e3 * abs(euler.force[0]) and ns.force[0] > 0.0
+    assert abs(ns.force[1]) <= 1e-12 * ns.force[0]
+    assert ns.cd > 0.0
