@@ -38,6 +38,10 @@ class Body:
     semi: tuple = (0.5, 0.5, 0.5)  # ellipsoid semi-axes
     poly: object = None            # polygon: (m, 2) section vertices across the span axis
     span_axis: int = 1             # polygon: the axis it is extruded along
+    # velocity of the wall, in units of the free-stream speed (the records'
+    # qb, bc_cutcell.f90:47-55): a function of the (m, 3) wall points
+    # returning (m, 3) velocities; None for a wall at rest
+    wall_velocity: object = None
 
     def _across(self, a, b, c):
         """The two coordinates across the span axis."""
@@ -253,7 +257,8 @@ def make_block_arrays(spec: BlockSpec, body: Body):
         area[m] = [hy * hz, hx * hz, hx * hy][ax]
     spec.arrays = dict(blank=np.ascontiguousarray(blank.ravel()), nmir=nm, ccid=ccid, scid=scid,
                        faceid=faceid, zz=zz, npoint=npoint, ijkdex=ijkdex, coef=coef, nvec=nvec,
-                       qb=np.zeros((nm, 3)), area=area)
+                       qb=(np.ascontiguousarray(body.wall_velocity(xw), dtype=np.float64)
+                           if (nm and body.wall_velocity is not None) else np.zeros((nm, 3))), area=area)
     return spec
 
 
@@ -401,10 +406,24 @@ def embedded_hierarchy(body, center, h_fine, n, nlevel, coarsen=(True, True, Fal
     return levels
 
 
-def cylinder_slab(n=256, span=2, nlevel=3, extent=20.0, mach=0.3, mcyc_fine=500, smoo=0.6, **kw):
-    """Inviscid flow past a D=1 cylinder cut into an n x n x span slab over
-    [-extent, extent]^2, periodic span, characteristic far field."""
-    body = Body("cylinder", radius=0.5)
+def rotating(omega, center=(0.0, 0.0, 0.0)):
+    """Wall velocity of a body turning at omega about the z axis through
+    center: (-omega*(y-cy), omega*(x-cx), 0)."""
+    def vel(xw):
+        xw = np.asarray(xw, dtype=np.float64)
+        out = np.zeros_like(xw)
+        out[:, 0] = -omega * (xw[:, 1] - center[1])
+        out[:, 1] = omega * (xw[:, 0] - center[0])
+        return out
+    return vel
+
+
+def cylinder_slab(n=256, span=2, nlevel=3, extent=20.0, mach=0.3, mcyc_fine=500, smoo=0.6, omega=0.0, **kw):
+    """Flow past a D=1 cylinder cut into an n x n x span slab over
+    [-extent, extent]^2, periodic span, characteristic far field; omega != 0
+    turns the wall about the cylinder axis (in free-stream speed per unit
+    length)."""
+    body = Body("cylinder", radius=0.5, wall_velocity=rotating(omega) if omega else None)
     h = 2.0 * extent / n
     lo = (-extent, -extent, -0.5 * span * h)
     hi = (extent, extent, 0.5 * span * h)

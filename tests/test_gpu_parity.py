@@ -28,6 +28,10 @@ CASES = {
     # psmoo + progon3 (variable coefficients) in place of psmoo_old
     "sphere_psmoo": lambda: small_sphere(irs_variant=1),
     "cylinder_psmoo": lambda: small_cylinder(irs_variant=1),
+    # a turning wall (the records' qb, bc_cutcell.f90:47-55): Euler reflection about the wall
+    # velocity, and the no-slip wall moving with it
+    "cylinder_rotating": lambda: small_cylinder(omega=0.8),
+    "cylinder_ns_rotating": lambda: small_cylinder(eqntype=A.MGE_EQN_NS, reynolds=40.0, mach=0.2, omega=0.8),
 }
 
 
@@ -109,7 +113,7 @@ def test_transfer(gpulib, name, path):
 
 
 @pytest.mark.parametrize("path", PATHS)
-@pytest.mark.parametrize("name,mgtype", [("cylinder", 1), ("sphere", 2), ("cylinder_ns", 1)])
+@pytest.mark.parametrize("name,mgtype", [("cylinder", 1), ("sphere", 2), ("cylinder_ns", 1), ("cylinder_ns_rotating", 1)])
 def test_solve(gpulib, name, mgtype, path):
     case = CASES[name]()
     case.prm.mgtype = mgtype

@@ -214,3 +214,24 @@ def test_viscous_wall_stress_drags_the_body_at_free_stream():
     assert ns.force[0] > 1e3 * abs(euler.force[0]) and ns.force[0] > 0.0
     assert abs(ns.force[1]) <= 1e-12 * ns.force[0]
     assert ns.cd > 0.0
+
+
+def test_turning_wall_breaks_the_up_down_symmetry():
+    """A cylinder at rest in a uniform stream keeps Cl = 0 by symmetry (without
+    residual smoothing, whose blank skipping is directional); with the wall
+    turning, the records' wall velocity enters the reflected states and the
+    wall stress, and a lift appears after a few cycles."""
+    from code_mge_gb300 import _abi as A
+    from parity import small_cylinder
+    out = {}
+    for omega in (0.0, 0.8, -0.8):
+        case = small_cylinder(mach=0.2, eqntype=A.MGE_EQN_NS, reynolds=40.0, omega=omega, mcyc_fine=6, smoo=0.0)
+        case.prm.mcyc[0] = 2
+        assert (np.abs(case.levels[-1][0].arrays["qb"]).max() > 0.0) == (omega != 0.0)
+        _, _, f = OracleCycle(case).solve()
+        out[omega] = f
+    assert abs(out[0.0].cl) < 1e-10
+    # counter-clockwise turning with the stream along +x: the wall moves with the
+    # stream below the body, and the lift points down (the Magnus force)
+    assert out[0.8].cl < -1e-3
+    assert abs(out[0.8].cl + out[-0.8].cl) <= 1e-10 * abs(out[0.8].cl)
