@@ -450,7 +450,7 @@ def run_pattern(args):
     if args.pattern == "batched":
         sizes = tuple(int(x) for x in args.sizes.split(","))
         reqs = SV.batched_sweep_requests(args.cases, sizes=sizes, precision=A.MGE_PREC_MIXED, tol=args.tol,
-                                         max_cycles=args.max_cycles)
+                                         max_cycles=args.max_cycles, retire_stall=args.retire_stall)
         srv = SV.Server(SV.GpuBackend(coop_ctas=args.coop_ctas), max_active=args.cases)
         t0 = time.perf_counter()
         for r in reqs:
@@ -462,7 +462,7 @@ def run_pattern(args):
         # the FP64 plain path on the same cases, one at a time
         plain, t0 = [], time.perf_counter()
         for r in SV.batched_sweep_requests(args.cases, sizes=sizes, precision=A.MGE_PREC_FP64, tol=args.tol,
-                                           max_cycles=args.max_cycles):
+                                           max_cycles=args.max_cycles, retire_stall=args.retire_stall):
             r.arrival = t0
             one = SV.Server(SV.GpuBackend(coop_ctas=0), max_active=1)
             one.submit(r)
@@ -475,9 +475,11 @@ def run_pattern(args):
         dcd = [abs(mix[r.rid].cd - r.cd) for r in both]
         per_case = [{"rid": r.rid, "n": r.n, "mach": round(r.mach, 4), "alpha_deg": round(r.alpha_deg, 3),
                      "semi": [round(x, 3) for x in r.semi],
-                     "fp64": {"cycles": r.cycles, "converged": r.converged, "cd": r.cd, "error": r.error},
+                     "fp64": {"cycles": r.cycles, "converged": r.converged, "stalled": r.stalled, "cd": r.cd,
+                              "error": r.error},
                      "mixed": {"cycles": mix[r.rid].cycles, "fp64_from_cycle": mix[r.rid].refined_at,
-                               "converged": mix[r.rid].converged, "cd": mix[r.rid].cd, "error": mix[r.rid].error},
+                               "converged": mix[r.rid].converged, "stalled": mix[r.rid].stalled,
+                               "cd": mix[r.rid].cd, "error": mix[r.rid].error},
                      "abs_dcd": (abs(mix[r.rid].cd - r.cd) if r.cd is not None and mix[r.rid].cd is not None
                                  else None)} for r in plain]
         line = {"pattern": "batched sweep", "metric": "converged solves/s", "unit": "solves/s",
@@ -486,7 +488,8 @@ def run_pattern(args):
                 "max_abs_dcd_vs_fp64": max(dcd) if dcd else None, "dcd_cases": len(dcd), "cases": args.cases,
                 "per_case": per_case,
                 "config": {"sizes": sizes, "tol_drop": args.tol, "levels": 3, "cycle": "W",
-                           "precision": "FP32 coarse / FP64 fine", "seed": 20261203},
+                           "precision": "FP32 coarse / FP64 fine", "seed": 20261203,
+                           "max_cycles": args.max_cycles, "retire_stall": args.retire_stall},
                 "batched": batched, "fp64_serial": serial, "peak_active": srv.peak_active}
         print(json.dumps(line), flush=True)
         return 0
@@ -526,6 +529,9 @@ def main():
     ap.add_argument("--sizes", default="32,48,64,96,128")
     ap.add_argument("--tol", type=float, default=1e-8)
     ap.add_argument("--max-cycles", type=int, default=2000)
+    ap.add_argument("--retire-stall", type=int, default=0,
+                    help="batched sweep: retire a case whose FP64 residual has not improved by 5%% for this many "
+                         "cycles (both forms; 0 runs it to --max-cycles)")
     ap.add_argument("--rate", type=float, default=4.0)
     ap.add_argument("--duration", type=float, default=300.0)
     ap.add_argument("--drain", type=float, default=120.0)

@@ -41,6 +41,10 @@ class Request:
     max_cycles: int = 2000
     refine_drop: float = 1e-6  # mixed form: switch to FP64 at this residual drop ...
     refine_stall: int = 40     # ... or once the residual has not improved by 5 % for this many cycles
+    # retire (not converged) once the residual, in FP64 (the plain form, or the
+    # mixed form after its switch), has not improved by 5 % for this many
+    # cycles: a case caught in a limit cycle; 0 runs it to max_cycles
+    retire_stall: int = 0
     # results
     t_admit: float = None
     t_done: float = None
@@ -50,6 +54,7 @@ class Request:
     cd: float = None
     cl: float = None
     converged: bool = False  # retired on the residual drop (not on max_cycles)
+    stalled: bool = False    # retired by retire_stall
     refined_at: int = None   # finest cycle of the switch to FP64 (mixed form)
     error: str = None
 
@@ -140,12 +145,13 @@ class FakeBackend:
     """Deterministic stand-in used by the CPU tests: each case's residual falls
     geometrically per cycle; a cycle completes after `latency` polls."""
 
-    def __init__(self, free_bytes=1 << 34, rate=0.7, latency=2, floor32=0.0):
+    def __init__(self, free_bytes=1 << 34, rate=0.7, latency=2, floor32=0.0, floor64=0.0):
         self.free = free_bytes
         self.rate = rate
         self.latency = latency
         self.launched = 0
         self.floor32 = floor32     # mixed form: the residual stalls here until refined
+        self.floor64 = floor64     # the residual in FP64 stalls here (a limit cycle)
 
     def free_memory(self):
         return self.free
@@ -166,6 +172,8 @@ class FakeBackend:
         nxt = h["res"] * self.rate
         if h["case"].prm.precision == A.MGE_PREC_MIXED and not h.get("refined"):
             nxt = max(nxt, self.floor32)
+        else:
+            nxt = max(nxt, self.floor64)
         h["res"] = nxt
         return 0, h["res"]
 
@@ -305,13 +313,17 @@ class Server:
                         continue
                     s.refined = True
                     s.req.refined_at = s.cycles_fine
+                    s.best, s.best_at = res, s.cycles_fine  # the FP64 stall window starts here
                     if s.req.tol >= s.req.refine_drop:
                         # the drop counts only once an FP64 cycle confirms it
                         self._advance(s)
                         continue
                 conv = bool(s.ini) and res <= s.req.tol * s.ini
-                if conv or s.cycles_fine >= s.req.max_cycles or res != res:
+                fp64 = s.req.precision == A.MGE_PREC_FP64 or s.refined
+                stall_out = s.req.retire_stall > 0 and fp64 and s.cycles_fine - s.best_at >= s.req.retire_stall
+                if conv or stall_out or s.cycles_fine >= s.req.max_cycles or res != res:
                     s.req.converged = conv
+                    s.req.stalled = stall_out and not conv
                     self._retire(s)
                     continue
             self._advance(s)
@@ -350,7 +362,7 @@ def poisson_requests(rate, duration, seed=20261204, sizes=(64, 256), mach=(0.1, 
 
 
 def batched_sweep_requests(count=64, seed=20261203, sizes=(32, 48, 64, 96, 128), precision=A.MGE_PREC_MIXED,
-                           tol=1e-8, max_cycles=2000):
+                           tol=1e-8, max_cycles=2000, retire_stall=0):
     """The batched sweep: `count` ellipsoid cases with seeded sizes, semi-axes,
     Mach and angle of attack, all present at t = 0."""
     rng = np.random.default_rng(seed)
@@ -359,7 +371,8 @@ def batched_sweep_requests(count=64, seed=20261203, sizes=(32, 48, 64, 96, 128),
         n = int(rng.choice(sizes))
         semi = tuple(float(x) for x in rng.uniform(0.5, 2.0, 3))
         out.append(Request(q, "ellipsoid", n, float(rng.uniform(0.2, 0.8)), float(rng.uniform(-5.0, 10.0)),
-                           tol=tol, precision=precision, arrival=0.0, semi=semi, max_cycles=max_cycles))
+                           tol=tol, precision=precision, arrival=0.0, semi=semi, max_cycles=max_cycles,
+                           retire_stall=retire_stall))
     return out
 
 
@@ -371,6 +384,7 @@ def summarize(done, t_wall):
         "requests": len(done),
         "completed": len(ok),
         "converged": len(conv),
+        "stalled": sum(1 for r in ok if r.stalled),
         "failed": len(done) - len(ok),
         "solves_per_s": len(conv) / t_wall if t_wall > 0 else None,
         "p50_s": float(np.percentile(lat, 50)) if lat.size else None,

@@ -61,6 +61,24 @@ def test_mixed_case_refines_when_its_residual_stalls():
     assert d.cycles < 80
 
 
+def test_case_caught_in_a_limit_cycle_is_retired_when_asked():
+    # the fake's FP64 residual stops at 1e-6, above the 1e-8 tolerance
+    for precision in (A.MGE_PREC_FP64, A.MGE_PREC_MIXED):
+        done = {}
+        for retire in (0, 30):
+            be = S.FakeBackend(rate=0.5, latency=1, floor32=1e-4, floor64=1e-6)
+            srv = S.Server(be, reserve_bytes=0, clock=FakeClock())
+            srv.submit(S.Request(0, "sphere", 16, 0.5, tol=1e-8, max_cycles=400, precision=precision,
+                                 refine_stall=20, retire_stall=retire))
+            (done[retire],) = srv.run(idle_sleep=0)
+        assert not done[0].converged and not done[0].stalled and done[0].cycles == 400
+        d = done[30]
+        assert not d.converged and d.stalled and d.error is None
+        # the window opens at the switch to FP64 (mixed) or at the last 5 % gain
+        assert d.cycles < 100
+        assert d.cycles - (d.refined_at or 0) >= 30
+
+
 def test_poisson_and_sweep_generators_are_seeded():
     a = S.poisson_requests(4.0, 10.0)
     b = S.poisson_requests(4.0, 10.0)
