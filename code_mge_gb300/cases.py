@@ -13,10 +13,16 @@ library's own preprocessor for analytic bodies:
 * one mirror record per (fluid cell, solid face neighbour) pair, in Fortran
   cell order then face order, with ``faceid`` 1..6 for a solid neighbour at
   -i,-j,-k,+i,+j,+k (efluxb.f90:70-110), the wall normal, and an
-  interpolation cloud for the solid cell centre reflected about the wall: the
-  trilinear 2x2x2 cell-centre stencil around the reflected point with solid
-  and zero-weight cells dropped and the weights renormalised
-  (bc_cutcell.f90:78-97 consumes ``ijkdex``/``coef``).
+  interpolation cloud for the solid cell centre reflected about the wall
+  (bc_cutcell.f90:78-97 consumes ``ijkdex``/``coef``).  Two cloud forms:
+  ``trilinear`` (default): the 2x2x2 cell-centre stencil around the
+  reflected point with solid and zero-weight cells dropped and the weights
+  renormalised; ``rbf``: the eight fluid cell centres nearest the reflected
+  point, weighted by multiquadric radial-basis interpolation with a constant
+  term (the kind of cloud the reference's solid_ipolcoef builds through the
+  rbf_nodal / rbfmq_basis interfaces of inc/rbfit.h and inc/rbasis.h; their
+  implementation is not in the reference tree, so the node choice and the
+  shape parameter here are this module's own).
 
 All geometry is computed in float64 numpy; the same arrays feed the GPU
 library and the CPU oracle.
@@ -42,6 +48,7 @@ class Body:
     # qb, bc_cutcell.f90:47-55): a function of the (m, 3) wall points
     # returning (m, 3) velocities; None for a wall at rest
     wall_velocity: object = None
+    cloud: str = "trilinear"       # interpolation clouds of the records: "trilinear" or "rbf"
 
     def _across(self, a, b, c):
         """The two coordinates across the span axis."""
@@ -230,7 +237,14 @@ def make_block_arrays(spec: BlockSpec, body: Body):
         fr = g - q0
         lim = np.array([P[0] - 2, P[1] - 2, P[2] - 2])
         q0 = np.clip(q0, 0, lim)
-        for m in range(nm):
+        if body.cloud == "rbf":
+            for m in range(nm):
+                pts, wts = rbf_cloud(xr[m], q0[m], blank, (ox, oy, oz), (hx, hy, hz), tuple(ccid[m]))
+                npoint[m] = len(pts)
+                for q, (pt, wgt) in enumerate(zip(pts, wts)):
+                    ijkdex[m, q] = pt
+                    coef[m, q] = wgt
+        for m in (range(nm) if body.cloud != "rbf" else ()):
             pts, wts = [], []
             for dk in (0, 1):
                 for dj in (0, 1):
@@ -260,6 +274,49 @@ def make_block_arrays(spec: BlockSpec, body: Body):
                        qb=(np.ascontiguousarray(body.wall_velocity(xw), dtype=np.float64)
                            if (nm and body.wall_velocity is not None) else np.zeros((nm, 3))), area=area)
     return spec
+
+
+def mq_weights(nodes, x, csq):
+    """Multiquadric radial-basis weights w with f(x) ~ sum w_i f(nodes_i):
+    the interpolant sum_j a_j sqrt(|y - n_j|^2 + csq) + b through the nodes,
+    with sum_j a_j = 0, evaluated at x.  The weights sum to 1, so constants
+    are reproduced exactly."""
+    nodes = np.asarray(nodes, dtype=np.float64)
+    n = len(nodes)
+    d2 = np.sum((nodes[:, None, :] - nodes[None, :, :]) ** 2, axis=2)
+    M = np.ones((n + 1, n + 1))
+    M[:n, :n] = np.sqrt(d2 + csq)
+    M[n, n] = 0.0
+    rhs = np.ones(n + 1)
+    rhs[:n] = np.sqrt(np.sum((nodes - np.asarray(x)) ** 2, axis=1) + csq)
+    return np.linalg.solve(M, rhs)[:n]
+
+
+def rbf_cloud(x, q0, blank, origin, h, fallback):
+    """The (at most MGE_MAX_CLOUD) fluid cell centres nearest the point x
+    among the 4x4x4 cells around it, and their multiquadric weights; the
+    shape parameter is the cloud's mean distance from its centroid."""
+    P = blank.shape[::-1]  # (Pi, Pj, Pk); blank is indexed [k, j, i]
+    cand = []
+    for dk in range(-1, 3):
+        for dj in range(-1, 3):
+            for di in range(-1, 3):
+                ci, cj, ck = q0[0] + di, q0[1] + dj, q0[2] + dk
+                if not (0 <= ci < P[0] and 0 <= cj < P[1] and 0 <= ck < P[2]) or blank[ck, cj, ci] == 0:
+                    continue
+                c = np.array([origin[0] + (ci - 1.5) * h[0], origin[1] + (cj - 1.5) * h[1],
+                              origin[2] + (ck - 1.5) * h[2]])
+                cand.append((float(np.sum((c - x) ** 2)), (ci, cj, ck), c))
+    if not cand:
+        return [fallback], [1.0]
+    cand.sort(key=lambda t: (t[0], t[1][2], t[1][1], t[1][0]))
+    cand = cand[:A.MGE_MAX_CLOUD]
+    nodes = np.array([t[2] for t in cand])
+    if len(nodes) == 1:
+        return [cand[0][1]], [1.0]
+    lref = float(np.mean(np.sqrt(np.sum((nodes - nodes.mean(axis=0)) ** 2, axis=1))))
+    w = mq_weights(nodes, x, lref * lref)
+    return [t[1] for t in cand], [float(v) for v in w]
 
 
 def _ptr(a, ctype):
@@ -418,12 +475,13 @@ def rotating(omega, center=(0.0, 0.0, 0.0)):
     return vel
 
 
-def cylinder_slab(n=256, span=2, nlevel=3, extent=20.0, mach=0.3, mcyc_fine=500, smoo=0.6, omega=0.0, **kw):
+def cylinder_slab(n=256, span=2, nlevel=3, extent=20.0, mach=0.3, mcyc_fine=500, smoo=0.6, omega=0.0,
+                  cloud="trilinear", **kw):
     """Flow past a D=1 cylinder cut into an n x n x span slab over
     [-extent, extent]^2, periodic span, characteristic far field; omega != 0
     turns the wall about the cylinder axis (in free-stream speed per unit
     length)."""
-    body = Body("cylinder", radius=0.5, wall_velocity=rotating(omega) if omega else None)
+    body = Body("cylinder", radius=0.5, wall_velocity=rotating(omega) if omega else None, cloud=cloud)
     h = 2.0 * extent / n
     lo = (-extent, -extent, -0.5 * span * h)
     hi = (extent, extent, 0.5 * span * h)
@@ -434,9 +492,10 @@ def cylinder_slab(n=256, span=2, nlevel=3, extent=20.0, mach=0.3, mcyc_fine=500,
     return Case("cylinder_slab_%dx%dx%d" % (n, n, span), prm, levels, body, ref_area=1.0 * span * h)
 
 
-def sphere_box(n=192, nlevel=4, extent=10.0, mach=0.5, mgtype=2, mcyc_fine=400, smoo=0.6, radius=0.5, **kw):
+def sphere_box(n=192, nlevel=4, extent=10.0, mach=0.5, mgtype=2, mcyc_fine=400, smoo=0.6, radius=0.5,
+               cloud="trilinear", **kw):
     """3-D inviscid flow past a D=1 sphere in an n^3 box [-extent, extent]^3."""
-    body = Body("sphere", radius=radius)
+    body = Body("sphere", radius=radius, cloud=cloud)
     lo, hi = (-extent,) * 3, (extent,) * 3
     levels = same_domain_hierarchy(body, lo, hi, (n, n, n), nlevel)
     mcyc = [max(1, mcyc_fine // 8)] * (nlevel - 1) + [mcyc_fine]

@@ -15,9 +15,9 @@ be built and run through this library.
   flow, numerics and domain boundary types of the job sheet, turned into
   parameters as input_param.f90:17-114 does.
 
-The cut-cell records are this library's own (trilinear clouds): the
-reference's ``solid_ipolcoef`` belongs to its fcode library, which is not
-part of the reference tree.
+The cut-cell records are this library's own (trilinear or multiquadric
+radial-basis clouds): the reference's ``solid_ipolcoef`` belongs to its fcode
+library, which is not part of the reference tree.
 """
 import re
 
@@ -146,11 +146,13 @@ def _list(v):
 
 
 # ------------------------------------------------------------------ the case
-def case_from_reference(pin_path, p3d_path, jobsheet_path, span_axis=1, nlevel=None, mcyc=None, **overrides):
+def case_from_reference(pin_path, p3d_path, jobsheet_path, span_axis=1, nlevel=None, mcyc=None, cloud="trilinear",
+                        **overrides):
     """A Case from the reference's inputs: the grids of the grid file (one
     per level; grids sharing a level would need the same-level overlap
     exchange, which is not built), the extruded body of the plot3d surface,
-    and the job sheet's flow, numerics and domain boundary types.  Keyword
+    and the job sheet's flow, numerics and domain boundary types.  ``cloud``
+    picks the records' interpolation clouds ("trilinear" or "rbf").  Keyword
     overrides go to ``cases.params``."""
     js = read_jobsheet(jobsheet_path)
     flow, num, ctl = js.get("FLOW", {}), js.get("NUMERICS", {}), js.get("CONTROL", {})
@@ -162,7 +164,7 @@ def case_from_reference(pin_path, p3d_path, jobsheet_path, span_axis=1, nlevel=N
     if nlevel is not None:
         levels = levels[:nlevel]
     poly = section_polygon(read_plot3d(p3d_path), span_axis)
-    body = K.Body("polygon", poly=poly, span_axis=span_axis)
+    body = K.Body("polygon", poly=poly, span_axis=span_axis, cloud=cloud)
     bct = domain_bctypes(jobsheet_path)
     specs = []
     for li, L in enumerate(levels):

@@ -32,6 +32,9 @@ CASES = {
     # velocity, and the no-slip wall moving with it
     "cylinder_rotating": lambda: small_cylinder(omega=0.8),
     "cylinder_ns_rotating": lambda: small_cylinder(eqntype=A.MGE_EQN_NS, reynolds=40.0, mach=0.2, omega=0.8),
+    # multiquadric radial-basis clouds in place of the trilinear ones
+    "cylinder_rbf": lambda: small_cylinder(cloud="rbf"),
+    "sphere_rbf": lambda: small_sphere(cloud="rbf"),
 }
 
 
