@@ -122,6 +122,11 @@ struct IrsTables {
   const double* e1;   // pivot of row q (index 0..l)
   const double* e1r;  // RN(1/pivot)
   const double* e2;   // elimination factor
+  // the same in single precision for the FP32 sweeps: the rounded pivot, the
+  // single-precision RN(1/pivot) of that rounded pivot, the rounded factor
+  const float* e1f;
+  const float* e1rf;
+  const float* e2f;
 };
 
 // one euler update as a single cooperative launch (small grids)

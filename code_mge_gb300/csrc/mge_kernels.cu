@@ -60,6 +60,14 @@ __device__ __forceinline__ double rcp_4h(const DevBlock<double>& b, int d) { ret
 __device__ __forceinline__ float rcp_4h(const DevBlock<float>& b, int d) { return b.r4hf[d]; }
 __device__ __forceinline__ double rcp_vol(const DevBlock<double>& b) { return b.rvol; }
 __device__ __forceinline__ float rcp_vol(const DevBlock<float>& b) { return b.rvolf; }
+// the line-sweep pivots in the sweep's precision (the FP32 sweeps read the
+// single-precision tables: no conversion per cell)
+__device__ __forceinline__ double irs_e1(const IrsTables& t, int q, double) { return t.e1[q]; }
+__device__ __forceinline__ float irs_e1(const IrsTables& t, int q, float) { return t.e1f[q]; }
+__device__ __forceinline__ double irs_e1r(const IrsTables& t, int q, double) { return t.e1r[q]; }
+__device__ __forceinline__ float irs_e1r(const IrsTables& t, int q, float) { return t.e1rf[q]; }
+__device__ __forceinline__ double irs_e2(const IrsTables& t, int q, double) { return t.e2[q]; }
+__device__ __forceinline__ float irs_e2(const IrsTables& t, int q, float) { return t.e2f[q]; }
 template <typename T> __device__ __forceinline__ T fdimT(T a, T b) { return a > b ? a - b : T(0); }
 template <typename T> __device__ __forceinline__ T fmaxT(T a, T b) { return a > b ? a : b; }
 template <typename T> __device__ __forceinline__ T fminT(T a, T b) { return a < b ? a : b; }
@@ -1146,7 +1154,7 @@ __device__ __forceinline__ void body_irs(const DevBlock<T>& b, const IrsTables& 
     long long c = c0 + 2 * st;
     TC x = (TC)d[c];
     if (b.blank[c] != 0) {
-      x = x / (TC)tb.e1[2];
+      x = x / irs_e1(tb, 2, TC(0));
       d[c] = (T)x;
     }
     prev = x;
@@ -1165,8 +1173,8 @@ __device__ __forceinline__ void body_irs(const DevBlock<T>& b, const IrsTables& 
         const long long c = c0 + (q0 + u) * st;
         xb[u] = (TC)d[c];
         bk[u] = b.blank[c];
-        pb[u] = (TC)tb.e1[q0 + u];
-        rb[u] = (TC)tb.e1r[q0 + u];
+        pb[u] = irs_e1(tb, q0 + u, TC(0));
+        rb[u] = irs_e1r(tb, q0 + u, TC(0));
       }
 #pragma unroll
     for (int u = 0; u < K; u++)
@@ -1186,7 +1194,7 @@ __device__ __forceinline__ void body_irs(const DevBlock<T>& b, const IrsTables& 
         const long long c = c0 + (q0 - u) * st;
         xb[u] = (TC)d[c];
         bk[u] = b.blank[c];
-        pb[u] = (TC)tb.e2[q0 - u];
+        pb[u] = irs_e2(tb, q0 - u, TC(0));
       }
 #pragma unroll
     for (int u = 0; u < K; u++)
@@ -1255,7 +1263,7 @@ __global__ void __launch_bounds__(LT) k_irs_smem(DevBlock<T> b, IrsTables tb, TC
     {
       TC xv = x[sidx(r, 0)];
       if (bl[sidx(r, 0)] != 0) {
-        xv = xv / (TC)tb.e1[2];
+        xv = xv / irs_e1(tb, 2, TC(0));
         x[sidx(r, 0)] = xv;
       }
       prev = xv;
@@ -1263,7 +1271,7 @@ __global__ void __launch_bounds__(LT) k_irs_smem(DevBlock<T> b, IrsTables tb, TC
     for (int q = 1; q < len; q++) {
       TC xv = x[sidx(r, q)];
       if (bl[sidx(r, q)] != 0) {
-        xv = mdiv(xv - bb * prev, (TC)tb.e1[q + 2], (TC)tb.e1r[q + 2]);
+        xv = mdiv(xv - bb * prev, irs_e1(tb, q + 2, TC(0)), irs_e1r(tb, q + 2, TC(0)));
         x[sidx(r, q)] = xv;
       }
       prev = xv;
@@ -1271,7 +1279,7 @@ __global__ void __launch_bounds__(LT) k_irs_smem(DevBlock<T> b, IrsTables tb, TC
     for (int q = len - 2; q >= 0; q--) {
       TC xv = x[sidx(r, q)];
       if (bl[sidx(r, q)] != 0) {
-        xv = xv - (TC)tb.e2[q + 2] * prev;
+        xv = xv - irs_e2(tb, q + 2, TC(0)) * prev;
         x[sidx(r, q)] = xv;
       }
       prev = xv;

@@ -63,6 +63,7 @@ struct Block {
   double *rec_coef = nullptr, *rec_nvec = nullptr, *rec_qb = nullptr, *rec_area = nullptr;
   void *rec_wsol = nullptr, *rec_psol = nullptr, *rec_wall = nullptr;
   double* irs = nullptr;
+  float* irs32 = nullptr;
   IrsTables tabs[3];
   double *rt_partial = nullptr, *rt_cur = nullptr, *forces = nullptr;
   int npart = 1;
@@ -601,10 +602,20 @@ int commit_block(mge_ctx* c, Block& b, double* scratch) {
     all.insert(all.end(), e2.begin(), e2.end());
   }
   CK(cudaMemcpy(b.irs, all.data(), all.size() * 8, cudaMemcpyHostToDevice));
+  // single-precision tables: the FP32 sweeps then need no conversion per cell
+  std::vector<float> all32(all.size());
+  for (size_t q = 0; q < all.size(); q++) all32[q] = (float)all[q];
+  for (int d = 0; d < 3; d++)
+    for (int q = 0; q < lens[d] + 2; q++) all32[offs[d][1] + q] = 1.0f / all32[offs[d][0] + q];
+  if ((rc = dalloc(c, &b.irs32, all32.size()))) return rc;
+  CK(cudaMemcpy(b.irs32, all32.data(), all32.size() * 4, cudaMemcpyHostToDevice));
   for (int d = 0; d < 3; d++) {
     b.tabs[d].e1 = b.irs + offs[d][0];
     b.tabs[d].e1r = b.irs + offs[d][1];
     b.tabs[d].e2 = b.irs + offs[d][2];
+    b.tabs[d].e1f = b.irs32 + offs[d][0];
+    b.tabs[d].e1rf = b.irs32 + offs[d][1];
+    b.tabs[d].e2f = b.irs32 + offs[d][2];
   }
   b.npart = rtrms_partials((long long)b.nx * b.ny * b.nz);
   if ((rc = dalloc(c, &b.rt_partial, b.npart)) || (rc = dalloc(c, &b.rt_cur, 1)) || (rc = dalloc(c, &b.forces, 8)))
