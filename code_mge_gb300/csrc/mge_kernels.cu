@@ -30,6 +30,7 @@
 #include <cooperative_groups.h>
 #include <algorithm>
 #include <cstring>
+#include <type_traits>
 
 #include "exact_ops.cuh"
 #include "fast_pow.cuh"
@@ -1209,13 +1210,121 @@ __device__ __forceinline__ void body_irs(const DevBlock<T>& b, const IrsTables& 
   }
 }
 
+// The FP32 sweeps of the mixed form's finest level, whose storage is FP64.
+// body_irs<double, float, D> converts every value on its way in and out of
+// each sweep, and on this part those conversions issue at the FP64 rate.
+// Here the i sweep reads dw and leaves its results in an FP32 copy (in the
+// stage scratch, free after the residual pass); the j sweep works in the
+// copy; the k sweep writes its results back to dw.  A float stored as double
+// and read back is the same float, so every value is the one body_irs gives;
+// blanked cells keep their dw, as there.
+template <typename TS, typename TO, int D>
+__device__ __forceinline__ void body_irs_mixed(const DevBlock<double>& b, const IrsTables& tb, float bb,
+                                               const TS* src, float* mid, TO* out, long long t) {
+  constexpr bool fill = !std::is_same<TS, float>::value;  // the i sweep: every cell into the copy
+  constexpr bool back = !std::is_same<TO, float>::value;  // the k sweep: results back to dw
+  const long long lines = irs_lines<double, D>(b);
+  const int v = (int)(t / lines);
+  const long long ln = t - (long long)v * lines;
+  long long c0, st;
+  int l;
+  if (D == 0) {
+    int j = 2 + (int)(ln % b.ny), k = 2 + (int)(ln / b.ny);
+    c0 = cidx(b.Pi, b.Pj, 0, j, k);
+    st = 1;
+    l = b.il;
+  } else if (D == 1) {
+    int i = 2 + (int)(ln % b.nx), k = 2 + (int)(ln / b.nx);
+    c0 = cidx(b.Pi, b.Pj, i, 0, k);
+    st = b.Pi;
+    l = b.jl;
+  } else {
+    int i = 2 + (int)(ln % b.nx), j = 2 + (int)(ln / b.nx);
+    c0 = cidx(b.Pi, b.Pj, i, j, 0);
+    st = (long long)b.Pi * b.Pj;
+    l = b.kl;
+  }
+  const TS* s = src + (long long)v * b.N;
+  float* m = mid + (long long)v * b.N;
+  TO* o = out + (long long)v * b.N;
+  float prev;
+  {
+    const long long c = c0 + 2 * st;
+    float x = (float)s[c];
+    if (b.blank[c] != 0) {
+      x = x / irs_e1(tb, 2, 0.0f);
+      m[c] = x;
+    } else if (fill) {
+      m[c] = x;
+    }
+    prev = x;
+  }
+  constexpr int K = 8;
+  float xb[K], pb[K], rb[K];
+  unsigned char bk[K];
+  for (int q0 = 3; q0 <= l; q0 += K) {
+#pragma unroll
+    for (int u = 0; u < K; u++)
+      if (q0 + u <= l) {
+        const long long c = c0 + (q0 + u) * st;
+        xb[u] = (float)s[c];
+        bk[u] = b.blank[c];
+        pb[u] = irs_e1(tb, q0 + u, 0.0f);
+        rb[u] = irs_e1r(tb, q0 + u, 0.0f);
+      }
+#pragma unroll
+    for (int u = 0; u < K; u++)
+      if (q0 + u <= l) {
+        float x = xb[u];
+        if (bk[u] != 0) {
+          x = mdiv(x - bb * prev, pb[u], rb[u]);
+          m[c0 + (q0 + u) * st] = x;
+        } else if (fill) {
+          m[c0 + (q0 + u) * st] = x;
+        }
+        prev = x;
+      }
+  }
+  // the backward pass does not revisit row l: its forward result is final
+  if (back && b.blank[c0 + l * st] != 0) o[c0 + l * st] = (TO)prev;
+  for (int q0 = l - 1; q0 >= 2; q0 -= K) {
+#pragma unroll
+    for (int u = 0; u < K; u++)
+      if (q0 - u >= 2) {
+        const long long c = c0 + (q0 - u) * st;
+        xb[u] = m[c];
+        bk[u] = b.blank[c];
+        pb[u] = irs_e2(tb, q0 - u, 0.0f);
+      }
+#pragma unroll
+    for (int u = 0; u < K; u++)
+      if (q0 - u >= 2) {
+        float x = xb[u];
+        if (bk[u] != 0) {
+          x = x - pb[u] * prev;
+          o[c0 + (q0 - u) * st] = (TO)x;
+        }
+        prev = x;
+      }
+  }
+}
+
+template <typename TS, typename TO, int D>
+__global__ void k_irs_mixed(DevBlock<double> b, IrsTables tb, float bb, const TS* src, float* mid, TO* out) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < 5 * irs_lines<double, D>(b)) body_irs_mixed<TS, TO, D>(b, tb, bb, src, mid, out, t);
+}
+
 // Shared-memory variant of body_irs: a block stages LT whole lines of one
 // variable (and their blanking) in shared memory with coalesced loads, each
 // of its first LT threads runs the reference's sweep on one line there, and
 // the block writes the lines back coalesced.  Arithmetic and order per line
 // are those of body_irs.
-template <typename T, typename TC, int D, int LT>
-__global__ void __launch_bounds__(LT) k_irs_smem(DevBlock<T> b, IrsTables tb, TC bb) {
+// Loads from src and stores to dst (both dw, except for the FP32 copy of the
+// mixed form's i sweep: dw in, the copy out, every cell of the tile written)
+template <typename T, typename TC, int D, int LT, typename TS, typename TO>
+__device__ __forceinline__ void body_irs_smem(const DevBlock<T>& b, const IrsTables& tb, TC bb, const TS* src,
+                                              TO* dst) {
   extern __shared__ unsigned char smem_raw[];
   const long long lines = irs_lines<T, D>(b);
   const long long ntile = (lines + LT - 1) / LT;
@@ -1228,7 +1337,8 @@ __global__ void __launch_bounds__(LT) k_irs_smem(DevBlock<T> b, IrsTables tb, TC
   const int S = (D == 0) ? (len | 1) : LT;                  // odd row stride for line-major tiles
   TC* x = (TC*)smem_raw;
   unsigned char* bl = smem_raw + sizeof(TC) * (size_t)LT * (len + 1);
-  T* d = b.dw + (long long)v * b.N;
+  const TS* d = src + (long long)v * b.N;
+  TO* dout = dst + (long long)v * b.N;
   const long long N = b.N;
   (void)N;
   // element (line r, row q) of the tile -> global cell
@@ -1289,9 +1399,20 @@ __global__ void __launch_bounds__(LT) k_irs_smem(DevBlock<T> b, IrsTables tb, TC
   for (int e = threadIdx.x; e < LT * len; e += blockDim.x) {
     int rr, q;
     if (D == 0) { rr = e / len; q = e - rr * len; } else { q = e / LT; rr = e - q * LT; }
-    if (rr < nl) d[cell(rr, q)] = (T)x[sidx(rr, q)];
+    if (rr < nl) dout[cell(rr, q)] = (TO)x[sidx(rr, q)];
   }
   (void)tot;
+}
+
+template <typename T, typename TC, int D, int LT>
+__global__ void __launch_bounds__(LT) k_irs_smem(DevBlock<T> b, IrsTables tb, TC bb) {
+  body_irs_smem<T, TC, D, LT>(b, tb, bb, (const T*)b.dw, b.dw);
+}
+
+// the mixed form's i sweep in shared-memory tiles: dw in, the FP32 copy out
+template <int LT>
+__global__ void __launch_bounds__(LT) k_irs_smem_fill(DevBlock<double> b, IrsTables tb, float bb, float* cp) {
+  body_irs_smem<double, float, 0, LT>(b, tb, bb, (const double*)b.dw, cp);
 }
 
 template <typename TC, int LT>
@@ -2405,6 +2526,26 @@ void launch_irs_part_t(int part, const DevBlock<T>& b, const PhysParams& P, cons
     }
     return;
   }
+  if constexpr (std::is_same<T, double>::value && std::is_same<TC, float>::value) {
+    // FP32 sweeps on FP64 storage: one FP32 copy through the three sweeps
+    float* cp = (float*)b.F;
+    if (part == 0) {
+      // the tuned form of the i sweep: global-memory lines or shared-memory tiles
+      constexpr int LT = 64;
+      const size_t sm = irs_smem_bytes<float, LT>((b.il - 1) | 1);
+      if (variant && variant[0] == 1 && sm <= 200 * 1024)
+        k_irs_smem_fill<LT><<<(unsigned)(5 * ((irs_lines_h(b, 0) + LT - 1) / LT)), LT, sm, s>>>(b, tab[0], bb, cp);
+      else
+        k_irs_mixed<double, float, 0><<<LAUNCH_N(5 * irs_lines_h(b, 0)), 0, s>>>(b, tab[0], bb, b.dw, cp, cp);
+    }
+    if (part == 1)
+      k_irs_mixed<float, float, 1><<<LAUNCH_N(5 * irs_lines_h(b, 1)), 0, s>>>(b, tab[1], bb, cp, cp, cp);
+    if (part == 2) {
+      k_irs_mixed<float, double, 2><<<LAUNCH_N(5 * irs_lines_h(b, 2)), 0, s>>>(b, tab[2], bb, cp, cp, b.dw);
+      k_update<T><<<LAUNCH_N(ncell), 0, s>>>(b, P, Au);
+    }
+    return;
+  }
   if (part == 0) launch_irs_dir<T, TC, 0>(b, tab[0], bb, s, variant ? variant[0] : 0);
   if (part == 1) launch_irs_dir<T, TC, 1>(b, tab[1], bb, s, variant ? variant[1] : 0);
   if (part == 2) {
@@ -2503,6 +2644,7 @@ void init_kernel_attributes() {
   MGE_SMEM_ATTR(double, float)
   MGE_SMEM_ATTR(float, float)
 #undef MGE_SMEM_ATTR
+  cudaFuncSetAttribute(k_irs_smem_fill<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
 }
 
 // grid of the cooperative kernel: every block resident at once
