@@ -108,6 +108,8 @@ struct PhysParams {
   double lim_e2[5];         // van Albada floor per primitive variable
   double rgm1;              // RN(1/(gamma-1))
   float rgm1f;              // RN(1/(gamma-1)) in single precision, of the single-precision gamma-1
+  double rgamma;            // RN(1/gamma)
+  float rgammaf;            // RN(1/gamma) in single precision, of the single-precision gamma
 };
 
 // error word bits

@@ -55,6 +55,8 @@ __device__ __forceinline__ float mdiv(float a, float b, float y) {
 // block's precision, so that mdiv gives the correctly rounded quotient
 __device__ __forceinline__ double rcp_gm1(const PhysParams& P, double) { return P.rgm1; }
 __device__ __forceinline__ float rcp_gm1(const PhysParams& P, float) { return P.rgm1f; }
+__device__ __forceinline__ double rcp_gamma(const PhysParams& P, double) { return P.rgamma; }
+__device__ __forceinline__ float rcp_gamma(const PhysParams& P, float) { return P.rgammaf; }
 __device__ __forceinline__ double rcp_h(const DevBlock<double>& b, int d) { return b.rh[d]; }
 __device__ __forceinline__ float rcp_h(const DevBlock<float>& b, int d) { return b.rhf[d]; }
 __device__ __forceinline__ double rcp_4h(const DevBlock<double>& b, int d) { return b.r4h[d]; }
@@ -1649,22 +1651,26 @@ __device__ void body_bc_face(const DevBlock<T>& b, const PhysParams& P, int face
     T wp[5];
     for (int v = 0; v < 5; v++) wp[v] = b.w[v * N + p1];
     T pph = b.p[p1];
-    T vel_norm = (wp[1] * fn0 + wp[2] * fn1 + wp[3] * fn2) / wp[0];
+    // the quotients by the cell's density share one reciprocal, those by
+    // gamma-1 and gamma take the host's (mdiv: the same roundings as the
+    // divisions, with a shorter dependent chain)
+    const T y0 = T(1) / wp[0], gm1 = gamma - T(1), rg1 = rcp_gm1(P, T(0)), rgam = rcp_gamma(P, T(0));
+    T vel_norm = mdiv(wp[1] * fn0 + wp[2] * fn1 + wp[3] * fn2, wp[0], y0);
     T out[5], pout;
     bool set = false;
     const T u0a = (T)P.u0[ax];
+    const T rmi = u0a * fnn - mdiv(T(2) * (T)P.c0, gm1, rg1);
     if (vel_norm <= T(0)) {
       T rhoe = wp[0];
-      T ue = wp[1 + ax] / rhoe;
+      T ue = mdiv(wp[1 + ax], rhoe, y0);
       T pe = pph;
-      T ce = sqrt(gamma * pe / rhoe);
-      T rpo = ue * fnn + T(2) * ce / (gamma - T(1));
-      T rmi = u0a * fnn - T(2) * (T)P.c0 / (gamma - T(1));
+      T ce = sqrt(mdiv(gamma * pe, rhoe, y0));
+      T rpo = ue * fnn + mdiv(T(2) * ce, gm1, rg1);
       T vv[3] = {(T)P.u0[0], (T)P.u0[1], (T)P.u0[2]};
       vv[ax] = T(0.5) * (rpo + rmi) * fnn;
       T ci = T(0.25) * (gamma - T(1)) * (rpo - rmi);
       T si = (T)P.si_far;
-      T cc = ci * ci / gamma;
+      T cc = mdiv(ci * ci, gamma, rgam);
       T rhoi = pow_gm(P, si * cc, gm);
       T prei = rhoi * cc;
       out[0] = rhoi;
@@ -1676,16 +1682,15 @@ __device__ void body_bc_face(const DevBlock<T>& b, const PhysParams& P, int face
       set = true;
     } else if (vel_norm > T(0)) {
       T rhoi = wp[0];
-      T vv[3] = {wp[1] / rhoi, wp[2] / rhoi, wp[3] / rhoi};
+      T vv[3] = {mdiv(wp[1], rhoi, y0), mdiv(wp[2], rhoi, y0), mdiv(wp[3], rhoi, y0)};
       T prei = pph;
       T si = pow_gamma(P, rhoi, gamma) / prei;
-      T ci = sqrt(gamma * prei / rhoi);
-      T rpo = vv[ax] * fnn + T(2) * ci / (gamma - T(1));
-      T rmi = u0a * fnn - T(2) * (T)P.c0 / (gamma - T(1));
+      T ci = sqrt(mdiv(gamma * prei, rhoi, y0));
+      T rpo = vv[ax] * fnn + mdiv(T(2) * ci, gm1, rg1);
       T ve[3] = {vv[0], vv[1], vv[2]};
       ve[ax] = T(0.5) * (rpo + rmi) * fnn;
       T ce = T(0.25) * (gamma - T(1)) * (rpo - rmi);
-      T cc = ce * ce / gamma;
+      T cc = mdiv(ce * ce, gamma, rgam);
       T rhoe = pow_gm(P, si * cc, gm);
       T pe = rhoe * cc;
       out[0] = rhoe;
@@ -1696,12 +1701,17 @@ __device__ void body_bc_face(const DevBlock<T>& b, const PhysParams& P, int face
       pout = pe;
       set = true;
     }
-    if (set) {
-      for (int v = 0; v < 5; v++) b.w[v * N + d1] = out[v];
+    if (set) {  // both ghost layers take the new state
+      for (int v = 0; v < 5; v++) {
+        b.w[v * N + d1] = out[v];
+        b.w[v * N + d2] = out[v];
+      }
       b.p[d1] = pout;
+      b.p[d2] = pout;
+    } else {  // vel_norm NaN: the second layer copies the first as it stands
+      for (int v = 0; v < 5; v++) b.w[v * N + d2] = b.w[v * N + d1];
+      b.p[d2] = b.p[d1];
     }
-    for (int v = 0; v < 5; v++) b.w[v * N + d2] = b.w[v * N + d1];
-    b.p[d2] = b.p[d1];
   } else if (kind == -50) {  // bc_symm.f90
     for (int v = 0; v < 5; v++) b.w[v * N + d1] = b.w[v * N + p1];
     b.w[(1 + ax) * N + d1] = -b.w[(1 + ax) * N + p1];

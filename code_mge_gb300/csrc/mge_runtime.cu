@@ -410,6 +410,8 @@ void build_phys(mge_ctx* c) {
   for (int q = 0; q < 5; q++) Q.lim_e2[q] = 1e-6 * ref[q] * ref[q] / (P.limfac > 0.0 ? P.limfac : 1.0);
   Q.rgm1 = 1.0 / (P.gamma - 1.0);
   Q.rgm1f = 1.0f / ((float)P.gamma - 1.0f);
+  Q.rgamma = 1.0 / P.gamma;
+  Q.rgammaf = 1.0f / (float)P.gamma;
 }
 
 // psmoo.f90:136-166 pivots for a line of l-1 unknowns (rows 2..l)
