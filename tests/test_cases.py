@@ -56,3 +56,9 @@ def test_cycle_visits():
     assert S.cycle_visits(3, 1)[0][1:4] == [1, 2, 1]
     case = K.sphere_box(n=192, nlevel=4, extent=10.0, mgtype=2)
     assert S.cell_updates_per_cycle(case) == 192 ** 3 + 3 * 96 ** 3 + 6 * 48 ** 3 + 4 * 24 ** 3
+    # the NS cylinder workload: 4 embedded levels of 512x512x2 cells, V-cycle
+    # (finest and coarsest once, the middle levels twice)
+    assert S.cycle_visits(4, 1)[0][1:5] == [1, 2, 2, 1]
+    cyl = K.cylinder_embedded(n=512, span=2, nlevel=4, h_fine=1.0 / 96.0, mach=0.2)
+    assert cyl.cells_per_level() == [512 * 512 * 2] * 4
+    assert S.cell_updates_per_cycle(cyl) == 6 * 512 * 512 * 2
