@@ -493,11 +493,13 @@ def cylinder_slab(n=256, span=2, nlevel=3, extent=20.0, mach=0.3, mcyc_fine=500,
 
 
 def sphere_box(n=192, nlevel=4, extent=10.0, mach=0.5, mgtype=2, mcyc_fine=400, smoo=0.6, radius=0.5,
-               cloud="trilinear", **kw):
-    """3-D inviscid flow past a D=1 sphere in an n^3 box [-extent, extent]^3."""
+               cloud="trilinear", bctype=(-20,) * 6, **kw):
+    """3-D inviscid flow past a D=1 sphere in an n^3 box [-extent, extent]^3.
+    bctype: the six faces' boundary conditions (bcond.f90:16-42), far field
+    by default."""
     body = Body("sphere", radius=radius, cloud=cloud)
     lo, hi = (-extent,) * 3, (extent,) * 3
-    levels = same_domain_hierarchy(body, lo, hi, (n, n, n), nlevel)
+    levels = same_domain_hierarchy(body, lo, hi, (n, n, n), nlevel, bctype=bctype)
     mcyc = [max(1, mcyc_fine // 8)] * (nlevel - 1) + [mcyc_fine]
     prm = params(mach, nlevel=nlevel, mcyc=mcyc, mgtype=mgtype, smoo=smoo, **kw)
     return Case("sphere_%d^3" % n, prm, levels, body, ref_area=math.pi * radius ** 2)

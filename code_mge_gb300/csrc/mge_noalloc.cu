@@ -28,7 +28,29 @@ static __device__ __align__(256) double g_rtrms_partials[kMaxPartials];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
+// Device address of g_rtrms_partials per device, as last looked up outside a
+// stream capture.  A call inside a capture cannot look it up and reuses this.
 double* g_scratch[kMaxDevices] = {nullptr};
+
+// The device address of the static scratch on the current device.  Outside a
+// capture it is looked up on every call: after cudaDeviceReset, or after the
+// primary context is destroyed and made again, the module loads anew and the
+// array may sit elsewhere.  Inside a capture the address of the last call
+// made outside one is used (none yet: an error).
+int scratch_address(int dev, cudaStream_t s, double** out) {
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cap) != cudaSuccess) return MGE_ECUDA;
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (cap == cudaStreamCaptureStatusNone) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_rtrms_partials) != cudaSuccess) return MGE_ECUDA;
+    g_scratch[dev] = (double*)p;
+  } else if (!g_scratch[dev]) {
+    return MGE_EBADCFG;  // first call on this device made inside a capture
+  }
+  *out = g_scratch[dev];
+  return MGE_OK;
+}
 
 __global__ void k_noalloc_partial(const double* __restrict__ dw, const double* __restrict__ vdtim,
                                   const int32_t* __restrict__ blank, int nx, int ny, int nz, double cfl, int vt,
@@ -74,22 +96,18 @@ extern "C" int mge_residual_norm_noalloc(const double* dw_rho, const double* vdt
   if (ncell > kMaxCells) return MGE_EBADCFG;  // more partial sums than the static scratch holds
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return MGE_ECUDA;
+  // an error left pending by earlier work is not this call's: report it
+  // without clearing it, and launch nothing
+  if (cudaPeekAtLastError() != cudaSuccess) return MGE_ECUDA;
+  cudaStream_t s = (cudaStream_t)stream;
   double* scratch = nullptr;
-  {
-    // first call on a device: resolve the device address of the static array
-    // (the host-side symbol is only a stand-in, never a device address)
-    std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_scratch[dev]) {
-      void* p = nullptr;
-      if (cudaGetSymbolAddress(&p, g_rtrms_partials) != cudaSuccess) return MGE_ECUDA;
-      g_scratch[dev] = (double*)p;
-    }
-    scratch = g_scratch[dev];
-  }
+  const int rc = scratch_address(dev, s, &scratch);
+  if (rc != MGE_OK) return rc;
   int npart = (int)((ncell + kCellsPerPartial - 1) / kCellsPerPartial);
   if (npart < 1) npart = 1;
-  cudaStream_t s = (cudaStream_t)stream;
   k_noalloc_partial<<<npart, kThreads, 0, s>>>(dw_rho, vdtim, blank, nx, ny, nz, cfl, vt, dtim, scratch, npart);
+  if (cudaGetLastError() != cudaSuccess) return MGE_ECUDA;
   k_noalloc_final<<<1, 32, 0, s>>>(scratch, npart, (double)ncell, norm_out);
-  return cudaGetLastError() == cudaSuccess ? MGE_OK : MGE_ECUDA;
+  if (cudaGetLastError() != cudaSuccess) return MGE_ECUDA;
+  return MGE_OK;
 }

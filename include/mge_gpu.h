@@ -253,10 +253,17 @@ int mge_kernel_times(mge_ctx* ctx, int level, int reps, double* ms_out, int nout
  * It allocates nothing: its partial sums live in a static 32 KiB device
  * array, which limits it to nx*ny*nz <= 8,388,608 cells (MGE_EBADCFG beyond).
  * dw_rho: density residual dw(:,:,:,1); vdtim: local time steps; blank:
- * int32 blanking, all in the (0:ib,0:jb,0:kb) layout; norm_out: one device
- * double; stream: a cudaStream_t or NULL.  The first call on a device looks
- * up the array's device address; make that first call before any stream
- * capture.  All calls share the array: calls that overlap on the GPU race. */
+ * int32 blanking as the reference's integer blank array holds it (not the
+ * one-byte blank a context keeps on the device), all in the
+ * (0:ib,0:jb,0:kb) layout; dtim: the global time step, read when vt = 1;
+ * norm_out: one device double; stream: a cudaStream_t or NULL.
+ * Every call made outside a stream capture looks up the array's device
+ * address afresh (a device reset may move it); a call inside a capture uses
+ * the address of the last call made outside one, so make one call on each
+ * device before any capture (MGE_EBADCFG otherwise).  An error already
+ * pending on the calling thread is returned as MGE_ECUDA, not cleared, and
+ * nothing is launched.  All calls share the array: calls that overlap on
+ * the GPU race. */
 int mge_residual_norm_noalloc(const double* dw_rho, const double* vdtim, const int32_t* blank,
                               int nx, int ny, int nz, double cfl, int vt, double dtim,
                               double* norm_out, void* stream);

@@ -35,6 +35,10 @@ CASES = {
     # multiquadric radial-basis clouds in place of the trilinear ones
     "cylinder_rbf": lambda: small_cylinder(cloud="rbf"),
     "sphere_rbf": lambda: small_sphere(cloud="rbf"),
+    # symmetry planes (bc_symm.f90:27-82) on four faces of the box, the flow along x between them
+    "sphere_symm": lambda: small_sphere(bctype=(-20, -50, -50, -20, -50, -50)),
+    # reflecting walls (bc_wall.f90:28-89) on the j faces, symmetry on the k faces
+    "sphere_wall": lambda: small_sphere(bctype=(-20, -80, -50, -20, -80, -50)),
 }
 
 

@@ -235,3 +235,46 @@ def test_turning_wall_breaks_the_up_down_symmetry():
     # stream below the body, and the lift points down (the Magnus force)
     assert out[0.8].cl < -1e-3
     assert abs(out[0.8].cl + out[-0.8].cl) <= 1e-10 * abs(out[0.8].cl)
+
+
+def test_symmetry_planes_preserve_the_free_stream():
+    # bc_symm.f90:27-82 mirrors the face-normal momentum; with the flow along
+    # x the j and k symmetry planes leave the free stream as it is
+    case = K.free_stream_box(n=(12, 10, 8), nlevel=1, mach=0.6, bctype=(-20, -50, -50, -20, -50, -50))
+    o = OracleCycle(case)
+    o.timestep(1)
+    o.euler(1, ncyc=1, lres=True)
+    assert np.abs(physical(o.field("dw", 1), o.spec(1))).max() < 1e-14
+    o.euler(1, ncyc=1)
+    assert o.rtrms(1, 1) < 1e-13
+
+
+def test_symmetry_and_wall_ghosts_follow_the_reference_formulas():
+    """After a stage, the face ghosts (tangential indices physical) of a
+    symmetry face and a wall face hold exactly the values of bc_symm.f90:
+    57-80 and bc_wall.f90:50-86, including the wall's second pressure ghost
+    taken from the first physical cell (bc_wall.f90:59-60)."""
+    case = K.sphere_box(n=16, nlevel=1, extent=2.0, radius=0.6, mcyc_fine=3,
+                        bctype=(-20, -50, -50, -20, -80, -50))
+    o = OracleCycle(case)
+    o.solve()
+    o.timestep(1)
+    o.euler_partial(1, 1)
+    w, p = o.field("w", 1), o.field("p", 1)
+    nx, ny, nz = o.spec(1).n
+    il, jl, kl = nx + 1, ny + 1, nz + 1
+    I, Kk = slice(2, il + 1), slice(2, kl + 1)
+    # face 2, symmetry at j = 1.5: ghosts 1 and 0 mirror cells 2 and 3, v negated
+    for g, q in ((1, 2), (0, 3)):
+        want = w[:, Kk, q, I].copy()
+        want[2] = -want[2]
+        assert np.array_equal(w[:, Kk, g, I], want)
+        assert np.array_equal(p[Kk, g, I], p[Kk, q, I])
+    # face 5, wall at j = jl + 0.5: all three momenta negated
+    for g, q in ((jl + 1, jl), (jl + 2, jl - 1)):
+        want = w[:, Kk, q, I].copy()
+        want[1:4] = -want[1:4]
+        assert np.array_equal(w[:, Kk, g, I], want)
+        assert np.array_equal(p[Kk, g, I], p[Kk, jl, I])
+    # the flow is not trivial there: the walls' momenta are not zero
+    assert np.abs(w[1, Kk, jl, I]).min() > 0.0
