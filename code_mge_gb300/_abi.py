@@ -31,7 +31,7 @@ ERROR_NAMES = {
 MGE_EQN_EULER, MGE_EQN_NS = 0, 1
 MGE_DIS_CENTRAL, MGE_DIS_ROE1, MGE_DIS_ROE2 = 0, 1, 2
 MGE_DISSIP_SCALAR, MGE_DISSIP_MATRIX = 0, 1
-MGE_PREC_FP64, MGE_PREC_MIXED = 0, 1
+MGE_PREC_FP64, MGE_PREC_MIXED, MGE_PREC_REFINED = 0, 1, 2
 MGE_MAX_STAGE = 8
 MGE_MAX_LEVEL = 16
 MGE_MAX_CLOUD = 8

@@ -84,6 +84,7 @@ struct StageArgs {
   int irs;          // odd stage with smoo > 0: defer the update to the line sweeps
   int vt;
   int tmode;        // unsteady source term: 0 none, 1 first step (itime 1), 2 BDF2 (itime > 1)
+  int fast;         // the contracted FP64 residual of the mixed form's finest level (JST central, Euler)
 };
 
 struct PhysParams {
@@ -112,11 +113,14 @@ struct PhysParams {
   float rgammaf;            // RN(1/gamma) in single precision, of the single-precision gamma
 };
 
-// error word bits
+// error word: the kernels set it only while it is zero (atomicCAS), so it
+// holds the first stop in launch order, the one the reference's sequential
+// run would have stopped at
 enum : unsigned {
   ERR_NEGPRESS = 1u,
   ERR_ZERORHO = 2u,
   ERR_NAN = 4u,
+  ERR_NANRES = 8u,  // NaN residual norm (solver.f90:180)
 };
 
 // IRS pivot tables of one block direction (psmoo.f90:136-166)
@@ -165,7 +169,7 @@ template <typename T> void launch_solut(const DevBlock<T>& b, const PhysParams& 
 template <typename T> void launch_cutcell(const DevBlock<T>& b, const PhysParams& P, unsigned* err, cudaStream_t s);
 template <typename T> void launch_bcond(const DevBlock<T>& b, const PhysParams& P, cudaStream_t s);
 template <typename T> void launch_rtrms(const DevBlock<T>& b, const PhysParams& P, int vt, double* partial,
-                                        int npartial, double* out, cudaStream_t s);
+                                        int npartial, double* out, cudaStream_t s, unsigned* err = nullptr);
 template <typename T> void launch_depvars_all(const DevBlock<T>& b, const PhysParams& P, cudaStream_t s);
 template <typename T> void launch_copy_ws(const DevBlock<T>& b, cudaStream_t s);
 template <typename T> void launch_save_wn(const DevBlock<T>& b, cudaStream_t s);

@@ -108,7 +108,7 @@ __device__ __forceinline__ unsigned long long body_timestep(const DevBlock<T>& b
   TC y = TC(1) / w0;
   TC cc = mdiv(gamma * pc, w0, y);
   if (cc < TC(0) || cc != cc) {  // timestep.f90:45-48
-    atomicOr(err, ERR_NEGPRESS);
+    atomicCAS(err, 0u, (unsigned)ERR_NEGPRESS);  // the first stop in launch order wins
     return mine;
   }
   cc = sqrt(fmaxT(cc, TC(0)));
@@ -229,7 +229,13 @@ __device__ __forceinline__ T van_albada(T a, T b, T e2);
 // direction goes to dlt[dir][var], once per cell.  A face takes the slope of
 // its lower cell for the left state and that of its upper cell for the right
 // state, the same van_albada(q(c)-q(c-1), q(c+1)-q(c)) it would form itself.
-template <typename T, bool SLOPES = false>
+//
+// FAST: the contracted form of the mixed precision's finest level (JST
+// central scheme, Euler): the cell flux takes the velocity q = (w_d s)/rho
+// once and multiplies, F(v) = q w(v), instead of rounding each product
+// before its division.  The result is the same quantity to an FP64 rounding
+// or two, not the reference's bit pattern.
+template <typename T, bool SLOPES = false, bool FAST = false>
 __device__ __forceinline__ void body_prep(const DevBlock<T>& b, const PhysParams& P, int dissip_on, long long t) {
   const int ex = b.ie, ey = b.je;  // count = ie (cells 1..ie)
   int i = 1 + (int)(t % ex);
@@ -272,7 +278,24 @@ __device__ __forceinline__ void body_prep(const DevBlock<T>& b, const PhysParams
   }
   // the MUSCL Roe faces take their central flux from the reconstructed
   // states, not from the cell fluxes
-  if (P.distype != 2) {
+  if (FAST) {
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      const T s = (T)b.s[d];
+      const T f0 = w[1 + d] * s;
+      const T q = f0 * y;
+      T f1 = q * w[1], f2 = q * w[2], f3 = q * w[3];
+      if (d == 0) f1 = fma(p, s, f1);
+      if (d == 1) f2 = fma(p, s, f2);
+      if (d == 2) f3 = fma(p, s, f3);
+      T* F = b.F + (long long)(d * 5) * N + c;
+      F[0] = f0;
+      F[N] = f1;
+      F[2 * N] = f2;
+      F[3 * N] = f3;
+      F[4 * N] = q * Hc;
+    }
+  } else if (P.distype != 2) {
 #pragma unroll
     for (int d = 0; d < 3; d++) {
       T s = (T)b.s[d];
@@ -677,6 +700,52 @@ __device__ __forceinline__ void body_face(const DevBlock<T>& b, const PhysParams
   if (ip && jp) face_dir<T, 2, SCH>(b, P, dissip_on, cd, i, j, k);
 }
 
+// The contracted form's dissipation face (scalar JST, dflux.f90:87-112): the
+// combine pass forms the convective part from the cell fluxes, so only dfs is
+// written.  The face's coefficients take lambda once, dis2*lambda and
+// dis4*lambda, and each variable is one product and two multiply-adds.
+template <typename T, int D>
+__device__ __forceinline__ void face_diss_fast(const DevBlock<T>& b, const PhysParams& P, T cd, int i, int j, int k) {
+  const long long N = b.N;
+  const long long st = D == 0 ? 1 : (D == 1 ? (long long)b.Pi : (long long)b.Pi * b.Pj);
+  const long long c = cidx(b.Pi, b.Pj, i, j, k);
+  const int q = D == 0 ? i : (D == 1 ? j : k);
+  const int lq = D == 0 ? b.il : (D == 1 ? b.jl : b.kl);
+  const int bq = lq + 2;
+  const T* fpd = b.fp + (long long)D * N;
+  const T f_m2 = (q - 2 == 0) ? T(0) : fpd[c - 2 * st];
+  const T f_p1 = (q + 1 == bq) ? T(0) : fpd[c + st];
+  const T ep = max_nonneg(max_nonneg(max_nonneg(f_m2, fpd[c - st]), fpd[c]), f_p1);
+  const long long cm = (q - 1 < 2) ? c : c - st;
+  const long long cp = (q > lq) ? c - st : c;
+  const T lam = mulhalf(b.lam[cm] + b.lam[cp]);
+  const T dis2 = (T)P.vis2 * ep;
+  const T dis4 = gt_nonneg((T)P.vis4, dis2) ? (T)P.vis4 - dis2 : T(0);
+  const T a2 = (dis2 * cd) * lam, a4 = (dis4 * cd) * lam;
+  const T* Dl = b.dlt + (long long)(D * 5) * N;
+  T* Df = b.dfs + (long long)(D * 5) * N;
+#pragma unroll
+  for (int v = 0; v < 5; v++) {
+    const T d0 = Dl[v * N + c];
+    const T dm = (q - 1 == 1) ? d0 : Dl[v * N + c - st];
+    const T dp = (q + 1 == bq) ? d0 : Dl[v * N + c + st];
+    const T t3 = fma(T(-2), d0, dp + dm);
+    Df[v * N + c] = fma(a2, d0, -(a4 * t3));
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void body_face_diss(const DevBlock<T>& b, const PhysParams& P, T cd, long long t) {
+  const int ex = b.ie - 1, ey = b.je - 1;  // 2..ie
+  int i = 2 + (int)(t % ex);
+  int j = 2 + (int)((t / ex) % ey);
+  int k = 2 + (int)(t / ((long long)ex * ey));
+  bool jp = j <= b.jl, kp = k <= b.kl, ip = i <= b.il;
+  if (jp && kp) face_diss_fast<T, 0>(b, P, cd, i, j, k);
+  if (ip && kp) face_diss_fast<T, 1>(b, P, cd, i, j, k);
+  if (ip && jp) face_diss_fast<T, 2>(b, P, cd, i, j, k);
+}
+
 // --------------------------------------------------------------- stage: cut-cell record terms
 // A record's corrections take dense face fluxes out and wall fluxes in.  The
 // wall side depends only on the state (w, p, H, lambda, wsol, psol), not on
@@ -713,7 +782,7 @@ __device__ void rec_wall_terms(const DevBlock<T>& b, const PhysParams& P, int di
   T s = (T)b.s[D];
   T wc[5];
   for (int v = 0; v < 5; v++) wc[v] = b.w[v * N + c];
-  if (fabs(wc[0]) < T(1.0e-8)) atomicOr(err, ERR_ZERORHO);
+  if (fabs(wc[0]) < T(1.0e-8)) atomicCAS(err, 0u, (unsigned)ERR_ZERORHO);
   T psol = b.rec_psol[m];
   T wsol[5];
   for (int v = 0; v < 5; v++) wsol[v] = b.rec_wsol[5 * m + v];
@@ -925,7 +994,12 @@ __device__ __forceinline__ T unsteady_lam(const DevBlock<T>& b, const PhysParams
 // The cut-cell records act here in record order on the cell they touch: the
 // dense face pair out, the wall pair in, from this stage's face fluxes and
 // the record pass's wall terms (rec_wall_terms).
-template <typename T>
+//
+// FAST (the contracted form, JST central scheme): the convective part of dw
+// is the central difference of the cell fluxes, efs(q) - efs(q+1) =
+// 0.5*(F(q-1) - F(q+1)) in each direction, so no convective face pass runs;
+// a record's dense face pair takes the same difference.
+template <typename T, bool FAST = false>
 __device__ __forceinline__ void body_combine(const DevBlock<T>& b, const PhysParams& P, const StageArgs& A,
                                              unsigned* err, long long t) {
   const int nxl = b.nx, nyl = b.ny;
@@ -937,15 +1011,26 @@ __device__ __forceinline__ void body_combine(const DevBlock<T>& b, const PhysPar
   const long long sj = b.Pi, sk = (long long)b.Pi * b.Pj;
   const int tg = b.cutmap[c];
   T dwv[5], fwv[5];
-  const T* Ex = b.efs;
-  const T* Ey = b.efs + 5 * N;
-  const T* Ez = b.efs + 10 * N;
+  if (FAST) {
+    const T* Fx = b.F;
+    const T* Fy = b.F + 5 * N;
+    const T* Fz = b.F + 10 * N;
 #pragma unroll
-  for (int v = 0; v < 5; v++) {
-    T a = Ex[v * N + c] - Ex[v * N + c + 1];
-    a = a + Ey[v * N + c] - Ey[v * N + c + sj];
-    a = a + Ez[v * N + c] - Ez[v * N + c + sk];
-    dwv[v] = a;
+    for (int v = 0; v < 5; v++) {
+      const T a = (Fx[v * N + c - 1] - Fx[v * N + c + 1]) + (Fy[v * N + c - sj] - Fy[v * N + c + sj]);
+      dwv[v] = mulhalf(a + (Fz[v * N + c - sk] - Fz[v * N + c + sk]));
+    }
+  } else {
+    const T* Ex = b.efs;
+    const T* Ey = b.efs + 5 * N;
+    const T* Ez = b.efs + 10 * N;
+#pragma unroll
+    for (int v = 0; v < 5; v++) {
+      T a = Ex[v * N + c] - Ex[v * N + c + 1];
+      a = a + Ey[v * N + c] - Ey[v * N + c + sj];
+      a = a + Ez[v * N + c] - Ez[v * N + c + sk];
+      dwv[v] = a;
+    }
   }
   // fw: blending and dissipation (euler.f90:127-135, dflux.f90:116-238)
   const T fac = T(1) - (T)A.cd;
@@ -989,13 +1074,22 @@ __device__ __forceinline__ void body_combine(const DevBlock<T>& b, const PhysPar
         }
       }
     }
+    if (FAST) {
 #pragma unroll
-    for (int v = 0; v < 5; v++) {
-      T a = vis[v];
-      a = a + (Dx[v * N + c] - Dx[v * N + c + 1]);
-      a = a + (Dy[v * N + c] - Dy[v * N + c + sj]);
-      a = a + (Dz[v * N + c] - Dz[v * N + c + sk]);
-      fwv[v] = a;
+      for (int v = 0; v < 5; v++) {
+        const T a = (Dx[v * N + c] - Dx[v * N + c + 1]) + (Dy[v * N + c] - Dy[v * N + c + sj]);
+        const T d = a + (Dz[v * N + c] - Dz[v * N + c + sk]);
+        fwv[v] = A.scale_fw ? fma(b.fw[v * N + c], fac, d) : d;
+      }
+    } else {
+#pragma unroll
+      for (int v = 0; v < 5; v++) {
+        T a = vis[v];
+        a = a + (Dx[v * N + c] - Dx[v * N + c + 1]);
+        a = a + (Dy[v * N + c] - Dy[v * N + c + sj]);
+        a = a + (Dz[v * N + c] - Dz[v * N + c + sk]);
+        fwv[v] = a;
+      }
     }
   } else {
 #pragma unroll
@@ -1014,9 +1108,10 @@ __device__ __forceinline__ void body_combine(const DevBlock<T>& b, const PhysPar
       const T* Wm = b.rec_wall + 25LL * m;
       if (!(op & 1)) {  // efluxb on the cut cell: the dense face pair out, the wall pair in
         const T* E = b.efs + (long long)(D * 5) * N;
+        const T* Fd = b.F + (long long)(D * 5) * N;
 #pragma unroll
         for (int v = 0; v < 5; v++) {
-          const T x = E[v * N + cm] - E[v * N + cm + st];
+          const T x = FAST ? mulhalf(Fd[v * N + cm - st] - Fd[v * N + cm + st]) : E[v * N + cm] - E[v * N + cm + st];
           dwv[v] = dwv[v] - x;
           dwv[v] = dwv[v] + Wm[v] - Wm[5 + v];
         }
@@ -1081,9 +1176,15 @@ __device__ __forceinline__ void body_combine(const DevBlock<T>& b, const PhysPar
       for (int v = 0; v < 5; v++) dwv[v] = mdiv(dwv[v], lam, rl);
     }
   }
-  const T bl = (T)b.blank[c];
+  if (FAST) {
+    if (b.blank[c] == 0)
 #pragma unroll
-  for (int v = 0; v < 5; v++) dwv[v] = dwv[v] * bl;
+      for (int v = 0; v < 5; v++) dwv[v] = T(0);
+  } else {
+    const T bl = (T)b.blank[c];
+#pragma unroll
+    for (int v = 0; v < 5; v++) dwv[v] = dwv[v] * bl;
+  }
   if (A.lres) {
 #pragma unroll
     for (int v = 0; v < 5; v++) b.dw[v * N + c] = dwv[v];
@@ -1091,7 +1192,7 @@ __device__ __forceinline__ void body_combine(const DevBlock<T>& b, const PhysPar
   }
   // time-step scaling, euler.f90:364-372: de = fn*vdtim/cellvolume
   T vd = A.vt ? (T)(*b.dtim) : b.vdtim[c];
-  T de = mdiv((T)A.fn * vd, (T)b.vol, rcp_vol(b));
+  T de = FAST ? ((T)A.fn * vd) * rcp_vol(b) : mdiv((T)A.fn * vd, (T)b.vol, rcp_vol(b));
 #pragma unroll
   for (int v = 0; v < 5; v++) dwv[v] = de * dwv[v];
   if (A.irs) {
@@ -1309,6 +1410,115 @@ __device__ __forceinline__ void body_irs_mixed(const DevBlock<double>& b, const 
         prev = x;
       }
   }
+}
+
+// The mixed form's i sweep with one warp per (line, variable).  A psmoo_old
+// row is an affine map of the row before it, x(q) = a(q) x(q-1) + c(q):
+// forward a = -bb/e1(q), c = dw(q)/e1(q) on unblanked rows and a = 0,
+// c = dw(q) on blanked ones (the row keeps its value, and the next row
+// takes it as its predecessor); backward a = -e2(q), c = x(q) on unblanked
+// rows.  Each lane composes the maps of K consecutive rows, a warp scan of
+// the composed maps gives every lane the value entering its rows, and the
+// lane applies its maps in order.  Loads and stores of a warp cover one
+// contiguous line.  FP32 arithmetic on the FP64 residual; the result goes
+// to the FP32 copy the j and k sweeps continue on (every row of the line,
+// blanked rows with their unsmoothed value).
+template <int K>
+__global__ void __launch_bounds__(256) k_irs_scan_i(DevBlock<double> b, IrsTables tb, float bb, float* cp) {
+  const long long lines = (long long)b.ny * b.nz;
+  const long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (wid >= 5 * lines) return;  // uniform over the warp
+  const int v = (int)(wid / lines);
+  const long long ln = wid - (long long)v * lines;
+  const int j = 2 + (int)(ln % b.ny), k = 2 + (int)(ln / b.ny);
+  const long long c0 = cidx(b.Pi, b.Pj, 0, j, k);
+  const int l = b.il;
+  const double* src = b.dw + (long long)v * b.N + c0;
+  float* dst = cp + (long long)v * b.N + c0;
+  const uint8_t* bl = b.blank + c0;
+  const int q0 = 2 + lane * K;
+  float x[K];
+  unsigned bk = 0;
+  // forward: the lane's maps, composed in row order
+  float ca = 1.f, cc = 0.f;
+#pragma unroll
+  for (int u = 0; u < K; u++) {
+    const int q = q0 + u;
+    if (q <= l) {
+      const float d = (float)src[q];
+      float a = 0.f, c = d;
+      if (bl[q] != 0) {
+        bk |= 1u << u;
+        const float r = irs_e1r(tb, q, 0.0f);
+        a = q == 2 ? 0.f : -bb * r;
+        c = d * r;
+      }
+      x[u] = c;
+      ca = a * ca;
+      cc = fmaf(a, cc, c);
+    } else {
+      x[u] = 0.f;
+    }
+  }
+  // inclusive scan over the lanes in row order, then the value entering
+  // this lane's first row (row 2's map ignores its input: a = 0)
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const float pa = __shfl_up_sync(0xffffffffu, ca, off), pc = __shfl_up_sync(0xffffffffu, cc, off);
+    if (lane >= off) {
+      cc = fmaf(ca, pc, cc);
+      ca = ca * pa;
+    }
+  }
+  float prev = __shfl_up_sync(0xffffffffu, cc, 1);
+  if (lane == 0) prev = 0.f;
+#pragma unroll
+  for (int u = 0; u < K; u++) {
+    const int q = q0 + u;
+    if (q <= l && q > 2 && (bk >> u & 1u)) x[u] = fmaf(-bb * irs_e1r(tb, q, 0.0f), prev, x[u]);
+    if (q <= l) prev = x[u];
+  }
+  // backward: rows l-1 down to 2; row l keeps its forward value
+  ca = 1.f;
+  cc = 0.f;
+#pragma unroll
+  for (int u = K - 1; u >= 0; u--) {
+    const int q = q0 + u;
+    if (q <= l) {
+      const float a = (q < l && (bk >> u & 1u)) ? -irs_e2(tb, q, 0.0f) : 0.f;
+      ca = a * ca;
+      cc = fmaf(a, cc, x[u]);
+    }
+  }
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const float pa = __shfl_down_sync(0xffffffffu, ca, off), pc = __shfl_down_sync(0xffffffffu, cc, off);
+    if (lane + off < 32) {
+      cc = fmaf(ca, pc, cc);
+      ca = ca * pa;
+    }
+  }
+  prev = __shfl_down_sync(0xffffffffu, cc, 1);
+  if (lane == 31) prev = 0.f;
+#pragma unroll
+  for (int u = K - 1; u >= 0; u--) {
+    const int q = q0 + u;
+    if (q <= l) {
+      if (q < l && (bk >> u & 1u)) x[u] = fmaf(-irs_e2(tb, q, 0.0f), prev, x[u]);
+      prev = x[u];
+      dst[q] = x[u];
+    }
+  }
+}
+
+// the rows a lane of k_irs_scan_i takes for a line of len rows (0: none fits)
+inline int irs_scan_k(int len) {
+  const int need = (len + 31) / 32;
+  const int ks[] = {2, 4, 6, 8, 12, 16};
+  for (int q : ks)
+    if (need <= q) return q;
+  return 0;
 }
 
 template <typename TS, typename TO, int D>
@@ -1596,7 +1806,7 @@ __device__ void body_cutcell(const DevBlock<T>& b, const PhysParams& P, unsigned
   wsol[4] = psol / gm1 + T(0.5) * (wsol[1] * wsol[1] + wsol[2] * wsol[2] + wsol[3] * wsol[3]) / wsol[0];
   bool nan = false;
   for (int v = 0; v < 5; v++) nan |= (wsol[v] != wsol[v]);
-  if (nan && !P.eqn_ns) atomicOr(err, ERR_NAN);
+  if (nan && !P.eqn_ns) atomicCAS(err, 0u, (unsigned)ERR_NAN);
   for (int v = 0; v < 5; v++) ws[v] = wsol[v];
   b.rec_psol[m] = psol;
 }
@@ -1920,14 +2130,19 @@ __global__ void k_rtrms_partial(DevBlock<T> b, double cfl, int vt, double* parti
   body_rtrms_partial(b, cfl, vt, partial, npart, blockIdx.x);
 }
 
-__device__ __forceinline__ void body_rtrms_final(const double* partial, int npart, double ncell, double* out) {
+// a NaN norm is the stop of solver.f90:180, recorded in launch order like
+// the kernels' other stops (err may be null)
+__device__ __forceinline__ void body_rtrms_final(const double* partial, int npart, double ncell, double* out,
+                                                 unsigned* err) {
   double a = 0.0;
   for (int q = 0; q < npart; q++) a = a + partial[q];
-  *out = sqrt(a / ncell);
+  const double r = sqrt(a / ncell);
+  *out = r;
+  if (err && r != r) atomicCAS(err, 0u, (unsigned)ERR_NANRES);
 }
 
-__global__ void k_rtrms_final(const double* partial, int npart, double ncell, double* out) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) body_rtrms_final(partial, npart, ncell, out);
+__global__ void k_rtrms_final(const double* partial, int npart, double ncell, double* out, unsigned* err) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) body_rtrms_final(partial, npart, ncell, out, err);
 }
 
 // --------------------------------------------------------------- small whole-array kernels
@@ -2231,10 +2446,10 @@ __global__ void k_forces(DevBlock<T> b, double ox, double oy, double oz, double 
 }
 
 // =============================================================== one-launch-per-phase kernels
-template <typename T, bool SLOPES>
+template <typename T, bool SLOPES, bool FAST = false>
 __global__ void __launch_bounds__(256, SLOPES ? 3 : 6) k_prep(DevBlock<T> b, PhysParams P, int dissip_on) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < (long long)b.ie * b.je * b.ke) body_prep<T, SLOPES>(b, P, dissip_on, t);
+  if (t < (long long)b.ie * b.je * b.ke) body_prep<T, SLOPES, FAST>(b, P, dissip_on, t);
 }
 // the velocities of every cell, ghosts included, into F[0..2] for the MUSCL
 // Roe form (one reciprocal of the density and mdiv: the IEEE quotients)
@@ -2251,6 +2466,12 @@ template <typename T>
 __global__ void __launch_bounds__(256, 4) k_face(DevBlock<T> b, PhysParams P, int dissip_on, T cd) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t < (long long)(b.ie - 1) * (b.je - 1) * (b.ke - 1)) body_face<T, FACE_CENTRAL>(b, P, dissip_on, cd, t);
+}
+// the contracted form's dissipation faces (no convective face fluxes)
+template <typename T>
+__global__ void __launch_bounds__(256, 4) k_face_diss(DevBlock<T> b, PhysParams P, T cd) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < (long long)(b.ie - 1) * (b.je - 1) * (b.ke - 1)) body_face_diss<T>(b, P, cd, t);
 }
 // the Roe faces (MUSCL states, upwind flux, and the viscous flux with NS)
 template <typename T>
@@ -2279,10 +2500,10 @@ __global__ void __launch_bounds__(256) k_face_conv(DevBlock<T> b) {
     for (int v = 0; v < 5; v++) E[v * N + c] = mulhalf(F[v * N + c] + F[v * N + c - sts[d]]);
   }
 }
-template <typename T>
+template <typename T, bool FAST = false>
 __global__ void k_combine(DevBlock<T> b, PhysParams P, StageArgs A, unsigned* err) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < (long long)b.nx * b.ny * b.nz) body_combine<T>(b, P, A, err, t);
+  if (t < (long long)b.nx * b.ny * b.nz) body_combine<T, FAST>(b, P, A, err, t);
 }
 template <typename T, typename TC, int D>
 __global__ void k_irs(DevBlock<T> b, IrsTables tb, TC bb) {
@@ -2361,12 +2582,22 @@ __global__ void __launch_bounds__(256, 1) k_euler_coop(DevBlock<T> b, PhysParams
   const long long nface = (long long)(b.ie - 1) * (b.je - 1) * (b.ke - 1);
   for (int m = 1; m <= E.mstage; m++) {
     const StageArgs& A = E.st[m - 1];
-    for (long long t = gt; t < nprep; t += gs) body_prep(b, P, A.dissip_on, t);
-    g.sync();
-    for (long long t = gt; t < nface; t += gs) body_face(b, P, A.dissip_on, (T)A.cd, t);
+    if (A.fast) {
+      for (long long t = gt; t < nprep; t += gs) body_prep<T, false, true>(b, P, A.dissip_on, t);
+      g.sync();
+      if (A.dissip_on)
+        for (long long t = gt; t < nface; t += gs) body_face_diss(b, P, (T)A.cd, t);
+    } else {
+      for (long long t = gt; t < nprep; t += gs) body_prep(b, P, A.dissip_on, t);
+      g.sync();
+      for (long long t = gt; t < nface; t += gs) body_face(b, P, A.dissip_on, (T)A.cd, t);
+    }
     for (long long t = gt; t < b.nmir; t += gs) rec_wall_terms(b, P, A.dissip_on, (T)A.cd, E.err, (int)t);
     g.sync();
-    for (long long t = gt; t < ncell; t += gs) body_combine<T>(b, P, A, E.err, t);
+    if (A.fast)
+      for (long long t = gt; t < ncell; t += gs) body_combine<T, true>(b, P, A, E.err, t);
+    else
+      for (long long t = gt; t < ncell; t += gs) body_combine<T>(b, P, A, E.err, t);
     g.sync();
     if (E.lres) return;
     if (A.irs && P.irs_kind == 1) {
@@ -2406,7 +2637,7 @@ __global__ void __launch_bounds__(256, 1) k_euler_coop(DevBlock<T> b, PhysParams
     for (int part = blockIdx.x; part < E.npart; part += gridDim.x)
       body_rtrms_partial(b, P.cfl, P.vt, E.rt_partial, E.npart, part);
     g.sync();
-    if (gt == 0) body_rtrms_final(E.rt_partial, E.npart, (double)ncell, E.rt_out);
+    if (gt == 0) body_rtrms_final(E.rt_partial, E.npart, (double)ncell, E.rt_out, E.err);
   }
   if (E.trace && blockIdx.x == 0 && threadIdx.x == 0) E.trace[255] = (unsigned long long)ntr;
 }
@@ -2454,7 +2685,9 @@ void launch_stage_part(int part, const DevBlock<T>& b, const PhysParams& P, cons
                        cudaStream_t s) {
   if (part == 0) {
     long long n1 = (long long)b.ie * b.je * b.ke;
-    if (P.distype == 2) {
+    if (A.fast) {
+      k_prep<T, false, true><<<LAUNCH_N(n1), 0, s>>>(b, P, A.dissip_on);
+    } else if (P.distype == 2) {
       k_prim<T><<<LAUNCH_N(b.N), 0, s>>>(b);
       k_prep<T, true><<<LAUNCH_N(n1), 0, s>>>(b, P, A.dissip_on);
     } else {
@@ -2462,7 +2695,9 @@ void launch_stage_part(int part, const DevBlock<T>& b, const PhysParams& P, cons
     }
   } else if (part == 1) {
     long long n2 = (long long)(b.ie - 1) * (b.je - 1) * (b.ke - 1);
-    if (!A.dissip_on && P.distype == 0)
+    if (A.fast) {
+      if (A.dissip_on) k_face_diss<T><<<LAUNCH_N(n2), 0, s>>>(b, P, (T)A.cd);
+    } else if (!A.dissip_on && P.distype == 0)
       k_face_conv<T><<<LAUNCH_N(n2), 0, s>>>(b);
     else if (P.distype == 0)
       k_face<T><<<LAUNCH_N(n2), 0, s>>>(b, P, A.dissip_on, (T)A.cd);
@@ -2472,7 +2707,10 @@ void launch_stage_part(int part, const DevBlock<T>& b, const PhysParams& P, cons
     if (b.nmir > 0) k_rec_wall<T><<<LAUNCH_N(b.nmir), 0, s>>>(b, P, A.dissip_on, (T)A.cd, err);
   } else if (part == 3) {
     long long n3 = (long long)b.nx * b.ny * b.nz;
-    k_combine<T><<<LAUNCH_N(n3), 0, s>>>(b, P, A, err);
+    if (A.fast)
+      k_combine<T, true><<<LAUNCH_N(n3), 0, s>>>(b, P, A, err);
+    else
+      k_combine<T><<<LAUNCH_N(n3), 0, s>>>(b, P, A, err);
   }
 }
 
@@ -2543,7 +2781,17 @@ void launch_irs_part_t(int part, const DevBlock<T>& b, const PhysParams& P, cons
       // the tuned form of the i sweep: global-memory lines or shared-memory tiles
       constexpr int LT = 64;
       const size_t sm = irs_smem_bytes<float, LT>((b.il - 1) | 1);
-      if (variant && variant[0] == 1 && sm <= 200 * 1024)
+      const int kk = irs_scan_k(b.il - 1);
+      const long long nthr = 32 * 5 * irs_lines_h(b, 0);
+      if (variant && variant[0] == 2 && kk) {
+        const unsigned g = (unsigned)nblk(nthr, 256);
+        if (kk == 2) k_irs_scan_i<2><<<g, 256, 0, s>>>(b, tab[0], bb, cp);
+        if (kk == 4) k_irs_scan_i<4><<<g, 256, 0, s>>>(b, tab[0], bb, cp);
+        if (kk == 6) k_irs_scan_i<6><<<g, 256, 0, s>>>(b, tab[0], bb, cp);
+        if (kk == 8) k_irs_scan_i<8><<<g, 256, 0, s>>>(b, tab[0], bb, cp);
+        if (kk == 12) k_irs_scan_i<12><<<g, 256, 0, s>>>(b, tab[0], bb, cp);
+        if (kk == 16) k_irs_scan_i<16><<<g, 256, 0, s>>>(b, tab[0], bb, cp);
+      } else if (variant && variant[0] == 1 && sm <= 200 * 1024)
         k_irs_smem_fill<LT><<<(unsigned)(5 * ((irs_lines_h(b, 0) + LT - 1) / LT)), LT, sm, s>>>(b, tab[0], bb, cp);
       else
         k_irs_mixed<double, float, 0><<<LAUNCH_N(5 * irs_lines_h(b, 0)), 0, s>>>(b, tab[0], bb, b.dw, cp, cp);
@@ -2625,9 +2873,9 @@ void launch_bcond(const DevBlock<T>& b, const PhysParams& P, cudaStream_t s) {
 
 template <typename T>
 void launch_rtrms(const DevBlock<T>& b, const PhysParams& P, int vt, double* partial, int npartial, double* out,
-                  cudaStream_t s) {
+                  cudaStream_t s, unsigned* err) {
   k_rtrms_partial<T><<<npartial, RT_THREADS, 0, s>>>(b, P.cfl, vt, partial, npartial);
-  k_rtrms_final<<<1, 32, 0, s>>>(partial, npartial, (double)b.nx * b.ny * b.nz, out);
+  k_rtrms_final<<<1, 32, 0, s>>>(partial, npartial, (double)b.nx * b.ny * b.nz, out, err);
 }
 
 template <typename TS, typename TD>
@@ -2791,7 +3039,8 @@ void launch_forces(const DevBlock<T>& b, const double* origin, const double* h, 
                               const int*, const StageArgs*);                                                    \
   template void launch_cutcell<T>(const DevBlock<T>&, const PhysParams&, unsigned*, cudaStream_t);              \
   template void launch_bcond<T>(const DevBlock<T>&, const PhysParams&, cudaStream_t);                           \
-  template void launch_rtrms<T>(const DevBlock<T>&, const PhysParams&, int, double*, int, double*, cudaStream_t); \
+  template void launch_rtrms<T>(const DevBlock<T>&, const PhysParams&, int, double*, int, double*, cudaStream_t, \
+                                unsigned*);                                                                    \
   template void launch_depvars_all<T>(const DevBlock<T>&, const PhysParams&, cudaStream_t);                     \
   template void launch_copy_ws<T>(const DevBlock<T>&, cudaStream_t);                                            \
   template void launch_save_wn<T>(const DevBlock<T>&, cudaStream_t);                                            \

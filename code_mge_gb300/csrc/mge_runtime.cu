@@ -49,6 +49,7 @@ struct Block {
   // device allocations; state fields hold doubles, or floats when f32
   bool f32 = false;    // FP32 storage and arithmetic (coarse levels of the mixed mode)
   bool aux32 = false;  // FP32 time step and smoothing on FP64 storage (finest level of the mixed mode)
+  bool fast = false;   // the contracted FP64 residual (finest level of the mixed and refined forms)
   bool use_coop = false;   // run timestep + euler as one cooperative launch
   int irs_var[3] = {0, 0, 0};  // line-sweep variant per direction (autotuned)
   size_t esz = 8;
@@ -170,6 +171,7 @@ int check_err(mge_ctx* c) {
     if (w & ERR_NEGPRESS) return fail(c, MGE_ENEGPRESS, "timestep: negative or NaN c^2 (timestep.f90:45-48)");
     if (w & ERR_ZERORHO) return fail(c, MGE_EZERORHO, "efluxb: zero density at a cut cell (efluxb.f90:61-64)");
     if (w & ERR_NAN) return fail(c, MGE_ENAN, "bc_cutcell: wsol is NaN (bc_cutcell.f90:147-156)");
+    if (w & ERR_NANRES) return fail(c, MGE_ENAN, "NaN residual (solver.f90:180)");
   }
   return MGE_OK;
 }
@@ -216,7 +218,10 @@ void enqueue_euler(mge_ctx* c, Block& b, int mgl, int mlvl, bool lres, bool lfir
     L.lfir = lfir;
     L.lres = lres;
     L.rt = want_rt;
-    for (int m = 1; m <= mstage; m++) L.st[m - 1] = stage_args(P, m, mgl, mlvl, lres, lfir, itime);
+    for (int m = 1; m <= mstage; m++) {
+      L.st[m - 1] = stage_args(P, m, mgl, mlvl, lres, lfir, itime);
+      L.st[m - 1].fast = b.fast;
+    }
     for (int d = 0; d < 3; d++) L.tab[d] = b.tabs[d];
     L.rt_partial = b.rt_partial;
     L.npart = b.npart;
@@ -257,6 +262,7 @@ void enqueue_euler(mge_ctx* c, Block& b, int mgl, int mlvl, bool lres, bool lfir
     }
     for (int m = 1; m <= mstage; m++) {
       StageArgs A = stage_args(P, m, mgl, mlvl, lres, lfir, itime);
+      A.fast = b.fast;
       launch_stage<T>(D, c->P, A, c->d_err, c->stream, c->side, c->ev_fork, c->ev_join);
       if (lres) return;
       if (A.irs) launch_irs<T>(D, c->P, b.tabs, c->stream, b.aux32, b.irs_var, &A);
@@ -272,7 +278,7 @@ void enqueue_euler(mge_ctx* c, Block& b, int mgl, int mlvl, bool lres, bool lfir
         launch_bcond<T>(D, c->P, c->stream);
       }
     }
-    if (want_rt) launch_rtrms<T>(D, c->P, P.vt, b.rt_partial, b.npart, b.rt_cur, c->stream);
+    if (want_rt) launch_rtrms<T>(D, c->P, P.vt, b.rt_partial, b.npart, b.rt_cur, c->stream, c->d_err);
   });
 }
 
@@ -832,6 +838,17 @@ int mge_add_block(mge_ctx* c, const mge_block_desc* d, int level, int serial) {
   return MGE_OK;
 }
 
+// The contracted FP64 residual applies to the finest level of the mixed and
+// refined forms, for the steady JST central scheme (scalar dissipation) of
+// the Euler equations; MGE_FAST_RESIDUAL=0 turns it off.
+static bool fast_residual(const mge_ctx* c, bool finest, int precision) {
+  const char* e = getenv("MGE_FAST_RESIDUAL");
+  if (e && e[0] == '0') return false;
+  const mge_params& P = c->prm;
+  return finest && precision != MGE_PREC_FP64 && P.distype == MGE_DIS_CENTRAL && P.eqntype == MGE_EQN_EULER &&
+         P.dissip == MGE_DISSIP_SCALAR && P.execmode == 0;
+}
+
 int mge_commit(mge_ctx* c) {
   if (!c) return MGE_EBADCFG;
   if (c->committed) return MGE_OK;
@@ -855,6 +872,7 @@ int mge_commit(mge_ctx* c) {
       // with its time step and residual smoothing in FP32 arithmetic
       b.f32 = mixed && (l + 1 < c->lv.size());
       b.aux32 = mixed && !b.f32;
+      b.fast = fast_residual(c, l + 1 == c->lv.size(), c->prm.precision);
       b.esz = b.f32 ? 4 : 8;
       b.use_coop = (long long)b.nx * b.ny * b.nz <= c->coop_max_cells;
       if ((rc = commit_block(c, b, c->scratch))) return rc;
@@ -923,7 +941,9 @@ static int autotune_block(mge_ctx* c, Block& b, bool tune_path) {
     for (int d = 0; d < 3; d++) {
       float best = 1e30f;
       int bv = 0;
-      for (int v = 0; v < 2; v++) {
+      // variant 2, the warp-scan i sweep, exists for the mixed form's finest level
+      const int nvar = (d == 0 && b.aux32 && !b.f32) ? 3 : 2;
+      for (int v = 0; v < nvar; v++) {
         int var[3] = {0, 0, 0};
         var[d] = v;
         float t = time_it([&] {
@@ -971,7 +991,8 @@ int mge_init_flow(mge_ctx* c) {  // init_flow.f90:46-96
   int rc = check_err(c);
   if (rc) return rc;
   // a fixed plan "level:CIJK,..." (C = 1 cooperative euler, I/J/K = line-sweep
-  // form per direction) replaces tuning for the levels it names, so that a
+  // form per direction: 0 global lines, 1 shared-memory tiles, 2 the mixed
+  // form's warp-scan i sweep) replaces tuning for the levels it names, so that a
   // run can repeat the launch forms another run chose
   std::vector<bool> fixed(c->lv.size(), false);
   for (size_t pos = 0; pos < c->plan.size();) {
@@ -985,7 +1006,10 @@ int mge_init_flow(mge_ctx* c) {  // init_flow.f90:46-96
     if (lvl < 1 || lvl > (int)c->lv.size()) return fail(c, MGE_EBADCFG, "MGE_TUNE_PLAN: bad level " + item);
     for (Block& b : c->lv[lvl - 1]) {
       b.use_coop = item[colon + 1] == '1';
-      for (int d = 0; d < 3; d++) b.irs_var[d] = item[colon + 2 + d] == '1' ? 1 : 0;
+      for (int d = 0; d < 3; d++) {
+        const char f = item[colon + 2 + d];
+        b.irs_var[d] = (f == '1' || f == '2') ? f - '0' : 0;
+      }
     }
     fixed[lvl - 1] = true;
   }
@@ -1012,14 +1036,18 @@ static void dfree(mge_ctx* c, void* p, size_t bytes) {
 // blocks change their storage (state converted, scratch fields re-zeroed),
 // the finest block toggles its FP32 time step and smoothing.
 int mge_set_precision(mge_ctx* c, int precision) {
-  if (!c || !c->committed || (precision != MGE_PREC_FP64 && precision != MGE_PREC_MIXED)) return MGE_EBADCFG;
+  if (!c || !c->committed ||
+      (precision != MGE_PREC_FP64 && precision != MGE_PREC_MIXED && precision != MGE_PREC_REFINED))
+    return MGE_EBADCFG;
   CK(cudaSetDevice(c->device));
   CK(cudaStreamSynchronize(c->stream));
   const bool mixed = precision == MGE_PREC_MIXED;
   for (size_t l = 0; l < c->lv.size(); l++)
     for (Block& b : c->lv[l]) {
-      const bool f32 = mixed && (l + 1 < c->lv.size());
-      b.aux32 = mixed && !f32;
+      const bool finest = l + 1 == c->lv.size();
+      const bool f32 = mixed && !finest;
+      b.aux32 = precision != MGE_PREC_FP64 && finest;
+      b.fast = fast_residual(c, finest, precision);
       if (f32 == b.f32) continue;
       const size_t oes = b.esz, nes = f32 ? 4 : 8;
       const long long N = b.N;
@@ -1078,7 +1106,11 @@ int mge_upload_state(mge_ctx* c, int level, int serial, const double* w) {
   } else {
     CK(cudaMemcpyAsync(b->w, w, 5 * b->N * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   }
+  // what init_flow.f90:46-66 does after read_solut: depvars, bc_cutcell (the
+  // records' solid state from the new cells), bcond
   enqueue_simple(c, *b, 0);
+  enqueue_simple(c, *b, 4);
+  enqueue_simple(c, *b, 2);
   return check_err(c);
 }
 
@@ -1443,6 +1475,7 @@ int mge_cycle_poll(mge_ctx* c, int ncyc, double* max_res) {
     if (w & ERR_NEGPRESS) return fail(c, MGE_ENEGPRESS, "timestep: negative or NaN c^2 (timestep.f90:45-48)");
     if (w & ERR_ZERORHO) return fail(c, MGE_EZERORHO, "efluxb: zero density at a cut cell (efluxb.f90:61-64)");
     if (w & ERR_NAN) return fail(c, MGE_ENAN, "bc_cutcell: wsol is NaN (bc_cutcell.f90:147-156)");
+    if (w & ERR_NANRES) return fail(c, MGE_ENAN, "NaN residual (solver.f90:180)");
   }
   auto& fin = c->lv[mlvl - 1];
   double mr = 1000.0;
@@ -1562,6 +1595,7 @@ int mge_kernel_times(mge_ctx* c, int level, int reps, double* ms_out, int nout) 
       A.lres = 0;
       A.irs = (m % 2 != 0) && P.smoo > 0.0;
       A.vt = P.vt;
+      A.fast = b.fast;
       for (int part = 0; part < 4 && !rc; part++) {
         const double before = tot[1 + part];
         rc = timed(1 + part, [&] {
@@ -1622,7 +1656,7 @@ int mge_solve(mge_ctx* c, const mge_solve_opts* o, double* hist, int hist_len, i
         // mixed form: FP32 coarse corrections stall near an eps32-sized residual
         // drop; refine to FP64 once the drop reaches refine_drop
         if (c->prm.precision == MGE_PREC_MIXED && o && o->refine_drop > 0.0 && max_res <= o->refine_drop * ini_res)
-          if ((rc = mge_set_precision(c, MGE_PREC_FP64))) return rc;
+          if ((rc = mge_set_precision(c, MGE_PREC_REFINED))) return rc;
       }
       if (mlvl > 1) {  // convergence (solver.f90:237-239); the single-grid level runs all its cycles
         double drop = P.conv_drop > 0.0 ? P.conv_drop : 1.0e6;

@@ -131,7 +131,7 @@ class GpuBackend:
         return self.lib.mge_prolong_async(h.ctx, mlvl)
 
     def refine(self, h):
-        return self.lib.mge_set_precision(h.ctx, A.MGE_PREC_FP64)
+        return self.lib.mge_set_precision(h.ctx, A.MGE_PREC_REFINED)
 
     def finish(self, h):
         f = h.forces()

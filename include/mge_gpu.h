@@ -54,6 +54,8 @@ extern "C" {
 
 #define MGE_PREC_FP64    0  /* plain: every level and kernel in FP64 */
 #define MGE_PREC_MIXED   1  /* FP32 coarse levels, IRS and time step; FP64 finest R(w), update, norms, forces */
+#define MGE_PREC_REFINED 2  /* what a mixed solve refines to: FP64 on every level; the finest level keeps
+                               the mixed form's FP32 time step and IRS and its FP64 residual form */
 
 #define MGE_MAX_STAGE   8
 #define MGE_MAX_LEVEL  16
@@ -169,7 +171,10 @@ int mge_commit(mge_ctx* ctx);
 /* Free-stream start, then depvars + bc_cutcell + bcond (init_flow.f90:46-96). */
 int mge_init_flow(mge_ctx* ctx);
 
-/* Host <-> device state in the Fortran layout above. p may be NULL. */
+/* Host <-> device state in the Fortran layout above. p may be NULL.
+ * mge_upload_state then does what init_flow.f90:46-66 does after read_solut:
+ * depvars, bc_cutcell (the records' solid state from the new cells; a NaN
+ * there returns MGE_ENAN as bc_cutcell.f90:147-156 stops) and bcond. */
 int mge_upload_state(mge_ctx* ctx, int level, int serial, const double* w);
 int mge_download_state(mge_ctx* ctx, int level, int serial, double* w, double* p);
 /* Download any per-cell field by name: "w","p","dw","fw","wn","ws","wr","qf",
@@ -207,11 +212,21 @@ int mge_cycle_async(mge_ctx* ctx, int mlvl);
 int mge_cycle_poll(mge_ctx* ctx, int ncyc, double* max_res);
 int mge_prolong_async(mge_ctx* ctx, int mlvl);
 
-/* Switch a committed context between MGE_PREC_FP64 and MGE_PREC_MIXED in
- * place (the coarse levels' state is converted; graphs are re-captured).  The
- * mixed form's FP32 coarse corrections carry rounding of the size of the
- * coarse truncation error, so its residual stalls near a 1e-7 drop; switching
- * to FP64 there finishes the solve at FP64 accuracy. */
+/* Switch a committed context between MGE_PREC_FP64, MGE_PREC_MIXED and
+ * MGE_PREC_REFINED in place (the coarse levels' state is converted; graphs
+ * are re-captured).  The mixed form's FP32 coarse corrections carry rounding
+ * of the size of the coarse truncation error, so its residual stalls near a
+ * 1e-7 drop; switching to MGE_PREC_REFINED there (FP64 coarse levels) ends
+ * the stall and finishes the solve at FP64 accuracy.
+ *
+ * On the finest level, the mixed and refined forms evaluate the JST central
+ * residual of the Euler equations in a contracted FP64 form: fused
+ * multiply-adds, the cell flux as velocity times state, and the convective
+ * part as the central difference 0.5*(F(q-1) - F(q+1)) of the cell fluxes
+ * instead of the difference of two averaged face fluxes.  It is the same
+ * FP64 quantity up to a few roundings, not the reference's bit pattern
+ * (MGE_PREC_FP64 keeps that).  MGE_FAST_RESIDUAL=0 in the environment turns
+ * it off. */
 int mge_set_precision(mge_ctx* ctx, int precision);
 
 /* Launch forms the autotuner chose for a block at mge_init_flow: *coop = 1

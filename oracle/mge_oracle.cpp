@@ -1967,8 +1967,11 @@ int mgeo_upload_state(mgeo_ctx* c, int level, int serial, const double* w) {
   OBlock* b = getb(c, level, serial);
   if (!b) return MGE_ENOTFOUND;
   std::memcpy(b->w.data(), w, 5 * b->N * sizeof(double));
+  // init_flow.f90:46-66 after read_solut: depvars, bc_cutcell, bcond
   depvars_all(c->prm, *b);
-  return MGE_OK;
+  int rc = bc_cutcell(c, *b);
+  if (rc) return rc;
+  return bcond(c, *b);
 }
 
 int mgeo_download_field(mgeo_ctx* c, int level, int serial, const char* name, double* out, size_t count) {
