@@ -463,6 +463,29 @@ def embedded_hierarchy(body, center, h_fine, n, nlevel, coarsen=(True, True, Fal
     return levels
 
 
+def cylinder_split(n=32, span=2, mach=0.3, overlap=4, mcyc_fine=4, **kw):
+    """Flow past a D=1 cylinder on two levels: an n x n x span slab over
+    [-4,4]^2 (h = 8/n), and embedded in it two fine blocks side by side in x
+    (h/2), x in [-2, overlap*h/2] and [0, 2], y in [-2, 2], that share
+    `overlap` fine cells around x = 0 and exchange ghost cells there
+    (bc_overlap).  The body is cut in both fine blocks."""
+    body = Body("cylinder", radius=0.5)
+    hc = 8.0 / n
+    hf = 0.5 * hc
+    lo = (-4.0, -4.0, -0.5 * span * hc)
+    coarse = BlockSpec(n=(n, n, span), h=(hc, hc, hc), origin=lo, bctype=(-20, -20, -60, -20, -20, -60))
+    row = []
+    for x0, x1 in ((-2.0, overlap * hf), (0.0, 2.0)):
+        nxf = int(round((x1 - x0) / hf))
+        off = (int(round((x0 - lo[0]) / hc)), int(round((-2.0 - lo[1]) / hc)), 0)
+        spec = BlockSpec(n=(nxf, int(round(4.0 / hf)), span), h=(hf, hf, hc), origin=(x0, -2.0, lo[2]),
+                         bctype=(0, 0, -60, 0, 0, -60), parent=1, ratio=(2, 2, 1), offset=off)
+        row.append(make_block_arrays(spec, body))
+    levels = [[make_block_arrays(coarse, body)], row]
+    prm = params(mach, nlevel=2, mcyc=[1, mcyc_fine], mgtype=1, **kw)
+    return Case("cylinder_split_%d" % n, prm, levels, body, ref_area=1.0 * span * hc)
+
+
 def rotating(omega, center=(0.0, 0.0, 0.0)):
     """Wall velocity of a body turning at omega about the z axis through
     center: (-omega*(y-cy), omega*(x-cx), 0)."""

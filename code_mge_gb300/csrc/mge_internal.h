@@ -186,6 +186,9 @@ void launch_embed(const DevBlock<TF>& f, const DevBlock<TC>& c, const int ratio[
                   const PhysParams& P, cudaStream_t s);
 template <typename T> void launch_forces(const DevBlock<T>& b, const double* origin, const double* h,
                                          const double* center, double mu, double* out7, cudaStream_t s);
+template <typename T>
+void launch_overlap(const DevBlock<T>& g, const DevBlock<T>& p, const long long* dst, const long long* src,
+                    const double* fac, long long n, const PhysParams& P, cudaStream_t s);
 int rtrms_partials(long long ncells);
 void init_kernel_attributes();
 void launch_convert(const void* src, bool src32, void* dst, bool dst32, long long n, cudaStream_t s);

@@ -2329,6 +2329,32 @@ __global__ void k_addw(DevBlock<TF> f, DevBlock<TC> c, Xfer X, int fmg, const do
   }
 }
 
+// bc_overlap.f90:32-90: ghost cell dst[t] of block g takes the trilinear
+// interpolation of partner p's state from the 2x2x2 cells at src[t] (its
+// physical cells: no cell is both read and written), then depvars
+template <typename T>
+__global__ void k_overlap(DevBlock<T> g, DevBlock<T> p, const long long* __restrict__ dst,
+                          const long long* __restrict__ src, const double* __restrict__ fac, long long n,
+                          double gamma) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const long long q = dst[t], s = src[t];
+  const long long sj = p.Pi, sk = (long long)p.Pi * p.Pj;
+  const double* f = fac + 8 * t;
+  T wv[5];
+#pragma unroll
+  for (int v = 0; v < 5; v++) {
+    double acc = 0.0;
+    int nn = 0;
+    for (int dk = 0; dk < 2; dk++)
+      for (int dj = 0; dj < 2; dj++)
+        for (int di = 0; di < 2; di++) acc = acc + (double)p.w[v * p.N + s + di + dj * sj + dk * sk] * f[nn++];
+    wv[v] = (T)acc;
+    g.w[v * g.N + q] = wv[v];
+  }
+  g.p[q] = depvars((T)gamma, wv);
+}
+
 // bc_embed.f90:47-143: fine ghost cells whose centre lies in the parent
 template <typename TF, typename TC>
 __global__ void k_embed(DevBlock<TF> f, DevBlock<TC> c, Xfer X, double gamma) {
@@ -3017,6 +3043,12 @@ void launch_embed(const DevBlock<TF>& f, const DevBlock<TC>& c, const int ratio[
 }
 
 template <typename T>
+void launch_overlap(const DevBlock<T>& g, const DevBlock<T>& p, const long long* dst, const long long* src,
+                    const double* fac, long long n, const PhysParams& P, cudaStream_t s) {
+  if (n > 0) k_overlap<T><<<LAUNCH_N(n), 0, s>>>(g, p, dst, src, fac, n, P.gamma);
+}
+
+template <typename T>
 void launch_forces(const DevBlock<T>& b, const double* origin, const double* h, const double* center, double mu,
                    double* out7, cudaStream_t s) {
   k_forces<T><<<1, 256, 0, s>>>(b, origin[0], origin[1], origin[2], h[0], h[1], h[2], center[0], center[1], center[2],
@@ -3047,7 +3079,9 @@ void launch_forces(const DevBlock<T>& b, const double* origin, const double* h, 
   template void launch_copy_wn<T>(const DevBlock<T>&, cudaStream_t);                                            \
   template void launch_init_free<T>(const DevBlock<T>&, const PhysParams&, cudaStream_t);                       \
   template void launch_forces<T>(const DevBlock<T>&, const double*, const double*, const double*, double, double*,  \
-                                 cudaStream_t);
+                                 cudaStream_t);                                                                  \
+  template void launch_overlap<T>(const DevBlock<T>&, const DevBlock<T>&, const long long*, const long long*,        \
+                                  const double*, long long, const PhysParams&, cudaStream_t);
 MGE_INST(double)
 MGE_INST(float)
 #undef MGE_INST

@@ -46,6 +46,16 @@ struct Block {
   int parent = -1, ratio[3] = {1, 1, 1}, offset[3] = {0, 0, 0};
   std::vector<int32_t> blank_h;
   std::vector<HRec> recs;
+  // same-level overlap (bc_overlap.f90:32-90): per partner block of the
+  // level, the ghost cells of this block inside the partner's physical
+  // cells, the partner's stencil base cell and the 8 trilinear weights
+  struct Overlap {
+    int partner = 0;  // serial
+    long long n = 0;
+    long long *dst = nullptr, *src = nullptr;
+    double* fac = nullptr;
+  };
+  std::vector<Overlap> ovl;
   // device allocations; state fields hold doubles, or floats when f32
   bool f32 = false;    // FP32 storage and arithmetic (coarse levels of the mixed mode)
   bool aux32 = false;  // FP32 time step and smoothing on FP64 storage (finest level of the mixed mode)
@@ -319,6 +329,25 @@ void enqueue_simple(mge_ctx* c, Block& b, int what) {
   });
 }
 
+// bc_overlap.f90:32-90 on level mgl: every block's ghost cells inside a
+// partner's physical cells, partners in serial order (a later partner's
+// value stands where two overlap)
+void enqueue_overlap(mge_ctx* c, int mgl) {
+  auto& L = c->lv[mgl - 1];
+  for (Block& g : L)
+    for (const Block::Overlap& o : g.ovl) {
+      Block& p = L[o.partner - 1];
+      with_dev(g, [&](auto& DG) {
+        using T = typename std::remove_reference_t<decltype(DG)>::value_type;
+        with_dev(p, [&](auto& DP) {
+          using TP = typename std::remove_reference_t<decltype(DP)>::value_type;
+          if constexpr (std::is_same<T, TP>::value)
+            launch_overlap<T>(DG, DP, o.dst, o.src, o.fac, o.n, c->P, c->stream);
+        });
+      });
+    }
+}
+
 void enqueue_movco(mge_ctx* c, int mgl) {  // movco.f90:21-47
   for (Block& b : c->lv[mgl - 1]) {
     cudaMemsetAsync(b.marker, 0, (size_t)b.N, c->stream);
@@ -328,6 +357,7 @@ void enqueue_movco(mge_ctx* c, int mgl) {  // movco.f90:21-47
     enqueue_simple(c, b, 0);
     enqueue_simple(c, b, 1);
   }
+  enqueue_overlap(c, mgl);
   for (Block& b : c->lv[mgl - 1]) enqueue_simple(c, b, 2);
 }
 
@@ -344,6 +374,7 @@ void enqueue_movfin(mge_ctx* c, int mgl, int mlvl) {  // movfin.f90:20-39
     Block& pb = c->lv[mgl - 2][f.parent - 1];
     enqueue_addw_embed(c, f, pb, fmg, true);
   }
+  enqueue_overlap(c, mgl);
   for (Block& f : c->lv[mgl - 1]) enqueue_simple(c, f, 2);
 }
 
@@ -356,16 +387,25 @@ void enqueue_cycle(mge_ctx* c, int mlvl) {
     for (;;) {  // lopr
       icyc[mgl] += 1;
       bool lfir = (mgl != mlvl);
-      for (Block& b : c->lv[mgl - 1]) enqueue_euler(c, b, mgl, mlvl, false, lfir, 0, mgl == mlvl, true);
+      for (Block& b : c->lv[mgl - 1]) {  // solver.f90:151-158
+        enqueue_euler(c, b, mgl, mlvl, false, lfir, 0, mgl == mlvl, true);
+        enqueue_overlap(c, mgl);
+      }
       if (mlvl == 1) return;
-      for (Block& b : c->lv[mgl - 1]) enqueue_euler(c, b, mgl, mlvl, true, false, 0, false);
+      for (Block& b : c->lv[mgl - 1]) {  // solver.f90:197-201
+        enqueue_euler(c, b, mgl, mlvl, true, false, 0, false);
+        enqueue_overlap(c, mgl);
+      }
       mgl = mgl - 1;
       enqueue_movco(c, mgl);
       if (mgl == 1) break;
     }
     bool lfir = true;
     for (;;) {  // lopp
-      for (Block& b : c->lv[mgl - 1]) enqueue_euler(c, b, mgl, mlvl, false, lfir, 0, false, true);
+      for (Block& b : c->lv[mgl - 1]) {  // solver.f90:215-222
+        enqueue_euler(c, b, mgl, mlvl, false, lfir, 0, false, true);
+        enqueue_overlap(c, mgl);
+      }
       lfir = false;
       mgl = mgl + 1;
       enqueue_movfin(c, mgl, mlvl);
@@ -838,6 +878,71 @@ int mge_add_block(mge_ctx* c, const mge_block_desc* d, int level, int serial) {
   return MGE_OK;
 }
 
+// Stencil of ghost cell (i,j,k) of block g on block p of the same level, the
+// construction of the prolongation (cell centre, containing cell, base of the
+// 2x2x2 stencil clamped to p's physical cells); false outside p's physical cells
+static bool overlap_stencil(const Block& g, const Block& p, int i, int j, int k, int* sh, double* fac) {
+  const int ic[3] = {i, j, k}, lc[3] = {p.il, p.jl, p.kl}, nc[3] = {p.nx, p.ny, p.nz};
+  double xi[3];
+  for (int d = 0; d < 3; d++) {
+    const double x = g.origin[d] + ((double)ic[d] - 1.5) * g.h[d];
+    const double u = (x - p.origin[d]) / p.h[d];
+    if (u < 0.0 || u >= (double)nc[d]) return false;
+    int s = (int)std::floor(u + 1.5);
+    if (s < 2) s = 2;
+    if (s > lc[d] - 1) s = lc[d] - 1;
+    sh[d] = s;
+    xi[d] = u + 1.5 - (double)s;
+  }
+  const double x = xi[0], y = xi[1], z = xi[2];
+  fac[0] = (1.0 - x) * (1.0 - y) * (1.0 - z);
+  fac[1] = x * (1.0 - y) * (1.0 - z);
+  fac[2] = (1.0 - x) * y * (1.0 - z);
+  fac[3] = x * y * (1.0 - z);
+  fac[4] = (1.0 - x) * (1.0 - y) * z;
+  fac[5] = x * (1.0 - y) * z;
+  fac[6] = (1.0 - x) * y * z;
+  fac[7] = x * y * z;
+  return true;
+}
+
+// the overlap lists of every block (levels with one block have none)
+static int build_overlaps(mge_ctx* c) {
+  for (auto& L : c->lv) {
+    if (L.size() < 2) continue;
+    for (Block& g : L)
+      for (Block& p : L) {
+        if (&g == &p) continue;
+        std::vector<long long> dst, src;
+        std::vector<double> fac;
+        for (int i = 0; i <= g.ib; i++)
+          for (int j = 0; j <= g.jb; j++)
+            for (int k = 0; k <= g.kb; k++) {
+              if (i >= 2 && i <= g.il && j >= 2 && j <= g.jl && k >= 2 && k <= g.kl) continue;
+              int sh[3];
+              double f[8];
+              if (!overlap_stencil(g, p, i, j, k, sh, f)) continue;
+              dst.push_back((long long)i + (long long)g.Pi * (j + (long long)g.Pj * k));
+              src.push_back((long long)sh[0] + (long long)p.Pi * (sh[1] + (long long)p.Pj * sh[2]));
+              fac.insert(fac.end(), f, f + 8);
+            }
+        if (dst.empty()) continue;
+        Block::Overlap o;
+        o.partner = p.serial;
+        o.n = (long long)dst.size();
+        int rc;
+        if ((rc = dalloc(c, &o.dst, dst.size())) || (rc = dalloc(c, &o.src, src.size())) ||
+            (rc = dalloc(c, &o.fac, fac.size())))
+          return rc;
+        CK(cudaMemcpy(o.dst, dst.data(), dst.size() * sizeof(long long), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(o.src, src.data(), src.size() * sizeof(long long), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(o.fac, fac.data(), fac.size() * sizeof(double), cudaMemcpyHostToDevice));
+        g.ovl.push_back(o);
+      }
+  }
+  return MGE_OK;
+}
+
 // The contracted FP64 residual applies to the finest level of the mixed and
 // refined forms, for the steady JST central scheme (scalar dissipation) of
 // the Euler equations; MGE_FAST_RESIDUAL=0 turns it off.
@@ -877,6 +982,7 @@ int mge_commit(mge_ctx* c) {
       b.use_coop = (long long)b.nx * b.ny * b.nz <= c->coop_max_cells;
       if ((rc = commit_block(c, b, c->scratch))) return rc;
     }
+  if ((rc = build_overlaps(c))) return rc;
   // the set-up copies ran on the legacy stream; order them before the context stream
   CK(cudaDeviceSynchronize());
   c->committed = true;
@@ -1232,9 +1338,11 @@ int mge_movfin(mge_ctx* c, int mgl, int mlvl) {
 }
 
 int mge_bc_overlap(mge_ctx* c, int mgl) {
-  // one block per level in the hierarchies this library builds: nothing overlaps
-  if (!c || mgl < 1 || mgl > (int)c->lv.size()) return MGE_ENOTFOUND;
-  return MGE_OK;
+  if (!c || !c->committed || mgl < 1 || mgl > (int)c->lv.size()) return MGE_ENOTFOUND;
+  CK(cudaSetDevice(c->device));
+  enqueue_overlap(c, mgl);
+  CK(cudaGetLastError());
+  return check_err(c);
 }
 
 int mge_get_rtrms(mge_ctx* c, int level, int serial, int ncyc, double* out) {
@@ -1559,7 +1667,9 @@ int mge_kernel_times(mge_ctx* c, int level, int reps, double* ms_out, int nout) 
   Block& b = *bp;
   const mge_params& P = c->prm;
   const int NK = 11;
-  double tot[NK] = {0}, face_stage[MGE_MAX_STAGE] = {0};
+  // per stage: prep, face and combine pass times (the stages differ in the
+  // work the passes do)
+  double tot[NK] = {0}, stage_ms[3][MGE_MAX_STAGE] = {};
   int cnt[NK] = {0};
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
@@ -1604,7 +1714,7 @@ int mge_kernel_times(mge_ctx* c, int level, int reps, double* ms_out, int nout) 
             launch_stage_part<T>(part, D, c->P, A, c->d_err, c->stream);
           });
         });
-        if (part == 1) face_stage[m - 1] += tot[2] - before;
+        if (part != 2) stage_ms[part == 3 ? 2 : part][m - 1] += tot[1 + part] - before;
       }
       if (A.irs)
         for (int part = 0; part < 3 && !rc; part++)
@@ -1629,7 +1739,11 @@ int mge_kernel_times(mge_ctx* c, int level, int reps, double* ms_out, int nout) 
   cudaEventDestroy(e1);
   if (rc) return rc;
   for (int q = 0; q < NK && q < nout; q++) ms_out[q] = cnt[q] ? tot[q] / cnt[q] : 0.0;
-  for (int m = 0; m < P.mstage && NK + m < nout; m++) ms_out[NK + m] = face_stage[m] / reps;
+  // [NK, NK+mstage): face pass per stage; then prep per stage; then combine per stage
+  const int order[3] = {1, 0, 2};
+  for (int q = 0; q < 3; q++)
+    for (int m = 0; m < P.mstage && NK + q * P.mstage + m < nout; m++)
+      ms_out[NK + q * P.mstage + m] = stage_ms[order[q]][m] / reps;
   return check_err(c);
 }
 

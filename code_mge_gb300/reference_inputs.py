@@ -148,19 +148,17 @@ def _list(v):
 # ------------------------------------------------------------------ the case
 def case_from_reference(pin_path, p3d_path, jobsheet_path, span_axis=1, nlevel=None, mcyc=None, cloud="trilinear",
                         **overrides):
-    """A Case from the reference's inputs: the grids of the grid file (one
-    per level; grids sharing a level would need the same-level overlap
-    exchange, which is not built), the extruded body of the plot3d surface,
-    and the job sheet's flow, numerics and domain boundary types.  ``cloud``
-    picks the records' interpolation clouds ("trilinear" or "rbf").  Keyword
-    overrides go to ``cases.params``."""
+    """A Case from the reference's inputs: the grids of the grid file (the
+    grids of one level, in name order, are that level's blocks; each takes
+    as parent the block of the level above that holds it, and blocks of a
+    level exchange ghost cells where they overlap, bc_overlap), the extruded
+    body of the plot3d surface, and the job sheet's flow, numerics and domain
+    boundary types.  ``cloud`` picks the records' interpolation clouds
+    ("trilinear" or "rbf").  Keyword overrides go to ``cases.params``."""
     js = read_jobsheet(jobsheet_path)
     flow, num, ctl = js.get("FLOW", {}), js.get("NUMERICS", {}), js.get("CONTROL", {})
     grids = sorted(read_pin(pin_path), key=lambda g: g["name"])
     levels = sorted({g["level"] for g in grids})
-    for L in levels:
-        if sum(1 for g in grids if g["level"] == L) > 1:
-            raise ValueError("level %d has several grids: the same-level overlap exchange is not built" % L)
     if nlevel is not None:
         levels = levels[:nlevel]
     poly = section_polygon(read_plot3d(p3d_path), span_axis)
@@ -168,20 +166,23 @@ def case_from_reference(pin_path, p3d_path, jobsheet_path, span_axis=1, nlevel=N
     bct = domain_bctypes(jobsheet_path)
     specs = []
     for li, L in enumerate(levels):
-        g = [x for x in grids if x["level"] == L][0]
-        n = tuple(p - 1 for p in g["points"])
-        h = tuple(g["length"][a] / n[a] for a in range(3))
-        # the grid's first point is the lower corner of its first cell
-        spec = K.BlockSpec(n=n, h=h, origin=tuple(g["origin"]), bctype=bct)
-        if li > 0:
-            pb = specs[-1]
-            ratio = tuple(int(round(pb.h[a] / h[a])) for a in range(3))
-            off = tuple(int(round((g["origin"][a] - pb.origin[a]) / pb.h[a])) for a in range(3))
-            spec.parent, spec.ratio, spec.offset = 1, ratio, off
-            # embedded grids take their ghost cells from the parent (bc_embed),
-            # except across a periodic span they share with it
-            spec.bctype = tuple(b if b == -60 and ratio[q % 3] == 1 else 0 for q, b in enumerate(bct))
-        specs.append(K.make_block_arrays(spec, body))
+        row = []
+        for g in [x for x in grids if x["level"] == L]:
+            n = tuple(p - 1 for p in g["points"])
+            h = tuple(g["length"][a] / n[a] for a in range(3))
+            # the grid's first point is the lower corner of its first cell
+            spec = K.BlockSpec(n=n, h=h, origin=tuple(g["origin"]), bctype=bct)
+            if li > 0:
+                parent = _parent_of(spec, specs[-1])
+                pb = specs[-1][parent - 1]
+                ratio = tuple(int(round(pb.h[a] / h[a])) for a in range(3))
+                off = tuple(int(round((g["origin"][a] - pb.origin[a]) / pb.h[a])) for a in range(3))
+                spec.parent, spec.ratio, spec.offset = parent, ratio, off
+                # embedded grids take their ghost cells from the parent (bc_embed),
+                # except across a periodic span they share with it
+                spec.bctype = tuple(b if b == -60 and ratio[q % 3] == 1 else 0 for q, b in enumerate(bct))
+            row.append(K.make_block_arrays(spec, body))
+        specs.append(row)
     eqn = A.MGE_EQN_NS if num.get("eqntype", "e").lower().startswith("n") else A.MGE_EQN_EULER
     dist = {"c": A.MGE_DIS_CENTRAL, "r1": A.MGE_DIS_ROE1, "r2": A.MGE_DIS_ROE2}[num.get("distype", "c").lower()]
     kw = dict(
@@ -206,7 +207,21 @@ def case_from_reference(pin_path, p3d_path, jobsheet_path, span_axis=1, nlevel=N
     kw["mcyc"] = mcyc
     kw.update(overrides)
     prm = K.params(**kw)
-    span = specs[-1].n[span_axis] * specs[-1].h[span_axis]
+    span = specs[-1][0].n[span_axis] * specs[-1][0].h[span_axis]
     chord = float(np.ptp(poly[:, 0]))
     name = "reference_" + pin_path.replace("\\", "/").rsplit("/", 1)[-1].rsplit(".", 1)[0]
-    return K.Case(name, prm, [[s] for s in specs], body, ref_area=chord * span)
+    return K.Case(name, prm, specs, body, ref_area=chord * span)
+
+
+def _parent_of(spec, row):
+    """Serial of the block of the level above whose physical box holds the
+    block's (to a thousandth of the coarse cell)."""
+    lo = spec.origin
+    hi = tuple(spec.origin[a] + spec.n[a] * spec.h[a] for a in range(3))
+    for q, pb in enumerate(row):
+        tol = [1e-3 * pb.h[a] for a in range(3)]
+        plo = pb.origin
+        phi = tuple(pb.origin[a] + pb.n[a] * pb.h[a] for a in range(3))
+        if all(lo[a] >= plo[a] - tol[a] and hi[a] <= phi[a] + tol[a] for a in range(3)):
+            return q + 1
+    raise ValueError("grid at %s lies in no grid of the level above" % (lo,))

@@ -257,7 +257,9 @@ long long mge_launch_count(const mge_ctx* ctx);
  * the average ms per launch of {timestep, prep, face, rec, combine, irs_i,
  * irs_j, irs_k_update, cutcell, bcond, rtrms} into ms_out[0..10] ("rec" is
  * the cut-cell wall-term pass), and, when nout allows, the face pass of stage
- * m into ms_out[10 + m].  Advances the state of that level. */
+ * m (1-based) into ms_out[10 + m], the prep pass of stage m into
+ * ms_out[10 + mstage + m] and the combine pass into ms_out[10 + 2*mstage + m].
+ * Advances the state of that level. */
 int mge_kernel_times(mge_ctx* ctx, int level, int reps, double* ms_out, int nout);
 
 /* Residual norm rtrms (the quantity of euler.f90:431-447) of one block from

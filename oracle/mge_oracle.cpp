@@ -1776,6 +1776,57 @@ void bc_embed(mgeo_ctx* c, int lvl) {
   }
 }
 
+/* Stencil of ghost cell (i,j,k) of block g on block p of the same level:
+ * cell_center, eval_x2cell and shft_cell of bc_overlap.f90:63-73 (absent
+ * helpers; the same construction as the prolongation's).  False when the
+ * centre lies outside p's physical cells (eval_x2cell err). */
+bool overlap_stencil(const OBlock& g, const OBlock& p, int i, int j, int k, int* sh, double* fac) {
+  const int ic[3] = {i, j, k};
+  const int lc[3] = {p.il, p.jl, p.kl};
+  const int ncp[3] = {p.nx, p.ny, p.nz};
+  double xi[3];
+  for (int d = 0; d < 3; d++) {
+    const double x = g.origin[d] + ((double)ic[d] - 1.5) * g.h[d];  // cell centre
+    const double u = (x - p.origin[d]) / p.h[d];                     // in p's cells, 0 at its lower face
+    if (u < 0.0 || u >= (double)ncp[d]) return false;
+    coarse_stencil(u, lc[d], sh[d], xi[d]);
+  }
+  trilinear_factor(xi[0], xi[1], xi[2], fac);
+  return true;
+}
+
+/* bc_overlap.f90:32-90: for every block of the level and every other block
+ * it overlaps, the ghost cells (two layers) whose centre lies in the other
+ * block's physical cells take the trilinear interpolation of its state,
+ * then depvars.  Blocks and partners in serial order, cells i, j, k with k
+ * innermost as the reference loops them; a ghost cell inside two partners
+ * keeps the later one's value. */
+void bc_overlap(mgeo_ctx* c, int lvl) {
+  auto& L = c->lv[lvl - 1];
+  if (L.size() < 2) return;
+  for (OBlock& g : L)
+    for (OBlock& p : L) {
+      if (&g == &p) continue;
+      for (int i = 0; i <= g.ib; i++)
+        for (int j = 0; j <= g.jb; j++)
+          for (int k = 0; k <= g.kb; k++) {
+            if (i >= 2 && i <= g.il && j >= 2 && j <= g.jl && k >= 2 && k <= g.kl) continue;
+            int sh[3];
+            double fac[8];
+            if (!overlap_stencil(g, p, i, j, k, sh, fac)) continue;
+            for (int v = 0; v < 5; v++) {
+              double acc = 0.0;
+              int nn = 0;
+              for (int dk = 0; dk < 2; dk++)
+                for (int dj = 0; dj < 2; dj++)
+                  for (int di = 0; di < 2; di++) acc = acc + p.W(sh[0] + di, sh[1] + dj, sh[2] + dk, v) * fac[nn++];
+              g.W(i, j, k, v) = acc;
+            }
+            depvars_cell(c->prm, g, i, j, k);
+          }
+    }
+}
+
 int movco(mgeo_ctx* c, int mgl) {  // movco.f90:21-47
   if (mgl < 1 || mgl > (int)c->lv.size()) return fail(c, MGE_ENOTFOUND, "movco: bad level");
   for (OBlock& b : c->lv[mgl - 1]) {
@@ -1786,7 +1837,7 @@ int movco(mgeo_ctx* c, int mgl) {  // movco.f90:21-47
         for (int k = 2; k <= b.kl; k++)
           for (int v = 0; v < 5; v++) b.wn[v * b.N + b.I(i, j, k)] = b.W(i, j, k, v);
   }
-  // bc_overlap(mgl): one block per level, no same-level overlap
+  bc_overlap(c, mgl);
   for (OBlock& b : c->lv[mgl - 1]) {
     int rc = bcond(c, b);
     if (rc) return rc;
@@ -1799,6 +1850,7 @@ int movfin(mgeo_ctx* c, int mgl, int mlvl) {  // movfin.f90:20-39
   for (OBlock& b : c->lv[mgl - 1]) addw(c, b, mgl, mlvl);
   for (OBlock& b : c->lv[mgl - 1]) depvars_all(c->prm, b);
   bc_embed(c, mgl);
+  bc_overlap(c, mgl);
   for (OBlock& b : c->lv[mgl - 1]) {
     int rc = bcond(c, b);
     if (rc) return rc;
@@ -2055,8 +2107,8 @@ int mgeo_euler_partial(mgeo_ctx* c, int level, int serial, int itime, int ncyc, 
 int mgeo_movco(mgeo_ctx* c, int mgl) { return movco(c, mgl); }
 int mgeo_movfin(mgeo_ctx* c, int mgl, int mlvl) { return movfin(c, mgl, mlvl); }
 int mgeo_bc_overlap(mgeo_ctx* c, int mgl) {
-  (void)c;
-  (void)mgl;
+  if (mgl < 1 || mgl > (int)c->lv.size()) return MGE_ENOTFOUND;
+  bc_overlap(c, mgl);
   return MGE_OK;
 }
 
@@ -2157,9 +2209,10 @@ static int oracle_cycle(mgeo_ctx* c, int mlvl, int ncyc, double* max_res_out, do
     for (;;) {  // lopr
       icyc[mgl] += 1;
       bool lfir = (mgl != mlvl);
-      for (OBlock& b : c->lv[mgl - 1]) {
+      for (OBlock& b : c->lv[mgl - 1]) {  // solver.f90:151-158
         if ((rc = timestep(c, b))) return rc;
         if ((rc = euler(c, b, itime, ncyc, mgl, mlvl, false, lfir, 0))) return rc;
+        bc_overlap(c, mgl);
       }
       if (mgl == mlvl) {  // solver.f90:160-186
         double max_res = 1000.0;
@@ -2172,17 +2225,20 @@ static int oracle_cycle(mgeo_ctx* c, int mlvl, int ncyc, double* max_res_out, do
         *max_res_out = max_res;
       }
       if (mlvl == 1) return MGE_OK;  // cycle lop0
-      for (OBlock& b : c->lv[mgl - 1])
+      for (OBlock& b : c->lv[mgl - 1]) {  // solver.f90:197-201
         if ((rc = euler(c, b, itime, ncyc, mgl, mlvl, true, false, 0))) return rc;
+        bc_overlap(c, mgl);
+      }
       mgl = mgl - 1;
       if ((rc = movco(c, mgl))) return rc;
       if (mgl == 1) break;
     }
     bool lfir = true;
     for (;;) {  // lopp
-      for (OBlock& b : c->lv[mgl - 1]) {
+      for (OBlock& b : c->lv[mgl - 1]) {  // solver.f90:215-222
         if ((rc = timestep(c, b))) return rc;
         if ((rc = euler(c, b, itime, ncyc, mgl, mlvl, false, lfir, 0))) return rc;
+        bc_overlap(c, mgl);
       }
       lfir = false;
       mgl = mgl + 1;

@@ -5,8 +5,7 @@ run the same comparisons on the blocks the benchmark times:
 - the 192^3 sphere (4-level W-cycle, JST scalar, IRS 0.6), one developed
   W-cycle, then each of the five stages of a finest-level update;
 - the 512x512x2 laminar Navier-Stokes cylinder at h = D/96 (Roe MUSCL +
-  viscous fluxes, 4 embedded levels), the same.
-
+  viscous fluxes, 4 embedded levels), the same;
 - the 256x256x2 cylinder slab exactly as the first workload states it
   (M=0.3, JST k2=0.5, k4=1/64, IRS 0.6, 3-level V-cycle, 500 finest cycles):
   the whole residual history and the converged Cd and Cl.

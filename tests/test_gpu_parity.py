@@ -202,3 +202,25 @@ def test_mixed_paths_in_one_hierarchy(gpulib):
     ho, _, _ = o.solve()
     assert np.max(np.abs(hg - ho) / np.abs(ho)) <= 1e-11
     compare(g, o, "w", 3, rtol=1e-11, phys_only=False)
+
+
+@pytest.mark.parametrize("path", PATHS)
+def test_same_level_overlap(gpulib, path):
+    """Two fine blocks of one level that share 4 cells around the body
+    (bc_overlap.f90:32-90 after every block's update, in movco and in
+    movfin): whole solve, both blocks' states, against the oracle."""
+    case = K.cylinder_split(n=32, overlap=4, mcyc_fine=4)
+    g, o = pair(case, path=path)
+    hg, ng, fg = g.solve()
+    ho, no, fo = o.solve()
+    assert ng == no
+    assert np.max(np.abs(hg - ho) / np.abs(ho)) <= 1e-11
+    for s in (1, 2):
+        a, b = g.field("w", 2, serial=s), o.field("w", 2, serial=s)
+        assert np.max(np.abs(a - b)) <= 1e-11 * np.max(np.abs(b))
+    assert abs(fg.cd - fo.cd) <= 1e-9 * max(1.0, abs(fo.cd))
+    # the entry point alone, on the solved states
+    assert gpulib.mge_bc_overlap(g.ctx, 2) == 0 and o.lib.mgeo_bc_overlap(o.ctx, 2) == 0
+    for s in (1, 2):
+        a, b = g.field("w", 2, serial=s), o.field("w", 2, serial=s)
+        assert np.max(np.abs(a - b)) <= 1e-11 * np.max(np.abs(b))

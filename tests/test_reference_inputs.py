@@ -1,7 +1,8 @@
 """The reference's own case inputs (grid file, plot3d surface, job sheet)
 read into a case: the readers on a small set of inputs written here, the
-shipped cylinder inputs when the reference tree is at hand, and on the GPU a
-solve of the case built from such inputs against the oracle."""
+shipped cylinder inputs (copied into tests/fixtures), and on the GPU solves
+of cases built from such inputs, the shipped one included, against the
+oracle."""
 import os
 
 import numpy as np
@@ -10,7 +11,8 @@ import pytest
 from code_mge_gb300 import _abi as A
 from code_mge_gb300 import reference_inputs as R
 
-REF = "/root/reference/cylinder"
+# the reference's shipped cylinder inputs (tests/fixtures/copy_reference_inputs.py)
+REF = os.path.join(os.path.dirname(os.path.abspath(__file__)), "fixtures", "cylinder")
 
 
 def write_inputs(d, n=(32, 2, 32), nlevel=2):
@@ -106,13 +108,13 @@ def test_oracle_solves_a_case_from_written_inputs(tmp_path):
     assert n == 6 and hist[-1] < hist[0] and np.isfinite(f.cd)   # mcyc = 2:6
 
 
-@pytest.mark.skipif(not os.path.isdir(REF), reason="the reference tree is not here")
 def test_shipped_cylinder_inputs():
     pin, p3d, js = (os.path.join(REF, f) for f in ("cylinder05_1.pin", "cylinder.p3d", "jobsheet"))
     assert [g["name"] for g in R.read_pin(os.path.join(REF, "cylinder05_11122.pin"))] == \
         [101, 201, 301, 401, 402, 501, 502]
-    with pytest.raises(ValueError):   # two grids on level 4: same-level overlap is not built
-        R.case_from_reference(os.path.join(REF, "cylinder05_11122.pin"), p3d, js)
+    multi = R.case_from_reference(os.path.join(REF, "cylinder05_11122.pin"), p3d, js)
+    assert [len(row) for row in multi.levels] == [1, 1, 1, 2, 2]
+    assert [s.parent for s in multi.levels[4]] == [1, 2]   # 501 in 401, 502 in 402
     case = R.case_from_reference(pin, p3d, js)
     sp = case.levels[0][0]
     assert sp.n == (448, 8, 256) and case.prm.eqntype == A.MGE_EQN_NS and case.prm.vt == 0
@@ -132,3 +134,60 @@ def test_gpu_solves_a_case_from_written_inputs(gpulib, tmp_path):
     assert np.max(np.abs(hg - ho) / np.abs(ho)) <= 1e-11
     compare(g, o, "w", 2, rtol=1e-11, phys_only=False)
     assert abs(fg.cd - fo.cd) <= 1e-9 * max(1.0, abs(fo.cd))
+
+
+@pytest.mark.gpu
+def test_gpu_solves_the_shipped_cylinder_case(gpulib):
+    """cylinder05_1.pin + cylinder.p3d + jobsheet: Navier-Stokes (Re 500 as
+    input_param.f90:111-114 sets it), JST central, 448x8x256, three cycles
+    against the oracle on every host thread."""
+    from oracle import oracle as O
+    from parity import compare, pair
+    case = R.case_from_reference(*(os.path.join(REF, f) for f in ("cylinder05_1.pin", "cylinder.p3d", "jobsheet")))
+    assert case.prm.nlevel == 1
+    case.prm.mcyc[0] = 3
+    before = O.load().mgeo_get_threads()
+    O.set_threads(os.cpu_count() or 1)
+    try:
+        g, o = pair(case)
+        hg, ng, fg = g.solve(use_graph=1)
+        ho, no, fo = o.solve()
+    finally:
+        O.set_threads(before)
+    assert ng == no == 3
+    assert np.max(np.abs(hg - ho) / np.abs(ho)) <= 1e-11
+    compare(g, o, "w", 1, rtol=1e-11, phys_only=False)
+    assert abs(fg.cd - fo.cd) <= 1e-9 * max(1.0, abs(fo.cd))
+    g.close()
+    o.close()
+
+
+@pytest.mark.gpu
+def test_gpu_solves_the_shipped_multiblock_case(gpulib):
+    """cylinder05_11122.pin: five levels, two overlapping blocks on each of
+    the two finest (bc_overlap), Navier-Stokes, JST central; the FMG
+    sequence with one cycle per coarse level and two on the finest, against
+    the oracle on every host thread."""
+    from oracle import oracle as O
+    from parity import pair
+    case = R.case_from_reference(*(os.path.join(REF, f) for f in ("cylinder05_11122.pin", "cylinder.p3d",
+                                                                  "jobsheet")))
+    for q in range(case.prm.nlevel):
+        case.prm.mcyc[q] = 1
+    case.prm.mcyc[case.prm.nlevel - 1] = 2
+    before = O.load().mgeo_get_threads()
+    O.set_threads(os.cpu_count() or 1)
+    try:
+        g, o = pair(case)
+        hg, ng, fg = g.solve(use_graph=1)
+        ho, no, fo = o.solve()
+    finally:
+        O.set_threads(before)
+    assert ng == no == 2
+    assert np.max(np.abs(hg - ho) / np.abs(ho)) <= 1e-11
+    L = case.prm.nlevel
+    for s in (1, 2):
+        a, b = g.field("w", L, serial=s), o.field("w", L, serial=s)
+        assert np.max(np.abs(a - b)) <= 1e-11 * np.max(np.abs(b))
+    g.close()
+    o.close()
