@@ -62,7 +62,26 @@ FACE_DOUBLES_ROE_NS = 55
 # scales with the cells a launch covers.
 FACE_DRAM_BYTES_PER_CELL = 519.6
 FACE_FP64_PER_CELL = 118.2
+# The three passes of the residual on a stage with dissipation (stage 1),
+# plain FP64, from ncu captures on the 128^3 sphere (profiles/k_prep_sphere128.md,
+# profiles/k_face_sphere128.md, profiles/k_combine_sphere128.md):
+#   cells     which cells one thread each: "prep" [1..ie]^3, "face" [2..ie]^3, "phys" [2..il]^3
+#   alg       compulsory HBM bytes per cell
+#   dram      measured DRAM read + write bytes per cell
+#   fp64      measured FP64 thread instructions per cell (DADD + DMUL + DFMA)
+# prep reads w, p (6 doubles) and writes H, F, dlt, fp (34); face reads F, fp,
+# dlt, lambda (34) and writes efs, dfs (30); combine reads efs, dfs, vdtim
+# (31 doubles), blank (1 B), cutmap (4 B) and writes fw, dw (10 doubles).
+KERNEL_MODEL = {
+    "prep": {"cells": "prep", "alg": 40 * 8, "dram": 320.6, "fp64": 120.1},
+    "face": {"cells": "face", "alg": FACE_DOUBLES_DISSIP * 8, "dram": FACE_DRAM_BYTES_PER_CELL,
+             "fp64": FACE_FP64_PER_CELL},
+    "combine": {"cells": "phys", "alg": 41 * 8 + 5, "dram": 338.6, "fp64": 75.0},
+}
 FP64_LANES_PER_SM_CYCLE = 2      # GB300: 2 FP64 thread-operations per SM per cycle
+# FP64 thread instructions of every kernel of one finest-level update of the
+# 128^3 sphere (ncu), per cell-update, by precision form
+FP64_PER_CELL_UPDATE = {}
 GB300_SMS = 152
 LAUNCHES_PER_UPDATE = {"timestep": 1, "prep": 5, "face": 5, "rec": 5, "combine": 5, "irs_i": 3, "irs_j": 3,
                        "irs_k_update": 3, "cutcell": 5, "bcond": 5, "rtrms": 1}
@@ -87,6 +106,56 @@ def workload_case(precision="fp64", n=192, name="sphere192"):
                                    eqntype=A.MGE_EQN_NS, distype=A.MGE_DIS_ROE2, reynolds=40.0, precision=prec)
     return K.sphere_box(n=n, nlevel=4, extent=10.0, mach=0.5, mgtype=2, mcyc_fine=400, smoo=0.6,
                         precision=prec)
+
+
+def jst_euler(case):
+    return (case.prm.eqntype == A.MGE_EQN_EULER and case.prm.distype == A.MGE_DIS_CENTRAL
+            and case.prm.dissip == A.MGE_DISSIP_SCALAR)
+
+
+def kernel_roofline(case, kind, stage_ms, peak, pkind, fp64_peak):
+    """The roofline line of one pass on stage 1 (dissipation on) of the
+    finest-level update, from its CUDA-event time and KERNEL_MODEL; the
+    passes without a model get the whole update's line only."""
+    nx, ny, nz = case.levels[-1][0].n
+    cells = {"prep": (nx + 2) * (ny + 2) * (nz + 2), "face": (nx + 1) * (ny + 1) * (nz + 1), "phys": nx * ny * nz}
+    m = KERNEL_MODEL.get(kind)
+    if m is None or kind not in stage_ms or not jst_euler(case) or case.prm.precision != A.MGE_PREC_FP64:
+        # the Roe + viscous and the mixed passes: their byte models only
+        t = stage_ms["face"][0]
+        nf = cells["face"]
+        dbl = FACE_DOUBLES_DISSIP if jst_euler(case) else FACE_DOUBLES_ROE_NS
+        if case.prm.precision != A.MGE_PREC_FP64 and jst_euler(case):
+            dbl = 34  # the contracted form's dissipation faces: dlt, fp, lambda in, dfs out
+        alg = 8.0 * dbl * nf
+        ach = alg / (t * 1e-3) / 1e9 if t > 0 else 0.0
+        return ({"bound": "hbm", "kernel": "face pass (stage 1)", "achieved": ach, "peak": peak, "unit": "GB/s",
+                 "frac": ach / peak, "traffic": None, "algorithmic_bytes_per_launch": alg, "launch_ms": t,
+                 "peak_kind": pkind, "note": "dominant pass: %s; no DRAM capture of this form's pass" % kind}, None)
+    t = stage_ms[kind][0]
+    n = cells[m["cells"]]
+    alg = m["alg"] * n
+    ach = alg / (t * 1e-3) / 1e9 if t > 0 else 0.0
+    fp = m["fp64"] * n / (t * 1e-3) if t > 0 else 0.0
+    roof = {"bound": "hbm", "kernel": "k_%s (stage 1, dissipation on)" % kind, "achieved": ach, "peak": peak,
+            "unit": "GB/s", "frac": ach / peak, "traffic": m["dram"] * n, "algorithmic_bytes_per_launch": alg,
+            "launch_ms": t, "peak_kind": pkind,
+            "note": "the FP64 issue rate, not HBM, bounds this pass: see fp64_roofline; traffic scales the ncu "
+                    "capture's DRAM bytes per cell (128^3 sphere) to this launch's cells"}
+    fp64 = {"kernel": "k_%s (stage 1)" % kind, "achieved": fp / 1e12, "peak": fp64_peak / 1e12,
+            "unit": "T FP64 instr/s", "frac": fp / fp64_peak, "fp64_per_cell": m["fp64"],
+            "peak_basis": "2 FP64 thread-ops per SM per cycle x 152 SMs x median SM clock"}
+    return roof, fp64
+
+
+def l2_note(lib, cyc, sp):
+    field_mb = 5 * 8 * sp.dims[0] * sp.dims[1] * sp.dims[2] / 1e6
+    dev_mb = lib.mge_device_bytes(cyc.ctx) / 1e6
+    if field_mb > 129.0:
+        return "finest 5-variable fields of %.0f MB each exceed the 129 MB L2 (no flush needed)" % field_mb
+    return ("finest 5-variable fields of %.0f MB fit in the 129 MB L2, but one step streams the context's "
+            "%.0f MB of device fields (a stage's scratch alone is 64 fields of the finest block), so each step's "
+            "own traffic turns L2 over; no separate flush" % (field_mb, dev_mb))
 
 
 def run_profile(args):
@@ -308,32 +377,33 @@ def run_gpu(args):
     barrier()
     e2e_s = time.perf_counter() - t0
     e2e = R.whole_job_rate(args.steps * cu, e2e_s)
+    # the drop-in ends a solve with mge_download_state of the state (once per
+    # solve, not per cycle): timed on its own
+    t0 = time.perf_counter()
+    rc = lib.mge_download_state(cyc.ctx, L, 1, wptr, None)
+    dl_ms = 1e3 * (time.perf_counter() - t0) if rc == 0 else None
 
-    # per-kernel device times (CUDA events on the library stream), finest level
+    # per-kernel device times (CUDA events on the library stream), finest
+    # level; the prep, face and combine passes also per stage
     nk = len(A.KERNEL_KINDS)
-    ms = np.zeros(nk + case.prm.mstage)
+    ms_ = case.prm.mstage
+    ms = np.zeros(nk + 3 * ms_)
     lib.mge_kernel_times(cyc.ctx, L, 2, ms.ctypes.data_as(C.POINTER(C.c_double)), len(ms))
     kt = {k: float(ms[q]) for q, k in enumerate(A.KERNEL_KINDS)}
-    face_stage_ms = [float(x) for x in ms[nk:]]
+    stage_ms = {"face": [float(x) for x in ms[nk:nk + ms_]], "prep": [float(x) for x in ms[nk + ms_:nk + 2 * ms_]],
+                "combine": [float(x) for x in ms[nk + 2 * ms_:nk + 3 * ms_]]}
     share = {k: kt[k] * LAUNCHES_PER_UPDATE[k] for k in kt}
     tot = sum(share.values()) or 1.0
     dom = max(share, key=share.get)
     peak, pkind = hbm_peak_gbs()
     ncell = case.finest_cells
-    dims = sp.dims
-    face_cells = (dims[0] - 3) * (dims[1] - 3) * (dims[2] - 3)
-    t_face = face_stage_ms[0]                      # stage 1: dissipation on
-    # the measured per-cell traffic and FP64 count are those of the Euler JST
-    # face pass; the Roe + viscous pass gets its bytes model only
-    jst = case.prm.eqntype == A.MGE_EQN_EULER and case.prm.distype == A.MGE_DIS_CENTRAL
-    alg = 8.0 * (FACE_DOUBLES_DISSIP if jst else FACE_DOUBLES_ROE_NS) * face_cells
-    achieved = alg / (t_face * 1e-3) / 1e9 if t_face > 0 else 0.0
-    traffic = FACE_DRAM_BYTES_PER_CELL * face_cells if jst else None
     clk = (clocks.get("sm_mhz") or 2070.0) * 1e6
     fp64_peak = FP64_LANES_PER_SM_CYCLE * GB300_SMS * clk
-    fp64_achieved = FACE_FP64_PER_CELL * face_cells / (t_face * 1e-3) if (t_face > 0 and jst) else None
+    roof, fp64_roof = kernel_roofline(case, dom, stage_ms, peak, pkind, fp64_peak)
     upd_ms = sum(kt[k] * LAUNCHES_PER_UPDATE[k] for k in kt)
     whole_update_gbs = BYTES_PER_CELL_UPDATE_IRS * ncell / (upd_ms * 1e-3) / 1e9 if upd_ms > 0 else 0.0
+    fp64_upd = FP64_PER_CELL_UPDATE.get(args.precision) if jst_euler(case) else None
+    whole_update_fp64 = (fp64_upd * ncell / (upd_ms * 1e-3) / fp64_peak) if (fp64_upd and upd_ms > 0) else None
 
     # solution output of the finest level (upload_solut.f90:203-237) through
     # the C-ABI: device kernel, device-to-host copy of the 7 variables
@@ -363,26 +433,24 @@ def run_gpu(args):
                        "cell_updates_per_step": cu, "precision": args.precision,
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "launch_plan": plan,
-                       "l2": "finest fields of %.0f MB each exceed the 129 MB L2 (no flush needed)"
-                             % (5 * 8 * sp.dims[0] * sp.dims[1] * sp.dims[2] / 1e6)},
+                       "l2": l2_note(lib, cyc, sp)},
             "wall_ms_per_step": 1e3 * wall / args.steps,
             "residual_last": res[-1] if res else None,
-            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(w_np.nbytes), "d2h_bytes_per_step": 8},
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(w_np.nbytes), "d2h_bytes_per_step": 8,
+                    "note": "per step: the finest state uploaded from pinned host memory (mge_upload_state, which "
+                            "also runs depvars, bc_cutcell and bcond), one cycle, its residual read back; a solve "
+                            "downloads the state once at its end, timed in download_state"},
             "gpu_launches": None,
-            "roofline": {"bound": "hbm", "kernel": "k_face (stage 1, dissipation on)", "achieved": achieved,
-                         "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
-                         "algorithmic_bytes_per_launch": alg, "launch_ms": t_face, "peak_kind": pkind,
-                         "note": ("the FP64 issue rate, not HBM, bounds this kernel: see fp64_roofline" if jst else
-                                  "Roe + viscous face pass: 55 doubles per cell; its DRAM traffic is not captured")},
-            "fp64_roofline": {"kernel": "k_face (stage 1)", "achieved": fp64_achieved / 1e12,
-                              "peak": fp64_peak / 1e12, "unit": "T FP64 instr/s", "frac": fp64_achieved / fp64_peak,
-                              "fp64_per_cell": FACE_FP64_PER_CELL,
-                              "peak_basis": "2 FP64 thread-ops per SM per cycle x 152 SMs x median SM clock"}
-                             if fp64_achieved is not None else None,
-            "face_stage_ms": face_stage_ms,
+            "roofline": roof,
+            "fp64_roofline": fp64_roof,
+            "stage_ms": stage_ms,
             "upload_solut": {"ms": solut_ms, "cells": ncell, "d2h_bytes": int(sol.nbytes), "nval": nval.value},
-            "whole_update_hbm": {"achieved_gbs": whole_update_gbs, "frac": whole_update_gbs / peak,
-                                 "bytes_per_cell_update": BYTES_PER_CELL_UPDATE_IRS},
+            "download_state": {"ms": dl_ms, "d2h_bytes": int(w_np.nbytes)},
+            "whole_update": {"ms": upd_ms, "hbm_achieved_gbs": whole_update_gbs, "hbm_frac": whole_update_gbs / peak,
+                             "bytes_per_cell_update": BYTES_PER_CELL_UPDATE_IRS,
+                             "fp64_frac": whole_update_fp64, "fp64_per_cell_update": fp64_upd,
+                             "fp64_basis": "ncu FP64 thread instructions of every kernel of one finest-level update "
+                                           "(128^3 sphere), per cell-update, over the summed kernel time"},
             "kernel_ms": kt, "kernel_share": {k: share[k] / tot for k in share}, "dominant_kernel": dom,
             "clocks": clocks,
             "cpu_baseline": cpu,
