@@ -81,7 +81,7 @@ KERNEL_MODEL = {
 FP64_LANES_PER_SM_CYCLE = 2      # GB300: 2 FP64 thread-operations per SM per cycle
 # FP64 thread instructions of every kernel of one finest-level update of the
 # 128^3 sphere (ncu), per cell-update, by precision form
-FP64_PER_CELL_UPDATE = {}
+FP64_PER_CELL_UPDATE = {"fp64": 1793.9, "mixed": 1003.4}
 GB300_SMS = 152
 LAUNCHES_PER_UPDATE = {"timestep": 1, "prep": 5, "face": 5, "rec": 5, "combine": 5, "irs_i": 3, "irs_j": 3,
                        "irs_k_update": 3, "cutcell": 5, "bcond": 5, "rtrms": 1}
@@ -561,23 +561,52 @@ def run_pattern(args):
                 "batched": batched, "fp64_serial": serial, "peak_active": srv.peak_active}
         print(json.dumps(line), flush=True)
         return 0
-    # serving loop
+    # serving loop: the mixed form with continuous batching, then the serial
+    # FP64 plain path (one case at a time, FIFO) on the same seeded stream
+    # over the same window (arrivals plus a bounded drain)
     lo, hi = [int(x) for x in args.sizes.split(",")][:2] if "," in args.sizes else (64, 256)
-    reqs = SV.poisson_requests(args.rate, args.duration, sizes=(lo, hi), tol=args.tol, max_cycles=args.max_cycles)
-    srv = SV.Server(SV.GpuBackend(coop_ctas=args.coop_ctas))
-    t_start = time.perf_counter()
-    for r in reqs:
-        r.arrival += t_start
-        srv.submit(r)
-    done = srv.run(deadline=t_start + args.duration + args.drain)
-    wall = time.perf_counter() - t_start
-    st = SV.summarize(done, wall)
+
+    def cells(r):
+        return r.n * r.n * 2 if r.geometry == "cylinder" else r.n ** 3
+
+    def serve(precision, max_active):
+        reqs = SV.poisson_requests(args.rate, args.duration, sizes=(lo, hi), tol=args.tol,
+                                   max_cycles=args.max_cycles, precision=precision)
+        srv = SV.Server(SV.GpuBackend(coop_ctas=args.coop_ctas if max_active > 1 else 0), max_active=max_active)
+        t_start = time.perf_counter()
+        for r in reqs:
+            r.arrival += t_start
+            srv.submit(r)
+        done = srv.run(deadline=t_start + args.duration + args.drain)
+        wall = time.perf_counter() - t_start
+        # the cases still running at the deadline are not completions
+        for sl in list(srv.active):
+            srv.be.close(sl.handle)
+        st = SV.summarize(done, wall)
+        ok = [r for r in done if r.error is None]
+        st.update({"submitted": len(reqs), "finished": len(done), "unfinished": len(reqs) - len(done),
+                   "in_flight_at_deadline": len(srv.active), "never_admitted": len(srv.queue),
+                   "peak_active": srv.peak_active,
+                   "finest_cell_cycles_per_s": sum(r.cycles * cells(r) for r in ok) / wall if wall > 0 else None,
+                   "mean_finest_cells": float(np.mean([cells(r) for r in reqs])) if reqs else None})
+        return st
+
+    mixed = serve(A.MGE_PREC_MIXED, 64)
+    serial = serve(A.MGE_PREC_FP64, 1)
+    offered = args.rate
     line = {"pattern": "serving", "metric": "solves/s & p50/p99 time-to-converged", "unit": "solves/s",
-            "value": st["solves_per_s"], "p50_s": st["p50_s"], "p99_s": st["p99_s"],
-            "submitted": len(reqs), "completed": st["completed"], "unfinished": len(reqs) - len(done),
-            "peak_active": srv.peak_active,
+            "value": mixed["solves_per_s"], "p50_s": mixed["p50_s"], "p99_s": mixed["p99_s"],
+            "submitted": mixed["submitted"], "completed": mixed["converged"], "unfinished": mixed["unfinished"],
+            "peak_active": mixed["peak_active"], "offered_req_per_s": offered,
+            "overload": (offered / mixed["solves_per_s"]) if mixed["solves_per_s"] else None,
+            "mixed_continuous_batching": mixed, "fp64_serial": serial,
+            "speedup_solves_per_s": (mixed["solves_per_s"] / serial["solves_per_s"]) if serial["solves_per_s"]
+            else None,
             "config": {"arrivals": "Poisson %.1f req/s for %.0f s (seed 20261204)" % (args.rate, args.duration),
-                       "sizes": [lo, hi], "tol_drop": args.tol, "precision": "FP32 coarse / FP64 fine"}}
+                       "drain_s": args.drain, "sizes": [lo, hi], "tol_drop": args.tol,
+                       "max_cycles": args.max_cycles,
+                       "precision": "FP32 coarse / FP64 fine (contracted residual), refined to FP64 coarse",
+                       "baseline": "FP64 plain, one case at a time in arrival order, same stream and window"}}
     print(json.dumps(line), flush=True)
     return 0
 

@@ -1180,10 +1180,10 @@ __device__ __forceinline__ void body_combine(const DevBlock<T>& b, const PhysPar
     if (b.blank[c] == 0)
 #pragma unroll
       for (int v = 0; v < 5; v++) dwv[v] = T(0);
-  } else {
-    const T bl = (T)b.blank[c];
+  } else if (b.blank[c] == 0) {
+    // dw * blank: x * 1 is x itself, so only blanked cells multiply (by 0)
 #pragma unroll
-    for (int v = 0; v < 5; v++) dwv[v] = dwv[v] * bl;
+    for (int v = 0; v < 5; v++) dwv[v] = dwv[v] * T(0);
   }
   if (A.lres) {
 #pragma unroll
@@ -2106,9 +2106,20 @@ __device__ void body_rtrms_partial(const DevBlock<T>& b, double cfl, int vt, dou
   const long long lo = (long long)part * per, hi = min(tot, lo + per);
   double acc = 0.0;
   for (long long t = lo + threadIdx.x; t < hi; t += blockDim.x) {
-    int i = 2 + (int)(t % b.nx);
-    int j = 2 + (int)((t / b.nx) % b.ny);
-    int k = 2 + (int)(t / ((long long)b.nx * b.ny));
+    // 32-bit index arithmetic while the block's cells fit (the same cells)
+    int i, j, k;
+    if (tot < (1ll << 31)) {
+      const int t32 = (int)t, nxy = b.nx * b.ny;
+      k = t32 / nxy;
+      const int r = t32 - k * nxy;
+      j = r / b.nx;
+      i = r - j * b.nx;
+      i += 2, j += 2, k += 2;
+    } else {
+      i = 2 + (int)(t % b.nx);
+      j = 2 + (int)((t / b.nx) % b.ny);
+      k = 2 + (int)(t / ((long long)b.nx * b.ny));
+    }
     long long c = cidx(b.Pi, b.Pj, i, j, k);
     double de = cfl * (double)(vt ? *b.dtim : b.vdtim[c]);
     double rt = 0.0;
@@ -2130,19 +2141,27 @@ __global__ void k_rtrms_partial(DevBlock<T> b, double cfl, int vt, double* parti
   body_rtrms_partial(b, cfl, vt, partial, npart, blockIdx.x);
 }
 
-// a NaN norm is the stop of solver.f90:180, recorded in launch order like
-// the kernels' other stops (err may be null)
+// The partial sums in a fixed order by one warp: lane l adds the partials
+// l, l+32, l+64, ... in turn, then the lanes' sums fold in a fixed halving
+// tree.  A NaN norm is the stop of solver.f90:180, recorded in launch order
+// like the kernels' other stops (err may be null).  Every lane of warp 0
+// calls it.
 __device__ __forceinline__ void body_rtrms_final(const double* partial, int npart, double ncell, double* out,
                                                  unsigned* err) {
+  const int lane = threadIdx.x & 31;
   double a = 0.0;
-  for (int q = 0; q < npart; q++) a = a + partial[q];
-  const double r = sqrt(a / ncell);
-  *out = r;
-  if (err && r != r) atomicCAS(err, 0u, (unsigned)ERR_NANRES);
+  for (int q = lane; q < npart; q += 32) a = a + partial[q];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) a = a + __shfl_down_sync(0xffffffffu, a, o);
+  if (lane == 0) {
+    const double r = sqrt(a / ncell);
+    *out = r;
+    if (err && r != r) atomicCAS(err, 0u, (unsigned)ERR_NANRES);
+  }
 }
 
 __global__ void k_rtrms_final(const double* partial, int npart, double ncell, double* out, unsigned* err) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) body_rtrms_final(partial, npart, ncell, out, err);
+  if (blockIdx.x == 0 && threadIdx.x < 32) body_rtrms_final(partial, npart, ncell, out, err);
 }
 
 // --------------------------------------------------------------- small whole-array kernels
@@ -2663,7 +2682,7 @@ __global__ void __launch_bounds__(256, 1) k_euler_coop(DevBlock<T> b, PhysParams
     for (int part = blockIdx.x; part < E.npart; part += gridDim.x)
       body_rtrms_partial(b, P.cfl, P.vt, E.rt_partial, E.npart, part);
     g.sync();
-    if (gt == 0) body_rtrms_final(E.rt_partial, E.npart, (double)ncell, E.rt_out, E.err);
+    if (blockIdx.x == 0 && threadIdx.x < 32) body_rtrms_final(E.rt_partial, E.npart, (double)ncell, E.rt_out, E.err);
   }
   if (E.trace && blockIdx.x == 0 && threadIdx.x == 0) E.trace[255] = (unsigned long long)ntr;
 }

@@ -78,12 +78,16 @@ __global__ void k_noalloc_partial(const double* __restrict__ dw, const double* _
   if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
 }
 
+// one warp: lane l adds partials l, l+32, ... in turn, then a fixed halving
+// tree over the lanes (the order the cycle's own norm uses)
 __global__ void k_noalloc_final(const double* partial, int npart, double ncell, double* out) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) {
-    double a = 0.0;
-    for (int q = 0; q < npart; q++) a = a + partial[q];
-    *out = sqrt(a / ncell);
-  }
+  if (blockIdx.x != 0 || threadIdx.x >= 32) return;
+  const int lane = threadIdx.x;
+  double a = 0.0;
+  for (int q = lane; q < npart; q += 32) a = a + partial[q];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) a = a + __shfl_down_sync(0xffffffffu, a, o);
+  if (lane == 0) *out = sqrt(a / ncell);
 }
 
 }  // namespace

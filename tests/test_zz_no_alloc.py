@@ -57,8 +57,9 @@ def test_noalloc_norm_matches_the_cycle_twice(gpulib, cfl):
 
 def _fixed_order_norm(dw, vd, blank, n, cfl):
     """numpy restatement of the kernels' fixed-order reduction (vt = 0):
-    partial q sums cells [q*per, (q+1)*per) with 256 strided accumulators,
-    a halving tree over them, then the partials in order."""
+    partial q sums cells [q*per, (q+1)*per) with 256 strided accumulators
+    and a halving tree over them; then 32 lanes each add the partials
+    l, l+32, ... in turn, and a halving tree over the lanes."""
     nx, ny, nz = n
     tot = nx * ny * nz
     ph = lambda a: a[2:nz + 2, 2:ny + 2, 2:nx + 2].reshape(-1)  # (k, j, i) order: i fastest
@@ -76,10 +77,14 @@ def _fixed_order_norm(dw, vd, blank, n, cfl):
     while s > 0:
         acc[:, :s] = acc[:, :s] + acc[:, s:2 * s]
         s //= 2
-    a = 0.0
+    lanes = np.zeros(32)
     for q in range(npart):
-        a = a + float(acc[q, 0])
-    return float(np.sqrt(a / float(tot)))
+        lanes[q % 32] = lanes[q % 32] + acc[q, 0]
+    s = 16
+    while s > 0:
+        lanes[:s] = lanes[:s] + lanes[s:2 * s]
+        s //= 2
+    return float(np.sqrt(lanes[0] / float(tot)))
 
 
 def test_noalloc_norm_at_the_partial_cap(gpulib):
