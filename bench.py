@@ -519,7 +519,7 @@ def run_pattern(args):
         sizes = tuple(int(x) for x in args.sizes.split(","))
         reqs = SV.batched_sweep_requests(args.cases, sizes=sizes, precision=A.MGE_PREC_MIXED, tol=args.tol,
                                          max_cycles=args.max_cycles, retire_stall=args.retire_stall)
-        srv = SV.Server(SV.GpuBackend(coop_ctas=args.coop_ctas), max_active=args.cases)
+        srv = SV.Server(SV.GpuBackend(coop_ctas=args.coop_ctas), max_active=args.cases, group=not args.no_group)
         t0 = time.perf_counter()
         for r in reqs:
             r.arrival = t0
@@ -558,7 +558,10 @@ def run_pattern(args):
                 "config": {"sizes": sizes, "tol_drop": args.tol, "levels": 3, "cycle": "W",
                            "precision": "FP32 coarse / FP64 fine", "seed": 20261203,
                            "max_cycles": args.max_cycles, "retire_stall": args.retire_stall},
-                "batched": batched, "fp64_serial": serial, "peak_active": srv.peak_active}
+                "batched": batched, "fp64_serial": serial, "peak_active": srv.peak_active,
+                "group_cycles": srv.group_cycles,
+                "launch_form": "group cycles (one launch per phase over the cases at the same FMG level and "
+                               "precision form)" if not args.no_group else "one graph per case on its own stream"}
         print(json.dumps(line), flush=True)
         return 0
     # serving loop: the mixed form with continuous batching, then the serial
@@ -572,7 +575,8 @@ def run_pattern(args):
     def serve(precision, max_active):
         reqs = SV.poisson_requests(args.rate, args.duration, sizes=(lo, hi), tol=args.tol,
                                    max_cycles=args.max_cycles, precision=precision)
-        srv = SV.Server(SV.GpuBackend(coop_ctas=args.coop_ctas if max_active > 1 else 0), max_active=max_active)
+        srv = SV.Server(SV.GpuBackend(coop_ctas=args.coop_ctas if max_active > 1 else 0), max_active=max_active,
+                        group=max_active > 1 and not args.no_group)
         t_start = time.perf_counter()
         for r in reqs:
             r.arrival += t_start
@@ -633,6 +637,8 @@ def main():
     ap.add_argument("--duration", type=float, default=300.0)
     ap.add_argument("--drain", type=float, default=120.0)
     ap.add_argument("--coop-ctas", type=int, default=32)
+    ap.add_argument("--no-group", action="store_true",
+                    help="batched/serving: each case its own cycles (no group launches)")
     ap.add_argument("--workload", default="sphere192", choices=["sphere192", "cylinder512ns", "sphere128", "sphere96"])
     ap.add_argument("--profile", action="store_true", help="short run for ncu captures")
     ap.add_argument("--plan-out", default=None, help="write the tuned launch plan (MGE_TUNE_PLAN form) here")

@@ -173,6 +173,8 @@ PRODUCT_ONLY = [
     ("coop_trace", _i, [_vp, _i, _pd, _i]),
     ("cycle_async", _i, [_vp, _i]),
     ("cycle_poll", _i, [_vp, _i, _pd]),
+    ("group_cycle_async", _i, [_vp, _i, _i]),
+    ("group_cycle_poll", _i, [_vp, _i, _i, _pd, C.POINTER(C.c_int)]),
     ("prolong_async", _i, [_vp, _i]),
     ("set_coop_ctas", _i, [_vp, _i]),
     ("tuned", _i, [_vp, _i, _i, C.POINTER(_i), C.POINTER(_i)]),
@@ -193,7 +195,7 @@ HEADER_SYMBOLS = [
     "mge_last_error", "mge_add_block", "mge_commit", "mge_init_flow", "mge_upload_state",
     "mge_download_state", "mge_download_field", "mge_timestep", "mge_euler", "mge_movco",
     "mge_movfin", "mge_bc_overlap", "mge_get_rtrms", "mge_solve", "mge_forces_compute",
-    "mge_cycle", "mge_cycle_async", "mge_cycle_poll", "mge_prolong_async", "mge_set_coop_ctas", "mge_device_mem", "mge_tuned", "mge_set_precision",
+    "mge_cycle", "mge_cycle_async", "mge_cycle_poll", "mge_group_cycle_async", "mge_group_cycle_poll", "mge_prolong_async", "mge_set_coop_ctas", "mge_device_mem", "mge_tuned", "mge_set_precision",
     "mge_coop_trace", "mge_last_cycle_ms", "mge_launch_count", "mge_kernel_times", "mge_residual_norm_noalloc", "mge_euler_partial", "mge_device_bytes", "mge_sync",
     "mge_upload_solut", "mge_write_restart", "mge_read_restart", "mge_restart_format", "mge_restart_parse",
     "mge_time_advance",

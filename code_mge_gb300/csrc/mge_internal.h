@@ -148,6 +148,69 @@ struct EulerLaunch {
   int max_ctas;               // cap on the cooperative grid (0: occupancy limit)
 };
 
+// ---------------------------------------------------------------- several cases per launch
+// The same phase of a group of cases (one block per case: the blocks of one
+// level) in one launch.  Item kinds: the count of work items one case has
+// for a phase; every case's range is rounded up to whole 256-thread blocks.
+enum MultiKind {
+  MK_PHYS = 0,   // physical cells nx*ny*nz
+  MK_PREP,       // [1..ie]^3
+  MK_FACE,       // [2..ie]^3
+  MK_N,          // all cells N
+  MK_N5,         // 5N
+  MK_REC,        // cut-cell records
+  MK_IRS0,       // 5 * lines along i, j, k
+  MK_IRS1,
+  MK_IRS2,
+  MK_BC,         // boundary-pass items
+  MK_CORNER0,    // corner phases
+  MK_CORNER1,
+  MK_CORNER2,
+  MK_RTP,        // 256 * residual partial sums
+  MK_ONE,        // one thread block
+  MK_COUNT
+};
+
+// device arrays of one level of a group (built by the runtime)
+struct MultiLevel {
+  int nc = 0;
+  bool f32 = false, aux32 = false, fast = false;
+  void* B = nullptr;             // DevBlock<T>[nc]
+  PhysParams* P = nullptr;       // [nc]
+  unsigned** err = nullptr;      // [nc]
+  IrsTables* tab = nullptr;      // [3 nc]
+  double** rt_partial = nullptr; // [nc]
+  int* npart = nullptr;          // [nc]
+  double** rt_out = nullptr;     // [nc]
+  long long* off[MK_COUNT] = {};  // [nc + 1] per kind
+  long long tot[MK_COUNT] = {};
+};
+
+// the transfer between two levels of a group: child block f of each case and
+// its parent c on the level above
+enum MultiPairKind { MP_COLLC = 0, MP_CN, MP_FPHYS, MP_FN, MP_COUNT };
+struct MultiPair {
+  int nc = 0;
+  bool c32 = false, f32 = false;
+  void* C = nullptr;             // DevBlock<TC>[nc]
+  void* F = nullptr;             // DevBlock<TF>[nc]
+  void* X = nullptr;             // Xfer[nc]
+  uint8_t** marker = nullptr;    // [nc] the parents' markers
+  double** dc = nullptr;         // [nc] the cases' stage scratch
+  PhysParams* P = nullptr;       // [nc]
+  long long* off[MP_COUNT] = {};
+  long long tot[MP_COUNT] = {};
+};
+
+// the lockstep steps of the group cycle (mge_kernels.cu)
+void multi_euler(const MultiLevel& L, const StageArgs* A, int mstage, bool with_timestep, bool lfir, bool rt,
+                 cudaStream_t s);
+void multi_movco_level(const MultiLevel& L, const MultiPair* pair, cudaStream_t s);
+void multi_movfin_level(const MultiLevel& L, const MultiPair& pair, bool fmg, cudaStream_t s);
+void gather_residuals(const MultiLevel& L, double* res, unsigned* errs, cudaStream_t s);
+size_t xfer_size();
+void make_xfer_host(const int ratio[3], const int offset[3], void* out);
+
 // kernel launchers (mge_kernels.cu)
 template <typename T> int launch_euler_coop(const DevBlock<T>& b, const PhysParams& P, const EulerLaunch& L, int device,
                                             cudaStream_t s, bool aux32 = false);

@@ -2166,12 +2166,15 @@ __global__ void k_rtrms_final(const double* partial, int npart, double ncell, do
 
 // --------------------------------------------------------------- small whole-array kernels
 template <typename T>
-__global__ void k_depvars_all(DevBlock<T> b, double gamma) {
-  long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void body_depvars(const DevBlock<T>& b, double gamma, long long c) {
   if (c >= b.N) return;
   T wv[5];
   for (int v = 0; v < 5; v++) wv[v] = b.w[v * b.N + c];
   b.p[c] = depvars((T)gamma, wv);
+}
+template <typename T>
+__global__ void k_depvars_all(DevBlock<T> b, double gamma) {
+  body_depvars(b, gamma, (long long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 template <typename T>
@@ -2203,14 +2206,17 @@ __global__ void k_save_wn(DevBlock<T> b) {
 
 // wn = w on physical cells only (movco.f90:29-35)
 template <typename T>
-__global__ void k_copy_wn(DevBlock<T> b) {
-  long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void body_copy_wn(const DevBlock<T>& b, long long c) {
   if (c >= b.N) return;
   int i = (int)(c % b.Pi);
   int j = (int)((c / b.Pi) % b.Pj);
   int k = (int)(c / ((long long)b.Pi * b.Pj));
   if (!(i >= 2 && i <= b.il && j >= 2 && j <= b.jl && k >= 2 && k <= b.kl)) return;
   for (int v = 0; v < 5; v++) b.wn[v * b.N + c] = b.w[v * b.N + c];
+}
+template <typename T>
+__global__ void k_copy_wn(DevBlock<T> b) {
+  body_copy_wn(b, (long long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 template <typename T>
@@ -2245,9 +2251,13 @@ struct Xfer {
 
 // collc.f90:58-158 for the coarse cells under one child
 template <typename TC, typename TF>
-__global__ void k_collc(DevBlock<TC> c, DevBlock<TF> f, Xfer X, uint8_t* marker) {
+__device__ __forceinline__ long long collc_items(const DevBlock<TC>&, const DevBlock<TF>& f, const Xfer& X) {
+  return (long long)(f.nx / X.r[0]) * (f.ny / X.r[1]) * (f.nz / X.r[2]);
+}
+template <typename TC, typename TF>
+__device__ __forceinline__ void body_collc(const DevBlock<TC>& c, const DevBlock<TF>& f, const Xfer& X,
+                                           uint8_t* marker, long long t) {
   const int n0 = f.nx / X.r[0], n1 = f.ny / X.r[1], n2 = f.nz / X.r[2];
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long long)n0 * n1 * n2) return;
   int ic[3] = {X.o[0] + 2 + (int)(t % n0), X.o[1] + 2 + (int)((t / n0) % n1), X.o[2] + 2 + (int)(t / ((long long)n0 * n1))};
   if (ic[0] < 2 || ic[0] > c.il || ic[1] < 2 || ic[1] > c.jl || ic[2] < 2 || ic[2] > c.kl) return;
@@ -2288,6 +2298,10 @@ __global__ void k_collc(DevBlock<TC> c, DevBlock<TF> f, Xfer X, uint8_t* marker)
   }
   marker[cc] = 1;
 }
+template <typename TC, typename TF>
+__global__ void k_collc(DevBlock<TC> c, DevBlock<TF> f, Xfer X, uint8_t* marker) {
+  body_collc(c, f, X, marker, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
 
 __device__ __forceinline__ bool fine_to_coarse(const Xfer& X, int ncp0, int ncp1, int ncp2, int lc0, int lc1, int lc2,
                                                int i, int j, int k, int* sh, double* fac) {
@@ -2312,18 +2326,21 @@ __device__ __forceinline__ bool fine_to_coarse(const Xfer& X, int ncp0, int ncp1
 // the coarse correction w_c - ws_c of every coarse cell, formed once for the
 // 64 fine cells whose interpolation takes it (the same subtraction)
 template <typename TC>
-__global__ void k_addw_diff(DevBlock<TC> c, double* dc) {
-  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void body_addw_diff(const DevBlock<TC>& c, double* dc, long long q) {
   if (q >= c.N) return;
 #pragma unroll
   for (int v = 0; v < 5; v++) dc[v * c.N + q] = (double)c.w[v * c.N + q] - (double)c.ws[v * c.N + q];
+}
+template <typename TC>
+__global__ void k_addw_diff(DevBlock<TC> c, double* dc) {
+  body_addw_diff(c, dc, (long long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // addw.f90:83-188: w_f = store_w + I(w_c - ws_c), or I(w_c) in the FMG step;
 // dc holds w_c - ws_c (k_addw_diff) unless fmg
 template <typename TF, typename TC>
-__global__ void k_addw(DevBlock<TF> f, DevBlock<TC> c, Xfer X, int fmg, const double* dc) {
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void body_addw(const DevBlock<TF>& f, const DevBlock<TC>& c, const Xfer& X, int fmg,
+                                          const double* dc, long long t) {
   if (t >= (long long)f.nx * f.ny * f.nz) return;
   int i = 2 + (int)(t % f.nx), j = 2 + (int)((t / f.nx) % f.ny), k = 2 + (int)(t / ((long long)f.nx * f.ny));
   int sh[3];
@@ -2346,6 +2363,10 @@ __global__ void k_addw(DevBlock<TF> f, DevBlock<TC> c, Xfer X, int fmg, const do
     else
       f.w[v * f.N + q] = (TF)((double)f.w[v * f.N + q] + acc);
   }
+}
+template <typename TF, typename TC>
+__global__ void k_addw(DevBlock<TF> f, DevBlock<TC> c, Xfer X, int fmg, const double* dc) {
+  body_addw(f, c, X, fmg, dc, (long long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // bc_overlap.f90:32-90: ghost cell dst[t] of block g takes the trilinear
@@ -2376,8 +2397,8 @@ __global__ void k_overlap(DevBlock<T> g, DevBlock<T> p, const long long* __restr
 
 // bc_embed.f90:47-143: fine ghost cells whose centre lies in the parent
 template <typename TF, typename TC>
-__global__ void k_embed(DevBlock<TF> f, DevBlock<TC> c, Xfer X, double gamma) {
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void body_embed(const DevBlock<TF>& f, const DevBlock<TC>& c, const Xfer& X, double gamma,
+                                           long long t) {
   if (t >= f.N) return;
   int i = (int)(t % f.Pi), j = (int)((t / f.Pi) % f.Pj), k = (int)(t / ((long long)f.Pi * f.Pj));
   if (i >= 2 && i <= f.il && j >= 2 && j <= f.jl && k >= 2 && k <= f.kl) return;
@@ -2400,6 +2421,10 @@ __global__ void k_embed(DevBlock<TF> f, DevBlock<TC> c, Xfer X, double gamma) {
     }
   }
   f.p[q] = depvars((TF)gamma, wv);
+}
+template <typename TF, typename TC>
+__global__ void k_embed(DevBlock<TF> f, DevBlock<TC> c, Xfer X, double gamma) {
+  body_embed(f, c, X, gamma, (long long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // upload_solut.f90:203-237: the cell-centre output variables of the physical
@@ -2528,8 +2553,7 @@ __global__ void __launch_bounds__(256, 3) k_face_roe(DevBlock<T> b, PhysParams P
 // face fluxes efs(q) = 0.5*(F(q) + F(q-1)), the same expression as face_dir,
 // in a kernel small enough to keep the memory system busy
 template <typename T>
-__global__ void __launch_bounds__(256) k_face_conv(DevBlock<T> b) {
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void body_face_conv(const DevBlock<T>& b, long long t) {
   const int ex = b.ie - 1, ey = b.je - 1;
   if (t >= (long long)ex * ey * (b.ke - 1)) return;
   const int i = 2 + (int)(t % ex), j = 2 + (int)((t / ex) % ey), k = 2 + (int)(t / ((long long)ex * ey));
@@ -2544,6 +2568,10 @@ __global__ void __launch_bounds__(256) k_face_conv(DevBlock<T> b) {
 #pragma unroll
     for (int v = 0; v < 5; v++) E[v * N + c] = mulhalf(F[v * N + c] + F[v * N + c - sts[d]]);
   }
+}
+template <typename T>
+__global__ void __launch_bounds__(256) k_face_conv(DevBlock<T> b) {
+  body_face_conv(b, (long long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 template <typename T, bool FAST = false>
 __global__ void k_combine(DevBlock<T> b, PhysParams P, StageArgs A, unsigned* err) {
@@ -2686,6 +2714,213 @@ __global__ void __launch_bounds__(256, 1) k_euler_coop(DevBlock<T> b, PhysParams
   }
   if (E.trace && blockIdx.x == 0 && threadIdx.x == 0) E.trace[255] = (unsigned long long)ntr;
 }
+
+// =============================================================== several cases in one launch
+// The same phase of a group of cases in one launch: the cases' work items
+// laid end to end, each case's range rounded up to whole 256-thread blocks,
+// so that a thread block serves one case (the per-block reductions of the
+// time step minimum and the residual partial sums stay within a case).
+// Each case runs the same bodies in the same order as alone, so its results
+// are those of its own launches.
+template <typename T>
+struct MultiArgs {
+  const DevBlock<T>* B;
+  const PhysParams* P;
+  unsigned* const* err;
+  const IrsTables* tab;
+  double* const* rt_partial;
+  const int* npart;
+  double* const* rt_out;
+  const long long* off;
+  int nc;
+};
+
+__device__ __forceinline__ int multi_case(const long long* off, int nc, long long base) {
+  __shared__ int sq;
+  if (threadIdx.x == 0) {
+    int q = 0;
+    while (q + 1 < nc && off[q + 1] <= base) q++;
+    sq = q;
+  }
+  __syncthreads();
+  return sq;
+}
+
+template <typename T, typename F>
+__global__ void __launch_bounds__(256) k_multi(MultiArgs<T> M, F f) {
+  const long long base = (long long)blockIdx.x * 256;
+  const int q = multi_case(M.off, M.nc, base);
+  f(M, q, base - M.off[q] + threadIdx.x);
+}
+
+template <typename T> struct FDtimReset {
+  __device__ void operator()(const MultiArgs<T>& M, int q, long long t) const {
+    if (t == 0) *M.B[q].dtim = 10.0;
+  }
+};
+template <typename T, typename TC> struct FTimestep {
+  __device__ void operator()(const MultiArgs<T>& M, int q, long long t) const {
+    const DevBlock<T>& b = M.B[q];
+    unsigned long long mine = ~0ull;
+    if (t < (long long)b.nx * b.ny * b.nz) mine = body_timestep<T, TC>(b, M.P[q], M.err[q], t);
+    block_min_to(mine, b.dtim);
+  }
+};
+template <typename T> struct FCopyWs {
+  __device__ void operator()(const MultiArgs<T>& M, int q, long long t) const {
+    const DevBlock<T>& b = M.B[q];
+    if (t < 5 * b.N) b.ws[t] = b.w[t];
+  }
+};
+template <typename T> struct FSaveWn {
+  __device__ void operator()(const MultiArgs<T>& M, int q, long long t) const {
+    if (t < M.B[q].N) body_save_wn(M.B[q], t);
+  }
+};
+template <typename T, bool FAST> struct FPrep {
+  int dissip_on;
+  __device__ void operator()(const MultiArgs<T>& M, int q, long long t) const {
+    const DevBlock<T>& b = M.B[q];
+    if (t < (long long)b.ie * b.je * b.ke) body_prep<T, false, FAST>(b, M.P[q], dissip_on, t);
+  }
+};
+template <typename T> struct FFace {
+  int dissip_on;
+  T cd;
+  __device__ void operator()(const MultiArgs<T>& M, int q, long long t) const {
+    const DevBlock<T>& b = M.B[q];
+    if (t < (long long)(b.ie - 1) * (b.je - 1) * (b.ke - 1)) body_face<T, FACE_CENTRAL>(b, M.P[q], dissip_on, cd, t);
+  }
+};
+template <typename T> struct FFaceConv {
+  __device__ void operator()(const MultiArgs<T>& M, int q, long long t) const { body_face_conv(M.B[q], t); }
+};
+template <typename T> struct FFaceDiss {
+  T cd;
+  __device__ void operator()(const MultiArgs<T>& M, int q, long long t) const {
+    const DevBlock<T>& b = M.B[q];
+    if (t < (long long)(b.ie - 1) * (b.je - 1) * (b.ke - 1)) body_face_diss<T>(b, M.P[q], cd, t);
+  }
+};
+template <typename T> struct FRec {
+  int dissip_on;
+  T cd;
+  __device__ void operator()(const MultiArgs<T>& M, int q, long long t) const {
+    if (t < M.B[q].nmir) rec_wall_terms(M.B[q], M.P[q], dissip_on, cd, M.err[q], (int)t);
+  }
+};
+template <typename T, bool FAST> struct FCombine {
+  StageArgs A;
+  __device__ void operator()(const MultiArgs<T>& M, int q, long long t) const {
+    const DevBlock<T>& b = M.B[q];
+    if (t < (long long)b.nx * b.ny * b.nz) body_combine<T, FAST>(b, M.P[q], A, M.err[q], t);
+  }
+};
+template <typename T, typename TC, int D> struct FIrs {
+  __device__ void operator()(const MultiArgs<T>& M, int q, long long t) const {
+    const DevBlock<T>& b = M.B[q];
+    if (t < 5 * irs_lines<T, D>(b)) body_irs<T, TC, D>(b, M.tab[3 * q + D], (TC)(-M.P[q].smoo), t);
+  }
+};
+// the mixed form's finest level: FP32 sweeps on one FP32 copy of dw (in F)
+template <typename TS, typename TO, int D> struct FIrsMixed {
+  __device__ void operator()(const MultiArgs<double>& M, int q, long long t) const {
+    const DevBlock<double>& b = M.B[q];
+    if (t >= 5 * irs_lines<double, D>(b)) return;
+    float* cp = (float*)b.F;
+    const TS* src = D == 0 ? (const TS*)b.dw : (const TS*)cp;
+    TO* out = D == 2 ? (TO*)b.dw : (TO*)cp;
+    body_irs_mixed<TS, TO, D>(b, M.tab[3 * q + D], (float)(-M.P[q].smoo), src, cp, out, t);
+  }
+};
+template <typename T> struct FUpdate {
+  StageArgs A;
+  __device__ void operator()(const MultiArgs<T>& M, int q, long long t) const {
+    const DevBlock<T>& b = M.B[q];
+    if (t < (long long)b.nx * b.ny * b.nz) body_update(b, M.P[q], A, t);
+  }
+};
+template <typename T> struct FCutcell {
+  __device__ void operator()(const MultiArgs<T>& M, int q, long long t) const {
+    if (t < M.B[q].nmir) body_cutcell(M.B[q], M.P[q], M.err[q], (int)t);
+  }
+};
+template <typename T> struct FBcPass {
+  int pass;
+  __device__ void operator()(const MultiArgs<T>& M, int q, long long t) const {
+    if (t < bc_pass_items(M.B[q])) body_bc_pass(M.B[q], M.P[q], pass, t);
+  }
+};
+template <typename T> struct FCorner {
+  int phase;
+  __device__ void operator()(const MultiArgs<T>& M, int q, long long t) const {
+    if (t < corner_items(M.B[q], phase)) body_corner_item(M.B[q], M.P[q], phase, (int)t);
+  }
+};
+template <typename T> struct FDepvars {
+  __device__ void operator()(const MultiArgs<T>& M, int q, long long t) const { body_depvars(M.B[q], M.P[q].gamma, t); }
+};
+template <typename T> struct FCopyWn {
+  __device__ void operator()(const MultiArgs<T>& M, int q, long long t) const { body_copy_wn(M.B[q], t); }
+};
+// residual partial sums: thread block (case, part), 256 threads each
+template <typename T> struct FRtrmsPartial {
+  __device__ void operator()(const MultiArgs<T>& M, int q, long long t) const {
+    const int part = (int)(t / 256);
+    if (part < M.npart[q]) body_rtrms_partial(M.B[q], M.P[q].cfl, M.P[q].vt, M.rt_partial[q], M.npart[q], part);
+  }
+};
+template <typename T> struct FRtrmsFinal {
+  __device__ void operator()(const MultiArgs<T>& M, int q, long long t) const {
+    const DevBlock<T>& b = M.B[q];
+    if (t < 32) body_rtrms_final(M.rt_partial[q], M.npart[q], (double)b.nx * b.ny * b.nz, M.rt_out[q], M.err[q]);
+  }
+};
+
+// the transfers between the levels of a group: child f and parent c of each case
+template <typename TC, typename TF>
+struct MultiPairArgs {
+  const DevBlock<TC>* C;
+  const DevBlock<TF>* F;
+  const Xfer* X;
+  uint8_t* const* marker;
+  double* const* dc;
+  const PhysParams* P;
+  const long long* off;
+  int nc;
+};
+template <typename TC, typename TF, typename Fn>
+__global__ void __launch_bounds__(256) k_multi2(MultiPairArgs<TC, TF> M, Fn f) {
+  const long long base = (long long)blockIdx.x * 256;
+  const int q = multi_case(M.off, M.nc, base);
+  f(M, q, base - M.off[q] + threadIdx.x);
+}
+template <typename TC, typename TF> struct FMarkerClear {
+  __device__ void operator()(const MultiPairArgs<TC, TF>& M, int q, long long t) const {
+    if (t < M.C[q].N) M.marker[q][t] = 0;
+  }
+};
+template <typename TC, typename TF> struct FCollc {
+  __device__ void operator()(const MultiPairArgs<TC, TF>& M, int q, long long t) const {
+    body_collc(M.C[q], M.F[q], M.X[q], M.marker[q], t);
+  }
+};
+template <typename TC, typename TF> struct FAddwDiff {
+  __device__ void operator()(const MultiPairArgs<TC, TF>& M, int q, long long t) const {
+    body_addw_diff(M.C[q], M.dc[q], t);
+  }
+};
+template <typename TC, typename TF> struct FAddw {
+  int fmg;
+  __device__ void operator()(const MultiPairArgs<TC, TF>& M, int q, long long t) const {
+    body_addw(M.F[q], M.C[q], M.X[q], fmg, M.dc[q], t);
+  }
+};
+template <typename TC, typename TF> struct FEmbed {
+  __device__ void operator()(const MultiPairArgs<TC, TF>& M, int q, long long t) const {
+    body_embed(M.F[q], M.C[q], M.X[q], M.P[q].gamma, t);
+  }
+};
 
 // =============================================================== launchers
 constexpr int TPB = 256;
@@ -3072,6 +3307,187 @@ void launch_forces(const DevBlock<T>& b, const double* origin, const double* h, 
                    double* out7, cudaStream_t s) {
   k_forces<T><<<1, 256, 0, s>>>(b, origin[0], origin[1], origin[2], h[0], h[1], h[2], center[0], center[1], center[2],
                                 mu, out7);
+}
+
+// --------------------------------------------------------------- a group's lockstep steps
+size_t xfer_size() { return sizeof(Xfer); }
+void make_xfer_host(const int ratio[3], const int offset[3], void* out) {
+  Xfer X = make_xfer(ratio, offset);
+  memcpy(out, &X, sizeof(Xfer));
+}
+
+template <typename T, typename F>
+static void go_multi(const MultiLevel& L, MultiArgs<T>& M, int kind, F f, cudaStream_t s) {
+  if (L.tot[kind] <= 0) return;
+  M.off = L.off[kind];
+  k_multi<T, F><<<(unsigned)(L.tot[kind] / 256), 256, 0, s>>>(M, f);
+}
+
+template <typename T>
+static MultiArgs<T> multi_args(const MultiLevel& L) {
+  return MultiArgs<T>{(const DevBlock<T>*)L.B, L.P, L.err, L.tab, L.rt_partial, L.npart, L.rt_out, nullptr, L.nc};
+}
+
+template <typename T>
+static void multi_bcond(const MultiLevel& L, MultiArgs<T>& M, cudaStream_t s) {
+  for (int pass = 0; pass < 3; pass++) go_multi(L, M, MK_BC, FBcPass<T>{pass}, s);
+  go_multi(L, M, MK_CORNER0, FCorner<T>{0}, s);
+  go_multi(L, M, MK_CORNER1, FCorner<T>{1}, s);
+  go_multi(L, M, MK_CORNER2, FCorner<T>{2}, s);
+}
+
+// timestep (optionally) and euler.f90:1-462 on one block of every case: the
+// phases of enqueue_euler's per-phase path (line sweeps in global memory)
+template <typename T>
+static void multi_euler_t(const MultiLevel& L, const StageArgs* A, int mstage, bool with_timestep, bool lfir,
+                          bool rt, cudaStream_t s) {
+  MultiArgs<T> M = multi_args<T>(L);
+  if (with_timestep) {
+    go_multi(L, M, MK_ONE, FDtimReset<T>{}, s);
+    if (L.aux32)
+      go_multi(L, M, MK_PHYS, FTimestep<T, float>{}, s);
+    else
+      go_multi(L, M, MK_PHYS, FTimestep<T, T>{}, s);
+  }
+  if (lfir) go_multi(L, M, MK_N5, FCopyWs<T>{}, s);
+  go_multi(L, M, MK_N, FSaveWn<T>{}, s);
+  for (int m = 1; m <= mstage; m++) {
+    const StageArgs& a = A[m - 1];
+    if (L.fast) {
+      go_multi(L, M, MK_PREP, FPrep<T, true>{a.dissip_on}, s);
+      if (a.dissip_on) go_multi(L, M, MK_FACE, FFaceDiss<T>{(T)a.cd}, s);
+    } else {
+      go_multi(L, M, MK_PREP, FPrep<T, false>{a.dissip_on}, s);
+      if (a.dissip_on)
+        go_multi(L, M, MK_FACE, FFace<T>{a.dissip_on, (T)a.cd}, s);
+      else
+        go_multi(L, M, MK_FACE, FFaceConv<T>{}, s);
+    }
+    go_multi(L, M, MK_REC, FRec<T>{a.dissip_on, (T)a.cd}, s);
+    if (L.fast)
+      go_multi(L, M, MK_PHYS, FCombine<T, true>{a}, s);
+    else
+      go_multi(L, M, MK_PHYS, FCombine<T, false>{a}, s);
+    if (a.lres) return;
+    if (a.irs) {
+      if constexpr (std::is_same<T, double>::value) {
+        if (L.aux32) {
+          go_multi(L, M, MK_IRS0, FIrsMixed<double, float, 0>{}, s);
+          go_multi(L, M, MK_IRS1, FIrsMixed<float, float, 1>{}, s);
+          go_multi(L, M, MK_IRS2, FIrsMixed<float, double, 2>{}, s);
+        } else {
+          go_multi(L, M, MK_IRS0, FIrs<T, T, 0>{}, s);
+          go_multi(L, M, MK_IRS1, FIrs<T, T, 1>{}, s);
+          go_multi(L, M, MK_IRS2, FIrs<T, T, 2>{}, s);
+        }
+      } else {
+        go_multi(L, M, MK_IRS0, FIrs<T, T, 0>{}, s);
+        go_multi(L, M, MK_IRS1, FIrs<T, T, 1>{}, s);
+        go_multi(L, M, MK_IRS2, FIrs<T, T, 2>{}, s);
+      }
+      go_multi(L, M, MK_PHYS, FUpdate<T>{a}, s);
+    }
+    go_multi(L, M, MK_REC, FCutcell<T>{}, s);
+    multi_bcond(L, M, s);
+  }
+  if (rt) {
+    go_multi(L, M, MK_RTP, FRtrmsPartial<T>{}, s);
+    go_multi(L, M, MK_ONE, FRtrmsFinal<T>{}, s);
+  }
+}
+
+// every case's residual of the cycle and its error word, into two arrays
+template <typename T> struct FGather {
+  double* res;
+  unsigned* errs;
+  __device__ void operator()(const MultiArgs<T>& M, int q, long long t) const {
+    if (t == 0) {
+      res[q] = *M.rt_out[q];
+      errs[q] = *M.err[q];
+    }
+  }
+};
+
+void gather_residuals(const MultiLevel& L, double* res, unsigned* errs, cudaStream_t s) {
+  if (L.f32) {
+    MultiArgs<float> M = multi_args<float>(L);
+    go_multi(L, M, MK_ONE, FGather<float>{res, errs}, s);
+  } else {
+    MultiArgs<double> M = multi_args<double>(L);
+    go_multi(L, M, MK_ONE, FGather<double>{res, errs}, s);
+  }
+}
+
+void multi_euler(const MultiLevel& L, const StageArgs* A, int mstage, bool with_timestep, bool lfir, bool rt,
+                 cudaStream_t s) {
+  if (L.f32)
+    multi_euler_t<float>(L, A, mstage, with_timestep, lfir, rt, s);
+  else
+    multi_euler_t<double>(L, A, mstage, with_timestep, lfir, rt, s);
+}
+
+template <typename TC, typename TF, typename F>
+static void go_pair(const MultiPair& Pp, MultiPairArgs<TC, TF>& M, int kind, F f, cudaStream_t s) {
+  if (Pp.tot[kind] <= 0) return;
+  M.off = Pp.off[kind];
+  k_multi2<TC, TF, F><<<(unsigned)(Pp.tot[kind] / 256), 256, 0, s>>>(M, f);
+}
+
+template <typename TC, typename TF>
+static MultiPairArgs<TC, TF> pair_args(const MultiPair& Pp) {
+  return MultiPairArgs<TC, TF>{(const DevBlock<TC>*)Pp.C, (const DevBlock<TF>*)Pp.F, (const Xfer*)Pp.X, Pp.marker,
+                               Pp.dc, Pp.P, nullptr, Pp.nc};
+}
+
+// the pair's precisions: (coarse, fine) in {(double, double), (float, double), (float, float)}
+template <typename Fn>
+static void with_pair_types(const MultiPair& Pp, Fn&& fn) {
+  if (!Pp.c32 && !Pp.f32)
+    fn((double*)nullptr, (double*)nullptr);
+  else if (Pp.c32 && !Pp.f32)
+    fn((float*)nullptr, (double*)nullptr);
+  else
+    fn((float*)nullptr, (float*)nullptr);
+}
+
+// movco.f90:21-47 for the group: restriction of each case's child onto its
+// block on this level, depvars, wn, bcond (one block per level: no overlap)
+void multi_movco_level(const MultiLevel& L, const MultiPair* pair, cudaStream_t s) {
+  if (pair)
+    with_pair_types(*pair, [&](auto* tc, auto* tf) {
+      using TC = std::remove_pointer_t<decltype(tc)>;
+      using TF = std::remove_pointer_t<decltype(tf)>;
+      MultiPairArgs<TC, TF> M = pair_args<TC, TF>(*pair);
+      go_pair(*pair, M, MP_CN, FMarkerClear<TC, TF>{}, s);
+      go_pair(*pair, M, MP_COLLC, FCollc<TC, TF>{}, s);
+    });
+  auto rest = [&](auto* tp) {
+    using T = std::remove_pointer_t<decltype(tp)>;
+    MultiArgs<T> M = multi_args<T>(L);
+    go_multi(L, M, MK_N, FDepvars<T>{}, s);
+    go_multi(L, M, MK_N, FCopyWn<T>{}, s);
+    multi_bcond(L, M, s);
+  };
+  if (L.f32)
+    rest((float*)nullptr);
+  else
+    rest((double*)nullptr);
+}
+
+// movfin.f90:20-39 for the group: prolongation from each case's parent,
+// depvars, bc_embed, bcond
+void multi_movfin_level(const MultiLevel& L, const MultiPair& pair, bool fmg, cudaStream_t s) {
+  with_pair_types(pair, [&](auto* tc, auto* tf) {
+    using TC = std::remove_pointer_t<decltype(tc)>;
+    using TF = std::remove_pointer_t<decltype(tf)>;
+    MultiPairArgs<TC, TF> M = pair_args<TC, TF>(pair);
+    if (!fmg) go_pair(pair, M, MP_CN, FAddwDiff<TC, TF>{}, s);
+    go_pair(pair, M, MP_FPHYS, FAddw<TC, TF>{fmg ? 1 : 0}, s);
+    MultiArgs<TF> F = multi_args<TF>(L);
+    go_multi(L, F, MK_N, FDepvars<TF>{}, s);
+    go_pair(pair, M, MP_FN, FEmbed<TC, TF>{}, s);
+    multi_bcond(L, F, s);
+  });
 }
 
 // explicit instantiations

@@ -7,6 +7,7 @@
 // movco.f90, movfin.f90, solver.f90); mge_solve runs solver.f90's FMG loop
 // with each multigrid cycle captured once per FMG level and replayed.
 #include <algorithm>
+#include <atomic>
 #include <type_traits>
 #include <cmath>
 #include <cstdio>
@@ -130,6 +131,10 @@ struct mge_ctx {
   std::string plan;                      // fixed launch forms per level (MGE_TUNE_PLAN), instead of tuning
   int pending_mlvl = 0;                  // level of the cycle in flight (0: none)
   unsigned long long* coop_trace = nullptr;
+  unsigned long long uid = 0;            // process-unique id (group plans key on it)
+  unsigned gen = 0;                      // bumped whenever device fields move (precision switch)
+  void* group_pending = nullptr;         // the group plan whose cycle this case is in
+  cudaEvent_t ev_group = nullptr;        // this case's stream, ahead of a group cycle
 };
 
 namespace {
@@ -680,6 +685,10 @@ int commit_block(mge_ctx* c, Block& b, double* scratch) {
 }  // namespace
 
 // ====================================================================== C-ABI
+namespace {
+void drop_group_plans(const mge_ctx* c);  // the group plans that hold this case (below)
+}
+
 extern "C" {
 
 int mge_abi_version(void) { return MGE_ABI_VERSION; }
@@ -737,6 +746,10 @@ int mge_init(const mge_params* prm, int device, mge_ctx** out) {
   if (prm->irs_variant != 0 && prm->irs_variant != 1) return MGE_EBADCFG;
   if (prm->execmode != 0 && (prm->execmode != 1 || !(prm->dtstep > 0.0))) return MGE_EBADCFG;
   mge_ctx* c = new mge_ctx();
+  {
+    static std::atomic<unsigned long long> next_uid{1};
+    c->uid = next_uid++;
+  }
   c->prm = *prm;
   c->device = device;
   cudaError_t e = cudaSetDevice(device);
@@ -768,7 +781,9 @@ int mge_init(const mge_params* prm, int device, mge_ctx** out) {
 void mge_destroy(mge_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
+  drop_group_plans(c);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->ev_group) cudaEventDestroy(c->ev_group);
   for (cudaGraphExec_t g : c->graphs)
     if (g) cudaGraphExecDestroy(g);
   if (c->ev0) cudaEventDestroy(c->ev0);
@@ -1187,6 +1202,7 @@ int mge_set_precision(mge_ctx* c, int precision) {
       g = nullptr;
     }
   c->prm.precision = precision;
+  c->gen++;  // group plans holding this case's old fields are stale
   CK(cudaGetLastError());
   return check_err(c);
 }
@@ -1795,6 +1811,415 @@ int mge_sync(mge_ctx* c) {
   if (!c) return MGE_EBADCFG;
   CK(cudaSetDevice(c->device));
   return check_err(c);
+}
+
+}  // extern "C"
+
+// ================================================================ groups of cases in lockstep
+// Many cases (one context each) advance one multigrid cycle together: every
+// phase of the cycle runs as one launch over the block of that level of
+// every case (mge_kernels.cu, multi_*), whatever the cases' sizes, and the
+// whole lockstep cycle is one captured CUDA graph.  Each case runs the same
+// bodies in the same order as its own per-phase path, so its results are
+// those it would have alone.
+namespace {
+
+struct GroupPlan {
+  std::vector<mge_ctx*> cases;
+  std::vector<std::pair<unsigned long long, unsigned>> key;  // (uid, gen) per case
+  int mlvl = 0, device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, done = nullptr;
+  std::vector<MultiLevel> lv;  // per level
+  std::vector<MultiPair> pr;   // pr[l]: level l+1 (coarse) and l+2 (fine), 0-based l
+  std::vector<void*> allocs;
+  cudaGraphExec_t graph = nullptr;
+  long long graph_kernels = 0;
+  double* d_res = nullptr;     // gathered residuals of the cycle (one per case)
+  unsigned* d_errs = nullptr;  // gathered error words
+  double* h_res = nullptr;     // pinned
+  unsigned* h_errs = nullptr;  // pinned
+  unsigned long long last_use = 0;
+};
+
+std::mutex g_group_mu;
+std::vector<GroupPlan*> g_plans;
+unsigned long long g_plan_clock = 0;
+constexpr size_t kMaxPlans = 24;
+
+void destroy_plan(GroupPlan* G) {
+  cudaSetDevice(G->device);
+  if (G->stream) cudaStreamSynchronize(G->stream);
+  if (G->graph) cudaGraphExecDestroy(G->graph);
+  for (void* p : G->allocs) cudaFree(p);
+  if (G->h_res) cudaFreeHost(G->h_res);
+  if (G->h_errs) cudaFreeHost(G->h_errs);
+  if (G->ev0) cudaEventDestroy(G->ev0);
+  if (G->ev1) cudaEventDestroy(G->ev1);
+  if (G->done) cudaEventDestroy(G->done);
+  if (G->stream) cudaStreamDestroy(G->stream);
+  delete G;
+}
+
+template <typename T>
+int plan_upload(GroupPlan* G, T** dst, const std::vector<T>& v, std::string& why) {
+  void* p = nullptr;
+  if (cudaMalloc(&p, std::max<size_t>(v.size(), 1) * sizeof(T)) != cudaSuccess) {
+    cudaGetLastError();
+    why = "group: cudaMalloc";
+    return MGE_ENOMEM;
+  }
+  G->allocs.push_back(p);
+  if (!v.empty() && cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess) {
+    why = "group: cudaMemcpy";
+    return MGE_ECUDA;
+  }
+  *dst = (T*)p;
+  return MGE_OK;
+}
+
+// item counts of one case's block for each kind (MultiKind)
+void kind_counts(const Block& b, long long* n) {
+  const long long nx = b.nx, ny = b.ny, nz = b.nz;
+  n[MK_PHYS] = nx * ny * nz;
+  n[MK_PREP] = (nx + 2) * (ny + 2) * (nz + 2);
+  n[MK_FACE] = (nx + 1) * (ny + 1) * (nz + 1);
+  n[MK_N] = b.N;
+  n[MK_N5] = 5 * b.N;
+  n[MK_REC] = (long long)b.recs.size();
+  n[MK_IRS0] = 5 * ny * nz;
+  n[MK_IRS1] = 5 * nx * nz;
+  n[MK_IRS2] = 5 * nx * ny;
+  n[MK_BC] = 2 * ((long long)(b.jb + 1) * (b.kb + 1) + (long long)(b.ib + 1) * (b.kb + 1) +
+                  (long long)(b.ib + 1) * (b.jb + 1));
+  n[MK_CORNER0] = 4LL * (b.kl - 1) + 4LL * (b.jl - 1);
+  n[MK_CORNER1] = 4LL * (b.ib + 1);
+  n[MK_CORNER2] = 8;
+  n[MK_RTP] = 256LL * b.npart;
+  n[MK_ONE] = 1;
+}
+
+// prefix sums of counts rounded up to whole 256-thread blocks
+std::vector<long long> offsets(const std::vector<long long>& cnt) {
+  std::vector<long long> off(cnt.size() + 1, 0);
+  for (size_t q = 0; q < cnt.size(); q++) off[q + 1] = off[q] + (cnt[q] + 255) / 256 * 256;
+  return off;
+}
+
+// a plan for the cases, or an error (the cases cannot run in lockstep)
+int build_plan(mge_ctx* const* cs, int n, int mlvl, GroupPlan** out, std::string& why) {
+  mge_ctx* c0 = cs[0];
+  const mge_params& P0 = c0->prm;
+  const int nl = (int)c0->lv.size();
+  for (int q = 0; q < n; q++) {
+    const mge_ctx* c = cs[q];
+    const mge_params& P = c->prm;
+    if (!c->committed || c->device != c0->device) return why = "group: a case is not committed on this device", MGE_EBADCFG;
+    if ((int)c->lv.size() != nl || P.mstage != P0.mstage || P.mgtype != P0.mgtype || P.vt != P0.vt ||
+        P.cfl != P0.cfl || P.smoo != P0.smoo || P.irs_variant != 0 || P.execmode != 0 ||
+        P.distype != MGE_DIS_CENTRAL || P.eqntype != P0.eqntype || P.dissip != P0.dissip)
+      return why = "group: the cases' schedules or schemes differ", MGE_EBADCFG;
+    for (int m = 0; m < P.mstage; m++)
+      if (P.cstp[m] != P0.cstp[m] || P.cdis[m] != P0.cdis[m]) return why = "group: stage coefficients differ", MGE_EBADCFG;
+    for (int l = 0; l < nl; l++) {
+      if (c->lv[l].size() != 1) return why = "group: one block per level only", MGE_EBADCFG;
+      const Block& b = c->lv[l][0];
+      const Block& b0 = c0->lv[l][0];
+      if (b.f32 != b0.f32 || b.aux32 != b0.aux32 || b.fast != b0.fast)
+        return why = "group: the cases' precision forms differ", MGE_EBADCFG;
+    }
+    for (int r = 0; r < q; r++)
+      if (cs[r] == c) return why = "group: a case appears twice", MGE_EBADCFG;
+  }
+  GroupPlan* G = new GroupPlan();
+  G->cases.assign(cs, cs + n);
+  for (int q = 0; q < n; q++) G->key.push_back({cs[q]->uid, cs[q]->gen});
+  G->mlvl = mlvl;
+  G->device = c0->device;
+  int rc = MGE_OK;
+  auto bad = [&](int code) {
+    destroy_plan(G);
+    return code;
+  };
+  if (cudaStreamCreateWithFlags(&G->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&G->ev0) != cudaSuccess || cudaEventCreate(&G->ev1) != cudaSuccess ||
+      cudaEventCreateWithFlags(&G->done, cudaEventDisableTiming) != cudaSuccess)
+    return why = "group: stream or events", bad(MGE_ECUDA);
+  G->lv.resize(nl);
+  for (int l = 0; l < nl; l++) {
+    MultiLevel& L = G->lv[l];
+    const Block& b0 = c0->lv[l][0];
+    L.nc = n;
+    L.f32 = b0.f32;
+    L.aux32 = b0.aux32;
+    L.fast = b0.fast;
+    std::vector<DevBlock<double>> bd;
+    std::vector<DevBlock<float>> bf;
+    std::vector<PhysParams> pp;
+    std::vector<unsigned*> er;
+    std::vector<IrsTables> tb;
+    std::vector<double*> rp, ro;
+    std::vector<int> np;
+    std::vector<std::vector<long long>> cnt(MK_COUNT, std::vector<long long>(n));
+    for (int q = 0; q < n; q++) {
+      Block& b = cs[q]->lv[l][0];
+      if (b.f32)
+        bf.push_back(b.dev32);
+      else
+        bd.push_back(b.dev);
+      pp.push_back(cs[q]->P);
+      er.push_back(cs[q]->d_err);
+      for (int d = 0; d < 3; d++) tb.push_back(b.tabs[d]);
+      rp.push_back(b.rt_partial);
+      ro.push_back(b.rt_cur);
+      np.push_back(b.npart);
+      long long k[MK_COUNT];
+      kind_counts(b, k);
+      for (int m = 0; m < MK_COUNT; m++) cnt[m][q] = k[m];
+    }
+    if (L.f32)
+      rc = plan_upload(G, (DevBlock<float>**)&L.B, bf, why);
+    else
+      rc = plan_upload(G, (DevBlock<double>**)&L.B, bd, why);
+    if (!rc) rc = plan_upload(G, &L.P, pp, why);
+    if (!rc) rc = plan_upload(G, &L.err, er, why);
+    if (!rc) rc = plan_upload(G, &L.tab, tb, why);
+    if (!rc) rc = plan_upload(G, &L.rt_partial, rp, why);
+    if (!rc) rc = plan_upload(G, &L.npart, np, why);
+    if (!rc) rc = plan_upload(G, &L.rt_out, ro, why);
+    for (int m = 0; m < MK_COUNT && !rc; m++) {
+      std::vector<long long> off = offsets(cnt[m]);
+      L.tot[m] = off.back();
+      rc = plan_upload(G, &L.off[m], off, why);
+    }
+    if (rc) return bad(rc);
+  }
+  G->pr.resize(nl > 1 ? nl - 1 : 0);
+  for (int l = 0; l + 1 < nl; l++) {
+    MultiPair& M = G->pr[l];
+    M.nc = n;
+    M.c32 = G->lv[l].f32;
+    M.f32 = G->lv[l + 1].f32;
+    std::vector<DevBlock<double>> cd, fd;
+    std::vector<DevBlock<float>> cf, ff;
+    std::vector<unsigned char> xs(n * xfer_size());
+    std::vector<uint8_t*> mk;
+    std::vector<double*> dc;
+    std::vector<PhysParams> pp;
+    std::vector<std::vector<long long>> cnt(MP_COUNT, std::vector<long long>(n));
+    for (int q = 0; q < n; q++) {
+      Block& bc = cs[q]->lv[l][0];
+      Block& bf_ = cs[q]->lv[l + 1][0];
+      if (bf_.parent != 1) return why = "group: a fine block's parent is not the level's block", bad(MGE_EBADCFG);
+      if (bc.f32) cf.push_back(bc.dev32); else cd.push_back(bc.dev);
+      if (bf_.f32) ff.push_back(bf_.dev32); else fd.push_back(bf_.dev);
+      make_xfer_host(bf_.ratio, bf_.offset, xs.data() + q * xfer_size());
+      mk.push_back(bc.marker);
+      dc.push_back(cs[q]->scratch);
+      pp.push_back(cs[q]->P);
+      cnt[MP_COLLC][q] = (long long)(bf_.nx / bf_.ratio[0]) * (bf_.ny / bf_.ratio[1]) * (bf_.nz / bf_.ratio[2]);
+      cnt[MP_CN][q] = bc.N;
+      cnt[MP_FPHYS][q] = (long long)bf_.nx * bf_.ny * bf_.nz;
+      cnt[MP_FN][q] = bf_.N;
+    }
+    if (M.c32) rc = plan_upload(G, (DevBlock<float>**)&M.C, cf, why);
+    else rc = plan_upload(G, (DevBlock<double>**)&M.C, cd, why);
+    if (!rc) {
+      if (M.f32) rc = plan_upload(G, (DevBlock<float>**)&M.F, ff, why);
+      else rc = plan_upload(G, (DevBlock<double>**)&M.F, fd, why);
+    }
+    if (!rc) rc = plan_upload(G, (unsigned char**)&M.X, xs, why);
+    if (!rc) rc = plan_upload(G, &M.marker, mk, why);
+    if (!rc) rc = plan_upload(G, &M.dc, dc, why);
+    if (!rc) rc = plan_upload(G, &M.P, pp, why);
+    for (int m = 0; m < MP_COUNT && !rc; m++) {
+      std::vector<long long> off = offsets(cnt[m]);
+      M.tot[m] = off.back();
+      rc = plan_upload(G, &M.off[m], off, why);
+    }
+    if (rc) return bad(rc);
+  }
+  std::vector<double> z(n, 0.0);
+  std::vector<unsigned> ze(n, 0u);
+  if ((rc = plan_upload(G, &G->d_res, z, why)) || (rc = plan_upload(G, &G->d_errs, ze, why))) return bad(rc);
+  if (cudaMallocHost(&G->h_res, n * sizeof(double)) != cudaSuccess ||
+      cudaMallocHost(&G->h_errs, n * sizeof(unsigned)) != cudaSuccess)
+    return why = "group: pinned buffers", bad(MGE_ENOMEM);
+  *out = G;
+  return MGE_OK;
+}
+
+// euler on level `level` of every case (enqueue_euler's per-phase path)
+void group_euler(GroupPlan& G, int level, int mgl, int mlvl, bool lres, bool lfir, bool rt, bool with_timestep) {
+  const mge_params& P = G.cases[0]->prm;
+  StageArgs A[MGE_MAX_STAGE];
+  for (int m = 1; m <= P.mstage; m++) {
+    A[m - 1] = stage_args(P, m, mgl, mlvl, lres, lfir, 0);
+    A[m - 1].fast = G.lv[level - 1].fast;
+  }
+  multi_euler(G.lv[level - 1], A, P.mstage, with_timestep, lfir, rt && !lres, G.stream);
+}
+
+// solver.f90:127-234 for the group: enqueue_cycle with one launch per phase for all cases
+void enqueue_group_cycle(GroupPlan& G) {
+  const mge_params& P = G.cases[0]->prm;
+  const int mlvl = G.mlvl;
+  std::vector<int> icyc(G.lv.size() + 2, 0);
+  int mgl = mlvl;
+  for (;;) {    // lopmg
+    for (;;) {  // lopr
+      icyc[mgl] += 1;
+      const bool lfir = (mgl != mlvl);
+      group_euler(G, mgl, mgl, mlvl, false, lfir, mgl == mlvl, true);
+      if (mlvl == 1) return;
+      group_euler(G, mgl, mgl, mlvl, true, false, false, false);
+      mgl = mgl - 1;
+      multi_movco_level(G.lv[mgl - 1], &G.pr[mgl - 1], G.stream);
+      if (mgl == 1) break;
+    }
+    bool lfir = true;
+    for (;;) {  // lopp
+      group_euler(G, mgl, mgl, mlvl, false, lfir, false, true);
+      lfir = false;
+      mgl = mgl + 1;
+      multi_movfin_level(G.lv[mgl - 1], G.pr[mgl - 2], mgl - 1 == mlvl, G.stream);
+      if (mgl == mlvl) return;
+      if (icyc[mgl] != P.mgtype) break;
+      icyc[mgl] = 0;
+    }
+  }
+}
+
+void drop_group_plans(const mge_ctx* c) {
+  std::lock_guard<std::mutex> lk(g_group_mu);
+  for (size_t q = 0; q < g_plans.size();) {
+    GroupPlan* G = g_plans[q];
+    if (std::find(G->cases.begin(), G->cases.end(), c) != G->cases.end()) {
+      g_plans.erase(g_plans.begin() + q);
+      destroy_plan(G);
+    } else {
+      q++;
+    }
+  }
+}
+
+GroupPlan* find_plan(mge_ctx* const* cs, int n, int mlvl) {
+  for (GroupPlan* G : g_plans) {
+    if (G->mlvl != mlvl || (int)G->cases.size() != n) continue;
+    bool same = true;
+    for (int q = 0; q < n && same; q++)
+      same = G->cases[q] == cs[q] && G->key[q].first == cs[q]->uid && G->key[q].second == cs[q]->gen;
+    if (same) return G;
+  }
+  return nullptr;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mge_group_cycle_async(mge_ctx* const* cases, int n, int mlvl) {
+  if (!cases || n < 1) return MGE_EBADCFG;
+  for (int q = 0; q < n; q++)
+    if (!cases[q] || cases[q]->pending_mlvl || cases[q]->group_pending || mlvl < 1 ||
+        mlvl > (int)cases[q]->lv.size())
+      return MGE_EBADCFG;
+  mge_ctx* c = cases[0];
+  CK(cudaSetDevice(c->device));
+  std::lock_guard<std::mutex> lk(g_group_mu);
+  GroupPlan* G = find_plan(cases, n, mlvl);
+  if (!G) {
+    std::string why;
+    int rc = build_plan(cases, n, mlvl, &G, why);
+    if (rc) return fail(c, rc, why);
+    if (g_plans.size() >= kMaxPlans) {  // drop the least recently used plan with no cycle in flight
+      GroupPlan* old = nullptr;
+      for (GroupPlan* P : g_plans) {
+        bool busy = false;
+        for (mge_ctx* c : P->cases) busy = busy || c->group_pending == P;
+        if (!busy && (!old || P->last_use < old->last_use)) old = P;
+      }
+      if (old) {
+        g_plans.erase(std::find(g_plans.begin(), g_plans.end(), old));
+        destroy_plan(old);
+      }
+    }
+    g_plans.push_back(G);
+  }
+  G->last_use = ++g_plan_clock;
+  if (!G->graph) {
+    cudaGraph_t g;
+    CK(cudaStreamBeginCapture(G->stream, cudaStreamCaptureModeThreadLocal));
+    enqueue_group_cycle(*G);
+    gather_residuals(G->lv[mlvl - 1], G->d_res, G->d_errs, G->stream);
+    cudaError_t e = cudaStreamEndCapture(G->stream, &g);
+    if (e != cudaSuccess) return cuda_fail(c, e, "group: cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&G->graph, g, 0);
+    size_t nn = 0;
+    cudaGraphGetNodes(g, nullptr, &nn);
+    G->graph_kernels = (long long)nn;
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(c, e, "group: cudaGraphInstantiate");
+  }
+  // the cases' own streams first, the group cycle, then the cases' streams wait for it
+  for (int q = 0; q < n; q++) {
+    if (!cases[q]->ev_group) CK(cudaEventCreateWithFlags(&cases[q]->ev_group, cudaEventDisableTiming));
+    CK(cudaEventRecord(cases[q]->ev_group, cases[q]->stream));
+    CK(cudaStreamWaitEvent(G->stream, cases[q]->ev_group, 0));
+  }
+  CK(cudaEventRecord(G->ev0, G->stream));
+  CK(cudaGraphLaunch(G->graph, G->stream));
+  CK(cudaEventRecord(G->ev1, G->stream));
+  CK(cudaMemcpyAsync(G->h_res, G->d_res, n * sizeof(double), cudaMemcpyDeviceToHost, G->stream));
+  CK(cudaMemcpyAsync(G->h_errs, G->d_errs, n * sizeof(unsigned), cudaMemcpyDeviceToHost, G->stream));
+  CK(cudaEventRecord(G->done, G->stream));
+  for (int q = 0; q < n; q++) {
+    CK(cudaStreamWaitEvent(cases[q]->stream, G->done, 0));
+    cases[q]->group_pending = G;
+    cases[q]->launches += G->graph_kernels;
+  }
+  return MGE_OK;
+}
+
+// 1 while the group's cycle runs; then 0, with each case's finest residual in
+// max_res[q] and its stop (0 or an MGE_ code) in rc_out[q]
+int mge_group_cycle_poll(mge_ctx* const* cases, int n, int ncyc, double* max_res, int* rc_out) {
+  if (!cases || n < 1 || !max_res || !rc_out) return MGE_EBADCFG;
+  GroupPlan* G = (GroupPlan*)cases[0]->group_pending;
+  if (!G || (int)G->cases.size() != n) return MGE_EBADCFG;
+  for (int q = 0; q < n; q++)
+    if (cases[q] != G->cases[q] || cases[q]->group_pending != G) return MGE_EBADCFG;
+  mge_ctx* c = cases[0];
+  CK(cudaSetDevice(c->device));
+  cudaError_t e = cudaEventQuery(G->done);
+  if (e == cudaErrorNotReady) return 1;
+  if (e != cudaSuccess) return cuda_fail(c, e, "group_cycle_poll");
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, G->ev0, G->ev1);
+  for (int q = 0; q < n; q++) {
+    mge_ctx* cq = cases[q];
+    cq->group_pending = nullptr;
+    cq->last_cycle_ms = ms;
+    const unsigned w = G->h_errs[q];
+    const double r = G->h_res[q];
+    rc_out[q] = MGE_OK;
+    if (w) {
+      cudaMemsetAsync(cq->d_err, 0, sizeof(unsigned), cq->stream);
+      rc_out[q] = (w & ERR_NEGPRESS) ? fail(cq, MGE_ENEGPRESS, "timestep: negative or NaN c^2 (timestep.f90:45-48)")
+                  : (w & ERR_ZERORHO) ? fail(cq, MGE_EZERORHO, "efluxb: zero density at a cut cell (efluxb.f90:61-64)")
+                  : (w & ERR_NAN)     ? fail(cq, MGE_ENAN, "bc_cutcell: wsol is NaN (bc_cutcell.f90:147-156)")
+                                      : fail(cq, MGE_ENAN, "NaN residual (solver.f90:180)");
+    } else if (r != r) {
+      rc_out[q] = fail(cq, MGE_ENAN, "NaN residual (solver.f90:180)");
+    }
+    auto& fin = cq->lv[G->mlvl - 1];
+    if (ncyc >= 0) {
+      if ((int)fin[0].rtrms.size() <= ncyc) fin[0].rtrms.resize(ncyc + 1, 0.0);
+      fin[0].rtrms[ncyc] = r;
+    }
+    max_res[q] = r;
+  }
+  return MGE_OK;
 }
 
 }  // extern "C"

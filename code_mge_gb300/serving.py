@@ -130,6 +130,23 @@ class GpuBackend:
     def prolong(self, h, mlvl):
         return self.lib.mge_prolong_async(h.ctx, mlvl)
 
+    def launch_group(self, hs, mlvl):
+        """One lockstep cycle of several cases (mge_group_cycle_async);
+        returns a group token, or None when the cases cannot run together."""
+        arr = (C.c_void_p * len(hs))(*[h.ctx.value for h in hs])
+        if self.lib.mge_group_cycle_async(arr, len(hs), mlvl) != 0:
+            return None
+        return {"arr": arr, "n": len(hs), "res": (C.c_double * len(hs))(), "rcs": (C.c_int * len(hs))()}
+
+    def poll_group(self, g):
+        """1 while running; else (0, residuals, stop codes)."""
+        rc = self.lib.mge_group_cycle_poll(g["arr"], g["n"], -1, g["res"], g["rcs"])
+        if rc == 1:
+            return 1, None, None
+        if rc != 0:
+            return rc, [float("nan")] * g["n"], [rc] * g["n"]
+        return 0, list(g["res"]), list(g["rcs"])
+
     def refine(self, h):
         return self.lib.mge_set_precision(h.ctx, A.MGE_PREC_REFINED)
 
@@ -180,6 +197,22 @@ class FakeBackend:
     def prolong(self, h, mlvl):
         return 0
 
+    def launch_group(self, hs, mlvl):
+        self.groups = getattr(self, "groups", 0) + 1
+        for h in hs:
+            self.launch(h, mlvl)
+        return {"hs": hs, "out": {}}
+
+    def poll_group(self, g):
+        for q, h in enumerate(g["hs"]):
+            if q not in g["out"]:
+                rc, res = self.poll(h, 0)
+                if rc != 1:
+                    g["out"][q] = (rc, res)
+        if len(g["out"]) < len(g["hs"]):
+            return 1, None, None
+        return 0, [g["out"][q][1] for q in range(len(g["hs"]))], [g["out"][q][0] for q in range(len(g["hs"]))]
+
     def refine(self, h):
         h["refined"] = True
         return 0
@@ -206,17 +239,23 @@ class _Slot:
     refined: bool = False
     best: float = None         # best finest-level residual so far, and the cycle it came at
     best_at: int = 0
+    grouped: bool = False      # its cycle in flight is part of a group cycle
 
 
 class Server:
     """Continuous batching: admit while memory allows, keep every admitted case
     cycling, retire cases as they converge."""
 
-    def __init__(self, backend, reserve_bytes=2 << 30, max_active=64, clock=time.perf_counter):
+    def __init__(self, backend, reserve_bytes=2 << 30, max_active=64, clock=time.perf_counter, group=False):
         self.be = backend
         self.reserve = reserve_bytes
         self.max_active = max_active
         self.clock = clock
+        # group: the cycles of cases at the same FMG level and precision form
+        # launch together (one launch per phase over all of them)
+        self.group = group
+        self.inflight_groups = []  # (token, [slots])
+        self.group_cycles = 0
         self.queue = []           # (arrival, rid, request) min-heap
         self.active = []
         self.done = []
@@ -248,14 +287,18 @@ class Server:
             self.active.append(_Slot(r, case, h, case.prm.nlevel))
             self.peak_active = max(self.peak_active, len(self.active))
 
-    def _advance(self, s: _Slot):
-        """Launch the next cycle of a slot (or finish it); returns False when retired."""
+    def _prepare(self, s: _Slot):
+        """The FMG step to the next finer level when due, and the next cycle's count."""
         prm = s.case.prm
         if s.mlvl < s.nlevel and s.ncyc >= prm.mcyc[s.mlvl - 1]:
             self.be.prolong(s.handle, s.mlvl)        # FMG step to the next finer level
             s.mlvl += 1
             s.ncyc = 0
         s.ncyc += 1
+
+    def _advance(self, s: _Slot):
+        """Launch the next cycle of a slot (or finish it); returns False when retired."""
+        self._prepare(s)
         rc = self.be.launch(s.handle, s.mlvl)
         if rc != 0:
             self._retire(s, "cycle launch failed (%d)" % rc)
@@ -282,52 +325,91 @@ class Server:
         now = self.clock()
         self._admit(now)
         progressed = False
+        for tok, members in list(self.inflight_groups):
+            rc, res, rcs = self.be.poll_group(tok)
+            if rc == 1:
+                continue
+            self.inflight_groups.remove((tok, members))
+            progressed = True
+            for q, s in enumerate(members):
+                s.grouped = False
+                self._complete(s, rcs[q], res[q])
         for s in list(self.active):
-            if not s.inflight:
-                self._advance(s)
-                progressed = True
+            if not s.inflight or s.grouped:
                 continue
             rc, res = self.be.poll(s.handle, s.ncyc)
             if rc == 1:
                 continue
-            s.inflight = False
             progressed = True
-            if rc != 0:
-                self._retire(s, "cycle failed (%s)" % A.error_name(rc))
-                continue
-            if s.mlvl == s.nlevel:
-                s.cycles_fine += 1
-                if s.ncyc == 1:
-                    s.ini = res
-                s.req.residual = res
-                s.req.drop = res / s.ini if s.ini else None
-                if s.best is None or res < 0.95 * s.best:
-                    s.best, s.best_at = res, s.cycles_fine
-                # FP32 coarse corrections stall near eps32 * |tau|: switch to
-                # FP64 at the set drop, or as soon as the residual stops falling
-                stalled = s.req.refine_stall > 0 and s.cycles_fine - s.best_at >= s.req.refine_stall
-                if (s.req.precision == A.MGE_PREC_MIXED and not s.refined and s.ini
-                        and ((s.req.refine_drop > 0.0 and res <= s.req.refine_drop * s.ini) or stalled)):
-                    if self.be.refine(s.handle) != 0:
-                        self._retire(s, "precision refinement failed")
-                        continue
-                    s.refined = True
-                    s.req.refined_at = s.cycles_fine
-                    s.best, s.best_at = res, s.cycles_fine  # the FP64 stall window starts here
-                    if s.req.tol >= s.req.refine_drop:
-                        # the drop counts only once an FP64 cycle confirms it
-                        self._advance(s)
-                        continue
-                conv = bool(s.ini) and res <= s.req.tol * s.ini
-                fp64 = s.req.precision == A.MGE_PREC_FP64 or s.refined
-                stall_out = s.req.retire_stall > 0 and fp64 and s.cycles_fine - s.best_at >= s.req.retire_stall
-                if conv or stall_out or s.cycles_fine >= s.req.max_cycles or res != res:
-                    s.req.converged = conv
-                    s.req.stalled = stall_out and not conv
-                    self._retire(s)
-                    continue
-            self._advance(s)
+            self._complete(s, rc, res)
+        ready = [s for s in self.active if not s.inflight]
+        if ready:
+            progressed = True
+            self._launch(ready)
         return bool(self.active or self.queue), progressed
+
+    def _launch(self, ready):
+        if not self.group:
+            for s in ready:
+                self._advance(s)
+            return
+        for s in ready:
+            self._prepare(s)
+        groups = {}
+        for s in ready:
+            key = (s.mlvl, s.nlevel, s.req.precision, s.refined)
+            groups.setdefault(key, []).append(s)
+        for key, members in groups.items():
+            tok = self.be.launch_group([s.handle for s in members], key[0]) if len(members) > 1 else None
+            if tok is None:  # one case, or cases that cannot run together: their own cycles
+                for s in members:
+                    rc = self.be.launch(s.handle, s.mlvl)
+                    if rc != 0:
+                        self._retire(s, "cycle launch failed (%d)" % rc)
+                    else:
+                        s.inflight = True
+                continue
+            self.group_cycles += 1
+            for s in members:
+                s.inflight = True
+                s.grouped = True
+            self.inflight_groups.append((tok, members))
+
+    def _complete(self, s, rc, res):
+        """A slot's cycle has finished: residual bookkeeping, precision
+        switch, retirement; the slot is left ready for its next cycle."""
+        s.inflight = False
+        if rc != 0:
+            self._retire(s, "cycle failed (%s)" % A.error_name(rc))
+            return
+        if s.mlvl == s.nlevel:
+            s.cycles_fine += 1
+            if s.ncyc == 1:
+                s.ini = res
+            s.req.residual = res
+            s.req.drop = res / s.ini if s.ini else None
+            if s.best is None or res < 0.95 * s.best:
+                s.best, s.best_at = res, s.cycles_fine
+            # FP32 coarse corrections stall near eps32 * |tau|: switch to
+            # FP64 at the set drop, or as soon as the residual stops falling
+            stalled = s.req.refine_stall > 0 and s.cycles_fine - s.best_at >= s.req.refine_stall
+            if (s.req.precision == A.MGE_PREC_MIXED and not s.refined and s.ini
+                    and ((s.req.refine_drop > 0.0 and res <= s.req.refine_drop * s.ini) or stalled)):
+                if self.be.refine(s.handle) != 0:
+                    self._retire(s, "precision refinement failed")
+                    return
+                s.refined = True
+                s.req.refined_at = s.cycles_fine
+                s.best, s.best_at = res, s.cycles_fine  # the FP64 stall window starts here
+                if s.req.tol >= s.req.refine_drop:
+                    return  # the drop counts only once an FP64 cycle confirms it
+            conv = bool(s.ini) and res <= s.req.tol * s.ini
+            fp64 = s.req.precision == A.MGE_PREC_FP64 or s.refined
+            stall_out = s.req.retire_stall > 0 and fp64 and s.cycles_fine - s.best_at >= s.req.retire_stall
+            if conv or stall_out or s.cycles_fine >= s.req.max_cycles or res != res:
+                s.req.converged = conv
+                s.req.stalled = stall_out and not conv
+                self._retire(s)
 
     def run(self, idle_sleep=50e-6, deadline=None):
         while True:

@@ -212,6 +212,28 @@ int mge_cycle_async(mge_ctx* ctx, int mlvl);
 int mge_cycle_poll(mge_ctx* ctx, int ncyc, double* max_res);
 int mge_prolong_async(mge_ctx* ctx, int mlvl);
 
+/* Lockstep cycles of a group of cases (the batched sweep and the serving
+ * loop).  One multigrid cycle at FMG level mlvl for every case of the
+ * group: each phase of the cycle (time step, each stage's prep, face,
+ * record, combine passes, the line sweeps, the boundary passes, the
+ * transfers) is one launch over the block of that level of every case, and
+ * the whole cycle is one captured CUDA graph, so the launches of a cycle do
+ * not grow with the number of cases.  The reference's solver loops the
+ * blocks of one case (solver.f90:151-157); this runs that loop over the
+ * blocks of many cases at once, which has no counterpart there.  The cases
+ * must share the level count, the multigrid and stage schedule, the CFL
+ * number and the scheme (JST central, steady, psmoo_old smoothing), have one
+ * block per level, and be in the same precision form; their sizes, bodies
+ * and flow conditions may differ.  Each case's results are those of its own
+ * per-phase cycle with the line sweeps in global memory.  _async returns at
+ * once (MGE_EBADCFG when the cases cannot run together, with the reason in
+ * mge_last_error of the first case); _poll returns 1 while the cycle runs,
+ * then 0 with each case's finest-level residual in max_res[q] and its stop
+ * (0 or an MGE_ code, the reason in that case's mge_last_error) in
+ * rc_out[q].  A case takes part in one cycle at a time, group or single. */
+int mge_group_cycle_async(mge_ctx* const* cases, int n, int mlvl);
+int mge_group_cycle_poll(mge_ctx* const* cases, int n, int ncyc, double* max_res, int* rc_out);
+
 /* Switch a committed context between MGE_PREC_FP64, MGE_PREC_MIXED and
  * MGE_PREC_REFINED in place (the coarse levels' state is converted; graphs
  * are re-captured).  The mixed form's FP32 coarse corrections carry rounding

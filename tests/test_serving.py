@@ -34,6 +34,27 @@ def test_scheduler_completes_all_requests_in_fifo_admission():
     assert st["completed"] == 9 and st["converged"] == 9 and st["p99_s"] >= st["p50_s"]
 
 
+def test_group_mode_gives_every_request_the_same_cycles():
+    """Cases at the same FMG level and precision form advance in group
+    cycles; each request's cycle count, refinement point and outcome are
+    those of the one-case-at-a-time scheduling."""
+    def run(group):
+        be = S.FakeBackend(rate=0.6, latency=2, floor32=1e-5)
+        srv = S.Server(be, reserve_bytes=0, clock=FakeClock(), group=group)
+        reqs = [S.Request(q, ["sphere", "ellipsoid"][q % 2], 16, 0.3 + 0.05 * q, tol=1e-8, arrival=0.0,
+                          max_cycles=200, precision=A.MGE_PREC_MIXED if q % 3 else A.MGE_PREC_FP64,
+                          refine_drop=1e-6, refine_stall=0) for q in range(8)]
+        for r in reqs:
+            srv.submit(r)
+        done = sorted(srv.run(idle_sleep=0), key=lambda r: r.rid)
+        return done, srv, be
+    alone, _, _ = run(False)
+    grouped, srv, be = run(True)
+    assert [(r.cycles, r.converged, r.refined_at) for r in grouped] == \
+        [(r.cycles, r.converged, r.refined_at) for r in alone]
+    assert srv.group_cycles > 0 and be.groups == srv.group_cycles
+
+
 def test_admission_is_gated_by_free_memory():
     reqs = [S.Request(q, "sphere", 16, 0.4, tol=1e-2, arrival=0.0, max_cycles=50) for q in range(6)]
     one = S.case_bytes(S.build_case(reqs[0]))
