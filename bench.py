@@ -531,11 +531,21 @@ def run_pattern(args):
         plain, t0 = [], time.perf_counter()
         for r in SV.batched_sweep_requests(args.cases, sizes=sizes, precision=A.MGE_PREC_FP64, tol=args.tol,
                                            max_cycles=args.max_cycles, retire_stall=args.retire_stall):
+            if args.no_serial:
+                break
             r.arrival = t0
             one = SV.Server(SV.GpuBackend(coop_ctas=0), max_active=1)
             one.submit(r)
             plain += one.run()
         tp = time.perf_counter() - t0
+        if args.no_serial:  # the mixed sweep alone
+            line = {"pattern": "batched sweep", "metric": "converged solves/s", "unit": "solves/s",
+                    "value": batched["solves_per_s"], "baseline_fp64_serial": None, "cases": args.cases,
+                    "batched": batched, "group_cycles": srv.group_cycles, "peak_active": srv.peak_active,
+                    "per_case": [{"rid": r.rid, "n": r.n, "cycles": r.cycles, "converged": r.converged,
+                                  "cd": r.cd} for r in sorted(done, key=lambda r: r.rid)]}
+            print(json.dumps(line), flush=True)
+            return 0
         serial = SV.summarize(plain, tp)
         mix = {r.rid: r for r in done}
         both = [r for r in plain if r.error is None and mix[r.rid].error is None
@@ -637,6 +647,7 @@ def main():
     ap.add_argument("--duration", type=float, default=300.0)
     ap.add_argument("--drain", type=float, default=120.0)
     ap.add_argument("--coop-ctas", type=int, default=32)
+    ap.add_argument("--no-serial", action="store_true", help="batched: skip the FP64 one-at-a-time baseline")
     ap.add_argument("--no-group", action="store_true",
                     help="batched/serving: each case its own cycles (no group launches)")
     ap.add_argument("--workload", default="sphere192", choices=["sphere192", "cylinder512ns", "sphere128", "sphere96"])

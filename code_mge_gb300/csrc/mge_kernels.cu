@@ -835,7 +835,12 @@ __device__ void rec_wall_terms(const DevBlock<T>& b, const PhysParams& P, int di
   // dfluxb.f90:29-423; w(:,5) is the enthalpy here
   wsol[4] = wsol[4] + psol;
   auto pp = [&](int a) -> T { return b.p[c + a * st]; };
-  auto ww = [&](int a, int v) -> T { return v < 4 ? b.w[v * N + c + a * st] : b.H[c + a * st]; };
+  // the enthalpy formed here with the prep pass's addition: a record at the
+  // block's edge reaches the outer ghost layer, where the prep pass forms no H
+  auto ww = [&](int a, int v) -> T {
+    const long long q = c + a * st;
+    return v < 4 ? b.w[v * N + q] : b.w[4 * N + q] + b.p[q];
+  };
   auto lamc = [&](int a) -> T {
     // lambda with the ghost-copy rule of timestep.f90:227-282 along the record axis
     int q = (D == 0 ? i : (D == 1 ? j : k)) + a;

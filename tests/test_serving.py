@@ -111,7 +111,15 @@ def test_poisson_and_sweep_generators_are_seeded():
 
 
 @pytest.mark.gpu
-def test_results_are_the_same_alone_and_in_the_mix(gpulib):
+@pytest.mark.parametrize("group", [False, True])
+def test_results_are_the_same_alone_and_in_the_mix(gpulib, monkeypatch, group):
+    """Each result is bit-identical alone and in a mix of four, with the
+    mix's cases on their own cycles or in group cycles (the launch forms
+    pinned to the per-phase form with global-memory sweeps, the form a group
+    cycle runs)."""
+    if group:
+        monkeypatch.setenv("MGE_AUTOTUNE", "0")
+        monkeypatch.setenv("MGE_COOP_MAX_CELLS", "0")
     mk = lambda: [S.Request(0, "sphere", 16, 0.5, tol=1e-4, max_cycles=200),
                   S.Request(1, "ellipsoid", 24, 0.3, alpha_deg=4.0, tol=1e-4, max_cycles=200),
                   S.Request(2, "cylinder", 32, 0.4, tol=1e-4, max_cycles=200),
@@ -123,11 +131,12 @@ def test_results_are_the_same_alone_and_in_the_mix(gpulib):
         (d,) = srv.run()
         assert d.error is None
         alone[d.rid] = d
-    srv = S.Server(S.GpuBackend(), reserve_bytes=1 << 30)
+    srv = S.Server(S.GpuBackend(), reserve_bytes=1 << 30, group=group)
     for r in mk():
         srv.submit(r)
     mix = {d.rid: d for d in srv.run()}
     assert srv.peak_active == 4
+    assert (srv.group_cycles > 0) == group
     for rid, a in alone.items():
         m = mix[rid]
         assert m.error is None and m.cycles == a.cycles
