@@ -586,7 +586,7 @@ def run_pattern(args):
         reqs = SV.poisson_requests(args.rate, args.duration, sizes=(lo, hi), tol=args.tol,
                                    max_cycles=args.max_cycles, precision=precision)
         srv = SV.Server(SV.GpuBackend(coop_ctas=args.coop_ctas if max_active > 1 else 0), max_active=max_active,
-                        group=max_active > 1 and not args.no_group)
+                        group=max_active > 1 and not args.no_group, builders=2)
         t_start = time.perf_counter()
         for r in reqs:
             r.arrival += t_start

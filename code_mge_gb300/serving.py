@@ -4,9 +4,12 @@ Requests (geometry, grid size, Mach, angle, residual-drop tolerance) arrive
 over time.  Each admitted request becomes one resident case (one mge_ctx: its
 whole multigrid hierarchy stays in HBM until it converges).  Admission is
 gated by free device memory.  Every in-flight case advances by asynchronous
-multigrid cycles (mge_cycle_async / mge_cycle_poll) on its own stream, so the
-cycles of all admitted cases overlap on the GPU; a request that arrives
-while others run is admitted as soon as memory frees up.  A case follows the
+multigrid cycles: its own (mge_cycle_async / mge_cycle_poll, on its own
+stream), or, with ``group=True``, group cycles that advance all the cases at
+the same FMG level and precision form together, one launch per phase over all
+of them (mge_group_cycle_async / _poll).  A request that arrives while others
+run is admitted as soon as memory frees up; its case can be built on host
+threads ahead of its admission (``builders``).  A case follows the
 reference's full-multigrid schedule (solver.f90:119-259): mcyc cycles per
 coarse FMG level, then cycles on the finest level until its residual has
 dropped by the requested factor.
@@ -18,6 +21,7 @@ import ctypes as C
 import heapq
 import math
 import time
+from concurrent.futures import ThreadPoolExecutor
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -246,8 +250,15 @@ class Server:
     """Continuous batching: admit while memory allows, keep every admitted case
     cycling, retire cases as they converge."""
 
-    def __init__(self, backend, reserve_bytes=2 << 30, max_active=64, clock=time.perf_counter, group=False):
+    def __init__(self, backend, reserve_bytes=2 << 30, max_active=64, clock=time.perf_counter, group=False,
+                 builders=0, lookahead=4):
         self.be = backend
+        # builders > 0: the cases of the next `lookahead` arrived requests are
+        # built on host threads while the GPU works, instead of in the
+        # scheduler pass that admits them
+        self.builder = ThreadPoolExecutor(max_workers=builders) if builders else None
+        self.lookahead = lookahead
+        self.pending = {}
         self.reserve = reserve_bytes
         self.max_active = max_active
         self.clock = clock
@@ -265,10 +276,32 @@ class Server:
     def submit(self, r: Request):
         heapq.heappush(self.queue, (r.arrival, r.rid, r))
 
+    def _case_of(self, r):
+        """The request's case, once built (None while a host thread builds it)."""
+        if r.rid in self.cases:
+            return self.cases[r.rid]
+        if self.builder is None:
+            self.cases[r.rid] = build_case(r)
+            return self.cases[r.rid]
+        f = self.pending.get(r.rid)
+        if f is None:
+            f = self.pending[r.rid] = self.builder.submit(build_case, r)
+        if not f.done():
+            return None
+        del self.pending[r.rid]
+        self.cases[r.rid] = f.result()
+        return self.cases[r.rid]
+
     def _admit(self, now):
+        if self.builder is not None:
+            for _, _, r in heapq.nsmallest(self.lookahead, self.queue):
+                if r.arrival <= now and r.rid not in self.cases and r.rid not in self.pending:
+                    self.pending[r.rid] = self.builder.submit(build_case, r)
         while self.queue and self.queue[0][0] <= now and len(self.active) < self.max_active:
             r = self.queue[0][2]
-            case = self.cases.get(r.rid) or build_case(r)
+            case = self._case_of(r)
+            if case is None:
+                return  # still being built (FIFO: no overtaking)
             need = case_bytes(case)
             if self.active and self.be.free_memory() - need < self.reserve:
                 return  # wait for memory to free up (FIFO: no overtaking)
@@ -284,6 +317,7 @@ class Server:
                 heapq.heappush(self.queue, (r.arrival, r.rid, r))
                 return
             r.t_admit = self.clock()
+            self.cases.pop(r.rid, None)
             self.active.append(_Slot(r, case, h, case.prm.nlevel))
             self.peak_active = max(self.peak_active, len(self.active))
 
