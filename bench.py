@@ -78,6 +78,19 @@ KERNEL_MODEL = {
              "fp64": FACE_FP64_PER_CELL},
     "combine": {"cells": "phys", "alg": 41 * 8 + 5, "dram": 338.6, "fp64": 75.0},
 }
+# The mixed form's finest-level passes (the contracted FP64 residual), per
+# physical cell and averaged over the launches of one update, from the ncu
+# capture of a whole 128^3 update (profiles/update_fp64_counts_sphere128.md):
+# its prep pass (5 launches), dissipation face pass (3) and combine pass (5).
+# alg: prep reads w, p and writes H, F (stages 2, 4) or H, F, dlt, fp
+# (stages 1, 3, 5): 32.8 doubles on average; the face pass reads dlt, fp,
+# lambda and writes dfs: 34 doubles; combine reads F, dfs, fw, vdtim, blank,
+# cutmap and writes fw, dw: 41 doubles + 5 B.
+MIXED_MODEL = {
+    "prep": {"alg": 32.8 * 8, "dram": 1349.9 / 5, "fp64": 325.3 / 5, "launches": 5},
+    "face": {"alg": 34 * 8, "dram": 819.6 / 3, "fp64": 244.9 / 3, "launches": 3},
+    "combine": {"alg": 41 * 8 + 5, "dram": 1776.2 / 5, "fp64": 329.0 / 5, "launches": 5},
+}
 FP64_LANES_PER_SM_CYCLE = 2      # GB300: 2 FP64 thread-operations per SM per cycle
 # FP64 thread instructions of every kernel of one finest-level update of the
 # 128^3 sphere (ncu), per cell-update, by precision form
@@ -119,6 +132,24 @@ def kernel_roofline(case, kind, stage_ms, peak, pkind, fp64_peak):
     passes without a model get the whole update's line only."""
     nx, ny, nz = case.levels[-1][0].n
     cells = {"prep": (nx + 2) * (ny + 2) * (nz + 2), "face": (nx + 1) * (ny + 1) * (nz + 1), "phys": nx * ny * nz}
+    if case.prm.precision != A.MGE_PREC_FP64 and jst_euler(case) and kind in MIXED_MODEL:
+        # the mixed form: the pass's average launch over one update
+        m = MIXED_MODEL[kind]
+        runs = [x for x in stage_ms[kind] if x > 0.01]
+        t = sum(runs) / len(runs) if runs else 0.0
+        n = cells["phys"]
+        alg = m["alg"] * n
+        ach = alg / (t * 1e-3) / 1e9 if t > 0 else 0.0
+        fp = m["fp64"] * n / (t * 1e-3) if t > 0 else 0.0
+        name = {"prep": "k_prep (contracted form)", "face": "k_face_diss", "combine": "k_combine (contracted form)"}
+        roof = {"bound": "hbm", "kernel": name[kind] + ", average launch of an update", "achieved": ach,
+                "peak": peak, "unit": "GB/s", "frac": ach / peak, "traffic": m["dram"] * n,
+                "algorithmic_bytes_per_launch": alg, "launch_ms": t, "peak_kind": pkind,
+                "note": "per physical cell; the FP64 issue rate bounds this pass: see fp64_roofline"}
+        fp64 = {"kernel": roof["kernel"], "achieved": fp / 1e12, "peak": fp64_peak / 1e12, "unit": "T FP64 instr/s",
+                "frac": fp / fp64_peak, "fp64_per_cell": m["fp64"],
+                "peak_basis": "2 FP64 thread-ops per SM per cycle x 152 SMs x median SM clock"}
+        return roof, fp64
     m = KERNEL_MODEL.get(kind)
     if m is None or kind not in stage_ms or not jst_euler(case) or case.prm.precision != A.MGE_PREC_FP64:
         # the Roe + viscous and the mixed passes: their byte models only
