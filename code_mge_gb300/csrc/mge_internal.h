@@ -57,7 +57,7 @@ struct DevBlock {
   // cut-cell records
   int nmir;
   int m0;                   // first record with an empty cloud (nmir if none)
-  const int32_t* rec_i;     // [nmir][8]: ccid(3), faceid, zz, npoint, pad, pad
+  const int32_t* rec_i;     // [nmir][8]: ccid(3), faceid, zz, npoint, counted in the forces, pad
   const int32_t* rec_cloud; // [nmir][8][3]
   const double* rec_coef;   // [nmir][8]
   const double* rec_nvec;   // [nmir][3]

@@ -2480,6 +2480,7 @@ __global__ void k_forces(DevBlock<T> b, double ox, double oy, double oz, double 
   const double org[3] = {ox, oy, oz}, h[3] = {hx, hy, hz}, ctr[3] = {cx, cy, cz};
   for (int m = threadIdx.x; m < b.nmir; m += blockDim.x) {
     const int* ri = b.rec_i + 8 * m;
+    if (ri[6] == 0) continue;  // a wall face another block of the level counts
     int ax = ri[4] - 1;
     double sgn = ri[3] >= 4 ? 1.0 : -1.0;
     long long c = cidx(b.Pi, b.Pj, ri[0], ri[1], ri[2]);

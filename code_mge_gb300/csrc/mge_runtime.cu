@@ -538,6 +538,23 @@ void fill_view(Block& b, DevBlock<T>& d, void* scratch) {
   }
 }
 
+// Whether a record's wall face counts in the wall forces: blocks of one
+// level may overlap, and a wall face inside the physical cells of a block of
+// lower serial is that block's to count (each face once)
+bool record_counted(const mge_ctx* c, const Block& b, const int* ccid) {
+  for (const Block& o : c->lv[b.level - 1]) {
+    if (o.serial >= b.serial) continue;
+    bool inside = true;
+    const int n[3] = {o.nx, o.ny, o.nz};
+    for (int d = 0; d < 3 && inside; d++) {
+      const double x = b.origin[d] + ((double)ccid[d] - 1.5) * b.h[d];
+      inside = x >= o.origin[d] && x < o.origin[d] + n[d] * o.h[d];
+    }
+    if (inside) return false;
+  }
+  return true;
+}
+
 int commit_block(mge_ctx* c, Block& b, double* scratch) {
   const long long N = b.N;
   const size_t es = b.esz;
@@ -573,6 +590,7 @@ int commit_block(mge_ctx* c, Block& b, double* scratch) {
     ri[8 * m + 3] = t.faceid;
     ri[8 * m + 4] = t.zz;
     ri[8 * m + 5] = t.npoint;
+    ri[8 * m + 6] = record_counted(c, b, t.ccid) ? 1 : 0;
     for (int q = 0; q < MGE_MAX_CLOUD; q++) {
       rcf[8 * m + q] = t.coef[q];
       for (int e = 0; e < 3; e++) rcl[(8 * m + q) * 3 + e] = t.ijk[q][e];

@@ -1862,9 +1862,26 @@ int movfin(mgeo_ctx* c, int mgl, int mlvl) {  // movfin.f90:20-39
    pressure on each wall face and, with NS, the wall's viscous stress.  The
    body takes the momentum the solver's wall flux gives the fluid, with the
    opposite sign: -(S*tau) for a solid on the + side, S*tau on the - side. */
+/* whether a record's wall face counts: a face inside the physical cells of
+   a block of lower serial on the same level is that block's (each once) */
+bool record_counted(const mgeo_ctx* c, const OBlock& b, const int* ccid) {
+  for (const OBlock& o : c->lv[b.level - 1]) {
+    if (o.serial >= b.serial) continue;
+    bool inside = true;
+    const int n[3] = {o.nx, o.ny, o.nz};
+    for (int d = 0; d < 3 && inside; d++) {
+      const double x = b.origin[d] + ((double)ccid[d] - 1.5) * b.h[d];
+      inside = x >= o.origin[d] && x < o.origin[d] + n[d] * o.h[d];
+    }
+    if (inside) return false;
+  }
+  return true;
+}
+
 void forces_block(mgeo_ctx* c, OBlock& b, const mge_solve_opts* o, double* F, double* M) {
   const double Sd[3] = {std::fabs(b.si[0]), std::fabs(b.sj[1]), std::fabs(b.sk[2])};
   for (const ORec& t : b.z) {
+    if (!record_counted(c, b, t.ccid)) continue;
     int ax = t.zz - 1;
     double sgn = t.faceid >= 4 ? 1.0 : -1.0;
     double area = t.area;

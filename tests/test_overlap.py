@@ -54,3 +54,18 @@ def test_split_level_preserves_the_free_stream():
     for s in (1, 2):
         w = physical(o.field("w", 2, serial=s), case.levels[1][s - 1])
         assert np.abs(w[0] - 1.0).max() < 1e-12
+
+
+def test_wall_faces_of_overlapping_blocks_count_once():
+    """At the free stream the pressure is uniform, so the wall force of a
+    closed body is zero only if every wall face counts exactly once: the
+    faces inside the overlap belong to the block of lower serial."""
+    import ctypes as C
+    from code_mge_gb300 import _abi as A
+    case = K.cylinder_split(n=32, overlap=4)
+    o = OracleCycle(case)
+    opts = A.MgeSolveOpts()
+    opts.ref_area = case.ref_area
+    f = A.MgeForces()
+    assert o.lib.mgeo_forces_compute(o.ctx, 2, C.byref(opts), C.byref(f)) == 0
+    assert max(abs(v) for v in f.force) < 1e-12 * case.prm.p0
