@@ -447,6 +447,7 @@ def run_gpu(args):
                               C.byref(nval))
     solut_ms = 1e3 * (time.perf_counter() - t0) if rc == 0 else None
 
+    l2 = l2_note(lib, cyc, sp)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         dt = time_cpu_oracle(case, threads=1, cycles=1)
@@ -464,7 +465,7 @@ def run_gpu(args):
                        "cell_updates_per_step": cu, "precision": args.precision,
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "launch_plan": plan,
-                       "l2": l2_note(lib, cyc, sp)},
+                       "l2": l2},
             "wall_ms_per_step": 1e3 * wall / args.steps,
             "residual_last": res[-1] if res else None,
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(w_np.nbytes), "d2h_bytes_per_step": 8,
@@ -615,9 +616,10 @@ def run_pattern(args):
 
     def serve(precision, max_active):
         reqs = SV.poisson_requests(args.rate, args.duration, sizes=(lo, hi), tol=args.tol,
-                                   max_cycles=args.max_cycles, precision=precision)
+                                   max_cycles=args.max_cycles, precision=precision, retire_stall=args.retire_stall)
         srv = SV.Server(SV.GpuBackend(coop_ctas=args.coop_ctas if max_active > 1 else 0), max_active=max_active,
-                        group=max_active > 1 and not args.no_group, builders=2)
+                        group=max_active > 1 and not args.no_group, builders=2,
+                        max_cells=args.max_cells if max_active > 1 else 0)
         t_start = time.perf_counter()
         for r in reqs:
             r.arrival += t_start
@@ -629,7 +631,8 @@ def run_pattern(args):
             srv.be.close(sl.handle)
         st = SV.summarize(done, wall)
         ok = [r for r in done if r.error is None]
-        st.update({"submitted": len(reqs), "finished": len(done), "unfinished": len(reqs) - len(done),
+        st.update({"errors": [[r.rid, r.error] for r in done if r.error is not None][:8],
+                   "submitted": len(reqs), "finished": len(done), "unfinished": len(reqs) - len(done),
                    "in_flight_at_deadline": len(srv.active), "never_admitted": len(srv.queue),
                    "peak_active": srv.peak_active,
                    "finest_cell_cycles_per_s": sum(r.cycles * cells(r) for r in ok) / wall if wall > 0 else None,
@@ -649,7 +652,8 @@ def run_pattern(args):
             else None,
             "config": {"arrivals": "Poisson %.1f req/s for %.0f s (seed 20261204)" % (args.rate, args.duration),
                        "drain_s": args.drain, "sizes": [lo, hi], "tol_drop": args.tol,
-                       "max_cycles": args.max_cycles,
+                       "max_cycles": args.max_cycles, "retire_stall": args.retire_stall,
+                       "admission": "FIFO, by free memory and at most %d finest cells in flight" % args.max_cells,
                        "precision": "FP32 coarse / FP64 fine (contracted residual), refined to FP64 coarse",
                        "baseline": "FP64 plain, one case at a time in arrival order, same stream and window"}}
     print(json.dumps(line), flush=True)
@@ -679,6 +683,8 @@ def main():
     ap.add_argument("--drain", type=float, default=120.0)
     ap.add_argument("--coop-ctas", type=int, default=32)
     ap.add_argument("--no-serial", action="store_true", help="batched: skip the FP64 one-at-a-time baseline")
+    ap.add_argument("--max-cells", type=int, default=8000000,
+                    help="serving: admit while the cases in flight hold at most this many finest cells")
     ap.add_argument("--no-group", action="store_true",
                     help="batched/serving: each case its own cycles (no group launches)")
     ap.add_argument("--workload", default="sphere192", choices=["sphere192", "cylinder512ns", "sphere128", "sphere96"])

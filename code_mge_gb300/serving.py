@@ -251,8 +251,13 @@ class Server:
     cycling, retire cases as they converge."""
 
     def __init__(self, backend, reserve_bytes=2 << 30, max_active=64, clock=time.perf_counter, group=False,
-                 builders=0, lookahead=4):
+                 builders=0, lookahead=4, max_cells=0):
         self.be = backend
+        # max_cells > 0: admit while the cases in flight hold at most this many
+        # finest-level cells (one case is always admitted), so that under
+        # overload the admitted cases fill the GPU and finish, instead of every
+        # arrived case sharing it and none finishing
+        self.max_cells = max_cells
         # builders > 0: the cases of the next `lookahead` arrived requests are
         # built on host threads while the GPU works, instead of in the
         # scheduler pass that admits them
@@ -305,6 +310,9 @@ class Server:
             need = case_bytes(case)
             if self.active and self.be.free_memory() - need < self.reserve:
                 return  # wait for memory to free up (FIFO: no overtaking)
+            if (self.active and self.max_cells > 0 and
+                    sum(s.case.finest_cells for s in self.active) + case.finest_cells > self.max_cells):
+                return  # the GPU is full of work: wait for a case to finish
             heapq.heappop(self.queue)
             try:
                 h = self.be.open(case)
@@ -458,7 +466,7 @@ class Server:
 
 
 def poisson_requests(rate, duration, seed=20261204, sizes=(64, 256), mach=(0.1, 0.8), tol=1e-8,
-                     precision=A.MGE_PREC_MIXED, max_cycles=2000):
+                     precision=A.MGE_PREC_MIXED, max_cycles=2000, retire_stall=0):
     """Poisson arrivals (rate per second) over `duration` seconds; geometry
     uniform over sphere / ellipsoid / cylinder slab, n a multiple of 8 in
     [sizes], Mach uniform in [mach]."""
@@ -472,7 +480,8 @@ def poisson_requests(rate, duration, seed=20261204, sizes=(64, 256), mach=(0.1, 
         n = int(8 * rng.integers(sizes[0] // 8, sizes[1] // 8 + 1))
         out.append(Request(rid, g, n, float(rng.uniform(*mach)), float(rng.uniform(-5.0, 10.0)) if g != "sphere" else 0.0,
                            tol=tol, precision=precision, arrival=t,
-                           semi=tuple(float(x) for x in rng.uniform(0.5, 2.0, 3)), max_cycles=max_cycles))
+                           semi=tuple(float(x) for x in rng.uniform(0.5, 2.0, 3)), max_cycles=max_cycles,
+                           retire_stall=retire_stall))
         rid += 1
     return out
 

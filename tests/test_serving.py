@@ -55,6 +55,21 @@ def test_group_mode_gives_every_request_the_same_cycles():
     assert srv.group_cycles > 0 and be.groups == srv.group_cycles
 
 
+def test_admission_is_bounded_by_work_in_flight():
+    """max_cells: cases are admitted while those in flight hold at most that
+    many finest cells (one is always admitted), FIFO."""
+    reqs = [S.Request(q, "sphere", 16, 0.4, tol=1e-2, arrival=0.0, max_cycles=50) for q in range(6)]
+    one = S.build_case(reqs[0]).finest_cells
+    be = S.FakeBackend(rate=0.5, latency=1)
+    srv = S.Server(be, reserve_bytes=0, clock=FakeClock(), max_cells=2 * one + 1)
+    for r in reqs:
+        srv.submit(r)
+    done = srv.run(idle_sleep=0)
+    assert len(done) == 6 and all(r.converged for r in done)
+    assert srv.peak_active == 2
+    assert [r.rid for r in sorted(done, key=lambda r: r.t_admit)] == list(range(6))
+
+
 def test_admission_is_gated_by_free_memory():
     reqs = [S.Request(q, "sphere", 16, 0.4, tol=1e-2, arrival=0.0, max_cycles=50) for q in range(6)]
     one = S.case_bytes(S.build_case(reqs[0]))
