@@ -175,6 +175,7 @@ enum MultiKind {
 struct MultiLevel {
   int nc = 0;
   bool f32 = false, aux32 = false, fast = false;
+  bool coop = false;             // the update as one persistent cooperative launch (k_group_euler)
   void* B = nullptr;             // DevBlock<T>[nc]
   PhysParams* P = nullptr;       // [nc]
   unsigned** err = nullptr;      // [nc]

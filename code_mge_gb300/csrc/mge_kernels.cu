@@ -3424,8 +3424,162 @@ void gather_residuals(const MultiLevel& L, double* res, unsigned* errs, cudaStre
   }
 }
 
+// The whole update of every case of a group as ONE persistent cooperative
+// launch: the phases of multi_euler_t in the same order, a grid-wide barrier
+// between dependent phases, each phase's thread blocks of 256 items dealt
+// over the resident blocks (a block serves one case at a time, so the
+// per-block reductions stay within a case).  For the small levels, where a
+// phase's launch costs more than its work.
+struct GroupEuler {
+  const long long* off[MK_COUNT];
+  long long tot[MK_COUNT];
+  int mstage, do_timestep, lfir, rt, fast, aux32;
+  StageArgs st[8];  // the stages (at most 8)
+};
+
+__device__ __forceinline__ int case_of(const long long* off, int nc, long long base) {
+  int lo = 0, hi = nc - 1;  // the last q with off[q] <= base
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (off[mid] <= base) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+template <typename T, typename F>
+__device__ __forceinline__ void group_phase(const MultiArgs<T>& M, const GroupEuler& G, int kind, const F& f) {
+  const long long tot = G.tot[kind];
+  for (long long base = (long long)blockIdx.x * 256; base < tot; base += (long long)gridDim.x * 256) {
+    const int q = case_of(G.off[kind], M.nc, base);
+    f(M, q, base - G.off[kind][q] + threadIdx.x);
+  }
+}
+
+template <typename T, typename TA>
+__global__ void __launch_bounds__(256, 1) k_group_euler(MultiArgs<T> M, GroupEuler G) {
+  cg::grid_group grid = cg::this_grid();
+  if (G.do_timestep) {
+    group_phase(M, G, MK_ONE, FDtimReset<T>{});
+    grid.sync();
+    group_phase(M, G, MK_PHYS, FTimestep<T, TA>{});
+  }
+  if (G.lfir) group_phase(M, G, MK_N5, FCopyWs<T>{});
+  group_phase(M, G, MK_N, FSaveWn<T>{});
+  grid.sync();
+  for (int m = 1; m <= G.mstage; m++) {
+    const StageArgs& a = G.st[m - 1];
+    if (G.fast) {
+      group_phase(M, G, MK_PREP, FPrep<T, true>{a.dissip_on});
+      grid.sync();
+      if (a.dissip_on) group_phase(M, G, MK_FACE, FFaceDiss<T>{(T)a.cd});
+    } else {
+      group_phase(M, G, MK_PREP, FPrep<T, false>{a.dissip_on});
+      grid.sync();
+      if (a.dissip_on)
+        group_phase(M, G, MK_FACE, FFace<T>{a.dissip_on, (T)a.cd});
+      else
+        group_phase(M, G, MK_FACE, FFaceConv<T>{});
+    }
+    group_phase(M, G, MK_REC, FRec<T>{a.dissip_on, (T)a.cd});
+    grid.sync();
+    if (G.fast)
+      group_phase(M, G, MK_PHYS, FCombine<T, true>{a});
+    else
+      group_phase(M, G, MK_PHYS, FCombine<T, false>{a});
+    grid.sync();
+    if (a.lres) return;
+    if (a.irs) {
+      if constexpr (std::is_same<T, double>::value && std::is_same<TA, float>::value) {
+        group_phase(M, G, MK_IRS0, FIrsMixed<double, float, 0>{});
+        grid.sync();
+        group_phase(M, G, MK_IRS1, FIrsMixed<float, float, 1>{});
+        grid.sync();
+        group_phase(M, G, MK_IRS2, FIrsMixed<float, double, 2>{});
+      } else {
+        group_phase(M, G, MK_IRS0, FIrs<T, T, 0>{});
+        grid.sync();
+        group_phase(M, G, MK_IRS1, FIrs<T, T, 1>{});
+        grid.sync();
+        group_phase(M, G, MK_IRS2, FIrs<T, T, 2>{});
+      }
+      grid.sync();
+      group_phase(M, G, MK_PHYS, FUpdate<T>{a});
+      grid.sync();
+    }
+    group_phase(M, G, MK_REC, FCutcell<T>{});
+    grid.sync();
+    for (int pass = 0; pass < 3; pass++) {
+      group_phase(M, G, MK_BC, FBcPass<T>{pass});
+      grid.sync();
+    }
+    for (int phase = 0; phase < 3; phase++) {
+      group_phase(M, G, MK_CORNER0 + phase, FCorner<T>{phase});
+      grid.sync();
+    }
+  }
+  if (G.rt) {
+    group_phase(M, G, MK_RTP, FRtrmsPartial<T>{});
+    grid.sync();
+    group_phase(M, G, MK_ONE, FRtrmsFinal<T>{});
+  }
+}
+
+// resident blocks of the group kernel on the device (0: no cooperative launch)
+template <typename T, typename TA>
+static int group_grid() {
+  static int cached[64] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return 0;
+  if (cached[dev]) return cached[dev] > 0 ? cached[dev] : 0;
+  int nsm = 0, per = 0, coop = 0;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_group_euler<T, TA>, 256, 0);
+  cached[dev] = (coop && per > 0) ? nsm * per : -1;
+  return cached[dev] > 0 ? cached[dev] : 0;
+}
+
+// the group's update as one cooperative launch; false when it cannot run so
+template <typename T>
+static bool group_euler_coop(const MultiLevel& L, const StageArgs* A, int mstage, bool with_timestep, bool lfir,
+                             bool rt, cudaStream_t s) {
+  const bool mixed32 = std::is_same<T, double>::value && L.aux32;
+  const int gmax = mixed32 ? group_grid<T, float>() : group_grid<T, T>();
+  if (gmax <= 0) return false;
+  GroupEuler G;
+  memset(&G, 0, sizeof(G));
+  long long most = 0;
+  for (int k = 0; k < MK_COUNT; k++) {
+    G.off[k] = L.off[k];
+    G.tot[k] = L.tot[k];
+    most = std::max(most, L.tot[k] / 256);
+  }
+  G.mstage = mstage;
+  G.do_timestep = with_timestep;
+  G.lfir = lfir;
+  G.rt = rt;
+  G.fast = L.fast;
+  G.aux32 = L.aux32;
+  for (int m = 0; m < mstage && m < 8; m++) G.st[m] = A[m];
+  MultiArgs<T> M = multi_args<T>(L);
+  const int grid = (int)std::max<long long>(1, std::min<long long>(most, gmax));
+  void* args[] = {&M, &G};
+  void* fn = mixed32 ? (void*)k_group_euler<T, float> : (void*)k_group_euler<T, T>;
+  if (cudaLaunchCooperativeKernel(fn, grid, 256, args, 0, s) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return true;
+}
+
 void multi_euler(const MultiLevel& L, const StageArgs* A, int mstage, bool with_timestep, bool lfir, bool rt,
                  cudaStream_t s) {
+  if (L.coop) {
+    const bool done = L.f32 ? group_euler_coop<float>(L, A, mstage, with_timestep, lfir, rt, s)
+                            : group_euler_coop<double>(L, A, mstage, with_timestep, lfir, rt, s);
+    if (done) return;
+  }
   if (L.f32)
     multi_euler_t<float>(L, A, mstage, with_timestep, lfir, rt, s);
   else

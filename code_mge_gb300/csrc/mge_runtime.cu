@@ -2011,6 +2011,12 @@ int build_plan(mge_ctx* const* cs, int n, int mlvl, GroupPlan** out, std::string
       rc = plan_upload(G, &L.off[m], off, why);
     }
     if (rc) return bad(rc);
+    // small levels: the whole update of every case as one persistent
+    // cooperative launch (MGE_GROUP_COOP_MAX_CELLS: the group's cells up to
+    // which it does; 300,000 by default)
+    long long coop_max = 300000;
+    if (const char* e = getenv("MGE_GROUP_COOP_MAX_CELLS")) coop_max = atoll(e);
+    L.coop = L.tot[MK_PREP] <= coop_max;
   }
   G->pr.resize(nl > 1 ? nl - 1 : 0);
   for (int l = 0; l + 1 < nl; l++) {

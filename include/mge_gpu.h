@@ -216,9 +216,12 @@ int mge_prolong_async(mge_ctx* ctx, int mlvl);
  * loop).  One multigrid cycle at FMG level mlvl for every case of the
  * group: each phase of the cycle (time step, each stage's prep, face,
  * record, combine passes, the line sweeps, the boundary passes, the
- * transfers) is one launch over the block of that level of every case, and
- * the whole cycle is one captured CUDA graph, so the launches of a cycle do
- * not grow with the number of cases.  The reference's solver loops the
+ * transfers) is one launch over the block of that level of every case; on a
+ * level whose blocks hold at most MGE_GROUP_COOP_MAX_CELLS cells in all
+ * (environment, 300,000 by default) the whole update of every case is one
+ * persistent cooperative launch instead.  The whole cycle is one captured
+ * CUDA graph, so the launches of a cycle do not grow with the number of
+ * cases.  The reference's solver loops the
  * blocks of one case (solver.f90:151-157); this runs that loop over the
  * blocks of many cases at once, which has no counterpart there.  The cases
  * must share the level count, the multigrid and stage schedule, the CFL

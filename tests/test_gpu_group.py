@@ -1,5 +1,6 @@
 """Lockstep group cycles (mge_group_cycle_async / _poll): one launch per
-phase over the blocks of many cases of different sizes.
+phase over the blocks of many cases of different sizes, or, on the small
+levels, one persistent cooperative launch per update of every case.
 
 Each case of a group runs the same phase bodies in the same order as its
 own per-phase cycle, so the group's results must equal the cases' own
@@ -78,8 +79,10 @@ def _fmg_group(lib, cycs, cases):
     return hist
 
 
+@pytest.mark.parametrize("coop", ["0", "1000000000"])  # per-phase launches, or one persistent launch per update
 @pytest.mark.parametrize("precision", [A.MGE_PREC_FP64, A.MGE_PREC_MIXED])
-def test_group_cycles_equal_the_cases_own(gpulib, monkeypatch, precision):
+def test_group_cycles_equal_the_cases_own(gpulib, monkeypatch, precision, coop):
+    monkeypatch.setenv("MGE_GROUP_COOP_MAX_CELLS", coop)
     cases = _cases(precision)
     assert len({c.prm.nlevel for c in cases}) == 1
     single = _open(cases, monkeypatch)
