@@ -646,7 +646,9 @@ def run_pattern(args):
             "value": mixed["solves_per_s"], "p50_s": mixed["p50_s"], "p99_s": mixed["p99_s"],
             "submitted": mixed["submitted"], "completed": mixed["converged"], "unfinished": mixed["unfinished"],
             "peak_active": mixed["peak_active"], "offered_req_per_s": offered,
-            "overload": (offered / mixed["solves_per_s"]) if mixed["solves_per_s"] else None,
+            # requests finished (converged, retired as stalled or at max_cycles) per second
+            "service_req_per_s": mixed["finished"] / mixed["wall_s"] if mixed["wall_s"] else None,
+            "overload": (offered * mixed["wall_s"] / mixed["finished"]) if mixed["finished"] else None,
             "mixed_continuous_batching": mixed, "fp64_serial": serial,
             "speedup_solves_per_s": (mixed["solves_per_s"] / serial["solves_per_s"]) if serial["solves_per_s"]
             else None,

@@ -2348,6 +2348,40 @@ __device__ __forceinline__ void body_addw(const DevBlock<TF>& f, const DevBlock<
                                           const double* dc, long long t) {
   if (t >= (long long)f.nx * f.ny * f.nz) return;
   int i = 2 + (int)(t % f.nx), j = 2 + (int)((t / f.nx) % f.ny), k = 2 + (int)(t / ((long long)f.nx * f.ny));
+  if constexpr (std::is_same<TF, double>::value && std::is_same<TC, float>::value) {
+    // the mixed form's finest level under an FP32 coarse level: the coarse
+    // correction is FP32, so it is interpolated in FP32 (the same stencil
+    // and weights, exact in FP32 for power-of-two ratios) and added to the
+    // FP64 state in FP64
+    if (!fmg) {
+      const int ic[3] = {i, j, k}, nc[3] = {c.nx, c.ny, c.nz}, lc[3] = {c.il, c.jl, c.kl};
+      int sf[3];
+      float xf[3];
+      for (int d = 0; d < 3; d++) {
+        const float x = (float)ic[d] - 1.5f;
+        const float u = (float)X.o[d] + (X.rinv[d] > 0.0 ? x * (float)X.rinv[d] : x / (float)X.r[d]);
+        if (u < 0.0f || u >= (float)nc[d]) return;
+        int s = (int)floorf(u + 1.5f);
+        s = s < 2 ? 2 : (s > lc[d] - 1 ? lc[d] - 1 : s);
+        sf[d] = s;
+        xf[d] = u + 1.5f - (float)s;
+      }
+      const long long q = cidx(f.Pi, f.Pj, i, j, k);
+      if (f.blank[q] == 0) return;
+      const float wx[2] = {1.0f - xf[0], xf[0]}, wy[2] = {1.0f - xf[1], xf[1]}, wz[2] = {1.0f - xf[2], xf[2]};
+      for (int v = 0; v < 5; v++) {
+        float acc = 0.0f;
+        for (int dk = 0; dk < 2; dk++)
+          for (int dj = 0; dj < 2; dj++)
+            for (int di = 0; di < 2; di++) {
+              const long long cq = cidx(c.Pi, c.Pj, sf[0] + di, sf[1] + dj, sf[2] + dk);
+              acc = fmaf((float)dc[v * c.N + cq], wx[di] * wy[dj] * wz[dk], acc);
+            }
+        f.w[v * f.N + q] = f.w[v * f.N + q] + (double)acc;
+      }
+      return;
+    }
+  }
   int sh[3];
   double fac[8];
   if (!fine_to_coarse(X, c.nx, c.ny, c.nz, c.il, c.jl, c.kl, i, j, k, sh, fac)) return;
