@@ -80,8 +80,10 @@ def test_contracted_residual_is_the_fp64_residual(gpulib, monkeypatch, mk):
     cell fluxes).  On the same state, with the same FP32 time step, its dw,
     fw and updated state agree with the reference form's to FP64 rounding:
     relative to the field's largest value, 1e-10 on dw and fw (the residual
-    is a difference of fluxes up to 1e4 times larger) and 1e-12 on w; an FP32
-    evaluation would differ by 1e-7."""
+    is a difference of fluxes up to 1e4 times larger) and 1e-10 on w (the
+    FP32 line sweeps round the two updates apart by an FP32 ulp of the
+    update, itself some 1e-4 of the state); an FP32 residual would differ
+    by 1e-7 of the residual."""
     from code_mge_gb300.runtime import Cycle, physical
     from parity import rel_err
     case = mk()
@@ -106,6 +108,6 @@ def test_contracted_residual_is_the_fp64_residual(gpulib, monkeypatch, mk):
             assert rel_err(a, b) <= 1e-10, (lres, f, rel_err(a, b))
         if lres:  # a different evaluation, not the same bits
             assert not np.array_equal(fast.field("dw", L), ref.field("dw", L))
-    assert rel_err(fast.field("w", L), ref.field("w", L)) <= 1e-12
+    assert rel_err(fast.field("w", L), ref.field("w", L)) <= 1e-10
     ref.close()
     fast.close()
