@@ -14,7 +14,7 @@ module mge_gpu_mod
   integer(c_int), parameter :: MGE_EQN_EULER = 0, MGE_EQN_NS = 1
   integer(c_int), parameter :: MGE_DIS_CENTRAL = 0, MGE_DIS_ROE1 = 1, MGE_DIS_ROE2 = 2
   integer(c_int), parameter :: MGE_DISSIP_SCALAR = 0, MGE_DISSIP_MATRIX = 1
-  integer(c_int), parameter :: MGE_PREC_FP64 = 0, MGE_PREC_MIXED = 1
+  integer(c_int), parameter :: MGE_PREC_FP64 = 0, MGE_PREC_MIXED = 1, MGE_PREC_REFINED = 2
   integer, parameter :: MGE_MAX_STAGE = 8, MGE_MAX_LEVEL = 16, MGE_MAX_CLOUD = 8
 
   type, bind(C) :: mge_params
