@@ -2267,6 +2267,37 @@ __device__ __forceinline__ void body_collc(const DevBlock<TC>& c, const DevBlock
   int ic[3] = {X.o[0] + 2 + (int)(t % n0), X.o[1] + 2 + (int)((t / n0) % n1), X.o[2] + 2 + (int)(t / ((long long)n0 * n1))};
   if (ic[0] < 2 || ic[0] > c.il || ic[1] < 2 || ic[1] > c.jl || ic[2] < 2 || ic[2] > c.kl) return;
   const int lf[3] = {f.il, f.jl, f.kl};
+  if constexpr (std::is_same<TC, float>::value && std::is_same<TF, double>::value) {
+    // the mixed form's restriction from the FP64 finest level onto an FP32
+    // level: the values land in FP32 storage, so the averages are formed in
+    // FP32 (the same stencil; the 2:1 weights are exact in FP32)
+    int sf[3];
+    float xf[3];
+    for (int d = 0; d < 3; d++) {
+      const float tt = ((float)ic[d] - 1.5f - (float)X.o[d]) * (float)X.r[d];
+      int s = (int)floorf(tt + 1.5f);
+      s = s < 2 ? 2 : (s > lf[d] - 1 ? lf[d] - 1 : s);
+      sf[d] = s;
+      xf[d] = tt + 1.5f - (float)s;
+    }
+    const float wx[2] = {1.0f - xf[0], xf[0]}, wy[2] = {1.0f - xf[1], xf[1]}, wz[2] = {1.0f - xf[2], xf[2]};
+    const long long cc = cidx(c.Pi, c.Pj, ic[0], ic[1], ic[2]);
+    for (int v = 0; v < 5; v++) {
+      float ar = 0.0f, aw = 0.0f;
+      for (int dk = 0; dk < 2; dk++)
+        for (int dj = 0; dj < 2; dj++)
+          for (int di = 0; di < 2; di++) {
+            const long long fq = cidx(f.Pi, f.Pj, sf[0] + di, sf[1] + dj, sf[2] + dk);
+            const float wt = wx[di] * wy[dj] * wz[dk];
+            ar = fmaf((float)f.dw[v * f.N + fq] * f.rvolf, wt, ar);
+            aw = fmaf((float)f.w[v * f.N + fq], wt, aw);
+          }
+      c.wr[v * c.N + cc] = ar * (float)c.vol;
+      c.w[v * c.N + cc] = aw;
+    }
+    marker[cc] = 1;
+    return;
+  }
   int sh[3];
   double xi[3];
   for (int d = 0; d < 3; d++) {
