@@ -111,3 +111,33 @@ def test_group_refuses_cases_that_cannot_run_together(gpulib, monkeypatch):
     assert np.isfinite(cycs[1].cycle(1, ncyc=1))
     for c in cycs:
         c.close()
+
+
+def test_a_stop_in_one_case_leaves_the_others_of_the_group(gpulib, monkeypatch):
+    """A case whose state goes bad stops with the reference's code in its own
+    slot of the group's poll; the other cases' cycles are unaffected."""
+    cases = _cases(A.MGE_PREC_FP64)
+    single = _open(cases, monkeypatch)
+    group = _open(cases, monkeypatch)
+    L = 1
+    for c in single + group:
+        c.cycle(L, ncyc=1)
+    w = group[1].field("w", L).copy()
+    w[0, 4, 4, 4] = -abs(w[0, 4, 4, 4])  # a negative density: timestep.f90:45-48
+    group[1].upload(w, L)
+    n = len(group)
+    arr = (C.c_void_p * n)(*[c.ctx.value for c in group])
+    res = (C.c_double * n)()
+    rcs = (C.c_int * n)()
+    assert gpulib.mge_group_cycle_async(arr, n, L) == 0
+    rc = 1
+    while rc == 1:
+        rc = gpulib.mge_group_cycle_poll(arr, n, 2, res, rcs)
+    assert rc == 0
+    assert list(rcs) == [0, A.MGE_ENEGPRESS, 0]
+    assert b"timestep.f90:45-48" in gpulib.mge_last_error(group[1].ctx)
+    for q in (0, 2):
+        assert res[q] == single[q].cycle(L, ncyc=2)
+        assert np.array_equal(group[q].field("w", L), single[q].field("w", L))
+    for c in single + group:
+        c.close()
