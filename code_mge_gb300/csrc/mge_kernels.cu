@@ -1425,11 +1425,12 @@ __device__ __forceinline__ void body_irs_mixed(const DevBlock<double>& b, const 
 // rows.  Each lane composes the maps of K consecutive rows, a warp scan of
 // the composed maps gives every lane the value entering its rows, and the
 // lane applies its maps in order.  Loads and stores of a warp cover one
-// contiguous line.  FP32 arithmetic on the FP64 residual; the result goes
-// to the FP32 copy the j and k sweeps continue on (every row of the line,
-// blanked rows with their unsmoothed value).
-template <int K>
-__global__ void __launch_bounds__(256) k_irs_scan_i(DevBlock<double> b, IrsTables tb, float bb, float* cp) {
+// contiguous line.  FP32 arithmetic: on the FP64 residual of the mixed
+// form's finest level, the result going to the FP32 copy the j and k sweeps
+// continue on; or on an FP32 level's residual, in place (every row of the
+// line, blanked rows with their unsmoothed value).
+template <int K, typename T = double>
+__global__ void __launch_bounds__(256) k_irs_scan_i(DevBlock<T> b, IrsTables tb, float bb, float* cp) {
   const long long lines = (long long)b.ny * b.nz;
   const long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
@@ -1439,7 +1440,7 @@ __global__ void __launch_bounds__(256) k_irs_scan_i(DevBlock<double> b, IrsTable
   const int j = 2 + (int)(ln % b.ny), k = 2 + (int)(ln / b.ny);
   const long long c0 = cidx(b.Pi, b.Pj, 0, j, k);
   const int l = b.il;
-  const double* src = b.dw + (long long)v * b.N + c0;
+  const T* src = b.dw + (long long)v * b.N + c0;  // read whole into registers before any write
   float* dst = cp + (long long)v * b.N + c0;
   const uint8_t* bl = b.blank + c0;
   const int q0 = 2 + lane * K;
@@ -3095,6 +3096,20 @@ void launch_irs_dir(const DevBlock<T>& b, const IrsTables& tb, TC bb, cudaStream
   const int len = (D == 0 ? b.il : (D == 1 ? b.jl : b.kl)) - 1;
   constexpr int LT = 64;
   const size_t sm = irs_smem_bytes<TC, LT>(len | 1);
+  if constexpr (D == 0 && std::is_same<T, float>::value && std::is_same<TC, float>::value) {
+    const int kk = irs_scan_k(len);
+    if (variant == 2 && kk) {  // one warp per (line, variable), in place
+      const unsigned g = (unsigned)nblk(32 * 5 * lines, 256);
+      float* out = (float*)b.dw;
+      if (kk == 2) k_irs_scan_i<2, float><<<g, 256, 0, s>>>(b, tb, bb, out);
+      if (kk == 4) k_irs_scan_i<4, float><<<g, 256, 0, s>>>(b, tb, bb, out);
+      if (kk == 6) k_irs_scan_i<6, float><<<g, 256, 0, s>>>(b, tb, bb, out);
+      if (kk == 8) k_irs_scan_i<8, float><<<g, 256, 0, s>>>(b, tb, bb, out);
+      if (kk == 12) k_irs_scan_i<12, float><<<g, 256, 0, s>>>(b, tb, bb, out);
+      if (kk == 16) k_irs_scan_i<16, float><<<g, 256, 0, s>>>(b, tb, bb, out);
+      return;
+    }
+  }
   if (variant == 1 && sm <= 200 * 1024) {
     const long long grid = 5 * ((lines + LT - 1) / LT);
     k_irs_smem<T, TC, D, LT><<<(unsigned)grid, LT, sm, s>>>(b, tb, bb);

@@ -1080,8 +1080,9 @@ static int autotune_block(mge_ctx* c, Block& b, bool tune_path) {
     for (int d = 0; d < 3; d++) {
       float best = 1e30f;
       int bv = 0;
-      // variant 2, the warp-scan i sweep, exists for the mixed form's finest level
-      const int nvar = (d == 0 && b.aux32 && !b.f32) ? 3 : 2;
+      // variant 2, the warp-scan i sweep, exists for the FP32 sweeps (the
+      // mixed form's finest level and its FP32 levels)
+      const int nvar = (d == 0 && (b.aux32 || b.f32)) ? 3 : 2;
       for (int v = 0; v < nvar; v++) {
         int var[3] = {0, 0, 0};
         var[d] = v;

@@ -2,6 +2,8 @@
 on the finest level, FP64 finest residual, update, norm and forces.  The
 multigrid then acts as a defect correction: the converged answer must match
 the FP64 plain solve (and hence the FP64 oracle) to the stated tolerance."""
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -111,3 +113,32 @@ def test_contracted_residual_is_the_fp64_residual(gpulib, monkeypatch, mk):
     assert rel_err(fast.field("w", L), ref.field("w", L)) <= 1e-10
     ref.close()
     fast.close()
+
+
+def test_warp_scan_sweeps_agree_with_the_line_sweeps(gpulib, monkeypatch):
+    """The FP32 i sweep as a warp scan of affine row maps (launch-form digit 2),
+    on the mixed form's finest level and in place on its FP32 coarse levels,
+    against the sequential line sweeps (digit 0): the same solve to FP32
+    rounding of the smoothed residuals."""
+    from code_mge_gb300.runtime import Cycle
+    case = K.sphere_box(n=32, nlevel=3, extent=3.0, radius=0.7, mgtype=2, mcyc_fine=8, precision=A.MGE_PREC_MIXED)
+    runs = []
+    for digit in "02":
+        monkeypatch.setenv("MGE_TUNE_PLAN", ",".join("%d:0%s00" % (L, digit) for L in (1, 2, 3)))
+        g = Cycle(case)
+        tuned = []
+        for L in (1, 2, 3):
+            coop = C.c_int()
+            irs = (C.c_int * 3)()
+            assert gpulib.mge_tuned(g.ctx, L, 1, C.byref(coop), irs) == A.MGE_OK
+            tuned.append(irs[0])
+        hist, n, fo = g.solve()
+        runs.append((tuned, hist, g.field("w", 3), fo.cd))
+        g.close()
+    (t0, h0, w0, cd0), (t2, h2, w2, cd2) = runs
+    assert t0 == [0, 0, 0] and t2 == [2, 2, 2]
+    assert len(h0) == len(h2) > 0
+    assert not np.array_equal(h0, h2)  # the scan ran, and rounds differently
+    assert np.max(np.abs(h2 - h0) / h0) < 1e-4
+    assert np.max(np.abs(w2 - w0)) / np.max(np.abs(w0)) < 1e-6
+    assert abs(cd2 - cd0) < 1e-6 * max(1.0, abs(cd0))
