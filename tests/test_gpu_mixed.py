@@ -118,14 +118,17 @@ def test_contracted_residual_is_the_fp64_residual(gpulib, monkeypatch, mk):
 def test_warp_scan_sweeps_agree_with_the_line_sweeps(gpulib, monkeypatch):
     """The FP32 i sweep as a warp scan of affine row maps (launch-form digit 2),
     on the mixed form's finest level and in place on its FP32 coarse levels,
-    against the sequential line sweeps (digit 0): the same solve to FP32
-    rounding of the smoothed residuals."""
+    against the sequential line sweeps (digit 0).  Both round in FP32, in a
+    different order.  The scan must move the solve by about as much as the
+    mixed form's FP32 arithmetic moves it from the FP64 solve of the same
+    case: the early cycles amplify any rounding difference alike, so the two
+    differences are of one order, and the test allows a factor of 10."""
     from code_mge_gb300.runtime import Cycle
-    case = K.sphere_box(n=32, nlevel=3, extent=3.0, radius=0.7, mgtype=2, mcyc_fine=8, precision=A.MGE_PREC_MIXED)
+    make = lambda prec: K.sphere_box(n=32, nlevel=3, extent=3.0, radius=0.7, mgtype=2, mcyc_fine=8, precision=prec)
     runs = []
     for digit in "02":
         monkeypatch.setenv("MGE_TUNE_PLAN", ",".join("%d:0%s00" % (L, digit) for L in (1, 2, 3)))
-        g = Cycle(case)
+        g = Cycle(make(A.MGE_PREC_MIXED))
         tuned = []
         for L in (1, 2, 3):
             coop = C.c_int()
@@ -135,10 +138,16 @@ def test_warp_scan_sweeps_agree_with_the_line_sweeps(gpulib, monkeypatch):
         hist, n, fo = g.solve()
         runs.append((tuned, hist, g.field("w", 3), fo.cd))
         g.close()
+    monkeypatch.delenv("MGE_TUNE_PLAN")
+    g = Cycle(make(A.MGE_PREC_FP64))
+    h64, _, f64 = g.solve()
+    w64 = g.field("w", 3)
+    g.close()
     (t0, h0, w0, cd0), (t2, h2, w2, cd2) = runs
     assert t0 == [0, 0, 0] and t2 == [2, 2, 2]
-    assert len(h0) == len(h2) > 0
+    assert len(h0) == len(h2) == len(h64) > 0
     assert not np.array_equal(h0, h2)  # the scan ran, and rounds differently
-    assert np.max(np.abs(h2 - h0) / h0) < 1e-4
-    assert np.max(np.abs(w2 - w0)) / np.max(np.abs(w0)) < 1e-6
-    assert abs(cd2 - cd0) < 1e-6 * max(1.0, abs(cd0))
+    ratios = (np.max(np.abs(h2 - h0)) / np.max(np.abs(h0 - h64)),
+              np.max(np.abs(w2 - w0)) / np.max(np.abs(w0 - w64)),
+              abs(cd2 - cd0) / max(abs(cd0 - f64.cd), 1e-7 * abs(cd0)))
+    assert max(ratios) < 10.0, ratios
