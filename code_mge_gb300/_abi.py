@@ -86,6 +86,10 @@ _pi32 = C.POINTER(C.c_int32)
 _pd = C.POINTER(C.c_double)
 
 
+# MGE_ABI_VERSION of include/mge_gpu.h: the layout of the structs below
+MGE_ABI_VERSION = 2
+
+
 class MgeBlockDesc(C.Structure):
     _fields_ = [
         ("nx", _i),
@@ -114,6 +118,7 @@ class MgeBlockDesc(C.Structure):
         ("parent", _i),
         ("ratio", _i * 3),
         ("offset", _i * 3),
+        ("psurf", _pd),
     ]
 
 
@@ -154,6 +159,8 @@ SIGNATURES = [
     ("forces_compute", _i, [_vp, _i, C.POINTER(MgeSolveOpts), C.POINTER(MgeForces)]),
     ("upload_solut", _i, [_vp, _i, _i, _d, _pd, C.c_size_t, C.POINTER(_i)]),
     ("time_advance", _i, [_vp, C.POINTER(_i)]),
+    ("move_surface", _i, [_vp, _i, _i, _pd, _pd, _pd, _d]),
+    ("get_surface", _i, [_vp, _i, _i, _pd]),
 ]
 
 # entry points only the product library has (mge_init also takes the device)
@@ -198,7 +205,7 @@ HEADER_SYMBOLS = [
     "mge_cycle", "mge_cycle_async", "mge_cycle_poll", "mge_group_cycle_async", "mge_group_cycle_poll", "mge_prolong_async", "mge_set_coop_ctas", "mge_device_mem", "mge_tuned", "mge_set_precision",
     "mge_coop_trace", "mge_last_cycle_ms", "mge_launch_count", "mge_kernel_times", "mge_residual_norm_noalloc", "mge_euler_partial", "mge_device_bytes", "mge_sync",
     "mge_upload_solut", "mge_write_restart", "mge_read_restart", "mge_restart_format", "mge_restart_parse",
-    "mge_time_advance",
+    "mge_time_advance", "mge_move_surface", "mge_get_surface",
 ]
 
 

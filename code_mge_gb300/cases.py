@@ -272,7 +272,8 @@ def make_block_arrays(spec: BlockSpec, body: Body):
     spec.arrays = dict(blank=np.ascontiguousarray(blank.ravel()), nmir=nm, ccid=ccid, scid=scid,
                        faceid=faceid, zz=zz, npoint=npoint, ijkdex=ijkdex, coef=coef, nvec=nvec,
                        qb=(np.ascontiguousarray(body.wall_velocity(xw), dtype=np.float64)
-                           if (nm and body.wall_velocity is not None) else np.zeros((nm, 3))), area=area)
+                           if (nm and body.wall_velocity is not None) else np.zeros((nm, 3))), area=area,
+                       psurf=np.ascontiguousarray(xw, dtype=np.float64) if nm else np.zeros((0, 3)))
     return spec
 
 
@@ -349,6 +350,9 @@ def block_desc(spec: BlockSpec):
     d.parent = spec.parent
     d.ratio[:] = spec.ratio
     d.offset[:] = spec.offset
+    if a.get("psurf") is not None:
+        a["psurf"] = np.ascontiguousarray(a["psurf"], dtype=np.float64)
+        d.psurf = _ptr(a["psurf"], A.C.c_double)
     return d
 
 

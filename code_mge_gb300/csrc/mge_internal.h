@@ -256,5 +256,9 @@ void launch_overlap(const DevBlock<T>& g, const DevBlock<T>& p, const long long*
 int rtrms_partials(long long ncells);
 void init_kernel_attributes();
 void launch_convert(const void* src, bool src32, void* dst, bool dst32, long long n, cudaStream_t s);
+// movsurf.f90:31 and bc_cutcell.f90:50 over nmir records: pnew = psurf + pnew
+// (pnew holds the displacements on entry), qb = qb / vel_fs (qb holds the
+// wall velocities on entry)
+void launch_movsurf(long long nmir, const double* psurf, double* pnew, double* qb, double vel_fs, cudaStream_t s);
 
 }  // namespace mge

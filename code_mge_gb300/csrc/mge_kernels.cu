@@ -3258,6 +3258,20 @@ void launch_convert(const void* src, bool src32, void* dst, bool dst32, long lon
   else k_convert<double, double><<<nblk(n, TPB), TPB, 0, s>>>((const double*)src, (double*)dst, n);
 }
 
+// movsurf.f90:31 (pnew = psurf + disp) and the wall velocity of
+// bc_cutcell.f90:50 (qb = vel/vel_fs), one thread per record component
+__global__ void k_movsurf(long long n3, const double* psurf, double* pnew, double* qb, double vel_fs) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n3) return;
+  pnew[t] = psurf[t] + pnew[t];
+  qb[t] = qb[t] / vel_fs;
+}
+
+void launch_movsurf(long long nmir, const double* psurf, double* pnew, double* qb, double vel_fs, cudaStream_t s) {
+  if (nmir <= 0) return;
+  k_movsurf<<<nblk(3 * nmir, TPB), TPB, 0, s>>>(3 * nmir, psurf, pnew, qb, vel_fs);
+}
+
 // opt-in shared memory of the tiled line sweeps; called once per device at set-up
 void init_kernel_attributes() {
 #define MGE_SMEM_ATTR(T, TC)                                                                                     \

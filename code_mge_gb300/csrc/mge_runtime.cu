@@ -32,7 +32,7 @@ namespace {
 struct HRec {
   int ccid[3], scid[3], faceid, zz, npoint;
   int ijk[MGE_MAX_CLOUD][3];
-  double coef[MGE_MAX_CLOUD], nvec[3], qb[3], area;
+  double coef[MGE_MAX_CLOUD], nvec[3], qb[3], area, psurf[3];
 };
 
 struct Block {
@@ -73,6 +73,7 @@ struct Block {
   int32_t* cutmap = nullptr;
   int32_t *rec_i = nullptr, *rec_cloud = nullptr, *tgt_off = nullptr, *tgt_ops = nullptr;
   double *rec_coef = nullptr, *rec_nvec = nullptr, *rec_qb = nullptr, *rec_area = nullptr;
+  double *rec_psurf = nullptr, *rec_pnew = nullptr;  // [nmir][3] surface points, as given and as moved
   void *rec_wsol = nullptr, *rec_psol = nullptr, *rec_wall = nullptr;
   double* irs = nullptr;
   float* irs32 = nullptr;
@@ -581,7 +582,7 @@ int commit_block(mge_ctx* c, Block& b, double* scratch) {
     }
   std::vector<int32_t> ri(8 * std::max(nm, 1), 0), rcl(24 * std::max(nm, 1), 0);
   std::vector<double> rcf(8 * std::max(nm, 1), 0.0), rnv(3 * std::max(nm, 1), 0.0), rqb(3 * std::max(nm, 1), 0.0),
-      rar(std::max(nm, 1), 0.0);
+      rar(std::max(nm, 1), 0.0), rps(3 * std::max(nm, 1), 0.0);
   for (int m = 0; m < nm; m++) {
     const HRec& t = b.recs[m];
     ri[8 * m + 0] = t.ccid[0];
@@ -598,6 +599,7 @@ int commit_block(mge_ctx* c, Block& b, double* scratch) {
     for (int e = 0; e < 3; e++) {
       rnv[3 * m + e] = t.nvec[e];
       rqb[3 * m + e] = t.qb[e];
+      rps[3 * m + e] = t.psurf[e];
     }
     rar[m] = t.area;
   }
@@ -612,6 +614,7 @@ int commit_block(mge_ctx* c, Block& b, double* scratch) {
   if ((rc = dalloc(c, &b.rec_i, 8 * nma)) || (rc = dalloc(c, &b.rec_cloud, 24 * nma)) ||
       (rc = dalloc(c, &b.rec_coef, 8 * nma)) || (rc = dalloc(c, &b.rec_nvec, 3 * nma)) ||
       (rc = dalloc(c, &b.rec_qb, 3 * nma)) || (rc = dalloc(c, &b.rec_area, nma)) ||
+      (rc = dalloc(c, &b.rec_psurf, 3 * nma)) || (rc = dalloc(c, &b.rec_pnew, 3 * nma)) ||
       (rc = valloc(c, &b.rec_wsol, 5 * nma, es)) || (rc = valloc(c, &b.rec_psol, nma, es)) ||
       (rc = valloc(c, &b.rec_wall, 25 * nma, es)))
     return rc;
@@ -621,6 +624,8 @@ int commit_block(mge_ctx* c, Block& b, double* scratch) {
   CK(cudaMemcpy(b.rec_nvec, rnv.data(), rnv.size() * 8, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(b.rec_qb, rqb.data(), rqb.size() * 8, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(b.rec_area, rar.data(), rar.size() * 8, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b.rec_psurf, rps.data(), rps.size() * 8, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b.rec_pnew, rps.data(), rps.size() * 8, cudaMemcpyHostToDevice));
   // cut targets: per physical cell, the (record, role) ops in record order
   std::vector<int32_t> cutmap(N, -1);
   std::map<long long, std::vector<int32_t>> tg;
@@ -881,6 +886,7 @@ int mge_add_block(mge_ctx* c, const mge_block_desc* d, int level, int serial) {
       t.scid[q] = d->scid[3 * m + q];
       t.nvec[q] = d->nvec[3 * m + q];
       t.qb[q] = d->qb ? d->qb[3 * m + q] : 0.0;
+      t.psurf[q] = d->psurf ? d->psurf[3 * m + q] : 0.0;
     }
     t.faceid = d->faceid[m];
     t.zz = d->zz[m];
@@ -1477,6 +1483,35 @@ int mge_time_advance(mge_ctx* c, int* itime_out) {
   c->itime += 1;
   if (itime_out) *itime_out = c->itime;
   return MGE_OK;
+}
+
+int mge_move_surface(mge_ctx* c, int level, int serial, const double* disp, const double* norv, const double* vel,
+                     double vel_fs) {
+  Block* b = getb(c, level, serial);
+  if (!b || !c->committed) return MGE_ENOTFOUND;
+  if (c->group_pending) return fail(c, MGE_EBADCFG, "move_surface: a group cycle is in flight");
+  if (!(vel_fs > 0.0)) return fail(c, MGE_EBADCFG, "move_surface: vel_fs must be positive");
+  const long long nm = (long long)b->recs.size();
+  if (!nm) return MGE_OK;
+  if (!disp || !norv || !vel) return fail(c, MGE_EBADCFG, "move_surface: null record array");
+  CK(cudaSetDevice(c->device));
+  // queued behind the context's earlier work, so a cycle in flight sees the
+  // old surface and the next one the new
+  CK(cudaMemcpyAsync(b->rec_nvec, norv, 3 * nm * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(b->rec_pnew, disp, 3 * nm * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(b->rec_qb, vel, 3 * nm * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  launch_movsurf(nm, b->rec_psurf, b->rec_pnew, b->rec_qb, vel_fs, c->stream);
+  CK(cudaGetLastError());
+  return check_err(c);
+}
+
+int mge_get_surface(mge_ctx* c, int level, int serial, double* pnew) {
+  Block* b = getb(c, level, serial);
+  if (!b || !c->committed || !pnew) return MGE_ENOTFOUND;
+  CK(cudaSetDevice(c->device));
+  CK(cudaStreamSynchronize(c->stream));
+  CK(cudaMemcpy(pnew, b->rec_pnew, 3 * b->recs.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  return check_err(c);
 }
 
 int mge_forces_compute(mge_ctx* c, int level, const mge_solve_opts* o, mge_forces* out) {

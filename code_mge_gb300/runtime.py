@@ -39,8 +39,9 @@ def load_library():
     lib = C.CDLL(path)
     A.bind(lib, "mge_", A.SIGNATURES)
     A.bind(lib, "mge_", A.PRODUCT_ONLY)
-    if lib.mge_abi_version() != 1:
-        raise RuntimeError("libmge_gpu.so ABI mismatch")
+    if lib.mge_abi_version() != A.MGE_ABI_VERSION:
+        raise RuntimeError("libmge_gpu.so ABI mismatch: library %d, bindings %d" % (lib.mge_abi_version(),
+                                                                                    A.MGE_ABI_VERSION))
     _LIB = lib
     return lib
 
@@ -128,6 +129,27 @@ class Cycle:
         it = C.c_int(0)
         self._chk(self._fn("time_advance")(self.ctx, C.byref(it)), "time_advance")
         return it.value
+
+    def move_surface(self, level, disp, norv, vel, vel_fs, serial=1):
+        """movsurf.f90:28-35 for one block: per record pnew = psurf + disp, the
+        wall normal norv and the wall velocity vel/vel_fs ([nmir, 3] arrays in
+        record order)."""
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (disp, norv, vel)]
+        nm = self.spec(level, serial).arrays["nmir"]
+        for a in arrs:
+            if a.shape != (nm, 3):
+                raise ValueError("move_surface: arrays must be [%d, 3]" % nm)
+        ptr = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+        return self._chk(self._fn("move_surface")(self.ctx, level, serial, ptr(arrs[0]), ptr(arrs[1]), ptr(arrs[2]),
+                                                  float(vel_fs)), "move_surface")
+
+    def surface(self, level, serial=1):
+        """The records' moved points pnew, [nmir, 3]."""
+        nm = self.spec(level, serial).arrays["nmir"]
+        out = np.zeros((max(nm, 1), 3))
+        self._chk(self._fn("get_surface")(self.ctx, level, serial, out.ctypes.data_as(C.POINTER(C.c_double))),
+                  "get_surface")
+        return out[:nm]
 
     def forces(self, level=None):
         level = self.case.prm.nlevel if level is None else level

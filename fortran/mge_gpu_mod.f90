@@ -46,6 +46,7 @@ module mge_gpu_mod
     type(c_ptr)    :: coef, nvec, qb, area
     integer(c_int) :: parent
     integer(c_int) :: ratio(3), offset(3)
+    type(c_ptr)    :: psurf                   ! [nmir][3] z(m)%psurf, or c_null_ptr
   end type mge_block_desc
 
   type, bind(C) :: mge_forces
@@ -187,6 +188,22 @@ module mge_gpu_mod
       import :: c_int, c_ptr
       type(c_ptr), value :: ctx
       integer(c_int), intent(out) :: itime_out
+    end function
+    ! movsurf.f90:28-35 at solver.f90:117 (approxbc on), per block:
+    ! pnew = psurf + disp, normal norv, qb = vel/vel_fs; arrays (3, nmir)
+    integer(c_int) function mge_move_surface(ctx, level, serial, disp, norv, vel, vel_fs) &
+        bind(C, name="mge_move_surface")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: level, serial
+      real(c_double), intent(in) :: disp(*), norv(*), vel(*)
+      real(c_double), value :: vel_fs
+    end function
+    integer(c_int) function mge_get_surface(ctx, level, serial, pnew) bind(C, name="mge_get_surface")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: level, serial
+      real(c_double), intent(out) :: pnew(*)
     end function
     integer(c_int) function mge_residual_norm_noalloc(dw_rho, vdtim, blank, nx, ny, nz, cfl, vt, dtim, &
         norm_out, stream) bind(C, name="mge_residual_norm_noalloc")

@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define MGE_ABI_VERSION 1
+#define MGE_ABI_VERSION 2
 
 /* status codes */
 #define MGE_OK           0
@@ -127,6 +127,9 @@ typedef struct mge_block_desc {
   int    parent;                  /* serial of the parent block on level-1 */
   int    ratio[3];                /* h_parent / h per axis (1 or 2) */
   int    offset[3];               /* origin = parent origin + offset * h_parent */
+  /* the records' ray-surface intersection points z(m)%psurf, the base of the
+   * moved points of mge_move_surface; NULL = zeros */
+  const double*  psurf;           /* [nmir][3] */
 } mge_block_desc;
 
 /* Cut-cell wall forces (new: the reference has no Cl/Cd integrator): the
@@ -335,6 +338,28 @@ int mge_read_restart(mge_ctx* ctx, const char* path, const int* codes, int ncode
  * starts at 0 at mge_init_flow; the transient source of euler.f90:249-275
  * applies from itime 1 on. */
 int mge_time_advance(mge_ctx* ctx, int* itime_out);
+
+/* movsurf.f90:28-35 for one block, called where solver.f90:117 calls it (at
+ * the start of each physical step, approxbc on), with the kinematics the
+ * reference's FSI framework supplies per record, host arrays [nmir][3] in
+ * mge_add_block's record order:
+ *   pnew = psurf + disp   (movsurf.f90:31; read back by mge_get_surface)
+ *   wall normal = norv    (bc_cutcell.f90:49; normalised where it is used,
+ *                          bc_cutcell.f90:57-58, so it need not be unit)
+ *   qb = vel / vel_fs     (bc_cutcell.f90:50; vel_fs is input_param.f90:51's
+ *                          rm*sqrt(gamma*gas_pmean/gas_rhomean))
+ * The new normal and wall velocity take effect from the next stage on, in
+ * the cut-cell state, the wall fluxes and the no-slip wall.  The reference's
+ * approxbc-off state is the descriptor's nvec and qb; a context goes back to
+ * it by a call with disp 0, norv = nvec and vel = qb*vel_fs.  Ordered after
+ * the work already queued on the context; MGE_EBADCFG while the context is
+ * part of a group cycle in flight, or when vel_fs is not positive. */
+int mge_move_surface(mge_ctx* ctx, int level, int serial, const double* disp, const double* norv,
+                     const double* vel, double vel_fs);
+
+/* The records' moved points pnew [nmir][3] (psurf before the first
+ * mge_move_surface). */
+int mge_get_surface(mge_ctx* ctx, int level, int serial, double* pnew);
 
 /* The same text for one block, without a context or a GPU: returns the bytes
  * of the text (writing at most cap-1 of them and a NUL into buf when buf is

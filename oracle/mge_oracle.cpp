@@ -49,6 +49,7 @@ struct ORec {
   int ijk[MGE_MAX_CLOUD][3];
   double coef[MGE_MAX_CLOUD];
   double nvec[3], qb[3], area;
+  double psurf[3], pnew[3];  // the surface point and its moved position (movsurf.f90:31)
   double psol, wsol[5];
 };
 
@@ -1066,7 +1067,9 @@ int bcond(mgeo_ctx* c, OBlock& b) {
   return MGE_OK;
 }
 
-/* bc_cutcell.f90:40-268 (approxbc off: qb from the record, 0 for a fixed wall) */
+/* bc_cutcell.f90:40-268.  The normal and the wall velocity are the record's:
+   the descriptor's nvec and qb (approxbc off, qb 0 for a fixed wall), or
+   norv and vel/vel_fs after mgeo_move_surface (approxbc on, :47-50) */
 int bc_cutcell(mgeo_ctx* c, OBlock& b) {
   const mge_params& P = c->prm;
   for (size_t m = 0; m < b.z.size(); m++) {
@@ -1980,6 +1983,8 @@ int mgeo_add_block(mgeo_ctx* c, const mge_block_desc* d, int level, int serial) 
       t.scid[q] = d->scid[3 * m + q];
       t.nvec[q] = d->nvec[3 * m + q];
       t.qb[q] = d->qb ? d->qb[3 * m + q] : 0.0;
+      t.psurf[q] = d->psurf ? d->psurf[3 * m + q] : 0.0;
+      t.pnew[q] = t.psurf[q];
     }
     t.faceid = d->faceid[m];
     t.zz = d->zz[m];
@@ -2193,6 +2198,34 @@ int mgeo_time_advance(mgeo_ctx* c, int* itime_out) {
     }
   c->itime += 1;
   if (itime_out) *itime_out = c->itime;
+  return MGE_OK;
+}
+
+/* movsurf.f90:28-35 for one block, with bc_cutcell.f90:47-50's use of it:
+   pnew = psurf + disp, the normal norv, the wall velocity vel/vel_fs */
+int mgeo_move_surface(mgeo_ctx* c, int level, int serial, const double* disp, const double* norv,
+                      const double* vel, double vel_fs) {
+  OBlock* b = getb(c, level, serial);
+  if (!b) return MGE_ENOTFOUND;
+  if (!(vel_fs > 0.0)) return fail(c, MGE_EBADCFG, "move_surface: vel_fs must be positive");
+  if (b->z.empty()) return MGE_OK;
+  if (!disp || !norv || !vel) return fail(c, MGE_EBADCFG, "move_surface: null record array");
+  for (size_t m = 0; m < b->z.size(); m++) {
+    ORec& t = b->z[m];
+    for (int q = 0; q < 3; q++) {
+      t.pnew[q] = t.psurf[q] + disp[3 * m + q];
+      t.nvec[q] = norv[3 * m + q];
+      t.qb[q] = vel[3 * m + q] / vel_fs;
+    }
+  }
+  return MGE_OK;
+}
+
+int mgeo_get_surface(mgeo_ctx* c, int level, int serial, double* pnew) {
+  OBlock* b = getb(c, level, serial);
+  if (!b || !pnew) return MGE_ENOTFOUND;
+  for (size_t m = 0; m < b->z.size(); m++)
+    for (int q = 0; q < 3; q++) pnew[3 * m + q] = b->z[m].pnew[q];
   return MGE_OK;
 }
 

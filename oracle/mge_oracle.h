@@ -51,6 +51,9 @@ int  mgeo_forces_compute(mgeo_ctx* ctx, int level, const mge_solve_opts* opts,
 int  mgeo_upload_solut(mgeo_ctx* ctx, int level, int serial, double p_tot, double* solut,
                        size_t count, int* nval_out);
 int  mgeo_time_advance(mgeo_ctx* ctx, int* itime_out);
+int  mgeo_move_surface(mgeo_ctx* ctx, int level, int serial, const double* disp, const double* norv,
+                       const double* vel, double vel_fs);
+int  mgeo_get_surface(mgeo_ctx* ctx, int level, int serial, double* pnew);
 /* threads used by the loops of the oracle (1 = the serial mgsol analogue) */
 void mgeo_set_threads(int n);
 int  mgeo_get_threads(void);

@@ -45,18 +45,21 @@ def test_struct_layout_matches_c(tmp_path):
 #include "mge_gpu.h"
 int main(void){
  printf("%zu %zu %zu %zu\\n", sizeof(mge_params), sizeof(mge_block_desc), sizeof(mge_forces), sizeof(mge_solve_opts));
- printf("%zu %zu %zu %zu %zu\\n", offsetof(mge_params, mcyc), offsetof(mge_params, conv_drop),
-        offsetof(mge_block_desc, blank), offsetof(mge_block_desc, parent), offsetof(mge_block_desc, offset));
+ printf("%zu %zu %zu %zu %zu %zu\\n", offsetof(mge_params, mcyc), offsetof(mge_params, conv_drop),
+        offsetof(mge_block_desc, blank), offsetof(mge_block_desc, parent), offsetof(mge_block_desc, offset),
+        offsetof(mge_block_desc, psurf));
+ printf("%d\\n", MGE_ABI_VERSION);
  return 0;}''')
     exe = tmp_path / "lay"
     subprocess.check_call(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
-    a, b = subprocess.run([str(exe)], capture_output=True, text=True).stdout.split("\n")[:2]
+    a, b, v = subprocess.run([str(exe)], capture_output=True, text=True).stdout.split("\n")[:3]
     sizes = [int(x) for x in a.split()]
     offs = [int(x) for x in b.split()]
     assert sizes == [C.sizeof(A.MgeParams), C.sizeof(A.MgeBlockDesc), C.sizeof(A.MgeForces),
                      C.sizeof(A.MgeSolveOpts)]
     assert offs == [A.MgeParams.mcyc.offset, A.MgeParams.conv_drop.offset, A.MgeBlockDesc.blank.offset,
-                    A.MgeBlockDesc.parent.offset, A.MgeBlockDesc.offset.offset]
+                    A.MgeBlockDesc.parent.offset, A.MgeBlockDesc.offset.offset, A.MgeBlockDesc.psurf.offset]
+    assert int(v) == A.MGE_ABI_VERSION
 
 
 def test_init_rejects_bad_config_without_gpu(gpulib):
