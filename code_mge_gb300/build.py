@@ -16,7 +16,7 @@ OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libmge_gpu.so")
 ROOT = os.path.dirname(HERE)
 SOURCES = ["mge_kernels.cu", "mge_runtime.cu", "mge_noalloc.cu", "mge_restart.cpp"]
-HEADERS = ["mge_internal.h", "exact_ops.cuh", "fast_pow.cuh"]
+HEADERS = ["mge_internal.h", "exact_ops.cuh", "fast_pow.cuh", "soft_fp64.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "--fmad=false", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
               "-I", os.path.join(ROOT, "include")]

@@ -35,12 +35,18 @@
 #include "exact_ops.cuh"
 #include "fast_pow.cuh"
 #include "mge_internal.h"
+#include "soft_fp64.cuh"
 
 namespace cg = cooperative_groups;
 
 namespace mge {
 
 // --------------------------------------------------------------- helpers
+// a * b, for doubles on the integer pipes (soft_fp64.cuh: the same bits as
+// the FP64 multiply), so that a kernel bound by the FP64 issue rate can move
+// some of its independent products off the FP64 pipe
+__device__ __forceinline__ double smul(double a, double b) { return soft::mul(a, b); }
+__device__ __forceinline__ float smul(float a, float b) { return a * b; }
 __device__ __forceinline__ double mdiv(double a, double b, double y) {
   double q = a * y;
   double r = fma(-q, b, a);
@@ -51,6 +57,15 @@ __device__ __forceinline__ float mdiv(float a, float b, float y) {
   float r = fmaf(-q, b, a);
   return fmaf(r, y, q);
 }
+// mdiv with its first product on the integer pipes (smul, below): the same
+// quotient
+__device__ __forceinline__ double smul(double a, double b);
+__device__ __forceinline__ double smdiv(double a, double b, double y) {
+  double q = smul(a, y);
+  double r = fma(-q, b, a);
+  return fma(r, y, q);
+}
+__device__ __forceinline__ float smdiv(float a, float b, float y) { return mdiv(a, b, y); }
 // reciprocals the host prepares once, RN(1/x) of the divisor x in the
 // block's precision, so that mdiv gives the correctly rounded quotient
 __device__ __forceinline__ double rcp_gm1(const PhysParams& P, double) { return P.rgm1; }
@@ -106,17 +121,17 @@ __device__ __forceinline__ unsigned long long body_timestep(const DevBlock<T>& b
   TC w0 = (TC)b.w[c], w1 = (TC)b.w[N + c], w2 = (TC)b.w[2 * N + c], w3 = (TC)b.w[3 * N + c];
   TC pc = (TC)b.p[c];
   TC y = TC(1) / w0;
-  TC cc = mdiv(gamma * pc, w0, y);
+  TC cc = smdiv(smul(gamma, pc), w0, y);
   if (cc < TC(0) || cc != cc) {  // timestep.f90:45-48
     atomicCAS(err, 0u, (unsigned)ERR_NEGPRESS);  // the first stop in launch order wins
     return mine;
   }
   cc = sqrt(fmaxT(cc, TC(0)));
-  TC uu = mdiv(w1, w0, y), uv = mdiv(w2, w0, y), uw = mdiv(w3, w0, y);
+  TC uu = smdiv(w1, w0, y), uv = smdiv(w2, w0, y), uw = smdiv(w3, w0, y);
   // face vectors are axis-aligned: |u.s| = |u_d s_d|, |s| precomputed
-  TC ri = fabs(uu * (TC)b.s[0]) + cc * (TC)b.sqrt_ds[0];
-  TC rj = fabs(uv * (TC)b.s[1]) + cc * (TC)b.sqrt_ds[1];
-  TC rk = fabs(uw * (TC)b.s[2]) + cc * (TC)b.sqrt_ds[2];
+  TC ri = fabs(smul(uu, (TC)b.s[0])) + smul(cc, (TC)b.sqrt_ds[0]);
+  TC rj = fabs(smul(uv, (TC)b.s[1])) + smul(cc, (TC)b.sqrt_ds[1]);
+  TC rk = fabs(smul(uw, (TC)b.s[2])) + smul(cc, (TC)b.sqrt_ds[2]);
   TC lsum = ri + rj + rk;
   TC fict;
   if (P.eqn_ns) {  // viscous spectral radii, timestep.f90:141-178
@@ -145,7 +160,7 @@ __device__ __forceinline__ unsigned long long body_timestep(const DevBlock<T>& b
     const TC dtime = (TC(2) * (TC)P.dtstep) / (TC(3) * (TC)P.cfl);
     fict = fict < dtime ? fict : dtime;
   }
-  TC vd = fict * r;
+  TC vd = smul(fict, r);
   double vdd = (double)vd;
   if (vdd >= 0.0) mine = (unsigned long long)__double_as_longlong(vdd);
   if (b.blank[c] == 0) {  // timestep.f90:212-223
@@ -298,15 +313,17 @@ __device__ __forceinline__ void body_prep(const DevBlock<T>& b, const PhysParams
   } else if (P.distype != 2) {
 #pragma unroll
     for (int d = 0; d < 3; d++) {
+      // the products of this FP64-bound pass go to the integer pipes (smul);
+      // the fused steps of the quotients stay on the FP64 pipe
       T s = (T)b.s[d];
-      T f0 = w[1 + d] * s;  // sum(w(2:4)*ss) with the two zero components dropped
-      T f1 = mdiv(f0 * w[1], w[0], y);
-      T f2 = mdiv(f0 * w[2], w[0], y);
-      T f3 = mdiv(f0 * w[3], w[0], y);
-      if (d == 0) f1 = f1 + p * s;
-      if (d == 1) f2 = f2 + p * s;
-      if (d == 2) f3 = f3 + p * s;
-      T f4 = mdiv(f0 * Hc, w[0], y);
+      T f0 = smul(w[1 + d], s);  // sum(w(2:4)*ss) with the two zero components dropped
+      T f1 = smdiv(smul(f0, w[1]), w[0], y);
+      T f2 = smdiv(smul(f0, w[2]), w[0], y);
+      T f3 = smdiv(smul(f0, w[3]), w[0], y);
+      if (d == 0) f1 = f1 + smul(p, s);
+      if (d == 1) f2 = f2 + smul(p, s);
+      if (d == 2) f3 = f3 + smul(p, s);
+      T f4 = smdiv(smul(f0, Hc), w[0], y);
       T* F = b.F + (long long)(d * 5) * N + c;
       F[0] = f0;
       F[N] = f1;
@@ -662,11 +679,11 @@ __device__ __forceinline__ void face_dir(const DevBlock<T>& b, const PhysParams&
     T dm = (q - 1 == 1) ? d0 : Dl[v * N + c - st];
     T dp = (q + 1 == bq) ? d0 : Dl[v * N + c + st];
     T t3 = dp - mul2(d0) + dm;
-    out[v] = dis2 * d0 - dis4 * t3;
+    out[v] = smul(dis2, d0) - dis4 * t3;
   }
   if (!P.matrix) {
 #pragma unroll
-    for (int v = 0; v < 5; v++) out[v] = out[v] * lam;
+    for (int v = 0; v < 5; v++) out[v] = smul(out[v], lam);
   } else {
     T ss[3] = {T(0), T(0), T(0)};
     ss[D] = (T)b.s[D];
@@ -1290,7 +1307,7 @@ __device__ __forceinline__ void body_irs(const DevBlock<T>& b, const IrsTables& 
       if (q0 + u <= l) {
         TC x = xb[u];
         if (bk[u] != 0) {
-          x = mdiv(x - bb * prev, pb[u], rb[u]);
+          x = smdiv(x - bb * prev, pb[u], rb[u]);
           d[c0 + (q0 + u) * st] = (T)x;
         }
         prev = x;
@@ -1310,7 +1327,7 @@ __device__ __forceinline__ void body_irs(const DevBlock<T>& b, const IrsTables& 
       if (q0 - u >= 2) {
         TC x = xb[u];
         if (bk[u] != 0) {
-          x = x - pb[u] * prev;
+          x = x - smul(pb[u], prev);
           d[c0 + (q0 - u) * st] = (T)x;
         }
         prev = x;
@@ -2427,7 +2444,9 @@ __device__ __forceinline__ void body_addw(const DevBlock<TF>& f, const DevBlock<
         for (int di = 0; di < 2; di++) {
           long long cq = cidx(c.Pi, c.Pj, sh[0] + di, sh[1] + dj, sh[2] + dk);
           double val = fmg ? (double)c.w[v * c.N + cq] : dc[v * c.N + cq];
-          acc = acc + val * fac[nn++];
+          // half the products on the integer pipes (smul), half on the FP64 pipe
+          acc = acc + (dk ? smul(val, fac[nn]) : val * fac[nn]);
+          nn++;
         }
     if (fmg)
       f.w[v * f.N + q] = (TF)acc;
