@@ -92,8 +92,10 @@ template <typename T> __device__ __forceinline__ T fminT(T a, T b) { return a < 
 
 // depvars_one, depvars.f90:48-49
 template <typename T> __device__ __forceinline__ T depvars(T gamma, const T* w) {
-  T qq = T(0.5) * (w[1] * w[1] + w[2] * w[2] + w[3] * w[3]) / w[0];
-  return (gamma - T(1)) * fdimT(w[4], qq);
+  // the products on the integer pipes and the halving as an exponent step:
+  // the same bits as 0.5*(w1*w1 + w2*w2 + w3*w3)/w0 and (gamma-1)*dim(w4, qq)
+  T qq = mulhalf(smul(w[1], w[1]) + smul(w[2], w[2]) + smul(w[3], w[3])) / w[0];
+  return smul(gamma - T(1), fdimT(w[4], qq));
 }
 
 struct Idx {
@@ -679,7 +681,7 @@ __device__ __forceinline__ void face_dir(const DevBlock<T>& b, const PhysParams&
     T dm = (q - 1 == 1) ? d0 : Dl[v * N + c - st];
     T dp = (q + 1 == bq) ? d0 : Dl[v * N + c + st];
     T t3 = dp - mul2(d0) + dm;
-    out[v] = smul(dis2, d0) - dis4 * t3;
+    out[v] = smul(dis2, d0) - smul(dis4, t3);
   }
   if (!P.matrix) {
 #pragma unroll
@@ -1062,7 +1064,7 @@ __device__ __forceinline__ void body_combine(const DevBlock<T>& b, const PhysPar
     const T* Dz = b.dfs + 10 * N;
     T vis[5];
 #pragma unroll
-    for (int v = 0; v < 5; v++) vis[v] = A.scale_fw ? b.fw[v * N + c] * fac : T(0);
+    for (int v = 0; v < 5; v++) vis[v] = A.scale_fw ? smul(b.fw[v * N + c], fac) : T(0);
     if (P.eqn_ns) {  // viscous faces, then the viscous wall faces in record order
       const T* Vx = b.vfs;
       const T* Vy = b.vfs + 5 * N;
@@ -1115,7 +1117,7 @@ __device__ __forceinline__ void body_combine(const DevBlock<T>& b, const PhysPar
     }
   } else {
 #pragma unroll
-    for (int v = 0; v < 5; v++) fwv[v] = A.scale_fw ? b.fw[v * N + c] * fac : T(0);
+    for (int v = 0; v < 5; v++) fwv[v] = A.scale_fw ? smul(b.fw[v * N + c], fac) : T(0);
   }
   if (tg >= 0) {
     // cut-cell wall faces, this cell's records in record order: efluxb on dw
@@ -1214,9 +1216,9 @@ __device__ __forceinline__ void body_combine(const DevBlock<T>& b, const PhysPar
   }
   // time-step scaling, euler.f90:364-372: de = fn*vdtim/cellvolume
   T vd = A.vt ? (T)(*b.dtim) : b.vdtim[c];
-  T de = FAST ? ((T)A.fn * vd) * rcp_vol(b) : mdiv((T)A.fn * vd, (T)b.vol, rcp_vol(b));
+  T de = FAST ? ((T)A.fn * vd) * rcp_vol(b) : smdiv(smul((T)A.fn, vd), (T)b.vol, rcp_vol(b));
 #pragma unroll
-  for (int v = 0; v < 5; v++) dwv[v] = de * dwv[v];
+  for (int v = 0; v < 5; v++) dwv[v] = smul(de, dwv[v]);
   if (A.irs) {
 #pragma unroll
     for (int v = 0; v < 5; v++) b.dw[v * N + c] = dwv[v];
@@ -2336,8 +2338,9 @@ __device__ __forceinline__ void body_collc(const DevBlock<TC>& c, const DevBlock
       for (int dj = 0; dj < 2; dj++)
         for (int di = 0; di < 2; di++) {
           long long fq = cidx(f.Pi, f.Pj, sh[0] + di, sh[1] + dj, sh[2] + dk);
-          double val = mdiv((double)f.dw[v * f.N + fq], f.vol, f.rvol);
-          acc = acc + val * fac[nn++];
+          double val = smdiv((double)f.dw[v * f.N + fq], f.vol, f.rvol);
+          acc = acc + (dk ? smul(val, fac[nn]) : val * fac[nn]);
+          nn++;
         }
     c.wr[v * c.N + cc] = (TC)(acc * c.vol);
     acc = 0.0;
@@ -2346,7 +2349,8 @@ __device__ __forceinline__ void body_collc(const DevBlock<TC>& c, const DevBlock
       for (int dj = 0; dj < 2; dj++)
         for (int di = 0; di < 2; di++) {
           long long fq = cidx(f.Pi, f.Pj, sh[0] + di, sh[1] + dj, sh[2] + dk);
-          acc = acc + (double)f.w[v * f.N + fq] * fac[nn++];
+          acc = acc + (dk ? smul((double)f.w[v * f.N + fq], fac[nn]) : (double)f.w[v * f.N + fq] * fac[nn]);
+          nn++;
         }
     c.w[v * c.N + cc] = (TC)acc;
   }
