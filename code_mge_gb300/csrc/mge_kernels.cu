@@ -602,8 +602,10 @@ __device__ __noinline__ void visc_face(const DevBlock<T>& b, const PhysParams& P
 // Thread (i,j,k) in [2..ie]x[2..je]x[2..ke] owns the lower face of cell
 // (i,j,k) in each direction whose tangential indices are physical.
 // SCH: FACE_CENTRAL or FACE_ROE when the launch knows the scheme (each then
-// gets its own register allocation), FACE_ANY to test P.distype.
-enum { FACE_CENTRAL = 0, FACE_ROE = 1, FACE_ANY = 2 };
+// gets its own register allocation), FACE_ANY to test P.distype; FACE_JST:
+// the central scheme with scalar dissipation and no viscous flux, without
+// the registers the matrix dissipation and the viscous face would take.
+enum { FACE_CENTRAL = 0, FACE_ROE = 1, FACE_ANY = 2, FACE_JST = 3 };
 template <typename T, int D, int SCH>
 __device__ __forceinline__ void face_dir(const DevBlock<T>& b, const PhysParams& P, int dissip_on, T cd, int i, int j,
                                          int k) {
@@ -614,7 +616,7 @@ __device__ __forceinline__ void face_dir(const DevBlock<T>& b, const PhysParams&
   const int lq = D == 0 ? b.il : (D == 1 ? b.jl : b.kl);
   const int eq = lq + 1, bq = lq + 2;
   T* E = b.efs + (long long)(D * 5) * N;
-  if (P.eqn_ns && dissip_on) {  // viscous face flux, blended like the dissipation
+  if (SCH != FACE_JST && P.eqn_ns && dissip_on) {  // viscous face flux, blended like the dissipation
     T o[5];
     visc_face<T, D>(b, P, c, (T)fabs(b.s[D]), o);
     T* V = b.vfs + (long long)(D * 5) * N;
@@ -683,7 +685,7 @@ __device__ __forceinline__ void face_dir(const DevBlock<T>& b, const PhysParams&
     T t3 = dp - mul2(d0) + dm;
     out[v] = smul(dis2, d0) - smul(dis4, t3);
   }
-  if (!P.matrix) {
+  if (SCH == FACE_JST || !P.matrix) {
 #pragma unroll
     for (int v = 0; v < 5; v++) out[v] = smul(out[v], lam);
   } else {
@@ -2632,6 +2634,11 @@ __global__ void __launch_bounds__(256, 4) k_face(DevBlock<T> b, PhysParams P, in
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t < (long long)(b.ie - 1) * (b.je - 1) * (b.ke - 1)) body_face<T, FACE_CENTRAL>(b, P, dissip_on, cd, t);
 }
+template <typename T>
+__global__ void __launch_bounds__(256, 6) k_face_jst(DevBlock<T> b, PhysParams P, int dissip_on, T cd) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < (long long)(b.ie - 1) * (b.je - 1) * (b.ke - 1)) body_face<T, FACE_JST>(b, P, dissip_on, cd, t);
+}
 // the contracted form's dissipation faces (no convective face fluxes)
 template <typename T>
 __global__ void __launch_bounds__(256, 4) k_face_diss(DevBlock<T> b, PhysParams P, T cd) {
@@ -3074,6 +3081,8 @@ void launch_stage_part(int part, const DevBlock<T>& b, const PhysParams& P, cons
       if (A.dissip_on) k_face_diss<T><<<LAUNCH_N(n2), 0, s>>>(b, P, (T)A.cd);
     } else if (!A.dissip_on && P.distype == 0)
       k_face_conv<T><<<LAUNCH_N(n2), 0, s>>>(b);
+    else if (P.distype == 0 && !P.eqn_ns && !P.matrix)
+      k_face_jst<T><<<LAUNCH_N(n2), 0, s>>>(b, P, A.dissip_on, (T)A.cd);
     else if (P.distype == 0)
       k_face<T><<<LAUNCH_N(n2), 0, s>>>(b, P, A.dissip_on, (T)A.cd);
     else
