@@ -299,9 +299,9 @@ __device__ __forceinline__ void body_prep(const DevBlock<T>& b, const PhysParams
 #pragma unroll
     for (int d = 0; d < 3; d++) {
       const T s = (T)b.s[d];
-      const T f0 = w[1 + d] * s;
-      const T q = f0 * y;
-      T f1 = q * w[1], f2 = q * w[2], f3 = q * w[3];
+      const T f0 = smul(w[1 + d], s);
+      const T q = smul(f0, y);
+      T f1 = smul(q, w[1]), f2 = smul(q, w[2]), f3 = smul(q, w[3]);
       if (d == 0) f1 = fma(p, s, f1);
       if (d == 1) f2 = fma(p, s, f2);
       if (d == 2) f3 = fma(p, s, f3);
@@ -310,7 +310,7 @@ __device__ __forceinline__ void body_prep(const DevBlock<T>& b, const PhysParams
       F[N] = f1;
       F[2 * N] = f2;
       F[3 * N] = f3;
-      F[4 * N] = q * Hc;
+      F[4 * N] = smul(q, Hc);
     }
   } else if (P.distype != 2) {
 #pragma unroll
@@ -740,9 +740,9 @@ __device__ __forceinline__ void face_diss_fast(const DevBlock<T>& b, const PhysP
   const long long cm = (q - 1 < 2) ? c : c - st;
   const long long cp = (q > lq) ? c - st : c;
   const T lam = mulhalf(b.lam[cm] + b.lam[cp]);
-  const T dis2 = (T)P.vis2 * ep;
+  const T dis2 = smul((T)P.vis2, ep);
   const T dis4 = gt_nonneg((T)P.vis4, dis2) ? (T)P.vis4 - dis2 : T(0);
-  const T a2 = (dis2 * cd) * lam, a4 = (dis4 * cd) * lam;
+  const T a2 = smul(smul(dis2, cd), lam), a4 = smul(smul(dis4, cd), lam);
   const T* Dl = b.dlt + (long long)(D * 5) * N;
   T* Df = b.dfs + (long long)(D * 5) * N;
 #pragma unroll
@@ -751,7 +751,7 @@ __device__ __forceinline__ void face_diss_fast(const DevBlock<T>& b, const PhysP
     const T dm = (q - 1 == 1) ? d0 : Dl[v * N + c - st];
     const T dp = (q + 1 == bq) ? d0 : Dl[v * N + c + st];
     const T t3 = fma(T(-2), d0, dp + dm);
-    Df[v * N + c] = fma(a2, d0, -(a4 * t3));
+    Df[v * N + c] = fma(a2, d0, -smul(a4, t3));
   }
 }
 
