@@ -1255,7 +1255,10 @@ __device__ __forceinline__ long long irs_lines(const DevBlock<T>& b) {
   return D == 0 ? (long long)b.ny * b.nz : (D == 1 ? (long long)b.nx * b.nz : (long long)b.nx * b.ny);
 }
 
-template <typename T, typename TC, int D>
+// SC: the forward step's product bb*prev on the integer pipes too.  That
+// lengthens the serial chain of each line, so it pays only where many lines
+// run at once and the sweep is bound by the FP64 rate, not by the chain.
+template <typename T, typename TC, int D, bool SC = false>
 __device__ __forceinline__ void body_irs(const DevBlock<T>& b, const IrsTables& tb, TC bb, long long t) {
   const long long lines = irs_lines<T, D>(b);
   const int v = (int)(t / lines);
@@ -1311,7 +1314,7 @@ __device__ __forceinline__ void body_irs(const DevBlock<T>& b, const IrsTables& 
       if (q0 + u <= l) {
         TC x = xb[u];
         if (bk[u] != 0) {
-          x = smdiv(x - bb * prev, pb[u], rb[u]);
+          x = smdiv(x - (SC ? smul(bb, prev) : bb * prev), pb[u], rb[u]);
           d[c0 + (q0 + u) * st] = (T)x;
         }
         prev = x;
@@ -2680,10 +2683,10 @@ __global__ void k_combine(DevBlock<T> b, PhysParams P, StageArgs A, unsigned* er
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t < (long long)b.nx * b.ny * b.nz) body_combine<T, FAST>(b, P, A, err, t);
 }
-template <typename T, typename TC, int D>
+template <typename T, typename TC, int D, bool SC = false>
 __global__ void k_irs(DevBlock<T> b, IrsTables tb, TC bb) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < 5 * irs_lines<T, D>(b)) body_irs<T, TC, D>(b, tb, bb, t);
+  if (t < 5 * irs_lines<T, D>(b)) body_irs<T, TC, D, SC>(b, tb, bb, t);
 }
 template <typename T>
 __global__ void k_update(DevBlock<T> b, PhysParams P, StageArgs A) {
@@ -3146,7 +3149,10 @@ void launch_irs_dir(const DevBlock<T>& b, const IrsTables& tb, TC bb, cudaStream
     const long long grid = 5 * ((lines + LT - 1) / LT);
     k_irs_smem<T, TC, D, LT><<<(unsigned)grid, LT, sm, s>>>(b, tb, bb);
   } else {
-    k_irs<T, TC, D><<<LAUNCH_N(5 * lines), 0, s>>>(b, tb, bb);
+    if (5 * lines >= 150000)  // about 8 warps per scheduler: the sweep is bound by the FP64 rate
+      k_irs<T, TC, D, true><<<LAUNCH_N(5 * lines), 0, s>>>(b, tb, bb);
+    else
+      k_irs<T, TC, D><<<LAUNCH_N(5 * lines), 0, s>>>(b, tb, bb);
   }
 }
 
