@@ -47,6 +47,10 @@ namespace mge {
 // some of its independent products off the FP64 pipe
 __device__ __forceinline__ double smul(double a, double b) { return soft::mul(a, b); }
 __device__ __forceinline__ float smul(float a, float b) { return a * b; }
+// a / b, for doubles on the integer pipes (the same bits as the FP64
+// division, which costs about ten FP64 instructions)
+__device__ __forceinline__ double sdiv(double a, double b) { return soft::div(a, b); }
+__device__ __forceinline__ float sdiv(float a, float b) { return a / b; }
 __device__ __forceinline__ double mdiv(double a, double b, double y) {
   double q = a * y;
   double r = fma(-q, b, a);
@@ -94,7 +98,7 @@ template <typename T> __device__ __forceinline__ T fminT(T a, T b) { return a < 
 template <typename T> __device__ __forceinline__ T depvars(T gamma, const T* w) {
   // the products on the integer pipes and the halving as an exponent step:
   // the same bits as 0.5*(w1*w1 + w2*w2 + w3*w3)/w0 and (gamma-1)*dim(w4, qq)
-  T qq = mulhalf(smul(w[1], w[1]) + smul(w[2], w[2]) + smul(w[3], w[3])) / w[0];
+  T qq = sdiv(mulhalf(smul(w[1], w[1]) + smul(w[2], w[2]) + smul(w[3], w[3])), w[0]);
   return smul(gamma - T(1), fdimT(w[4], qq));
 }
 
@@ -122,7 +126,7 @@ __device__ __forceinline__ unsigned long long body_timestep(const DevBlock<T>& b
   const TC gamma = (TC)P.gamma;
   TC w0 = (TC)b.w[c], w1 = (TC)b.w[N + c], w2 = (TC)b.w[2 * N + c], w3 = (TC)b.w[3 * N + c];
   TC pc = (TC)b.p[c];
-  TC y = TC(1) / w0;
+  TC y = sdiv(TC(1), w0);
   TC cc = smdiv(smul(gamma, pc), w0, y);
   if (cc < TC(0) || cc != cc) {  // timestep.f90:45-48
     atomicCAS(err, 0u, (unsigned)ERR_NEGPRESS);  // the first stop in launch order wins
@@ -146,7 +150,7 @@ __device__ __forceinline__ unsigned long long body_timestep(const DevBlock<T>& b
     TC rvi = dtv * (s0 * s0), rvj = dtv * (s1 * s1), rvk = dtv * (s2 * s2);
     fict = (TC)b.vol / (lsum + (TC)P.cfac * (rvi + rvj + rvk));
   } else {
-    fict = (TC)b.vol / lsum;
+    fict = sdiv((TC)b.vol, lsum);
   }
   const TC plim = TC(0.001);
   TC pip = (TC)b.p[c + 1], pim = (TC)b.p[c - 1];
@@ -154,10 +158,10 @@ __device__ __forceinline__ unsigned long long body_timestep(const DevBlock<T>& b
   long long pl = (long long)b.Pi * b.Pj;
   TC pkp = (TC)b.p[c + pl], pkm = (TC)b.p[c - pl];
   TC p2 = mul2(pc);
-  TC dpi = fabs((pip - p2 + pim) / (pip + p2 + pim + plim));
-  TC dpj = fabs((pjp - p2 + pjm) / (pjp + p2 + pjm + plim));
-  TC dpk = fabs((pkp - p2 + pkm) / (pkp + p2 + pkm + plim));
-  TC r = TC(1) / (TC(1) + fminT((TC)P.dimcfl, mul2(dpi + dpj + dpk)));
+  TC dpi = fabs(sdiv(pip - p2 + pim, pip + p2 + pim + plim));
+  TC dpj = fabs(sdiv(pjp - p2 + pjm, pjp + p2 + pjm + plim));
+  TC dpk = fabs(sdiv(pkp - p2 + pkm, pkp + p2 + pkm + plim));
+  TC r = sdiv(TC(1), TC(1) + fminT((TC)P.dimcfl, mul2(dpi + dpj + dpk)));
   if (P.unsteady) {  // timestep.f90:85-99,180-190: at most 2*dtstep/(3*cfl)
     const TC dtime = (TC(2) * (TC)P.dtstep) / (TC(3) * (TC)P.cfl);
     fict = fict < dtime ? fict : dtime;
@@ -264,7 +268,7 @@ __device__ __forceinline__ void body_prep(const DevBlock<T>& b, const PhysParams
 #pragma unroll
   for (int v = 0; v < 5; v++) w[v] = b.w[v * N + c];
   T p = b.p[c];
-  T y = T(1) / w[0];
+  T y = sdiv(T(1), w[0]);
   T Hc = w[4] + p;
   b.H[c] = Hc;
   if (P.eqn_ns && dissip_on) {  // velocity and temperature, zero in solid cells (euler.f90:140-154)
@@ -354,19 +358,19 @@ __device__ __forceinline__ void body_prep(const DevBlock<T>& b, const PhysParams
     {
       T pm = b.p[c - 1], pp = b.p[c + 1], p2 = mul2(p);
       T pb = fabs(pm + p2 + pp);
-      b.fp[c] = (pb > T(0)) ? fabs(pm - p2 + pp) / pb : T(0);
+      b.fp[c] = (pb > T(0)) ? sdiv(fabs(pm - p2 + pp), pb) : T(0);
     }
     // j: abs(p(j+1) +2p(j) +p(j-1)), dflux.f90:131-136
     {
       T pm = b.p[c - b.Pi], pp = b.p[c + b.Pi], p2 = mul2(p);
       T pb = fabs(pp + p2 + pm);
-      b.fp[N + c] = (pb > T(0)) ? fabs(pp - p2 + pm) / pb : T(0);
+      b.fp[N + c] = (pb > T(0)) ? sdiv(fabs(pp - p2 + pm), pb) : T(0);
     }
     // k: abs(p(k-1) +2p(k) +p(k+1)), dflux.f90:188-193
     {
       T pm = b.p[c - pl], pp = b.p[c + pl], p2 = mul2(p);
       T pb = fabs(pm + p2 + pp);
-      b.fp[2 * N + c] = (pb > T(0)) ? fabs(pm - p2 + pp) / pb : T(0);
+      b.fp[2 * N + c] = (pb > T(0)) ? sdiv(fabs(pm - p2 + pp), pb) : T(0);
     }
   }
 }

@@ -1,11 +1,11 @@
-// soft_fp64.cuh -- IEEE-754 binary64 multiply and add, round to nearest
-// even, in 32- and 64-bit integer arithmetic.
+// soft_fp64.cuh -- IEEE-754 binary64 multiply, add and divide, round to
+// nearest even, in 32- and 64-bit integer arithmetic.
 //
 // GB300 issues FP64 at 2 thread-operations per SM per cycle: one FP64 warp
 // instruction holds a scheduler's FP64 pipe for 64 cycles, while its issue
 // slots and its integer pipes stay mostly idle in the stage kernels.  The
-// functions below compute the correctly rounded product and sum on the
-// integer pipes, so that a kernel can run part of its FP64 operations there,
+// functions below compute the correctly rounded product, sum and quotient on
+// the integer pipes, so that a kernel can run part of its FP64 operations there,
 // beside the native ones, with bit-identical results.
 //
 // The algorithm is the textbook one for binary floating point (unpack the
@@ -16,7 +16,7 @@
 // normal operands and a normal result.  Every other case (a zero,
 // subnormal, infinite or NaN operand, an overflow or an underflow) returns
 // the native operation, so the functions return exactly what IEEE-754
-// multiplication and addition return for all inputs.
+// multiplication, addition and division return for all inputs.
 //
 // The header compiles for the host as well, where the tests check it against
 // the host's own binary64 arithmetic.
@@ -67,9 +67,19 @@ MGE_SF_HD int clz64(uint64_t x) {  // x != 0
 #endif
 }
 
+// the high 64 bits of the 128-bit product of two 64-bit integers
+MGE_SF_HD uint64_t mulhi64(uint64_t x, uint64_t y) {
+#ifdef __CUDA_ARCH__
+  return __umul64hi(x, y);
+#else
+  return (uint64_t)(((unsigned __int128)x * y) >> 64);
+#endif
+}
+
 // the native operations, out of line, for the cases the integer forms leave
 MGE_SF_NOINLINE double native_mul(double a, double b) { return a * b; }
 MGE_SF_NOINLINE double native_add(double a, double b) { return a + b; }
+MGE_SF_NOINLINE double native_div(double a, double b) { return a / b; }
 
 // a * b
 MGE_SF_HD double mul(double a, double b) {
@@ -148,6 +158,63 @@ MGE_SF_HD double add(double a, double b) {
 }
 
 MGE_SF_HD double sub(double a, double b) { return add(a, from_bits(bits(b) ^ kSign)); }
+
+// a / b.  The significands' quotient comes from a reciprocal of the divisor
+// in 64-bit fixed point: an FP32 reciprocal of its leading 24 bits (about 23
+// correct bits), then two Newton steps x <- x + x(1 - d x) (about 60 bits).
+// The quotient estimate c, with one bit below the last significand bit, is
+// then within one unit of the true floor, and the exact remainder r = a - c b
+// (which fits in a signed 64-bit integer) corrects it and gives the sticky
+// bit for rounding to nearest even.
+MGE_SF_HD double div(double a, double b) {
+  const uint64_t A = bits(a), B = bits(b);
+  const uint32_t ea = (uint32_t)(A >> 52) & 0x7ffu, eb = (uint32_t)(B >> 52) & 0x7ffu;
+  const uint64_t ma = (A & kFrac) | kOne, mb = (B & kFrac) | kOne;  // [2^52, 2^53)
+  const bool ge = ma >= mb;                                          // quotient in [1, 2), else (1/2, 1)
+  // biased exponent of the result; 1..2045 leaves room for a rounding carry
+  const int32_t e = (int32_t)ea - (int32_t)eb + (ge ? 1023 : 1022);
+  if (ea - 1u >= 2046u || eb - 1u >= 2046u || (uint32_t)(e - 1) >= 2045u) return native_div(a, b);
+  // divisor d = mb 2^11 in [2^63, 2^64) stands for D = d / 2^64 in [1/2, 1);
+  // X stands for x = X / 2^62, an approximation of 1/D in (1, 2]
+  const uint64_t d = mb << 11;
+#ifdef __CUDA_ARCH__
+  const float x0 = __frcp_rn((float)(uint32_t)(d >> 40) * 5.9604644775390625e-8f);  // 1 / (d_hi / 2^24)
+  const uint32_t xb = __float_as_uint(x0);
+#else
+  const float x0 = 1.0f / ((float)(uint32_t)(d >> 40) * 5.9604644775390625e-8f);
+  uint32_t xb;
+  memcpy(&xb, &x0, 4);
+#endif
+  // x0 in (1, 2]: its significand (with the implicit bit) times 2^(39 + exponent)
+  uint64_t X = (uint64_t)((xb & 0x7fffffu) | 0x800000u) << (39 + ((xb >> 23) & 0xffu) - 127);
+  for (int it = 0; it < 2; it++) {
+    // x (1 - D x) 2^62 = X e / 2^62 with e = (1 - D x) 2^62, |e| < 2^41
+    const uint64_t p = mulhi64(d, X);  // D x 2^62
+    if (p <= (1ull << 62)) {
+      X += mulhi64(X, ((1ull << 62) - p) << 2);
+    } else {
+      X -= mulhi64(X, (p - (1ull << 62)) << 2);
+    }
+  }
+  // the quotient ma/mb times 2^62, within a few units
+  const uint64_t q = mulhi64(ma << 11, X);
+  // c: the quotient with the significand's 53 bits and one more, as an
+  // integer; its true floor is c - 1, c or c + 1
+  const uint32_t sh = ge ? 9u : 8u;
+  uint64_t c = q >> sh;
+  // r = ma 2^(53 or 54) - c mb, exactly, in the low 64 bits (|r| < 2^55)
+  int64_t r = (int64_t)((ma << (64u - 11u + (ge ? 0u : 1u))) - c * mb);
+  if (r < 0) {
+    c -= 1;
+    r += (int64_t)mb;
+  } else if (r >= (int64_t)mb) {
+    c += 1;
+    r -= (int64_t)mb;
+  }
+  uint64_t m = c >> 1;
+  m += (c & 1u) & ((uint64_t)(r != 0) | (m & 1u));
+  return from_bits(((A ^ B) & kSign) | (((uint64_t)(e - 1) << 52) + m));
+}
 
 }  // namespace soft
 }  // namespace mge

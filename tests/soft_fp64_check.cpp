@@ -1,4 +1,4 @@
-// Checks mge::soft::mul, add and sub (code_mge_gb300/csrc/soft_fp64.cuh)
+// Checks mge::soft::mul, add, sub and div (code_mge_gb300/csrc/soft_fp64.cuh)
 // bit for bit against the host's binary64 arithmetic (round to nearest
 // even, no contraction): edge values, then random operands drawn so that
 // every path of the algorithms is taken (all exponent gaps, cancellation,
@@ -31,12 +31,12 @@ static bool same(double x, double y) {
 
 static void check(double a, double b) {
   volatile double va = a, vb = b;
-  const double pm = va * vb, pa = va + vb, ps = va - vb;
-  const double qm = mul(a, b), qa = add(a, b), qs = sub(a, b);
-  cases += 3;
-  if (!same(pm, qm) || !same(pa, qa) || !same(ps, qs)) {
+  const double pm = va * vb, pa = va + vb, ps = va - vb, pd = va / vb;
+  const double qm = mul(a, b), qa = add(a, b), qs = sub(a, b), qd = div(a, b);
+  cases += 4;
+  if (!same(pm, qm) || !same(pa, qa) || !same(ps, qs) || !same(pd, qd)) {
     if (bad < 10)
-      printf("mismatch a=%a b=%a  mul %a/%a  add %a/%a  sub %a/%a\n", a, b, pm, qm, pa, qa, ps, qs);
+      printf("mismatch a=%a b=%a  mul %a/%a  add %a/%a  sub %a/%a  div %a/%a\n", a, b, pm, qm, pa, qa, ps, qs, pd, qd);
     bad++;
   }
 }
@@ -55,7 +55,7 @@ int main(int argc, char** argv) {
   for (double a : edge)
     for (double b : edge) check(a, b);
   for (long long q = 0; q < n; q++) {
-    const int kind = (int)(q % 8);
+    const int kind = (int)(q % 10);
     double a, b;
     if (kind == 0) {  // any bit patterns
       a = from_bits(next());
@@ -82,9 +82,18 @@ int main(int argc, char** argv) {
     } else if (kind == 6) {  // short significands: exact products, ties in sums
       a = from_bits(bits(rnd_exp(1000, 1050)) & ~0xFFFFFFFFFFull);
       b = from_bits(bits(rnd_exp(1000, 1050)) & ~0xFFFFFFFull);
-    } else {  // the magnitudes a flow solver sees
+    } else if (kind == 7) {  // the magnitudes a flow solver sees
       a = rnd_exp(1013, 1033);
       b = rnd_exp(1003, 1033);
+    } else if (kind == 8) {  // divisors with a significand at or just above 1 (or just below 2)
+      a = rnd_exp(1000, 1040);
+      const uint64_t low = next() % 4096;
+      b = from_bits(((uint64_t)(1000 + next() % 40) << 52) | ((next() & 1) ? low : kFrac - low));
+    } else {  // quotients that are exact, or a few ulps from exact
+      b = rnd_exp(1000, 1040);
+      const double qq = from_bits(bits(rnd_exp(1015, 1031)) & ~0xFFFFFFFFFull);
+      volatile double prod = b * qq;
+      a = from_bits(bits(prod) + (next() % 5) - 2);
     }
     check(a, b);
   }

@@ -1,5 +1,5 @@
-"""The device build of the integer-pipe binary64 multiply and add
-(soft_fp64.cuh) against the GB300's FP64 hardware, bit for bit, on 6 x 2^26
+"""The device build of the integer-pipe binary64 multiply, add and divide
+(soft_fp64.cuh) against the GB300's FP64 hardware, bit for bit, on 8 x 2^26
 operand pairs (the host build is checked in test_soft_fp64.py)."""
 import os
 import subprocess

@@ -1,6 +1,6 @@
-"""The integer-pipe binary64 multiply and add (soft_fp64.cuh) against the
-host's IEEE-754 arithmetic, bit for bit, on edge values and 8 million random
-operand pairs (CPU; the GPU builds of the same functions are checked in
+"""The integer-pipe binary64 multiply, add and divide (soft_fp64.cuh)
+against the host's IEEE-754 arithmetic, bit for bit, on edge values and 8
+million random operand pairs (CPU; the GPU builds of the same functions are checked in
 test_gpu_soft_fp64.py)."""
 import os
 import subprocess
