@@ -2155,10 +2155,10 @@ __device__ void body_rtrms_partial(const DevBlock<T>& b, double cfl, int vt, dou
       k = 2 + (int)(t / ((long long)b.nx * b.ny));
     }
     long long c = cidx(b.Pi, b.Pj, i, j, k);
-    double de = cfl * (double)(vt ? *b.dtim : b.vdtim[c]);
+    double de = smul(cfl, (double)(vt ? *b.dtim : b.vdtim[c]));
     double rt = 0.0;
-    if (b.blank[c] != 0) rt = (double)b.dw[c] / de;
-    acc = acc + rt * rt;
+    if (b.blank[c] != 0) rt = sdiv((double)b.dw[c], de);
+    acc = acc + smul(rt, rt);
   }
   sh[threadIdx.x] = acc;
   __syncthreads();
