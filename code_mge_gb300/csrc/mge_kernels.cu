@@ -1259,9 +1259,11 @@ __device__ __forceinline__ long long irs_lines(const DevBlock<T>& b) {
   return D == 0 ? (long long)b.ny * b.nz : (D == 1 ? (long long)b.nx * b.nz : (long long)b.nx * b.ny);
 }
 
-// SC: the forward step's product bb*prev on the integer pipes too.  That
-// lengthens the serial chain of each line, so it pays only where many lines
-// run at once and the sweep is bound by the FP64 rate, not by the chain.
+// SC: the products of the forward and backward steps on the integer pipes.
+// That lengthens the serial chain of each line, so it pays only where many
+// lines run at once and the sweep is bound by the FP64 rate; with few lines
+// (coarse levels, slabs) the chain's latency bounds it and the FP64 forms
+// are faster.
 template <typename T, typename TC, int D, bool SC = false>
 __device__ __forceinline__ void body_irs(const DevBlock<T>& b, const IrsTables& tb, TC bb, long long t) {
   const long long lines = irs_lines<T, D>(b);
@@ -1318,7 +1320,7 @@ __device__ __forceinline__ void body_irs(const DevBlock<T>& b, const IrsTables& 
       if (q0 + u <= l) {
         TC x = xb[u];
         if (bk[u] != 0) {
-          x = smdiv(x - (SC ? smul(bb, prev) : bb * prev), pb[u], rb[u]);
+          x = SC ? smdiv(x - smul(bb, prev), pb[u], rb[u]) : mdiv(x - bb * prev, pb[u], rb[u]);
           d[c0 + (q0 + u) * st] = (T)x;
         }
         prev = x;
@@ -1338,7 +1340,7 @@ __device__ __forceinline__ void body_irs(const DevBlock<T>& b, const IrsTables& 
       if (q0 - u >= 2) {
         TC x = xb[u];
         if (bk[u] != 0) {
-          x = x - smul(pb[u], prev);
+          x = x - (SC ? smul(pb[u], prev) : pb[u] * prev);
           d[c0 + (q0 - u) * st] = (T)x;
         }
         prev = x;
