@@ -141,14 +141,14 @@ __device__ __forceinline__ unsigned long long body_timestep(const DevBlock<T>& b
   TC lsum = ri + rj + rk;
   TC fict;
   if (P.eqn_ns) {  // viscous spectral radii, timestep.f90:141-178
-    const TC fmue = (TC)P.viscl / (TC)P.prlmean;
-    const TC f1 = TC(4) / w0 / TC(3);
-    const TC f2 = gamma / w0;
+    const TC fmue = sdiv((TC)P.viscl, (TC)P.prlmean);
+    const TC f1 = sdiv(sdiv(TC(4), w0), TC(3));
+    const TC f2 = sdiv(gamma, w0);
     const TC fac = fmaxT(f1, f2);
-    const TC dtv = fac * fmue / (TC)b.vol;
+    const TC dtv = sdiv(fac * fmue, (TC)b.vol);
     const TC s0 = (TC)b.s[0], s1 = (TC)b.s[1], s2 = (TC)b.s[2];
     TC rvi = dtv * (s0 * s0), rvj = dtv * (s1 * s1), rvk = dtv * (s2 * s2);
-    fict = (TC)b.vol / (lsum + (TC)P.cfac * (rvi + rvj + rvk));
+    fict = sdiv((TC)b.vol, lsum + (TC)P.cfac * (rvi + rvj + rvk));
   } else {
     fict = sdiv((TC)b.vol, lsum);
   }
@@ -275,7 +275,7 @@ __device__ __forceinline__ void body_prep(const DevBlock<T>& b, const PhysParams
     const bool solid = b.blank[c] == 0;
 #pragma unroll
     for (int a = 0; a < 3; a++) b.vt[a * N + c] = solid ? T(0) : mdiv(w[1 + a], w[0], y);
-    b.vt[3 * N + c] = solid ? T(0) : p / (w[0] * (T)P.gas_const);
+    b.vt[3 * N + c] = solid ? T(0) : sdiv(p, w[0] * (T)P.gas_const);
   }
   if (SLOPES) {
     const long long sts[3] = {1, (long long)b.Pi, (long long)b.Pi * b.Pj};
@@ -419,7 +419,7 @@ __device__ __forceinline__ T van_albada(T a, T b, T e2) {
   // uniform stretch) and e2 > 0: the numerator is e2*a + e2*b, a zero with
   // the sign of a + b, and so is the quotient
   if (a == T(0) && b == T(0) && e2 > T(0)) return a + b;
-  return ((b * b + e2) * a + (a * a + e2) * b) / (a * a + b * b + T(2) * e2);
+  return sdiv((b * b + e2) * a + (a * a + e2) * b, a * a + b * b + T(2) * e2);
 }
 
 // yl, yr: RN(1/wl[0]) and RN(1/wr[0]); every quotient below that shares a
@@ -436,7 +436,7 @@ __device__ __noinline__ void roe_diss(const PhysParams& P, int d, T S, const T* 
   T hl = mdiv(wl[4] + pl, wl[0], yl), hr = mdiv(wr[4] + pr, wr[0], yr);
   T rt = sqrt(mdiv(wr[0], wl[0], yl));
   T rh = rt * wl[0];
-  const T den = T(1) + rt, yden = T(1) / den;
+  const T den = T(1) + rt, yden = sdiv(T(1), den);
   T uh[3];
   for (int a = 0; a < 3; a++) uh[a] = mdiv(ul[a] + rt * ur[a], den, yden);
   T hh = mdiv(hl + rt * hr, den, yden);
@@ -449,12 +449,12 @@ __device__ __noinline__ void roe_diss(const PhysParams& P, int d, T S, const T* 
   T delta = (T)P.epsentr * (fabs(un) + ch);
   auto fix = [&](T lam) {
     T a = fabs(lam);
-    return (a < delta && delta > T(0)) ? (lam * lam + delta * delta) / (T(2) * delta) : a;
+    return (a < delta && delta > T(0)) ? sdiv(lam * lam + delta * delta, T(2) * delta) : a;
   };
   T l1 = fix(un - ch), l2 = fix(un), l5 = fix(un + ch);
-  const T c22 = T(2) * c2, yc22 = T(1) / c22;
+  const T c22 = T(2) * c2, yc22 = sdiv(T(1), c22);
   T a1 = mdiv(dp - rh * ch * dun, c22, yc22);
-  T a2 = dr - dp / c2;
+  T a2 = dr - sdiv(dp, c2);
   T a5 = mdiv(dp + rh * ch * dun, c22, yc22);
   T sh[3];
   for (int a = 0; a < 3; a++) sh[a] = rh * (du[a] - (a == d ? dun : T(0)));
@@ -493,7 +493,7 @@ __device__ __noinline__ void face_states(const DevBlock<T>& b, const PhysParams&
   T qv[4][5];  // primitive (rho,u,v,w,p) at q-2..q+1
   for (int o = 0; o < 4; o++) {
     long long co = c + (o - 2) * st;
-    T r = b.w[co], yr = T(1) / r;
+    T r = b.w[co], yr = sdiv(T(1), r);
     qv[o][0] = r;
     for (int a = 0; a < 3; a++) qv[o][1 + a] = mdiv(b.w[(1 + a) * N + co], r, yr);
     qv[o][4] = b.p[co];
@@ -634,7 +634,7 @@ __device__ __forceinline__ void face_dir(const DevBlock<T>& b, const PhysParams&
       face_states_pre<T, D>(b, P, c, q, wl, &pl, wr, &pr);
     else
       face_states<T, D>(b, P, c, q, P.distype == 2 ? 2 : 1, wl, &pl, wr, &pr);
-    const T yl = T(1) / wl[0], yr = T(1) / wr[0];
+    const T yl = sdiv(T(1), wl[0]), yr = sdiv(T(1), wr[0]);
     if (P.distype == 2) {
       T f1[5], f2[5];
       ceflux_gen<T>(D, wr, pr, (T)b.s[D], yr, f1);
