@@ -63,8 +63,8 @@ FACE_DOUBLES_ROE_NS = 55
 FACE_DRAM_BYTES_PER_CELL = 519.6
 FACE_FP64_PER_CELL = 118.2
 # The three passes of the residual on a stage with dissipation (stage 1),
-# plain FP64, from ncu captures on the 128^3 sphere (profiles/k_prep_sphere128.md,
-# profiles/k_face_sphere128.md, profiles/k_combine_sphere128.md):
+# plain FP64, from ncu captures of each pass on the 128^3 sphere (one launch
+# of stage 1, --set full):
 #   cells     which cells one thread each: "prep" [1..ie]^3, "face" [2..ie]^3, "phys" [2..il]^3
 #   alg       compulsory HBM bytes per cell
 #   dram      measured DRAM read + write bytes per cell
@@ -83,7 +83,8 @@ KERNEL_MODEL = {
 }
 # The mixed form's finest-level passes (the contracted FP64 residual), per
 # physical cell and averaged over the launches of one update, from the ncu
-# capture of a whole 128^3 update (profiles/update_fp64_counts_sphere128.md):
+# capture of every kernel of one 128^3 update (FP64 instruction and DRAM byte
+# counters):
 # its prep pass (5 launches), dissipation face pass (3) and combine pass (5).
 # alg: prep reads w, p and writes H, F (stages 2, 4) or H, F, dlt, fp
 # (stages 1, 3, 5): 32.8 doubles on average; the face pass reads dlt, fp,
