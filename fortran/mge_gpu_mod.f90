@@ -15,6 +15,8 @@ module mge_gpu_mod
   integer(c_int), parameter :: MGE_DIS_CENTRAL = 0, MGE_DIS_ROE1 = 1, MGE_DIS_ROE2 = 2
   integer(c_int), parameter :: MGE_DISSIP_SCALAR = 0, MGE_DISSIP_MATRIX = 1
   integer(c_int), parameter :: MGE_PREC_FP64 = 0, MGE_PREC_MIXED = 1, MGE_PREC_REFINED = 2
+  ! the layout of the types below; mge_abi_version() of the library must match
+  integer(c_int), parameter :: MGE_ABI_VERSION = 2
   integer, parameter :: MGE_MAX_STAGE = 8, MGE_MAX_LEVEL = 16, MGE_MAX_CLOUD = 8
 
   type, bind(C) :: mge_params
@@ -61,6 +63,9 @@ module mge_gpu_mod
   end type mge_solve_opts
 
   interface
+    integer(c_int) function mge_abi_version() bind(C, name="mge_abi_version")
+      import :: c_int
+    end function
     integer(c_int) function mge_init(prm, device, ctx) bind(C, name="mge_init")
       import :: c_int, c_ptr, mge_params
       type(mge_params), intent(in) :: prm
