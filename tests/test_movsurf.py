@@ -119,3 +119,30 @@ def test_heaving_unsteady_steps_run():
         assert cl[-1] < 0.0
     finally:
         o.close()
+
+
+def test_no_slip_wall_takes_the_moved_velocity():
+    """Navier-Stokes: bc_cutcell.f90:185 sets the solid state's momentum to
+    2 rho qb - m (the normal does not enter) and :201 its energy from psol;
+    on a uniform state that is, with qb = vel/vel_fs,
+        m_sol = 2 rho qb - m,  E_sol = p/(gamma-1) + |m_sol|^2/(2 rho)."""
+    case = K.cylinder_slab(n=32, span=2, nlevel=1, extent=4.0, mcyc_fine=4, eqntype=A.MGE_EQN_NS,
+                           distype=A.MGE_DIS_ROE2, reynolds=40.0)
+    sp = case.levels[0][0]
+    o = _oracle(case)
+    try:
+        gamma = case.prm.gamma
+        rho, u, v, p = 0.9, 0.25, 0.05, 1.0 / (gamma * 0.04)
+        w = np.zeros((5,) + tuple(sp.dims[::-1]))
+        w[0], w[1], w[2], w[3], w[4] = rho, rho * u, rho * v, 0.0, p / (gamma - 1.0) + 0.5 * rho * (u * u + v * v)
+        disp, norv, vel = rigid(sp, theta=0.2, dtheta=0.6, dy=0.3)
+        o.move_surface(1, disp, norv, vel, VEL_FS)
+        o.upload(w, 1)
+        got = o.field("wsol", 1)
+        m = np.array([rho * u, rho * v, 0.0])
+        msol = 2.0 * rho * (vel / VEL_FS) - m
+        want = np.concatenate([np.full((len(msol), 1), rho), msol,
+                               (p / (gamma - 1.0) + 0.5 * np.sum(msol * msol, axis=1) / rho)[:, None]], axis=1)
+        assert np.abs(got - want).max() <= 1e-12 * np.abs(want).max()
+    finally:
+        o.close()
